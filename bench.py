@@ -1,0 +1,315 @@
+#!/usr/bin/env python
+"""Throughput of the jax-sph hot path on GB300: particle-steps/s.
+
+Workload: 3D Taylor-Green vortex, 64^3 = 262,144 particles on the periodic
+(2 pi)^3 lattice, Wendland C2 kernel (h = dx, cutoff 2h), standard SPH with
+transport velocity (tvf = 1), Re = 1600, float32, neighbour list rebuilt every
+step. One step = one si_euler step (kick, drift, neighbour rebuild, WCSPH
+forward, bc_fn). Synthetic input: the reference's own initial condition
+(lattice + analytic velocity field), built by ``jaxsph_gb300.cases.tgv``.
+
+Default (our arm): resident rollout (``sph_step`` CUDA graphs), each timed step
+bracketed by CUDA events on the launching stream, L2 flushed (256 MiB write)
+between steps outside the events. ``--impl reference`` times the CPU
+restatement of the reference step (the oracle; JAX itself is not installable
+here) on all host threads. Under torchrun every rank runs an independent
+replica (weak scaling, no collective on the data path).
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+for _p in (ROOT, os.path.join(ROOT, "jax-sph_gb300")):
+    if _p not in sys.path:
+        sys.path.insert(0, _p)
+
+import numpy as np  # noqa: E402
+import torch  # noqa: E402
+
+METRIC = "particle-steps/s on 1 GB300: batched/adjoint vs plain at stated FP64 error"
+UNIT = "particle-steps/s"
+WORKLOAD = ("3D Taylor-Green vortex 64^3 = 262,144 particles, periodic (2pi)^3, WC2K h=dx "
+            "cutoff 2h, SPH + transport velocity (tvf=1), Re=1600, c0=10, float32, "
+            "neighbour rebuild every step")
+# Algorithmic bytes per particle (float32 / int32), the minimum unique state traffic
+STEP_BYTES = 128          # fused 3D TVF step: reads r,u,dudt,dvdt,m,eta,tag; writes r,u,v,dudt,dvdt,rho,p
+FORCE_BYTES = 76          # force pass: reads r,m,u,v,rho,p,eta (52 B); writes dudt,dvdt (24 B)
+DENSITY_BYTES = 24        # density pass: reads r,m (16 B); writes rho,p (8 B)
+BIN_BYTES = 104           # binning + kick-drift: reads r,m,u,v,dudt,dvdt,eta,tag (88 B -> 4+...)
+PHASES = ("binning+kick-drift", "density", "wall", "force")
+PHASE_KERNELS = ("k_hash_count/k_tile_scan/k_scatter/k_permute", "k_density", "k_wall", "k_force")
+PHASE_BYTES = (BIN_BYTES, DENSITY_BYTES, 0, FORCE_BYTES)
+
+
+def dist_env():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+def init_dist(ws, backend):
+    if ws > 1 and not torch.distributed.is_initialized():
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        torch.distributed.init_process_group(backend=backend)
+
+
+def max_over_ranks(x, ws, device):
+    if ws == 1:
+        return x
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(ws):
+    if ws > 1:
+        torch.distributed.barrier()
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi clock/throttle samples every 200 ms while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index):
+        self.gpu = gpu_index
+        self.f = tempfile.NamedTemporaryFile("w+", suffix=".csv", delete=False)
+        self.p = None
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.gpu}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=self.f, stderr=subprocess.DEVNULL)
+        except OSError:
+            self.p = None
+        return self
+
+    def __exit__(self, *a):
+        if self.p is not None:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.p.kill()
+
+    def summary(self):
+        if self.p is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.f.flush()
+        rows = []
+        with open(self.f.name) as fh:
+            for line in fh:
+                parts = [x.strip() for x in line.split(",")]
+                if len(parts) >= 9:
+                    rows.append(parts)
+        os.unlink(self.f.name)
+        if not rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["no samples"], "samples": 0}
+
+        def num(x):
+            try:
+                return float(x)
+            except ValueError:
+                return None
+
+        sm = [num(r[1]) for r in rows if num(r[1]) is not None]
+        mx = [num(r[2]) for r in rows if num(r[2]) is not None]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in rows for k in range(4) if r[5 + k] == "Active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(rows)}
+
+
+# ------------------------------------------------------------------ CPU timings
+def cpu_oracle_rate(n_side, max_steps, budget_s, threads):
+    """Oracle float32 si_euler steps on the same 3D TGV state, all host threads."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from jaxsph_gb300 import cases
+    from oracle_setup import oracle_case
+    import oracle
+
+    torch.set_num_threads(threads)
+    setup = cases.tgv(dim=3, dx=2 * np.pi / n_side)
+    solver, fns, bc, st = oracle_case(setup, torch.float32)
+    nb = fns.allocate(st["r"])
+    st, nb = oracle.sph.si_euler_advance(setup.dt, setup.tvf, st, nb, fns, solver, bc)  # warm-up
+    t0 = time.perf_counter()
+    steps = 0
+    while steps < max_steps:
+        st, nb = oracle.sph.si_euler_advance(setup.dt, setup.tvf, st, nb, fns, solver, bc)
+        steps += 1
+        if time.perf_counter() - t0 > budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return setup.n * steps / dt, steps, dt, setup.n
+
+
+def reference_arm(args, ws, rank):
+    if rank != 0:
+        return
+    threads = os.cpu_count() or 1
+    rate, steps, secs, n = cpu_oracle_rate(64, max(1, args.steps), 150.0, threads)
+    line = {
+        "impl": "reference", "metric": METRIC, "value": rate, "unit": UNIT, "n_gpus": args.gpus,
+        "steps": steps, "warmup": 1, "ms_per_step": 1000.0 * secs / steps,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (reference initial condition of the 3D TGV)",
+        "config": {"workload": WORKLOAD, "n_particles": n},
+        "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{steps} float32 oracle si_euler steps of the full 64^3 "
+                                   f"case (time-bounded, 150 s budget, after 1 warm-up step)"},
+        "e2e": {"value": rate, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+        "note": "reference jax[cpu] is not installable here (no JAX, no network); "
+                "the oracle restatement of the reference step stands in",
+    }
+    print(json.dumps(line))
+
+
+# ------------------------------------------------------------------ GPU arm
+def e2e_rate(setup, steps, device):
+    """The public drop-in API with host buffers: per step H2D of the state,
+    ``si_euler`` advance, D2H of the resulting state."""
+    from jaxsph_gb300 import integrator, simulate
+
+    wc = simulate.make_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    _, shift = setup.space()
+    adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
+    keys_in = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
+    host = {k: setup.state[k].contiguous().pin_memory() for k in keys_in}
+    keys_out = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
+    host_out = {k: torch.empty_like(host[k]).pin_memory() for k in keys_out}
+    h2d = sum(host[k].numel() * host[k].element_size() for k in keys_in)
+    d2h = sum(host_out[k].numel() * host_out[k].element_size() for k in keys_out)
+    dev = {k: v.to(device, non_blocking=True) for k, v in host.items()}
+    nb = fns.allocate(dev["r"])
+    st = dev
+    for _ in range(2):  # warm-up (engine creation, graph capture)
+        st, nb = adv(setup.dt, st, nb)
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(steps):
+        t0 = time.perf_counter()
+        dev = {k: v.to(device, non_blocking=True) for k, v in host.items()}
+        out, nb = adv(setup.dt, dev, nb)
+        for k in keys_out:
+            host_out[k].copy_(out[k], non_blocking=True)
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+        for k in keys_out:  # next step's host inputs
+            host[k].copy_(host_out[k])
+    t = float(np.mean(times))
+    return setup.n / t, h2d, d2h, t
+
+
+def gpu_arm(args, ws, rank, local):
+    from jaxsph_gb300 import cases, simulate
+
+    torch.cuda.set_device(local)
+    device = torch.device("cuda", local)
+    setup = cases.tgv(dim=3)
+    sim = simulate.Simulation(setup, device=device)
+    sim.run(max(args.warmup, 3))
+    torch.cuda.synchronize()
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(ws)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        for k in range(args.steps):
+            flush.fill_(k & 0xFF)
+            starts[k].record()
+            sim.engine.step(1)
+            ends[k].record()
+        torch.cuda.synchronize()
+    barrier(ws)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_ms = max_over_ranks(float(np.sum(step_ms)), ws, device)
+    status = sim.engine.read_status(clear=True)
+    launches = sim.engine.launch_count() * args.steps
+    n = setup.n
+    value = n * args.steps * ws / (total_ms / 1000.0)
+    # phase times, measured with CUDA events on the launching stream
+    phases = sim.engine.profile(20)
+    peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(peaks_path):
+        peaks = json.load(open(peaks_path))
+        hbm, peak_src = float(peaks["hbm_gbs"]), "measured"
+    else:
+        hbm, peak_src = 6800.0, "fallback"
+    dom = int(np.argmax(phases))
+    dom_ms = phases[dom]
+    dom_bytes = PHASE_BYTES[dom] * n
+    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else 0.0
+    step_ms_mean = total_ms / args.steps
+    step_achieved = STEP_BYTES * n / (step_ms_mean * 1e-3) / 1e9
+    line = {
+        "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": step_ms_mean, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (reference initial condition of the 3D TGV)",
+        "config": {"workload": WORKLOAD, "n_particles": n, "parallelism": f"replicas x{ws}",
+                   "l2": "flushed between timed steps (256 MiB write outside the events)"},
+        "roofline": {"bound": "hbm", "kernel": PHASE_KERNELS[dom], "achieved": achieved,
+                     "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
+                     "peak_source": peak_src, "alg_bytes_per_particle": PHASE_BYTES[dom],
+                     "traffic": None,
+                     "step": {"alg_bytes_per_particle": STEP_BYTES, "achieved": step_achieved,
+                              "frac": step_achieved / hbm}},
+        "phases_ms": dict(zip(PHASES, phases)),
+        "status": status,
+        "gpu_launches": launches,
+        "clocks": clocks.summary(),
+    }
+    if rank == 0 and ws == 1 and not args.no_e2e:
+        rate, h2d, d2h, t = e2e_rate(setup, min(args.steps, 30), device)
+        line["e2e"] = {"value": rate, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                       "d2h_bytes_per_step": d2h,
+                       "path": "si_euler drop-in advance, pinned host state in/out every step"}
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        threads = os.cpu_count() or 1
+        rate, steps, secs, n_cpu = cpu_oracle_rate(64, 2, 30.0, threads)
+        line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+                                "sample": f"{steps} float32 oracle si_euler step(s) of the full "
+                                          f"64^3 case after 1 warm-up step ({secs:.1f} s)"}
+    if rank == 0:
+        print(json.dumps(line))
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    ws, rank, local = dist_env()
+    if args.impl == "reference":
+        init_dist(ws, "gloo")
+        reference_arm(args, ws, rank)
+        return
+    init_dist(ws, "nccl")
+    gpu_arm(args, ws, rank, local)
+    if ws > 1:
+        torch.distributed.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,213 @@
+/*
+ * sph_gb300.h -- C ABI of the GB300 (sm_103a) jax-sph hot path.
+ *
+ * One handle owns the device workspace for a set of independent SPH cases
+ * ("instances", one for the plain path, many for the batched form) that share
+ * one dimension, kernel, solver and boundary-treatment configuration. All
+ * particle data crossing this ABI lives in device memory owned by the caller,
+ * laid out exactly like the reference's state dict (one row per particle,
+ * row-major (N, dim) float32 for vectors). The library never frees caller
+ * memory; only sph_create allocates.
+ *
+ * Every entry point returns an int status: 0 on success, otherwise a
+ * combination of the SPH_ERR_* bits below. Data-dependent conditions found on
+ * the device (the reference's PartitionErrorCode bits, non-finite values) are
+ * accumulated in a device status word and read with sph_read_status, the way
+ * the reference polls NeighborList.error (jax_md/partition.py:453-499,
+ * jax_sph/simulate.py:120-128). No exception crosses the ABI. Calls are
+ * stream-ordered on the stream passed as `stream` (a cudaStream_t, 0 = legacy
+ * default stream). A handle is thread-compatible: one host thread at a time.
+ *
+ * Reference interfaces replaced (paths within tumaer/jax-sph):
+ *   partition.neighbor_list(...).allocate / .update  jax_sph/partition.py:492-571,
+ *       jax_sph/jax_md/partition.py:723-1026        -> sph_nl_allocate, sph_nl_update,
+ *                                                       sph_nl_edges
+ *   WCSPH(...).forward_wrapper()(state, neighbors)   jax_sph/solver.py:613-951
+ *                                                    -> sph_forward
+ *   si_euler(...)(dt, state, neighbors)              jax_sph/integrator.py:8-58
+ *                                                    -> sph_step
+ */
+#ifndef SPH_GB300_H
+#define SPH_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define SPH_ABI_VERSION 1
+
+/* Reference PartitionErrorCode bits (jax_sph/jax_md/partition.py:453-457). */
+#define SPH_NEIGHBOR_LIST_OVERFLOW 0x1u
+#define SPH_CELL_LIST_OVERFLOW 0x2u
+#define SPH_CELL_SIZE_TOO_SMALL 0x4u
+#define SPH_MALFORMED_BOX 0x8u
+/* Library bits. */
+#define SPH_ERR_INVALID_ARG 0x100u
+#define SPH_ERR_CUDA 0x200u
+#define SPH_ERR_TIMEOUT 0x400u
+#define SPH_ERR_NONFINITE 0x800u
+/* A position hashed outside the cell grid (exactly on the upper box face);
+ * it is clamped into the last cell. */
+#define SPH_WARN_BOX_EDGE 0x1000u
+
+enum { SPH_KERNEL_QSK = 0, SPH_KERNEL_WC2K = 1 };   /* jax_sph/kernel.py:51-103 */
+enum { SPH_SOLVER_SPH = 0, SPH_SOLVER_RIE = 1 };    /* jax_sph/solver.py:676-694 */
+enum { SPH_EOS_TAIT = 0, SPH_EOS_RIEMANN = 1 };     /* jax_sph/eos.py:20-57 */
+
+/* External acceleration g_ext_fn(r) of the cases on the path. */
+enum {
+  SPH_GEXT_ZERO = 0,   /* TGV, LDC (cases/tgv.py:53, cases/ldc.py:124) */
+  SPH_GEXT_CONST = 1,  /* g everywhere (DB: (0,-g), cases/db.py:123-126) */
+  SPH_GEXT_BAND_X = 2, /* g.x where band_lo < y < band_hi (PF, cases/pf.py:122-131) */
+  SPH_GEXT_ARRAY = 3   /* per-particle array from SphStateView.g_ext */
+};
+
+/* Boundary condition bc_fn(state) applied after the forward pass by a step. */
+enum {
+  SPH_BC_NONE = 0,          /* TGV (cases/tgv.py:56-57) */
+  SPH_BC_SOLID_ZERO = 1,    /* u,v,dudt,dvdt = 0 on SOLID_WALL (PF, cases/pf.py:133-146) */
+  SPH_BC_SOLID_ZERO_P = 2,  /* as above and p = 0 (DB, cases/db.py:128-142) */
+  SPH_BC_LID = 3            /* SOLID_WALL at rest, MOVING_WALL at u_lid (LDC, cases/ldc.py:127-144) */
+};
+
+/* Configuration shared by every case of a handle. */
+typedef struct SphConfig {
+  int32_t dim;            /* 2 or 3 */
+  int32_t kernel;         /* SPH_KERNEL_* */
+  int32_t solver;         /* SPH_SOLVER_* */
+  int32_t is_rho_evol;    /* density evolution instead of summation */
+  int32_t is_bc_trick;    /* generalized wall boundary condition */
+  int32_t is_free_slip;
+  int32_t mask_self;      /* exclude self pairs from the neighbour list */
+  int32_t kahan;          /* compensated (Kahan) pair sums */
+  double capacity_multiplier; /* neighbour/cell capacity factor (reference 1.25) */
+} SphConfig;
+
+/* Per-case parameters (all in the reference's units). */
+typedef struct SphCase {
+  int64_t n;              /* particles of this case (cases are concatenated) */
+  double box[3];          /* periodic box side lengths (cast to float32 like the reference) */
+  double r_cutoff;        /* neighbour cutoff = kernel cutoff (3h QSK, 2h WC2K) */
+  double dx;              /* lattice spacing (artificial-viscosity h_ab) */
+  double h;               /* smoothing length */
+  double dt;              /* si_euler time step (advance(dt, ...)) */
+  double dt_solver;       /* WCSPH(dt=...) used by density evolution (solver.py:29, :790) */
+  double tvf;             /* transport-velocity factor of si_euler */
+  double c_ref;
+  int32_t eos;            /* SPH_EOS_* */
+  int32_t g_kind;         /* SPH_GEXT_* */
+  int32_t bc_kind;        /* SPH_BC_* */
+  int32_t pad0;
+  double p_ref, rho_ref, p_bg, gamma, u_ref;
+  double eta_limiter;     /* Riemann dissipation limiter, -1 = off */
+  double artificial_alpha;
+  double g[3];            /* SPH_GEXT_CONST / BAND_X magnitude vector */
+  double g_band_lo, g_band_hi;
+  double u_lid[3];
+} SphCase;
+
+/* Caller-owned device arrays in the reference state-dict layout
+ * (jax_sph/case_setup.py:164-181). Vectors are (n, dim) row-major float32.
+ * nw is needed only for the Riemann solver with the wall BC or free slip;
+ * g_ext only with SPH_GEXT_ARRAY. Unused pointers may be NULL. */
+typedef struct SphStateView {
+  int64_t n;
+  float* r;
+  const int32_t* tag;
+  float* u;
+  float* v;
+  float* dudt;
+  float* dvdt;
+  float* drhodt;
+  float* rho;
+  float* p;
+  const float* mass;
+  const float* eta;
+  const float* nw;
+  const float* g_ext;
+} SphStateView;
+
+/* Capacities of the reference's two-phase neighbour list
+ * (NeighborList.cell_list_capacity / max_occupancy). */
+typedef struct SphNLCapacity {
+  int64_t cell_capacity;  /* int(max cell occupancy * multiplier) */
+  int64_t max_occupancy;  /* edge capacity: int(edge count * multiplier) */
+  int64_t occupancy;      /* edges found at allocation */
+  int64_t max_cell_occupancy;
+} SphNLCapacity;
+
+typedef struct SphHandle SphHandle;
+
+/* Library ABI version (SPH_ABI_VERSION). */
+int sph_abi_version(void);
+/* Message of the last failing call on this host thread ("" if none). */
+const char* sph_last_error(void);
+
+/* Create a handle for `n_cases` cases sharing `cfg`. Allocates all device
+ * workspace (the only allocating call). Replaces the host-side construction
+ * done by neighbor_list(...) and WCSPH(...) (jax_sph/partition.py:492-571,
+ * jax_sph/solver.py:616-700). */
+int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases,
+               SphHandle** out);
+int sph_destroy(SphHandle* h);
+/* Replace the per-case physics parameters (dt, EOS, forcing, ...) of a
+ * handle. The particle counts, boxes and cutoffs must stay unchanged
+ * (they fix the workspace). */
+int sph_update_cases(SphHandle* h, const SphCase* cases, int32_t n_cases);
+
+/* Copy a state (original particle order) into the handle. */
+int sph_set_state(SphHandle* h, const SphStateView* state, void* stream);
+/* Write the handle's current state back in the original particle order. */
+int sph_get_state(SphHandle* h, SphStateView* state, void* stream);
+
+/* Neighbour list allocate (host-synchronous, like the reference's
+ * non-jittable allocate, jax_md/partition.py:911-1001): bins the current
+ * positions, measures the capacities and stores them in the handle. */
+int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out,
+                    void* stream);
+/* Set capacities explicitly (a NeighborList carried over from elsewhere). */
+int sph_nl_set_capacity(SphHandle* h, const SphNLCapacity* cap);
+/* Neighbour list update with fixed capacities (jax_md/partition.py:1003-1026):
+ * re-bins the current positions; sets SPH_CELL_LIST_OVERFLOW /
+ * SPH_NEIGHBOR_LIST_OVERFLOW in the status word when a capacity is exceeded. */
+int sph_nl_update(SphHandle* h, void* stream);
+/* Emit the sparse edge list of the last binning into idx[2][capacity]
+ * (row 0 = receiver/neighbour, row 1 = sender/particle, padding = n), sender
+ * ascending, receivers ascending per sender. *count_dev (device int64)
+ * receives the number of real edges; edges beyond `capacity` are dropped and
+ * flag SPH_NEIGHBOR_LIST_OVERFLOW (jax_md/partition.py:885-909, :956-976). */
+int sph_nl_edges(SphHandle* h, int32_t* idx, int64_t capacity, int64_t* count_dev,
+                 void* stream);
+
+/* WCSPH forward pass on the current state with the current binning
+ * (jax_sph/solver.py:705-949): density, EOS, wall BC, forces, transport
+ * velocity, artificial viscosity. No bc_fn is applied. */
+int sph_forward(SphHandle* h, void* stream);
+/* `nsteps` si_euler steps (jax_sph/integrator.py:22-56): kick, drift, neighbour
+ * update (rebuilt every step), forward, bc_fn. Replays a CUDA graph. */
+int sph_step(SphHandle* h, int32_t nsteps, void* stream);
+
+/* Kernel launches issued by one si_euler step of this handle. */
+int sph_step_launch_count(SphHandle* h, int32_t* count);
+/* Run `nsteps` steps eagerly, timing their phases with CUDA events on
+ * `stream` (where the kernels run): ms[0] binning with the fused kick-drift,
+ * ms[1] density pass, ms[2] wall pass, ms[3] force pass, averaged per step.
+ * Host-synchronous; the steps advance the state like sph_step. */
+int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream);
+
+/* Read (and optionally clear) the device status word. Synchronizes `stream`. */
+int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream);
+
+/* Float64 global diagnostics per case, computed on the GPU in double
+ * precision: out[c*8 + k] = {mass, mom_x, mom_y, mom_z, E_kin, u_max, rho_min,
+ * rho_max} of case c (fluid particles; E_kin follows jax_sph/utils.py:128-133).
+ * `out` is a device array of n_cases*8 doubles. */
+int sph_diagnostics(SphHandle* h, double* out, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* SPH_GB300_H */

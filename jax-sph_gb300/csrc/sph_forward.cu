@@ -1,0 +1,424 @@
+// WCSPH forward pass (jax_sph/solver.py:705-949) as three cell-tiled passes
+// over particles in cell-sorted order, one thread per receiving particle:
+//
+//   density pass  summation (solver.py:176-178) / SPH continuity (:24-30) /
+//                 Riemann continuity (:108-164), EOS (:801-802), Shepard wall
+//                 velocity for the Riemann wall BC (:547-552); counts edges.
+//   wall pass     generalized wall BC for the SPH solver (:431-530), wall
+//                 particles only, after every fluid pressure is known.
+//   force pass    standard (:221-256) or Riemann (:316-401) acceleration,
+//                 transport-velocity acceleration (:199-213), artificial
+//                 viscosity (:404-428), g_ext (:936) and, in a step, bc_fn.
+//
+// Pairs are never materialised: each thread walks its 3^d neighbour cells and
+// keeps exactly the reference's edges (receiver i, sender j) with
+// metric(r_j, r_i) < cutoff_sq; the physics then uses dr_ij = disp(r_i, r_j)
+// as the reference does. Sums are accumulated per receiver in registers in a
+// fixed order (deterministic, no atomics on physics values).
+#include "sph_internal.cuh"
+
+namespace sph {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr unsigned kFull = 0xffffffffu;
+
+inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
+
+__device__ __forceinline__ float3 f3(const float4& a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float dot3(const float3& a, const float3& b) {
+  return a.x * b.x + a.y * b.y + a.z * b.z;
+}
+
+// Per-case edge counter for the NEIGHBOR_LIST_OVERFLOW test: one reduction
+// and one atomic per case present in the warp (cases are contiguous, so
+// usually one).
+__device__ __forceinline__ void count_edges(int ci, int cnt, bool valid,
+                                            unsigned long long* edgecnt, const CaseDev* cases,
+                                            unsigned* status) {
+  const unsigned mask = __ballot_sync(kFull, valid);
+  if (!valid) return;
+  const int lane = threadIdx.x & 31;
+  unsigned remaining = mask;
+  while (remaining) {
+    const int leader = __ffs(remaining) - 1;
+    const int lci = __shfl_sync(mask, ci, leader);
+    const unsigned grp = __ballot_sync(mask, ci == lci);
+    const unsigned tot = __reduce_add_sync(mask, ci == lci ? (unsigned)cnt : 0u);
+    if (lane == leader) {
+      unsigned long long old = atomicAdd(&edgecnt[lci], (unsigned long long)tot);
+      if ((long long)(old + tot) > cases[lci].edge_cap)
+        atomicOr(status, SPH_NEIGHBOR_LIST_OVERFLOW);
+    }
+    remaining &= ~grp;
+  }
+}
+
+// ------------------------------------------------------------------ density pass
+// MODE 0: summation (fluid receivers), 1: SPH continuity, 2: Riemann
+// continuity (fluid receivers). `rie_shepard`: wall receivers compute the
+// Shepard average of fluid velocities instead (gwbc_fn_riemann_wrapper,
+// solver.py:547-552); `sph_gwbc`: the SPH wall BC follows, which ends with
+// rho = EOS^-1(p) for every particle (solver.py:516).
+template <int DIM, int KER, int MODE, bool KAHAN>
+__global__ void __launch_bounds__(kBlock)
+k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
+          int mask_self, int rie_shepard, int sph_gwbc, const float* g_arr, float4* R4,
+          float4* UT4, unsigned long long* edgecnt, unsigned* status) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool valid = i < N;
+  int ci = 0, cnt = 0;
+  if (valid) {
+    const int meta = b.META[i];
+    ci = case_of(meta);
+    const CaseDev& c = cases[ci];
+    const int tag = tag_of(meta);
+    const bool fluid = tag == FLUID;
+    const float4 ri = b.P4[i];
+    const float4 Ui = b.U4[i];
+    const float3 ui = f3(Ui);
+    const float rho_i = Ui.w;
+    const float p_i = b.V4[i].w;
+    const bool shepard = rie_shepard && !fluid;
+    float3 gi = make_float3(0.f, 0.f, 0.f);
+    if (MODE == 2) gi = g_ext<DIM>(c, ri, g_arr, b.ORIG[i]);
+    Acc<KAHAN> s0, sx, sy, sz;
+    for_each_candidate<DIM>(c, cellid[i] - c.cell_off, start, [&](int j) {
+      if (mask_self && j == i) return;
+      const float4 rj = b.P4[j];
+      if (!is_edge<DIM>(ri, rj, c)) return;
+      ++cnt;
+      if (MODE != 1 && !fluid && !shepard) return;
+      const float3 dr = pdisp3<DIM>(ri, rj, c);
+      const float d2 = sqd<DIM>(dr);
+      const float dist = d2 > 0.f ? __fsqrt_rn(d2) : 0.f;
+      if (shepard) {
+        if (tag_of(b.META[j]) == FLUID) {
+          const float w = kw<KER>(dist, c);
+          const float4 Uj = b.U4[j];
+          s0.add(w);
+          sx.add(w * Uj.x);
+          sy.add(w * Uj.y);
+          sz.add(w * Uj.z);
+        }
+        return;
+      }
+      if (MODE == 0) {
+        s0.add(kw<KER>(dist, c));
+        return;
+      }
+      const float4 Uj = b.U4[j];
+      const float3 uj = f3(Uj);
+      const float inv = 1.0f / (dist + kEps);
+      const float gw = kdw<KER>(dist, c);
+      if (MODE == 1) {
+        const float3 gv = make_float3(gw * dr.x * inv, gw * dr.y * inv, gw * dr.z * inv);
+        const float vj = rj.w / Uj.w;
+        s0.add(vj * ((ui.x - uj.x) * gv.x + (ui.y - uj.y) * gv.y + (ui.z - uj.z) * gv.z));
+        return;
+      }
+      // MODE 2, fluid receiver (rho_evol_riemann_fn, solver.py:108-164)
+      const int tj = tag_of(b.META[j]);
+      const float3 e = make_float3(dr.x * inv, dr.y * inv, dr.z * inv);
+      const float3 kg = make_float3(gw * e.x, gw * e.y, gw * e.z);
+      float uL, uR, pR, rhoR;
+      if (is_wall(tj)) {
+        const float3 nj = f3(b.NW4[j]);
+        uL = -dot3(ui, nj);
+        uR = -uL + 2.0f * dot3(uj, nj);
+        pR = p_i + rho_i * (-dot3(gi, dr));
+        rhoR = eos_rho(pR, c);
+      } else {
+        uL = -dot3(ui, e);
+        uR = -dot3(uj, e);
+        pR = b.V4[j].w;
+        rhoR = Uj.w;
+      }
+      const float Uavg = 0.5f * (uL + uR);
+      const float rho_avg = 0.5f * (rho_i + rhoR);
+      const float Ustar = Uavg + 0.5f * (p_i - pR) / (rho_avg * c.c_ref);
+      // v* = U*(-e) + (v_avg - U_avg(-e)),  v_avg = (u_i + u_j)/2
+      const float3 vstar = make_float3(-Ustar * e.x + (0.5f * (ui.x + uj.x) + Uavg * e.x),
+                                       -Ustar * e.y + (0.5f * (ui.y + uj.y) + Uavg * e.y),
+                                       -Ustar * e.z + (0.5f * (ui.z + uj.z) + Uavg * e.z));
+      const float3 dv = make_float3(ui.x - vstar.x, ui.y - vstar.y, ui.z - vstar.z);
+      s0.add(2.0f * rho_i * rj.w / Uj.w * dot3(dv, kg));
+    });
+    float rho_new = rho_i, drhodt = 0.f;
+    if (MODE == 0) {
+      if (fluid) rho_new = ri.w * s0.s;
+    } else if (MODE == 1) {
+      drhodt = rho_i * s0.s;
+      rho_new = rho_i + c.dt_rho * drhodt;
+    } else {
+      if (fluid) drhodt = s0.s;
+      rho_new = rho_i + c.dt_rho * drhodt;
+    }
+    if (UT4) {
+      if (shepard) {
+        const float den = s0.s + kEps;
+        UT4[i] = make_float4(sx.s / den, sy.s / den, sz.s / den, 0.f);
+      } else {
+        UT4[i] = make_float4(ui.x, ui.y, ui.z, 0.f);
+      }
+    }
+    float p_new = eos_p(rho_new, c);
+    if (sph_gwbc && fluid) rho_new = eos_rho(p_new, c);
+    R4[i] = make_float4(rho_new, p_new, drhodt, 0.f);
+    if (!isfinite(rho_new) || !isfinite(p_new)) atomicOr(status, SPH_ERR_NONFINITE);
+  }
+  count_edges(ci, cnt, valid, edgecnt, cases, status);
+}
+
+// ------------------------------------------------------------------ wall pass
+// gwbc_fn (solver.py:431-530) for wall receivers: Shepard sums over fluid
+// senders of u, v, p and rho*dr; writes u, v (U4/V4 xyz) and R4 (rho, p).
+template <int DIM, int KER, bool KAHAN>
+__global__ void __launch_bounds__(kBlock)
+k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
+       int mask_self, int free_slip, const float* g_arr, float4* R4) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int meta = b.META[i];
+  if (!is_wall(tag_of(meta))) return;
+  const CaseDev& c = cases[case_of(meta)];
+  const float4 ri = b.P4[i];
+  Acc<KAHAN> sw, su[3], sv[3], sp, sr[3];
+  for_each_candidate<DIM>(c, cellid[i] - c.cell_off, start, [&](int j) {
+    if (mask_self && j == i) return;
+    if (tag_of(b.META[j]) != FLUID) return;
+    const float4 rj = b.P4[j];
+    if (!is_edge<DIM>(ri, rj, c)) return;
+    const float3 dr = pdisp3<DIM>(ri, rj, c);
+    const float d2 = sqd<DIM>(dr);
+    const float dist = d2 > 0.f ? __fsqrt_rn(d2) : 0.f;
+    const float w = kw<KER>(dist, c);
+    const float4 Uj = b.U4[j], Vj = b.V4[j], Rj = R4[j];
+    sw.add(w);
+    su[0].add(w * Uj.x); su[1].add(w * Uj.y); su[2].add(w * Uj.z);
+    sv[0].add(w * Vj.x); sv[1].add(w * Vj.y); sv[2].add(w * Vj.z);
+    sp.add(w * Rj.y);
+    const float rw = Rj.x * w;
+    sr[0].add(rw * dr.x); sr[1].add(rw * dr.y); sr[2].add(rw * dr.z);
+  });
+  const float den = sw.s + kEps;
+  float3 uw = make_float3(su[0].s / den, su[1].s / den, su[2].s / den);
+  float3 vw = make_float3(sv[0].s / den, sv[1].s / den, sv[2].s / den);
+  if (free_slip) {
+    const float4 nw = b.NW4[i];
+    const float3 n = make_float3(-nw.x, -nw.y, -nw.z);
+    const float pu = dot3(uw, n), pv = dot3(vw, n);
+    uw = make_float3(n.x * pu, n.y * pu, n.z * pu);
+    vw = make_float3(n.x * pv, n.y * pv, n.z * pv);
+  }
+  const float4 Ui = b.U4[i], Vi = b.V4[i];
+  b.U4[i] = make_float4(2.f * Ui.x - uw.x, 2.f * Ui.y - uw.y, 2.f * Ui.z - uw.z, Ui.w);
+  b.V4[i] = make_float4(2.f * Vi.x - vw.x, 2.f * Vi.y - vw.y, 2.f * Vi.z - vw.z, Vi.w);
+  const float3 gi = g_ext<DIM>(c, ri, g_arr, b.ORIG[i]);
+  const float pw = (sp.s + (gi.x * sr[0].s + gi.y * sr[1].s + gi.z * sr[2].s)) / den;
+  const float drhodt = R4[i].z;
+  R4[i] = make_float4(eos_rho(pw, c), pw, drhodt, 0.f);
+}
+
+// ------------------------------------------------------------------ force pass
+// SOLVER 0: standard SPH with transport-velocity stress; 1: Riemann SPH.
+template <int DIM, int KER, int SOLVER, bool KAHAN>
+__global__ void __launch_bounds__(kBlock)
+k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
+        int mask_self, int bc_trick, int free_slip, const float* g_arr, const float4* R4,
+        const float4* UT4, bool apply_bc, unsigned* status) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int meta = b.META[i];
+  const CaseDev& c = cases[case_of(meta)];
+  const int tag = tag_of(meta);
+  const bool fluid_i = tag == FLUID;
+  const float4 ri = b.P4[i];
+  const float m_i = ri.w;
+  const float3 ui = f3(b.U4[i]);
+  const float3 vi = f3(b.V4[i]);
+  const float4 Ri = R4[i];
+  const float rho_i = Ri.x, p_i = Ri.y;
+  const float eta_i = b.ETA[i];
+  const float Vi = m_i / rho_i;
+  const float Vi2 = Vi * Vi;
+  const float inv_mi = 1.0f / m_i;
+  // A_i r = rho_i u_i ((v_i - u_i) . r)  (tvf_stress_fn, solver.py:216-218)
+  const float3 Ai = make_float3(rho_i * ui.x, rho_i * ui.y, rho_i * ui.z);
+  const float3 wi = make_float3(vi.x - ui.x, vi.y - ui.y, vi.z - ui.z);
+  const float3 gi = g_ext<DIM>(c, ri, g_arr, b.ORIG[i]);
+  const bool av = c.av_alpha != 0.0f;
+  const float mask_i = (SOLVER == 1 && bc_trick && free_slip) ? (fluid_i ? 1.f : 0.f) : 1.f;
+  Acc<KAHAN> ax, ay, az, tx, ty, tz;
+  for_each_candidate<DIM>(c, cellid[i] - c.cell_off, start, [&](int j) {
+    if (mask_self && j == i) return;
+    const float4 rj = b.P4[j];
+    if (!is_edge<DIM>(ri, rj, c)) return;
+    const float3 dr = pdisp3<DIM>(ri, rj, c);
+    const float d2 = sqd<DIM>(dr);
+    const float dist = d2 > 0.f ? __fsqrt_rn(d2) : 0.f;
+    const float gw = kdw<KER>(dist, c);
+    const float inv_d = 1.0f / (dist + kEps);
+    const float4 Rj = R4[j];
+    const float rho_j = Rj.x, p_j = Rj.y, m_j = rj.w;
+    const float Vj = m_j / rho_j;
+    const float cc = (Vi2 + Vj * Vj) * inv_mi * gw * inv_d;
+    const float3 uj = f3(b.U4[j]);
+    const int tj = tag_of(b.META[j]);
+    float3 a;
+    if (SOLVER == 0) {
+      const float3 vj = f3(b.V4[j]);
+      const float eta_j = b.ETA[j];
+      const float eta_ij = 2.f * eta_i * eta_j / (eta_i + eta_j + kEps);
+      const float p_ij = (rho_j * p_i + rho_i * p_j) / (rho_i + rho_j);
+      const float ki = dot3(wi, dr);
+      const float kj = dot3(make_float3(vj.x - uj.x, vj.y - uj.y, vj.z - uj.z), dr);
+      const float3 Ar = make_float3(0.5f * (Ai.x * ki + rho_j * uj.x * kj),
+                                    0.5f * (Ai.y * ki + rho_j * uj.y * kj),
+                                    0.5f * (Ai.z * ki + rho_j * uj.z * kj));
+      a = make_float3(cc * (-p_ij * dr.x + Ar.x + eta_ij * (ui.x - uj.x)),
+                      cc * (-p_ij * dr.y + Ar.y + eta_ij * (ui.y - uj.y)),
+                      cc * (-p_ij * dr.z + Ar.z + eta_ij * (ui.z - uj.z)));
+    } else {
+      const float3 e = make_float3(dr.x * inv_d, dr.y * inv_d, dr.z * inv_d);
+      const float3 kg = make_float3(gw * e.x, gw * e.y, gw * e.z);
+      const bool wj = is_wall(tj);
+      float uL, uR, pR, rhoR;
+      float3 ud = uj;
+      if (wj) {
+        const float3 nj = f3(b.NW4[j]);
+        uL = -dot3(ui, nj);
+        uR = -uL + 2.f * dot3(uj, nj);
+        pR = p_i + rho_i * (-dot3(gi, dr));
+        rhoR = eos_rho(pR, c);
+        const float4 ut = UT4[j];
+        ud = make_float3(2.f * uj.x - ut.x, 2.f * uj.y - ut.y, 2.f * uj.z - ut.z);
+      } else {
+        uL = -dot3(ui, e);
+        uR = -dot3(uj, e);
+        pR = p_j;
+        rhoR = rho_j;
+      }
+      const float P_avg = 0.5f * (p_i + pR);
+      const float rho_avg = 0.5f * (rho_i + rhoR);
+      const float eta_j = b.ETA[j];
+      const float eta_ij = 2.f * eta_i * eta_j / (eta_i + eta_j + kEps);
+      float beta;
+      if (c.eta_limiter == -1.0f) {
+        beta = c.c_ref;
+      } else {
+        beta = fminf(c.eta_limiter * fmaxf(uL - uR, 0.f), c.c_ref);
+      }
+      const float Pstar = P_avg + 0.5f * rho_avg * (uL - uR) * beta;
+      const float rr = rho_i * rho_j;
+      const float k9 = -2.f * m_j * (Pstar / rr);
+      const float k6 = 2.f * m_j * eta_ij / rr * inv_d * gw * mask_i;
+      a = make_float3(k9 * kg.x + k6 * (ui.x - ud.x), k9 * kg.y + k6 * (ui.y - ud.y),
+                      k9 * kg.z + k6 * (ui.z - ud.z));
+    }
+    if (av && fluid_i && tj == FLUID) {
+      const float rho_ab = 0.5f * (rho_i + rho_j);
+      const float num = m_j * c.av_alpha * c.av_hab * c.av_cab *
+                        ((ui.x - uj.x) * dr.x + (ui.y - uj.y) * dr.y + (ui.z - uj.z) * dr.z);
+      const float k = num * gw * inv_d / (rho_ab * (dist * dist + c.av_eps));
+      a.x += k * dr.x;
+      a.y += k * dr.y;
+      a.z += k * dr.z;
+    }
+    ax.add(a.x);
+    ay.add(a.y);
+    az.add(a.z);
+    // acceleration_tvf_fn: c * p_bg_i * r_ij
+    const float ct = cc * c.p_bg_tvf;
+    tx.add(ct * dr.x);
+    ty.add(ct * dr.y);
+    tz.add(ct * dr.z);
+  });
+  float3 dudt = make_float3(ax.s + gi.x, ay.s + gi.y, az.s + gi.z);
+  float3 dvdt = make_float3(tx.s, ty.s, tz.s);
+  if (DIM == 2) {
+    dudt.z = 0.f;
+    dvdt.z = 0.f;
+  }
+  if (apply_bc) {
+    dudt = bc_acc(dudt, tag, c);
+    dvdt = bc_acc(dvdt, tag, c);
+  }
+  if (!isfinite(dudt.x) || !isfinite(dudt.y) || !isfinite(dudt.z)) atomicOr(status, SPH_ERR_NONFINITE);
+  b.A4[i] = make_float4(dudt.x, dudt.y, dudt.z, Ri.z);
+  b.A2[i] = make_float4(dvdt.x, dvdt.y, dvdt.z, 0.f);
+}
+
+template <int DIM, int KER, bool KAHAN>
+void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int* cellid,
+               const int* start, unsigned long long* edgecnt, const float* g_arr, bool apply_bc,
+               bool has_walls) {
+  const int g = nblocks(L.N);
+  cudaStream_t st = L.stream;
+  const bool rie = L.solver == SPH_SOLVER_RIE;
+  const int rie_shepard = rie && L.bc_trick && !L.free_slip;
+  const int sph_gwbc = !rie && L.bc_trick;
+  float4* ut = rie ? UT4 : nullptr;
+#define SPH_DENSITY(MODE)                                                                 \
+  k_density<DIM, KER, MODE, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,  \
+                                                         L.mask_self, rie_shepard,        \
+                                                         sph_gwbc, g_arr, R4, ut, edgecnt, \
+                                                         L.status)
+  if (!L.rho_evol)
+    SPH_DENSITY(0);
+  else if (rie)
+    SPH_DENSITY(2);
+  else
+    SPH_DENSITY(1);
+#undef SPH_DENSITY
+  count_launch(L);
+  mark(L, 2);
+  if (sph_gwbc && has_walls) {
+    k_wall<DIM, KER, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start, L.mask_self,
+                                                  L.free_slip, g_arr, R4);
+    count_launch(L);
+  }
+  mark(L, 3);
+  if (rie)
+    k_force<DIM, KER, 1, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,
+                                                        L.mask_self, L.bc_trick, L.free_slip,
+                                                        g_arr, R4, UT4, apply_bc, L.status);
+  else
+    k_force<DIM, KER, 0, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,
+                                                        L.mask_self, L.bc_trick, L.free_slip,
+                                                        g_arr, R4, nullptr, apply_bc, L.status);
+  count_launch(L);
+  mark(L, 4);
+}
+
+template <int DIM, int KER>
+void forward_k(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int* cellid,
+               const int* start, unsigned long long* edgecnt, const float* g_arr, bool apply_bc,
+               bool has_walls) {
+  if (L.kahan)
+    forward_t<DIM, KER, true>(L, b, R4, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+  else
+    forward_t<DIM, KER, false>(L, b, R4, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+}
+
+}  // namespace
+
+void launch_forward(const LaunchCtx& L, Buffers b, const float4* /*R4*/, float4* R4w, float4* UT4,
+                    const int* cellid, const int* start, unsigned long long* edgecnt,
+                    const float* g_arr, bool apply_bc, bool has_walls) {
+  cudaMemsetAsync(edgecnt, 0, sizeof(unsigned long long) * L.n_cases, L.stream);
+  if (L.dim == 3) {
+    if (L.kernel == SPH_KERNEL_QSK)
+      forward_k<3, 0>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+    else
+      forward_k<3, 1>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+  } else {
+    if (L.kernel == SPH_KERNEL_QSK)
+      forward_k<2, 0>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+    else
+      forward_k<2, 1>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+  }
+}
+
+}  // namespace sph

@@ -1,0 +1,306 @@
+// Internal declarations of the GB300 jax-sph hot path (not part of the ABI).
+//
+// Device layout (particles always kept in cell-sorted order after a binning):
+//   P4  float4  (x, y, z, m)          positions + mass
+//   U4  float4  (u.xyz, rho_state)    velocity + state density
+//   V4  float4  (v.xyz, p_state)      transport velocity + state pressure
+//   A4  float4  (dudt.xyz, drhodt)    accelerations + density rate
+//   A2  float4  (dvdt.xyz, -)         transport acceleration
+//   ETA float, META int (case << 4 | tag), ORIG int (original index)
+//   NW4 float4  wall normals (Riemann/free-slip only)
+//   R4  float4  (rho_new, p_new, drhodt_new, -) produced by the density pass
+//   UT4 float4  Shepard-averaged wall velocity (Riemann + wall BC)
+// Every pass writes only arrays that no concurrent thread of the same pass
+// reads, so no pass needs a grid-wide barrier.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "../../include/sph_gb300.h"
+
+namespace sph {
+
+constexpr float kEps = 2.220446049250313e-16f;  // jnp.finfo(float).eps, solver.py:21
+constexpr int kTagBits = 4;
+constexpr int kTagMask = 0xF;
+
+enum Tag { FLUID = 0, SOLID_WALL = 1, MOVING_WALL = 2, DIRICHLET_WALL = 3 };
+
+// Per-case constants, all rounded to float32 the way the reference's
+// float32 program sees them.
+struct CaseDev {
+  float box[3], half[3];
+  float cell_size[3];
+  int nc[3];          // cells per side (1 along an axis with fewer than 3 cells)
+  int mult[3];        // hash multipliers (1, nx, nx*ny)
+  int use_cells;      // reference builds a cell list (cells >= 3 on every axis)
+  int cell_off, ncell;
+  int p_off, n;
+  int cell_cap;       // cell capacity for the CELL_LIST_OVERFLOW test
+  long long edge_cap; // neighbour-list capacity for NEIGHBOR_LIST_OVERFLOW
+  float cutoff_sq;
+  float inv_h, sigma, dsigma;  // W(r) = sigma*f(q); dW/dr = dsigma*g(q)
+  float dt, cv;       // f32(dt), f32(tvf*0.5*dt) of si_euler
+  float dt_rho;       // WCSPH dt of density evolution
+  int eos;
+  float p_ref, rho_ref, p_bg, gamma, inv_gamma, rie_k;  // rie_k = 100*u_ref^2
+  float p_bg_tvf;     // eos.p_fn(0)
+  float c_ref, eta_limiter;
+  float av_alpha, av_hab, av_cab, av_eps;
+  int g_kind;
+  float g[3], g_lo, g_hi;
+  int bc_kind;
+  float u_lid[3];
+};
+
+struct Buffers {
+  float4 *P4, *U4, *V4, *A4, *A2, *NW4;
+  float* ETA;
+  int *META, *ORIG;
+};
+
+// ------------------------------------------------------------------ helpers
+__device__ __forceinline__ int tag_of(int meta) { return meta & kTagMask; }
+__device__ __forceinline__ int case_of(int meta) { return meta >> kTagBits; }
+__device__ __forceinline__ bool is_wall(int tag) { return tag >= 1 && tag <= 3; }
+
+// jnp.mod(x, L) for L > 0: fmod then add L to a negative non-zero remainder.
+// For -L < x < 2L the fmod is x or x - L, both exact (Sterbenz), so the fast
+// branch equals fmodf bit for bit; other inputs take fmodf itself.
+__device__ __forceinline__ float jmod(float x, float L) {
+  if (x >= L) {
+    if (x < 2.0f * L) return __fsub_rn(x, L);
+  } else if (x >= 0.0f || x != x) {
+    return x;
+  } else if (x > -L) {
+    return __fadd_rn(x, L);
+  }
+  float t = fmodf(x, L);
+  if (t != 0.0f && t < 0.0f) t = __fadd_rn(t, L);
+  return t;
+}
+
+// periodic_displacement (jax_md/space.py:170-181), component-wise, no FMA.
+__device__ __forceinline__ float pdisp(float d, float L, float half) {
+  return __fsub_rn(jmod(__fadd_rn(d, half), L), half);
+}
+
+template <int DIM>
+__device__ __forceinline__ float3 pdisp3(const float4& a, const float4& b, const CaseDev& c) {
+  float3 r;
+  r.x = pdisp(__fsub_rn(a.x, b.x), c.box[0], c.half[0]);
+  r.y = pdisp(__fsub_rn(a.y, b.y), c.box[1], c.half[1]);
+  r.z = (DIM == 3) ? pdisp(__fsub_rn(a.z, b.z), c.box[2], c.half[2]) : 0.0f;
+  return r;
+}
+
+// square_distance summed left to right without contraction (space.py:184-192).
+template <int DIM>
+__device__ __forceinline__ float sqd(const float3& d) {
+  float s = __fadd_rn(__fmul_rn(d.x, d.x), __fmul_rn(d.y, d.y));
+  if (DIM == 3) s = __fadd_rn(s, __fmul_rn(d.z, d.z));
+  return s;
+}
+
+// Neighbour-list membership of edge (receiver a, sender b): the reference
+// prunes with metric(r[sender], r[receiver]) < cutoff_sq (partition.py:897).
+template <int DIM>
+__device__ __forceinline__ bool is_edge(const float4& recv, const float4& send, const CaseDev& c) {
+  return sqd<DIM>(pdisp3<DIM>(send, recv, c)) < c.cutoff_sq;
+}
+
+// Kernel value and radial derivative (kernel.py:51-103). KER 0 = quintic, 1 = Wendland C2.
+template <int KER>
+__device__ __forceinline__ float kw(float r, const CaseDev& c) {
+  float q = r * c.inv_h;
+  if (KER == 0) {
+    float q1 = fmaxf(0.0f, 1.0f - q), q2 = fmaxf(0.0f, 2.0f - q), q3 = fmaxf(0.0f, 3.0f - q);
+    float a = q3 * q3, b = q2 * q2, d = q1 * q1;
+    return c.sigma * (a * a * q3 - 6.0f * (b * b * q2) + 15.0f * (d * d * q1));
+  } else {
+    float q1 = fmaxf(0.0f, 1.0f - 0.5f * q);
+    float a = q1 * q1;
+    return c.sigma * (a * a * (2.0f * q + 1.0f));
+  }
+}
+
+template <int KER>
+__device__ __forceinline__ float kdw(float r, const CaseDev& c) {
+  float q = r * c.inv_h;
+  if (KER == 0) {
+    float q1 = fmaxf(0.0f, 1.0f - q), q2 = fmaxf(0.0f, 2.0f - q), q3 = fmaxf(0.0f, 3.0f - q);
+    float a = q3 * q3, b = q2 * q2, d = q1 * q1;
+    return c.dsigma * (a * a - 6.0f * (b * b) + 15.0f * (d * d));
+  } else {
+    float q1 = fmaxf(0.0f, 1.0f - 0.5f * q);
+    return c.dsigma * (q * (q1 * q1 * q1));
+  }
+}
+
+// Equations of state (eos.py:20-57).
+__device__ __forceinline__ float eos_p(float rho, const CaseDev& c) {
+  if (c.eos == SPH_EOS_TAIT) {
+    float x = rho / c.rho_ref;
+    if (c.gamma != 1.0f) x = powf(x, c.gamma);
+    return c.p_ref * (x - 1.0f) + c.p_bg;
+  }
+  return c.rie_k * (rho - c.rho_ref) + c.p_bg;
+}
+
+__device__ __forceinline__ float eos_rho(float p, const CaseDev& c) {
+  if (c.eos == SPH_EOS_TAIT) {
+    float x = (p + c.p_ref - c.p_bg) / c.p_ref;
+    if (c.gamma != 1.0f) x = powf(x, c.inv_gamma);
+    return c.rho_ref * x;
+  }
+  return (p - c.p_bg) / c.rie_k + c.rho_ref;
+}
+
+// External acceleration g_ext_fn(r) of the case (cases/*.py).
+template <int DIM>
+__device__ __forceinline__ float3 g_ext(const CaseDev& c, const float4& r, const float* garr,
+                                        int orig) {
+  float3 g = make_float3(0.f, 0.f, 0.f);
+  if (c.g_kind == SPH_GEXT_CONST) {
+    g = make_float3(c.g[0], c.g[1], c.g[2]);
+  } else if (c.g_kind == SPH_GEXT_BAND_X) {
+    if (r.y < c.g_hi && r.y > c.g_lo) g.x = c.g[0];
+  } else if (c.g_kind == SPH_GEXT_ARRAY && garr) {
+    g.x = garr[(size_t)orig * DIM + 0];
+    g.y = garr[(size_t)orig * DIM + 1];
+    if (DIM == 3) g.z = garr[(size_t)orig * DIM + 2];
+  }
+  return g;
+}
+
+// bc_fn on a velocity-like vector (u or v) of a particle with `tag`.
+__device__ __forceinline__ float3 bc_vel(float3 u, int tag, const CaseDev& c) {
+  if (c.bc_kind == SPH_BC_SOLID_ZERO || c.bc_kind == SPH_BC_SOLID_ZERO_P) {
+    if (tag == SOLID_WALL) u = make_float3(0.f, 0.f, 0.f);
+  } else if (c.bc_kind == SPH_BC_LID) {
+    if (tag == SOLID_WALL) u = make_float3(0.f, 0.f, 0.f);
+    if (tag == MOVING_WALL) u = make_float3(c.u_lid[0], c.u_lid[1], c.u_lid[2]);
+  }
+  return u;
+}
+// bc_fn on an acceleration (dudt or dvdt).
+__device__ __forceinline__ float3 bc_acc(float3 a, int tag, const CaseDev& c) {
+  if (c.bc_kind == SPH_BC_SOLID_ZERO || c.bc_kind == SPH_BC_SOLID_ZERO_P) {
+    if (tag == SOLID_WALL) a = make_float3(0.f, 0.f, 0.f);
+  } else if (c.bc_kind == SPH_BC_LID) {
+    if (tag == SOLID_WALL || tag == MOVING_WALL) a = make_float3(0.f, 0.f, 0.f);
+  }
+  return a;
+}
+__device__ __forceinline__ float bc_p(float p, int tag, const CaseDev& c) {
+  return (c.bc_kind == SPH_BC_SOLID_ZERO_P && tag == SOLID_WALL) ? 0.0f : p;
+}
+
+// Visit every particle of the 3^d periodic neighbour cells of `cell_local`
+// (the candidate set of jax_md/partition.py:832-856, as a set). Cells along x
+// are contiguous in the sorted order, so each (y, z) row is one or two ranges.
+template <int DIM, typename F>
+__device__ __forceinline__ void for_each_candidate(const CaseDev& c, int cell_local,
+                                                   const int* __restrict__ start, F&& f) {
+  const int nx = c.nc[0], ny = c.nc[1], nz = (DIM == 3) ? c.nc[2] : 1;
+  const int cx = cell_local % nx;
+  const int t = cell_local / nx;
+  const int cy = t % ny;
+  const int cz = (DIM == 3) ? t / ny : 0;
+  const int* cs = start + c.cell_off;
+  const int zr = (DIM == 3 && nz >= 3) ? 1 : 0;
+  const int yr = (ny >= 3) ? 1 : 0;
+  for (int dz = -zr; dz <= zr; ++dz) {
+    int zz = cz + dz;
+    zz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
+    for (int dy = -yr; dy <= yr; ++dy) {
+      int yy = cy + dy;
+      yy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
+      const int row = (zz * ny + yy) * nx;
+      int a0, b0, a1 = 0, b1 = -1;  // inclusive cell ranges
+      if (nx >= 3) {
+        if (cx == 0) {
+          a0 = row; b0 = row + 1; a1 = row + nx - 1; b1 = row + nx - 1;
+        } else if (cx == nx - 1) {
+          a0 = row + nx - 2; b0 = row + nx - 1; a1 = row; b1 = row;
+        } else {
+          a0 = row + cx - 1; b0 = row + cx + 1;
+        }
+      } else {
+        a0 = row; b0 = row + nx - 1;
+      }
+      const int e0 = cs[b0 + 1];
+      for (int j = cs[a0]; j < e0; ++j) f(j);
+      if (b1 >= a1) {
+        const int e1 = cs[b1 + 1];
+        for (int j = cs[a1]; j < e1; ++j) f(j);
+      }
+    }
+  }
+}
+
+// Compensated accumulation (Kahan) selected at compile time.
+template <bool KAHAN>
+struct Acc {
+  float s = 0.f, c = 0.f;
+  __device__ __forceinline__ void add(float x) {
+    if (KAHAN) {
+      float y = x - c;
+      float t = s + y;
+      c = (t - s) - y;
+      s = t;
+    } else {
+      s += x;
+    }
+  }
+};
+
+// ------------------------------------------------------------------ launchers
+struct Workspace;  // defined in sph_capi.cu
+
+struct LaunchCtx {
+  cudaStream_t stream;
+  int dim, kernel, solver;
+  int rho_evol, bc_trick, free_slip, mask_self, kahan;
+  long long N;
+  int n_cases;
+  const CaseDev* cases;   // device
+  unsigned* status;       // device
+  int* launches;          // optional host counter of kernel launches
+  cudaEvent_t* ev;        // optional phase events: bin start, bin end, density end,
+                          // wall end, force end
+};
+
+inline void count_launch(const LaunchCtx& L, int k = 1) {
+  if (L.launches) *L.launches += k;
+}
+inline void mark(const LaunchCtx& L, int i) {
+  if (L.ev) cudaEventRecord(L.ev[i], L.stream);
+}
+
+// sph_sort.cu
+void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out, const long long* case_off_dev);
+void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateView& s,
+                   bool from_forward, bool apply_bc);
+void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,
+                int* count, int* start, int* keyc, int* keys, int* tsrc, int* tkey, int* tcell,
+                int* scan_tmp, long long total_cells, bool drift, bool from_forward,
+                bool apply_bc);
+int launch_scan(cudaStream_t st, const int* in, int* out, long long n, int* tmp);
+void launch_edges(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
+                  int* rowcnt, int* rowoff, int* scan_tmp, int32_t* idx, long long capacity,
+                  long long* count_dev);
+void launch_row_counts(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
+                       int* rowcnt);
+void launch_diagnostics(const LaunchCtx& L, Buffers b, const float4* R4, bool from_forward,
+                        bool apply_bc, double* out);
+
+// sph_forward.cu
+void launch_forward(const LaunchCtx& L, Buffers b, const float4* R4, float4* R4w, float4* UT4,
+                    const int* cellid, const int* start, unsigned long long* edgecnt,
+                    const float* g_arr, bool apply_bc, bool has_walls);
+
+size_t scan_tmp_ints(long long n);
+
+}  // namespace sph

@@ -1,0 +1,509 @@
+// Cell binning (counting sort by cell hash, stable by original index), state
+// permutation with the fused si_euler kick-drift, exclusive scans, the sparse
+// edge-list emitter and the float64 diagnostics.
+//
+// The sorted order equals the reference's `argsort(hashes)` (a stable sort of
+// the original order, jax_md/partition.py:377): inside each cell particles are
+// ranked by original index, so the result does not depend on atomic order.
+#include "sph_internal.cuh"
+
+namespace sph {
+
+namespace {
+
+constexpr int kBlock = 256;
+constexpr unsigned kFull = 0xffffffffu;
+
+inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
+
+__device__ __forceinline__ float4 ld4(const float* p, int dim, long long i) {
+  float4 r;
+  r.x = p[i * dim];
+  r.y = p[i * dim + 1];
+  r.z = dim == 3 ? p[i * dim + 2] : 0.0f;
+  r.w = 0.0f;
+  return r;
+}
+__device__ __forceinline__ void st3(float* p, int dim, long long i, float x, float y, float z) {
+  p[i * dim] = x;
+  p[i * dim + 1] = y;
+  if (dim == 3) p[i * dim + 2] = z;
+}
+
+// ------------------------------------------------------------------ pack / unpack
+__global__ void k_pack(SphStateView s, int dim, Buffers o, const long long* case_off, int n_cases,
+                       unsigned* status) {
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= s.n) return;
+  int c = 0;
+  while (c + 1 < n_cases && i >= case_off[c + 1]) ++c;
+  int tag = s.tag[i];
+  if (tag < 0 || tag > 3) atomicOr(status, SPH_ERR_INVALID_ARG);
+  float4 r = ld4(s.r, dim, i);
+  r.w = s.mass[i];
+  float4 u = ld4(s.u, dim, i);
+  u.w = s.rho[i];
+  float4 v = ld4(s.v, dim, i);
+  v.w = s.p[i];
+  float4 a = ld4(s.dudt, dim, i);
+  a.w = s.drhodt ? s.drhodt[i] : 0.0f;
+  float4 b = ld4(s.dvdt, dim, i);
+  o.P4[i] = r;
+  o.U4[i] = u;
+  o.V4[i] = v;
+  o.A4[i] = a;
+  o.A2[i] = b;
+  o.ETA[i] = s.eta[i];
+  o.META[i] = (c << kTagBits) | (tag & kTagMask);
+  o.ORIG[i] = (int)i;
+  if (o.NW4) o.NW4[i] = s.nw ? ld4(s.nw, dim, i) : make_float4(0.f, 0.f, 0.f, 0.f);
+}
+
+// The state a step or forward left behind: density/pressure from the density
+// pass (R4) when the buffers hold a forward result, bc_fn when a step ran.
+struct Final {
+  float3 u, v;
+  float rho, p;
+};
+__device__ __forceinline__ Final finalize(const Buffers& b, const float4* R4, long long q,
+                                          const CaseDev& c, int tag, bool from_forward,
+                                          bool apply_bc) {
+  float4 U = b.U4[q], V = b.V4[q];
+  Final f;
+  f.u = make_float3(U.x, U.y, U.z);
+  f.v = make_float3(V.x, V.y, V.z);
+  if (from_forward) {
+    float4 R = R4[q];
+    f.rho = R.x;
+    f.p = R.y;
+  } else {
+    f.rho = U.w;
+    f.p = V.w;
+  }
+  if (apply_bc) {
+    f.u = bc_vel(f.u, tag, c);
+    f.v = bc_vel(f.v, tag, c);
+    f.p = bc_p(f.p, tag, c);
+  }
+  return f;
+}
+
+__global__ void k_unpack(SphStateView s, int dim, Buffers b, const float4* R4,
+                         const CaseDev* cases, bool from_forward, bool apply_bc) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= s.n) return;
+  int meta = b.META[q];
+  const CaseDev& c = cases[case_of(meta)];
+  int tag = tag_of(meta);
+  long long o = b.ORIG[q];
+  Final f = finalize(b, R4, q, c, tag, from_forward, apply_bc);
+  float4 r = b.P4[q], a = b.A4[q], a2 = b.A2[q];
+  st3(s.r, dim, o, r.x, r.y, r.z);
+  st3(s.u, dim, o, f.u.x, f.u.y, f.u.z);
+  st3(s.v, dim, o, f.v.x, f.v.y, f.v.z);
+  st3(s.dudt, dim, o, a.x, a.y, a.z);
+  st3(s.dvdt, dim, o, a2.x, a2.y, a2.z);
+  if (s.drhodt) s.drhodt[o] = a.w;
+  s.rho[o] = f.rho;
+  s.p[o] = f.p;
+}
+
+// ------------------------------------------------------------------ binning
+// si_euler kick-drift (integrator.py:26-30) in float32, one rounding per op.
+template <int DIM>
+__device__ __forceinline__ void kick_drift(float4& r, float3& u, float3& v, const float4& dudt,
+                                           const float4& dvdt, const CaseDev& c) {
+  u.x = __fadd_rn(u.x, __fmul_rn(c.dt, dudt.x));
+  u.y = __fadd_rn(u.y, __fmul_rn(c.dt, dudt.y));
+  v.x = __fadd_rn(u.x, __fmul_rn(c.cv, dvdt.x));
+  v.y = __fadd_rn(u.y, __fmul_rn(c.cv, dvdt.y));
+  r.x = jmod(__fadd_rn(r.x, __fmul_rn(c.dt, v.x)), c.box[0]);
+  r.y = jmod(__fadd_rn(r.y, __fmul_rn(c.dt, v.y)), c.box[1]);
+  if (DIM == 3) {
+    u.z = __fadd_rn(u.z, __fmul_rn(c.dt, dudt.z));
+    v.z = __fadd_rn(u.z, __fmul_rn(c.cv, dvdt.z));
+    r.z = jmod(__fadd_rn(r.z, __fmul_rn(c.dt, v.z)), c.box[2]);
+  }
+}
+
+// Cell of a position: hash = sum(int32(r / cell_size) * mult)
+// (jax_md/partition.py:367-368), axes with a single cell contribute 0.
+template <int DIM>
+__device__ __forceinline__ int cell_hash(const float4& r, const CaseDev& c, unsigned* status) {
+  float rr[3] = {r.x, r.y, r.z};
+  int h = 0;
+  bool finite = true;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    finite &= isfinite(rr[d]);
+    int ix = c.nc[d] > 1 ? __float2int_rz(__fdiv_rn(rr[d], c.cell_size[d])) : 0;
+    h += ix * c.mult[d];
+  }
+  if (!finite) {
+    atomicOr(status, SPH_ERR_NONFINITE);
+    h = 0;
+  } else if (h < 0 || h >= c.ncell) {
+    atomicOr(status, SPH_WARN_BOX_EDGE);
+    h = h < 0 ? 0 : c.ncell - 1;
+  }
+  return h;
+}
+
+template <int DIM>
+__global__ void k_hash_count(long long N, Buffers in, const float4* R4, const CaseDev* cases,
+                             int* count, int* keyc, int* keys, unsigned* status, bool drift,
+                             bool from_forward, bool apply_bc) {
+  long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool valid = k < N;
+  int cell = 0;
+  if (valid) {
+    int meta = in.META[k];
+    const CaseDev& c = cases[case_of(meta)];
+    float4 r = in.P4[k];
+    if (drift) {
+      Final f = finalize(in, R4, k, c, tag_of(meta), from_forward, apply_bc);
+      float3 u = f.u, v;
+      kick_drift<DIM>(r, u, v, in.A4[k], in.A2[k], c);
+    }
+    cell = c.cell_off + cell_hash<DIM>(r, c, status);
+  }
+  unsigned mask = __ballot_sync(kFull, valid);
+  if (!valid) return;
+  // warp-aggregated slot reservation: lanes of one cell share one atomic
+  unsigned peers = __match_any_sync(mask, cell);
+  int lane = threadIdx.x & 31;
+  int leader = __ffs(peers) - 1;
+  int rank = __popc(peers & ((1u << lane) - 1u));
+  int base = 0;
+  if (lane == leader) base = atomicAdd(&count[cell], __popc(peers));
+  base = __shfl_sync(peers, base, leader);
+  keyc[k] = cell;
+  keys[k] = base + rank;
+}
+
+__global__ void k_scatter(long long N, const int* keyc, const int* keys, const int* start,
+                          const int* orig, int* tsrc, int* tkey, int* tcell) {
+  long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  int cell = keyc[k];
+  int q = start[cell] + keys[k];
+  tsrc[q] = (int)k;
+  tkey[q] = orig[k];
+  tcell[q] = cell;
+}
+
+template <int DIM>
+__global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4,
+                          const CaseDev* cases, const int* start, const int* tsrc,
+                          const int* tkey, const int* tcell, int* cellid, unsigned* status,
+                          bool drift, bool from_forward, bool apply_bc) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool over = false;
+  if (q < N) {
+    int cell = tcell[q];
+    int a = start[cell], e = start[cell + 1];
+    int key = tkey[q];
+    int rank = 0;
+    for (int t = a; t < e; ++t) rank += (tkey[t] < key);
+    int dest = a + rank;
+    int src = tsrc[q];
+    int meta = in.META[src];
+    const CaseDev& c = cases[case_of(meta)];
+    int tag = tag_of(meta);
+    Final f = finalize(in, R4, src, c, tag, from_forward, apply_bc);
+    float4 r = in.P4[src];
+    float4 A = in.A4[src], B = in.A2[src];
+    float3 u = f.u, v = f.v;
+    if (drift) kick_drift<DIM>(r, u, v, A, B, c);
+    out.P4[dest] = r;
+    out.U4[dest] = make_float4(u.x, u.y, u.z, f.rho);
+    out.V4[dest] = make_float4(v.x, v.y, v.z, f.p);
+    out.A4[dest] = A;
+    out.A2[dest] = B;
+    out.ETA[dest] = in.ETA[src];
+    out.META[dest] = meta;
+    out.ORIG[dest] = key;
+    if (out.NW4) out.NW4[dest] = in.NW4[src];
+    cellid[dest] = cell;
+    over = c.use_cells && (e - a) > c.cell_cap;
+  }
+  if (__any_sync(kFull, over) && (threadIdx.x & 31) == 0) atomicOr(status, SPH_CELL_LIST_OVERFLOW);
+}
+
+// ------------------------------------------------------------------ scan
+constexpr int kScanThreads = 1024;
+constexpr int kScanItems = 4;
+constexpr int kTile = kScanThreads * kScanItems;
+
+// Block-wide exclusive scan of kTile ints; returns the tile total.
+__device__ int block_scan_tile(int* v /*[kScanItems]*/, int* smem /*[32]*/) {
+  int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int local = 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) {
+    int t = v[i];
+    v[i] = local;
+    local += t;
+  }
+  int x = local;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int y = __shfl_up_sync(kFull, x, o);
+    if (lane >= o) x += y;
+  }
+  if (lane == 31) smem[warp] = x;
+  __syncthreads();
+  if (warp == 0) {
+    int w = smem[lane];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      int y = __shfl_up_sync(kFull, w, o);
+      if (lane >= o) w += y;
+    }
+    smem[lane] = w;
+  }
+  __syncthreads();
+  int warp_excl = warp > 0 ? smem[warp - 1] : 0;
+  int total = smem[31];
+  int excl = warp_excl + x - local;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) v[i] += excl;
+  __syncthreads();
+  return total;
+}
+
+__global__ void k_tile_sums(const int* in, long long n, int* sums) {
+  __shared__ int smem[32];
+  long long base = blockIdx.x * (long long)kTile + threadIdx.x * kScanItems;
+  int v[kScanItems];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? in[base + i] : 0;
+  int total = block_scan_tile(v, smem);
+  if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+// Exclusive scan of `n` ints with an optional per-tile offset array;
+// out[n] receives the grand total when this block owns the last tile.
+__global__ void k_tile_scan(const int* in, long long n, int* out, const int* tile_off) {
+  __shared__ int smem[32];
+  long long base = blockIdx.x * (long long)kTile + threadIdx.x * kScanItems;
+  int v[kScanItems];
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? in[base + i] : 0;
+  int total = block_scan_tile(v, smem);
+  int off = tile_off ? tile_off[blockIdx.x] : 0;
+#pragma unroll
+  for (int i = 0; i < kScanItems; ++i)
+    if (base + i < n) out[base + i] = v[i] + off;
+  if (blockIdx.x == gridDim.x - 1 && threadIdx.x == 0) out[n] = off + total;
+}
+
+// ------------------------------------------------------------------ edges
+// Per-sender edge count: edge (receiver c, sender s) iff
+// metric(r[s], r[c]) < cutoff_sq (jax_md/partition.py:885-909).
+template <int DIM>
+__global__ void k_row_counts(long long N, Buffers b, const CaseDev* cases, const int* cellid,
+                             const int* start, int mask_self, int* rowcnt) {
+  long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  int meta = b.META[s];
+  const CaseDev& c = cases[case_of(meta)];
+  float4 rs = b.P4[s];
+  int cnt = 0;
+  for_each_candidate<DIM>(c, cellid[s] - c.cell_off, start, [&](int j) {
+    if (mask_self && j == s) return;
+    float4 rc = b.P4[j];
+    cnt += is_edge<DIM>(rc, rs, c);
+  });
+  rowcnt[b.ORIG[s]] = cnt;
+}
+
+template <int DIM>
+__global__ void k_emit(long long N, Buffers b, const CaseDev* cases, const int* cellid,
+                       const int* start, int mask_self, const int* rowoff, int32_t* idx,
+                       long long capacity) {
+  long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (s >= N) return;
+  int meta = b.META[s];
+  const CaseDev& c = cases[case_of(meta)];
+  float4 rs = b.P4[s];
+  int sender = b.ORIG[s];
+  long long off = rowoff[sender];
+  long long k = off;
+  for_each_candidate<DIM>(c, cellid[s] - c.cell_off, start, [&](int j) {
+    if (mask_self && j == s) return;
+    float4 rc = b.P4[j];
+    if (is_edge<DIM>(rc, rs, c)) {
+      if (k < capacity) {
+        idx[k] = b.ORIG[j];
+        idx[capacity + k] = sender;
+      }
+      ++k;
+    }
+  });
+  // receivers ascending per sender (insertion sort of the owned segment)
+  long long end = k < capacity ? k : capacity;
+  for (long long x = off + 1; x < end; ++x) {
+    int key = idx[x];
+    long long y = x - 1;
+    while (y >= off && idx[y] > key) {
+      idx[y + 1] = idx[y];
+      --y;
+    }
+    idx[y + 1] = key;
+  }
+}
+
+__global__ void k_pad_edges(int32_t* idx, long long capacity, const int* total_ptr, int n,
+                            long long* count_dev, unsigned* status) {
+  long long total = *total_ptr;
+  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i == 0) {
+    *count_dev = total;
+    if (total > capacity) atomicOr(status, SPH_NEIGHBOR_LIST_OVERFLOW);
+  }
+  for (long long k = total + i; k < capacity; k += (long long)gridDim.x * blockDim.x) {
+    idx[k] = n;
+    idx[capacity + k] = n;
+  }
+}
+
+// ------------------------------------------------------------------ diagnostics
+__device__ __forceinline__ void atomic_max_pos(double* a, double v) {
+  atomicMax((unsigned long long*)a, (unsigned long long)__double_as_longlong(v));
+}
+__device__ __forceinline__ void atomic_min_pos(double* a, double v) {
+  atomicMin((unsigned long long*)a, (unsigned long long)__double_as_longlong(v));
+}
+
+__global__ void k_diag_init(double* out, int n_cases) {
+  int i = threadIdx.x + blockIdx.x * blockDim.x;
+  if (i < n_cases * 8) {
+    int k = i % 8;
+    out[i] = k == 6 ? 1.0e300 : 0.0;
+  }
+}
+
+template <int DIM>
+__global__ void k_diagnostics(long long N, Buffers b, const float4* R4, const CaseDev* cases,
+                              bool from_forward, bool apply_bc, double* out) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= N) return;
+  int meta = b.META[q];
+  int ci = case_of(meta);
+  const CaseDev& c = cases[ci];
+  int tag = tag_of(meta);
+  Final f = finalize(b, R4, q, c, tag, from_forward, apply_bc);
+  double* o = out + ci * 8;
+  double umag = sqrt((double)f.u.x * f.u.x + (double)f.u.y * f.u.y + (double)f.u.z * f.u.z);
+  atomic_max_pos(o + 5, umag);
+  if (tag != FLUID) return;
+  double m = b.P4[q].w;
+  atomicAdd(o + 0, m);
+  atomicAdd(o + 1, m * f.u.x);
+  atomicAdd(o + 2, m * f.u.y);
+  atomicAdd(o + 3, m * f.u.z);
+  // get_ekin (jax_sph/utils.py:128-133): 0.5 * sum(v^2) * dx^dim over fluid
+  double vol = DIM == 3 ? (double)c.av_hab * c.av_hab * c.av_hab : (double)c.av_hab * c.av_hab;
+  atomicAdd(o + 4, 0.5 * vol *
+                       ((double)f.v.x * f.v.x + (double)f.v.y * f.v.y + (double)f.v.z * f.v.z));
+  atomic_min_pos(o + 6, (double)f.rho);
+  atomic_max_pos(o + 7, (double)f.rho);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ launchers
+size_t scan_tmp_ints(long long n) { return (size_t)((n + kTile - 1) / kTile) * 4 + 256; }
+
+int launch_scan(cudaStream_t st, const int* in, int* out, long long n, int* tmp) {
+  long long tiles = (n + kTile - 1) / kTile;
+  if (tiles <= 1) {
+    k_tile_scan<<<1, kScanThreads, 0, st>>>(in, n, out, nullptr);
+    return 1;
+  }
+  int* sums = tmp;
+  int* offs = tmp + tiles + 1;
+  k_tile_sums<<<(int)tiles, kScanThreads, 0, st>>>(in, n, sums);
+  int k = launch_scan(st, sums, offs, tiles, tmp + 2 * tiles + 2);
+  k_tile_scan<<<(int)tiles, kScanThreads, 0, st>>>(in, n, out, offs);
+  return k + 2;
+}
+
+void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out,
+                 const long long* case_off_dev) {
+  k_pack<<<nblocks(L.N), kBlock, 0, L.stream>>>(s, L.dim, out, case_off_dev, L.n_cases, L.status);
+}
+
+void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateView& s,
+                   bool from_forward, bool apply_bc) {
+  k_unpack<<<nblocks(L.N), kBlock, 0, L.stream>>>(s, L.dim, in, R4, L.cases, from_forward,
+                                                   apply_bc);
+}
+
+void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,
+                int* count, int* start, int* keyc, int* keys, int* tsrc, int* tkey, int* tcell,
+                int* scan_tmp, long long total_cells, bool drift, bool from_forward,
+                bool apply_bc) {
+  mark(L, 0);
+  cudaMemsetAsync(count, 0, sizeof(int) * (total_cells + 1), L.stream);
+  int g = nblocks(L.N);
+  if (L.dim == 3)
+    k_hash_count<3><<<g, kBlock, 0, L.stream>>>(L.N, in, R4, L.cases, count, keyc, keys,
+                                                 L.status, drift, from_forward, apply_bc);
+  else
+    k_hash_count<2><<<g, kBlock, 0, L.stream>>>(L.N, in, R4, L.cases, count, keyc, keys,
+                                                 L.status, drift, from_forward, apply_bc);
+  count_launch(L, 3 + launch_scan(L.stream, count, start, total_cells, scan_tmp));
+  k_scatter<<<g, kBlock, 0, L.stream>>>(L.N, keyc, keys, start, in.ORIG, tsrc, tkey, tcell);
+  if (L.dim == 3)
+    k_permute<3><<<g, kBlock, 0, L.stream>>>(L.N, in, out, R4, L.cases, start, tsrc, tkey,
+                                              tcell, cellid, L.status, drift, from_forward,
+                                              apply_bc);
+  else
+    k_permute<2><<<g, kBlock, 0, L.stream>>>(L.N, in, out, R4, L.cases, start, tsrc, tkey,
+                                              tcell, cellid, L.status, drift, from_forward,
+                                              apply_bc);
+  mark(L, 1);
+}
+
+void launch_row_counts(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
+                       int* rowcnt) {
+  int g = nblocks(L.N);
+  if (L.dim == 3)
+    k_row_counts<3><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.mask_self,
+                                                 rowcnt);
+  else
+    k_row_counts<2><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.mask_self,
+                                                 rowcnt);
+}
+
+void launch_edges(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
+                  int* rowcnt, int* rowoff, int* scan_tmp, int32_t* idx, long long capacity,
+                  long long* count_dev) {
+  launch_row_counts(L, b, cellid, start, rowcnt);
+  launch_scan(L.stream, rowcnt, rowoff, L.N, scan_tmp);
+  int g = nblocks(L.N);
+  if (L.dim == 3)
+    k_emit<3><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.mask_self, rowoff,
+                                           idx, capacity);
+  else
+    k_emit<2><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.mask_self, rowoff,
+                                           idx, capacity);
+  k_pad_edges<<<304, kBlock, 0, L.stream>>>(idx, capacity, rowoff + L.N, (int)L.N, count_dev,
+                                            L.status);
+}
+
+void launch_diagnostics(const LaunchCtx& L, Buffers b, const float4* R4, bool from_forward,
+                        bool apply_bc, double* out) {
+  k_diag_init<<<nblocks(L.n_cases * 8), kBlock, 0, L.stream>>>(out, L.n_cases);
+  int g = nblocks(L.N);
+  if (L.dim == 3)
+    k_diagnostics<3><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, from_forward, apply_bc,
+                                                  out);
+  else
+    k_diagnostics<2><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, from_forward, apply_bc,
+                                                  out);
+}
+
+}  // namespace sph

@@ -1,0 +1,28 @@
+"""jaxsph_gb300: the jax-sph per-step hot path on GB300 (sm_103a).
+
+Drop-in modules with the reference's call signatures:
+
+* ``space.periodic``                 (jax_sph/jax_md/space.py)
+* ``partition.neighbor_list``        (jax_sph/partition.py)
+* ``solver.WCSPH``                   (jax_sph/solver.py)
+* ``integrator.si_euler``            (jax_sph/integrator.py)
+* ``eos.TaitEoS`` / ``eos.RIEMANNEoS`` and the QSK / WC2K ``kernel`` classes
+
+plus ``cases`` (initial states of TGV, dam break, lid-driven cavity,
+Poiseuille flow) and ``simulate`` (resident and batched GPU rollouts).
+All arithmetic runs in ``libsph_gb300.so`` (hand-written CUDA, C ABI in
+``include/sph_gb300.h``); there is no CPU path.
+"""
+
+from . import eos, kernel, space  # noqa: F401
+from ._build import build  # noqa: F401
+from ._lib import SphError, load  # noqa: F401
+
+
+def __getattr__(name):
+    # modules that need torch.cuda are imported lazily
+    import importlib
+
+    if name in ("partition", "solver", "integrator", "cases", "simulate"):
+        return importlib.import_module(f".{name}", __name__)
+    raise AttributeError(name)

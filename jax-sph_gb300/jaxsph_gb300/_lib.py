@@ -1,0 +1,233 @@
+"""ctypes binding of ``libsph_gb300.so`` and the ``Engine`` handle wrapper.
+
+This is the Python side of the C ABI in ``include/sph_gb300.h``. There is no
+fallback: if the shared library cannot be loaded, or no CUDA device is
+present, every call raises.
+"""
+
+import ctypes
+import os
+
+import torch
+
+from . import _build
+
+# status bits (include/sph_gb300.h)
+NEIGHBOR_LIST_OVERFLOW = 0x1
+CELL_LIST_OVERFLOW = 0x2
+CELL_SIZE_TOO_SMALL = 0x4
+MALFORMED_BOX = 0x8
+ERR_INVALID_ARG = 0x100
+ERR_CUDA = 0x200
+ERR_TIMEOUT = 0x400
+ERR_NONFINITE = 0x800
+WARN_BOX_EDGE = 0x1000
+
+KERNELS = {"QSK": 0, "WC2K": 1}
+SOLVERS = {"SPH": 0, "RIE": 1}
+EOS_TAIT, EOS_RIEMANN = 0, 1
+GEXT_ZERO, GEXT_CONST, GEXT_BAND_X, GEXT_ARRAY = 0, 1, 2, 3
+BC_NONE, BC_SOLID_ZERO, BC_SOLID_ZERO_P, BC_LID = 0, 1, 2, 3
+
+
+class SphConfig(ctypes.Structure):
+    _fields_ = [("dim", ctypes.c_int32), ("kernel", ctypes.c_int32), ("solver", ctypes.c_int32),
+                ("is_rho_evol", ctypes.c_int32), ("is_bc_trick", ctypes.c_int32),
+                ("is_free_slip", ctypes.c_int32), ("mask_self", ctypes.c_int32),
+                ("kahan", ctypes.c_int32), ("capacity_multiplier", ctypes.c_double)]
+
+
+class SphCase(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64), ("box", ctypes.c_double * 3), ("r_cutoff", ctypes.c_double),
+                ("dx", ctypes.c_double), ("h", ctypes.c_double), ("dt", ctypes.c_double),
+                ("dt_solver", ctypes.c_double), ("tvf", ctypes.c_double),
+                ("c_ref", ctypes.c_double), ("eos", ctypes.c_int32), ("g_kind", ctypes.c_int32),
+                ("bc_kind", ctypes.c_int32), ("pad0", ctypes.c_int32),
+                ("p_ref", ctypes.c_double), ("rho_ref", ctypes.c_double),
+                ("p_bg", ctypes.c_double), ("gamma", ctypes.c_double),
+                ("u_ref", ctypes.c_double), ("eta_limiter", ctypes.c_double),
+                ("artificial_alpha", ctypes.c_double), ("g", ctypes.c_double * 3),
+                ("g_band_lo", ctypes.c_double), ("g_band_hi", ctypes.c_double),
+                ("u_lid", ctypes.c_double * 3)]
+
+
+class SphStateView(ctypes.Structure):
+    _fields_ = [("n", ctypes.c_int64)] + [
+        (k, ctypes.c_void_p) for k in ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho",
+                                       "p", "mass", "eta", "nw", "g_ext")]
+
+
+class SphNLCapacity(ctypes.Structure):
+    _fields_ = [("cell_capacity", ctypes.c_int64), ("max_occupancy", ctypes.c_int64),
+                ("occupancy", ctypes.c_int64), ("max_cell_occupancy", ctypes.c_int64)]
+
+
+EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sph_update_cases",
+           "sph_set_state", "sph_get_state", "sph_nl_allocate", "sph_nl_set_capacity",
+           "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_step_launch_count",
+           "sph_profile_step", "sph_read_status", "sph_diagnostics"]
+
+_LIB = None
+
+
+def load(build_if_missing=True):
+    """Load (building if needed) the shared library and declare its signatures."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    path = _build.LIB_PATH
+    if not os.path.exists(path):
+        if not build_if_missing:
+            raise RuntimeError(f"{path} is missing; run the build first")
+        _build.build()
+    lib = ctypes.CDLL(path)
+    P, I, V = ctypes.POINTER, ctypes.c_int, ctypes.c_void_p
+    lib.sph_abi_version.restype = I
+    lib.sph_last_error.restype = ctypes.c_char_p
+    lib.sph_create.argtypes = [P(SphConfig), P(SphCase), ctypes.c_int32, P(V)]
+    lib.sph_destroy.argtypes = [V]
+    lib.sph_update_cases.argtypes = [V, P(SphCase), ctypes.c_int32]
+    lib.sph_set_state.argtypes = [V, P(SphStateView), V]
+    lib.sph_get_state.argtypes = [V, P(SphStateView), V]
+    lib.sph_nl_allocate.argtypes = [V, ctypes.c_int64, P(SphNLCapacity), V]
+    lib.sph_nl_set_capacity.argtypes = [V, P(SphNLCapacity)]
+    lib.sph_nl_update.argtypes = [V, V]
+    lib.sph_nl_edges.argtypes = [V, V, ctypes.c_int64, V, V]
+    lib.sph_forward.argtypes = [V, V]
+    lib.sph_step.argtypes = [V, ctypes.c_int32, V]
+    lib.sph_step_launch_count.argtypes = [V, P(ctypes.c_int32)]
+    lib.sph_profile_step.argtypes = [V, ctypes.c_int32, P(ctypes.c_float), V]
+    lib.sph_read_status.argtypes = [V, P(ctypes.c_uint32), ctypes.c_int32, V]
+    lib.sph_diagnostics.argtypes = [V, V, V]
+    for name in EXPORTS:
+        if name not in ("sph_abi_version", "sph_last_error"):
+            getattr(lib, name).restype = I
+    if lib.sph_abi_version() != 1:
+        raise RuntimeError("libsph_gb300 ABI version mismatch")
+    _LIB = lib
+    return lib
+
+
+class SphError(RuntimeError):
+    """A failing C-ABI call (the message comes from ``sph_last_error``)."""
+
+    def __init__(self, code, msg):
+        super().__init__(f"{msg} (status 0x{code:x})")
+        self.code = code
+
+
+def _check(rc):
+    if rc != 0:
+        raise SphError(rc, _LIB.sph_last_error().decode())
+
+
+def _stream():
+    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+
+
+def _ptr(t):
+    return ctypes.c_void_p(t.data_ptr()) if t is not None else None
+
+
+def require_cuda():
+    if not torch.cuda.is_available():
+        raise RuntimeError("jaxsph_gb300 needs a CUDA device (GB300, sm_103a); none is available")
+
+
+class Engine:
+    """Owner of one ``SphHandle``: a set of cases with one configuration."""
+
+    def __init__(self, config: SphConfig, cases):
+        require_cuda()
+        self.lib = load()
+        self.config = config
+        self.cases = list(cases)
+        self.n = sum(int(c.n) for c in self.cases)
+        arr = (SphCase * len(self.cases))(*self.cases)
+        h = ctypes.c_void_p()
+        _check(self.lib.sph_create(ctypes.byref(config), arr, len(self.cases), ctypes.byref(h)))
+        self.h = h
+        self._keep = None  # tensors referenced by the last SphStateView
+
+    def __del__(self):
+        h = getattr(self, "h", None)
+        if h is not None and h.value and _LIB is not None:
+            _LIB.sph_destroy(h)
+            self.h = None
+
+    def update_cases(self, cases):
+        cases = list(cases)
+        arr = (SphCase * len(cases))(*cases)
+        _check(self.lib.sph_update_cases(self.h, arr, len(cases)))
+        self.cases = cases
+
+    @staticmethod
+    def view(state, n):
+        """SphStateView over a dict of contiguous float32/int32 CUDA tensors."""
+        v = SphStateView()
+        v.n = n
+        for k in ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta",
+                  "nw", "g_ext"):
+            t = state.get(k)
+            if t is not None:
+                if not t.is_cuda or not t.is_contiguous():
+                    raise ValueError(f"state['{k}'] must be a contiguous CUDA tensor")
+                want = torch.int32 if k == "tag" else torch.float32
+                if t.dtype != want:
+                    raise ValueError(f"state['{k}'] must be {want}, got {t.dtype}")
+                setattr(v, k, t.data_ptr())
+        return v
+
+    def set_state(self, state):
+        v = self.view(state, self.n)
+        self._keep = state
+        _check(self.lib.sph_set_state(self.h, ctypes.byref(v), _stream()))
+
+    def get_state(self, out):
+        v = self.view(out, self.n)
+        _check(self.lib.sph_get_state(self.h, ctypes.byref(v), _stream()))
+
+    def nl_allocate(self, extra_capacity=0):
+        cap = SphNLCapacity()
+        _check(self.lib.sph_nl_allocate(self.h, int(extra_capacity), ctypes.byref(cap), _stream()))
+        return cap
+
+    def nl_set_capacity(self, cell_capacity, max_occupancy):
+        cap = SphNLCapacity(int(cell_capacity), int(max_occupancy), 0, 0)
+        _check(self.lib.sph_nl_set_capacity(self.h, ctypes.byref(cap)))
+
+    def nl_update(self):
+        _check(self.lib.sph_nl_update(self.h, _stream()))
+
+    def nl_edges(self, capacity, device):
+        idx = torch.empty((2, int(capacity)), dtype=torch.int32, device=device)
+        count = torch.zeros(1, dtype=torch.int64, device=device)
+        _check(self.lib.sph_nl_edges(self.h, _ptr(idx), int(capacity), _ptr(count), _stream()))
+        return idx, count
+
+    def forward(self):
+        _check(self.lib.sph_forward(self.h, _stream()))
+
+    def step(self, nsteps=1):
+        _check(self.lib.sph_step(self.h, int(nsteps), _stream()))
+
+    def launch_count(self):
+        c = ctypes.c_int32(0)
+        _check(self.lib.sph_step_launch_count(self.h, ctypes.byref(c)))
+        return int(c.value)
+
+    def profile(self, nsteps):
+        """Average per-step milliseconds of (binning, density, wall, force)."""
+        ms = (ctypes.c_float * 4)()
+        _check(self.lib.sph_profile_step(self.h, int(nsteps), ms, _stream()))
+        return [float(x) for x in ms]
+
+    def read_status(self, clear=False):
+        s = ctypes.c_uint32(0)
+        _check(self.lib.sph_read_status(self.h, ctypes.byref(s), int(bool(clear)), _stream()))
+        return int(s.value)
+
+    def diagnostics(self, device):
+        out = torch.empty((len(self.cases), 8), dtype=torch.float64, device=device)
+        _check(self.lib.sph_diagnostics(self.h, _ptr(out), _stream()))
+        return out

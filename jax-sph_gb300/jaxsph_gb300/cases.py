@@ -1,0 +1,302 @@
+"""Initial states of the four cases on the hot path (host-side, one-off).
+
+Restates ``SimulationSetup.initialize`` (``jax_sph/case_setup.py:44-231``)
+for Taylor-Green vortex (``cases/tgv.py``), dam break (``cases/db.py``),
+lid-driven cavity (``cases/ldc.py``) and Poiseuille flow (``cases/pf.py``)
+with their YAML defaults, so that synthetic inputs have exactly the
+reference's shapes, particle order (walls first, lattice ``meshgrid`` order)
+and float32 rounding. Each ``g_ext_fn``/``bc_fn`` is a callable that also
+carries a ``spec`` the GPU engine evaluates inside its kernels.
+"""
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from . import _lib
+from .eos import RIEMANNEoS, TaitEoS
+from .space import periodic
+
+EPS = 2.220446049250313e-16  # jnp.finfo(float).eps (case_setup.py:26)
+FLUID, SOLID_WALL, MOVING_WALL, DIRICHLET_WALL = 0, 1, 2, 3  # utils.py:22-29
+
+
+# ------------------------------------------------------------ lattices (utils.py:35-77)
+def _grid(box, dx, dtype):
+    n = np.array(np.round(np.asarray(box, dtype=np.float64) / dx), dtype=int)
+    grid = np.meshgrid(*[np.arange(k) for k in n], indexing="xy")
+    idx = np.vstack([g.ravel() for g in grid]).T
+    if dtype == np.float32:
+        return (idx.astype(np.float32) + np.float32(0.5)) * np.float32(dx)
+    return (idx.astype(np.float64) + 0.5) * dx
+
+
+def pos_init_cartesian_2d(box, dx, dtype=np.float32):
+    """Particles at cell centres of a Cartesian grid, x fastest (utils.py:35-45)."""
+    return _grid(box, dx, dtype)
+
+
+def pos_init_cartesian_3d(box, dx, dtype=np.float32):
+    """3D grid in ``meshgrid(..., indexing="xy")`` order (utils.py:48-53)."""
+    return _grid(box, dx, dtype)
+
+
+def _add(r, offset, dtype):
+    return (r + np.asarray(offset, dtype=np.float64).astype(dtype)).astype(dtype)
+
+
+def pos_box_2d(fluid_box, dx, n_walls=3, dtype=np.float32):
+    """Wall layers around a 2D box: left, bottom, right, top (utils.py:56-77)."""
+    dxn = n_walls * dx
+    vertical = pos_init_cartesian_2d(np.array([dxn, fluid_box[1] + 2 * dxn]), dx, dtype)
+    horiz = pos_init_cartesian_2d(np.array([fluid_box[0], dxn]), dx, dtype)
+    wall_l = vertical.copy()
+    wall_b = _add(horiz, [dxn, 0.0], dtype)
+    wall_r = _add(vertical, [fluid_box[0] + dxn, 0.0], dtype)
+    wall_t = _add(horiz, [dxn, fluid_box[1] + dxn], dtype)
+    return np.concatenate([wall_l, wall_b, wall_r, wall_t])
+
+
+# ------------------------------------------------------------ g_ext / bc descriptors
+class GExt:
+    """External acceleration ``g_ext_fn(r)`` with a GPU spec (kind, vector, band)."""
+
+    def __init__(self, kind, g=(0.0, 0.0, 0.0), band=(0.0, 0.0)):
+        self.spec = dict(kind=kind, g=tuple(float(x) for x in g), band=tuple(band))
+
+    def __call__(self, r):
+        res = torch.zeros_like(r)
+        k, g, (lo, hi) = self.spec["kind"], self.spec["g"], self.spec["band"]
+        if k == _lib.GEXT_CONST:
+            for d in range(r.shape[1]):
+                res[:, d] = g[d]
+        elif k == _lib.GEXT_BAND_X:
+            band = (r[:, 1] < hi) & (r[:, 1] > lo)
+            res[:, 0] = torch.where(band, torch.full_like(r[:, 0], g[0]), torch.zeros_like(r[:, 0]))
+        return res
+
+
+class BC:
+    """Boundary condition ``bc_fn(state)`` with a GPU spec (kind, lid velocity)."""
+
+    def __init__(self, kind, u_lid=(0.0, 0.0, 0.0)):
+        self.spec = dict(kind=kind, u_lid=tuple(float(x) for x in u_lid))
+
+    def __call__(self, state):
+        k = self.spec["kind"]
+        if k == _lib.BC_NONE:
+            return state
+        st = dict(state)
+        tag = st["tag"]
+        solid = (tag == SOLID_WALL)[:, None]
+        lid = (tag == MOVING_WALL)[:, None]
+        for key in ("u", "v"):
+            x = torch.where(solid, torch.zeros_like(st[key]), st[key])
+            if k == _lib.BC_LID:
+                ul = torch.as_tensor(self.spec["u_lid"][:x.shape[1]], dtype=x.dtype, device=x.device)
+                x = torch.where(lid, ul.expand_as(x), x)
+            st[key] = x
+        for key in ("dudt", "dvdt"):
+            m = solid | lid if k == _lib.BC_LID else solid
+            st[key] = torch.where(m, torch.zeros_like(st[key]), st[key])
+        if k == _lib.BC_SOLID_ZERO_P:
+            st["p"] = torch.where(solid[:, 0], torch.zeros_like(st["p"]), st["p"])
+        return st
+
+
+# ------------------------------------------------------------ setup container
+@dataclass
+class CaseSetup:
+    """Everything ``SimulationSetup.initialize`` returns, plus solver settings."""
+
+    name: str
+    dim: int
+    dx: float
+    box: np.ndarray
+    state: dict
+    dt: float
+    sequence_length: int
+    c_ref: float
+    p_ref: float
+    p_bg: float
+    u_ref: float
+    viscosity: float
+    eos: object
+    g_ext_fn: GExt
+    bc_fn: BC
+    solver: dict = field(default_factory=dict)  # WCSPH keyword arguments
+    tvf: float = 0.0
+
+    @property
+    def n(self):
+        return int(self.state["r"].shape[0])
+
+    def space(self):
+        return periodic(self.box)
+
+    def to(self, device):
+        st = {k: v.to(device) for k, v in self.state.items()}
+        return st
+
+
+def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref=1.0,
+            c_ref_factor=10.0, gamma=1.0, p_bg_factor=0.0, g_ext_magnitude=0.0, cfl=0.25,
+            dt=None, t_end=1.0, solver_name="SPH", kernel="QSK", h_fac=1.0, tvf=0.0,
+            is_bc_trick=False, density_evolution=False, artificial_alpha=0.0,
+            free_slip=False, eta_limiter=3, g_ext=None, bc=None, nw=None, dtype=np.float32):
+    """The common part of ``initialize`` (case_setup.py:71-231)."""
+    c_ref = c_ref_factor * u_ref
+    p_ref = rho_ref * c_ref ** 2 / gamma
+    p_bg = p_bg_factor * p_ref
+    h = dx
+    mass_ref = h ** dim * rho_ref
+    dt_convective = cfl * h / (c_ref + u_ref)
+    dt_viscous = cfl * h ** 2 * rho_ref / (viscosity + EPS)
+    dt_body_force = cfl * (h / (g_ext_magnitude + EPS)) ** 0.5
+    dt_cfl = float(np.amin([dt_convective, dt_viscous, dt_body_force]))
+    dt = dt_cfl if dt is None else dt
+    sequence_length = int(t_end / dt)
+    if solver_name == "RIE":
+        eos = RIEMANNEoS(rho_ref, p_bg, u_ref)
+    else:
+        eos = TaitEoS(p_ref, rho_ref, p_bg, gamma)
+    n = r.shape[0]
+    t = torch.float32 if dtype == np.float32 else torch.float64
+    rho = torch.full((n,), rho_ref, dtype=t)
+    state = {
+        "r": torch.as_tensor(r, dtype=t),
+        "tag": torch.as_tensor(tag, dtype=torch.int32),
+        "u": torch.as_tensor(v, dtype=t),
+        "v": torch.as_tensor(v, dtype=t),
+        "dudt": torch.zeros((n, dim), dtype=t),
+        "dvdt": torch.zeros((n, dim), dtype=t),
+        "drhodt": torch.zeros((n,), dtype=t),
+        "rho": rho,
+        "p": eos.p_fn(rho),
+        "mass": torch.full((n,), mass_ref, dtype=t),
+        "eta": torch.full((n,), viscosity, dtype=t),
+        "nw": torch.as_tensor(nw if nw is not None else np.zeros((n, dim)), dtype=t),
+    }
+    g_ext = g_ext or GExt(_lib.GEXT_ZERO)
+    bc = bc or BC(_lib.BC_NONE)
+    state = bc(state)  # case_setup.py:203
+    solver = dict(solver=solver_name, kernel=kernel, h_fac=h_fac, is_bc_trick=is_bc_trick,
+                  is_rho_evol=density_evolution, artificial_alpha=artificial_alpha,
+                  is_free_slip=free_slip, eta_limiter=eta_limiter)
+    return CaseSetup(name, dim, dx, np.asarray(box, dtype=np.float64), state, dt,
+                     sequence_length, c_ref, p_ref, p_bg, u_ref, viscosity, eos, g_ext, bc,
+                     solver, tvf)
+
+
+# ------------------------------------------------------------ cases
+def tgv(dim=2, dx=None, viscosity=None, solver_name="SPH", tvf=None, kernel=None,
+        dtype=np.float32, t_end=5.0, **kw):
+    """Taylor-Green vortex (cases/tgv.py, cases/tgv.yaml).
+
+    2D: unit box, u = -cos(2 pi x) sin(2 pi y), v = sin(2 pi x) cos(2 pi y).
+    3D: box (2 pi)^3, u = sin x cos y cos z, v = -cos x sin y cos z, w = 0.
+    """
+    if dim == 2:
+        dx = 0.02 if dx is None else dx
+        box = np.array([1.0, 1.0])
+        r = pos_init_cartesian_2d(box, dx, dtype)
+        x, y = r[:, 0].astype(np.float64), r[:, 1].astype(np.float64)
+        v = np.stack([-np.cos(2 * np.pi * x) * np.sin(2 * np.pi * y),
+                      np.sin(2 * np.pi * x) * np.cos(2 * np.pi * y)], 1)
+        viscosity = 0.01 if viscosity is None else viscosity
+        kernel = kernel or "QSK"
+        tvf = 0.0 if tvf is None else tvf
+    else:
+        box = 2 * np.pi * np.array([1.0, 1.0, 1.0])
+        dx = 2 * np.pi / 64 if dx is None else dx
+        r = pos_init_cartesian_3d(box, dx, dtype)
+        x, y, z = (r[:, k].astype(np.float64) for k in range(3))
+        v = np.stack([np.sin(x) * np.cos(y) * np.cos(z), -np.cos(x) * np.sin(y) * np.cos(z),
+                      np.zeros_like(x)], 1)
+        viscosity = 1.0 / 1600.0 if viscosity is None else viscosity
+        kernel = kernel or "WC2K"
+        tvf = 1.0 if tvf is None else tvf
+    tag = np.full(r.shape[0], FLUID)
+    return _finish(f"tgv{dim}d", dim, dx, box, r, tag, v, viscosity=viscosity,
+                   solver_name=solver_name, kernel=kernel, tvf=tvf, t_end=t_end, dtype=dtype,
+                   density_evolution=(solver_name == "RIE"), **kw)
+
+
+def _nws_scipy(r, tag, dx, n_walls, offset_vec, wall_part_fn, dtype):
+    """Wall normals by nearest point of a 5x finer wall layer (utils.py:169-194)."""
+    from scipy.spatial import KDTree
+
+    wall = np.isin(tag, [SOLID_WALL, MOVING_WALL, DIRICHLET_WALL])
+    r_aligned = r[wall].astype(np.float64) - offset_vec
+    layer = wall_part_fn(dx / 5, 1).astype(np.float64) - offset_vec / n_walls / 5
+    dist, match = KDTree(layer).query(r_aligned, k=1)
+    dr = layer[match] - r_aligned
+    nw = np.zeros(r.shape, dtype=np.float64)
+    nw[wall] = dr / (dist[:, None] + EPS)
+    return nw.astype(dtype)
+
+
+def dam_break(dx=0.005, n_walls=3, dtype=np.float32, t_end=12.0, dt=None, **kw):
+    """2D dam break with Riemann SPH (cases/db.py, cases/db.yaml).
+
+    Tank 5.366 x 2.0 with 3 wall layers, water column 2 x 1, box offset 0.1.
+    ``dt`` defaults to the CFL step (db.yaml's 3e-4 violates CFL at dx=0.005).
+    """
+    L_wall, H_wall, L, H, box_offset = 5.366, 2.0, 2.0, 1.0, 0.1
+    g = 1.0
+    u_ref = 1.4142135623730951
+    box = np.array([L_wall + 2 * n_walls * dx + box_offset, H_wall + 2 * n_walls * dx + box_offset])
+    r_f = (pos_init_cartesian_2d(np.array([L, H]), dx, dtype) + dtype(n_walls * dx)).astype(dtype)
+
+    def walls(ddx, nw_):
+        return pos_box_2d(np.array([L_wall, H_wall]), ddx, nw_, dtype)
+
+    r_w = walls(dx, n_walls)
+    r = np.concatenate([r_w, r_f])
+    tag = np.concatenate([np.full(len(r_w), SOLID_WALL), np.full(len(r_f), FLUID)])
+    offset_vec = np.ones(2) * n_walls * dx
+    nw = _nws_scipy(r, tag, dx, n_walls, offset_vec, walls, dtype)
+    v = np.zeros_like(r, dtype=np.float64)
+    return _finish("db", 2, dx, box, r, tag, v, viscosity=0.00005, u_ref=u_ref,
+                   g_ext_magnitude=g, solver_name="RIE", kernel="QSK", is_bc_trick=True,
+                   density_evolution=True, artificial_alpha=0.1, t_end=t_end, dt=dt,
+                   g_ext=GExt(_lib.GEXT_CONST, (0.0, -g, 0.0)), bc=BC(_lib.BC_SOLID_ZERO_P),
+                   nw=nw, dtype=dtype, **kw)
+
+
+def lid_driven_cavity(dx=0.02, n_walls=3, viscosity=0.01, u_lid=1.0, dtype=np.float32,
+                      t_end=5.0, dt=None, **kw):
+    """2D lid-driven cavity (cases/ldc.py, cases/ldc.yaml): SPH with the wall BC."""
+    box = np.ones(2) + 2 * n_walls * dx
+    r_f = (pos_init_cartesian_2d(np.ones(2), dx, dtype) + dtype(n_walls * dx)).astype(dtype)
+    r_w = pos_box_2d(np.ones(2), dx, n_walls, dtype)
+    r = np.concatenate([r_w, r_f])
+    tag = np.concatenate([np.full(len(r_w), SOLID_WALL), np.full(len(r_f), FLUID)])
+    tag = np.where(r[:, 1].astype(np.float64) > box[1] - n_walls * dx, MOVING_WALL, tag)
+    v = np.zeros_like(r, dtype=np.float64)
+    return _finish("ldc", 2, dx, box, r, tag, v, viscosity=viscosity, p_bg_factor=0.01,
+                   is_bc_trick=True, t_end=t_end, dt=dt,
+                   bc=BC(_lib.BC_LID, (u_lid, 0.0, 0.0)), dtype=dtype, **kw)
+
+
+def poiseuille(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, g_ext_magnitude=1000.0,
+               dtype=np.float32, t_end=0.01, dt=None, **kw):
+    """2D Poiseuille flow (cases/pf.py, cases/pf.yaml): channel L=0.4, H=1, body force."""
+    L, H = 0.4, 1.0
+    dxn = n_walls * dx
+    box = np.array([L, H + 2 * dxn])
+    r_f = _add(pos_init_cartesian_2d(np.array([L, H]), dx, dtype), [0.0, dxn], dtype)
+    horiz = pos_init_cartesian_2d(np.array([L, dxn]), dx, dtype)
+    r_w = np.concatenate([horiz, _add(horiz, [0.0, H + dxn], dtype)])
+    r = np.concatenate([r_w, r_f])
+    tag = np.concatenate([np.full(len(r_w), SOLID_WALL), np.full(len(r_f), FLUID)])
+    v = np.zeros_like(r, dtype=np.float64)
+    g = GExt(_lib.GEXT_BAND_X, (g_ext_magnitude, 0.0, 0.0), (dxn, box[1] - dxn))
+    return _finish("pf", 2, dx, box, r, tag, v, viscosity=viscosity, u_ref=u_ref,
+                   g_ext_magnitude=g_ext_magnitude, is_bc_trick=True, t_end=t_end, dt=dt,
+                   g_ext=g, bc=BC(_lib.BC_SOLID_ZERO), dtype=dtype, **kw)
+
+
+CASES = {"tgv": tgv, "db": dam_break, "ldc": lid_driven_cavity, "pf": poiseuille}

@@ -1,0 +1,198 @@
+"""WCSPH forward pass: drop-in for ``jax_sph.solver.WCSPH`` (solver.py:613-951).
+
+``WCSPH(...).forward_wrapper()`` returns ``forward(state, neighbors) -> state``
+with the reference's state-dict contract. The computation runs in
+``libsph_gb300`` (density pass, generalized wall BC pass, force pass; see
+``csrc/sph_forward.cu``) in float32 on the GPU. The branches on the hot path
+are the SPH and Riemann solvers with density summation or evolution, the
+generalized wall boundary condition (no-slip and free-slip), transport
+velocity and artificial viscosity, over the quintic and Wendland C2 kernels.
+"""
+
+import numpy as np
+import torch
+
+from . import _lib
+from .kernel import make_kernel
+
+STATE_KEYS = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
+_VEC = ("r", "u", "v", "dudt", "dvdt", "nw")
+
+
+def prepare_state(state, dim, device="cuda"):
+    """Contiguous float32 / int32 CUDA copies of the fields the kernels read."""
+    n = int(state["r"].shape[0])
+    out = {}
+    for k in STATE_KEYS:
+        x = state.get(k)
+        if x is None:
+            if k == "nw":
+                continue
+            if k == "drhodt":
+                x = torch.zeros(n)
+            else:
+                raise KeyError(f"state is missing '{k}'")
+        t = torch.as_tensor(x)
+        want = torch.int32 if k == "tag" else torch.float32
+        t = t.to(device=device, dtype=want).contiguous()
+        if k in _VEC and (t.ndim != 2 or t.shape[1] != dim):
+            raise ValueError(f"state['{k}'] must have shape (N, {dim})")
+        out[k] = t
+    return out
+
+
+def empty_outputs(st):
+    return {k: torch.empty_like(st[k]) for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")}
+
+
+class WCSPH:
+    """Weakly compressible SPH solver with transport velocity formulation."""
+
+    def __init__(self, displacement_fn, eos, g_ext_fn, dx, dim, dt, c_ref, eta_limiter=3,
+                 diff_delta=0.02, diff_alpha=0.1, solver="SPH", kernel="QSK", h_fac=1.0,
+                 is_bc_trick=False, is_rho_evol=False, artificial_alpha=0.0,
+                 is_free_slip=False, is_rho_renorm=False, is_heat_conduction=False,
+                 kahan=False):
+        if solver not in _lib.SOLVERS:
+            raise NotImplementedError(
+                f"solver {solver!r}: the GPU hot path implements SPH and RIE")
+        if is_rho_renorm or is_heat_conduction:
+            raise NotImplementedError("density renormalisation and heat conduction are not on the path")
+        self.displacement_fn = displacement_fn
+        self.eos = eos
+        self.g_ext_fn = g_ext_fn
+        self.dx, self.dim, self.dt, self.c_ref = float(dx), int(dim), float(dt), float(c_ref)
+        self.eta_limiter = float(eta_limiter)
+        self.solver = solver
+        self.kernel = kernel
+        self._kernel_fn = make_kernel(kernel, h_fac * dx, dim)
+        self.is_bc_trick = bool(is_bc_trick)
+        self.is_rho_evol = bool(is_rho_evol)
+        self.artificial_alpha = float(artificial_alpha)
+        self.is_free_slip = bool(is_free_slip)
+        self.kahan = bool(kahan)
+        self._engines = {}
+
+    # ---------------------------------------------------------------- engine
+    def solver_flags(self):
+        return dict(kernel=_lib.KERNELS[self.kernel], solver=_lib.SOLVERS[self.solver],
+                    is_rho_evol=self.is_rho_evol, is_bc_trick=self.is_bc_trick,
+                    is_free_slip=self.is_free_slip, kahan=self.kahan)
+
+    def g_spec(self):
+        spec = getattr(self.g_ext_fn, "spec", None)
+        if spec is None:
+            return dict(kind=_lib.GEXT_ARRAY, g=(0.0, 0.0, 0.0), band=(0.0, 0.0))
+        return spec
+
+    def sph_case(self, nl_fns, n, dt=0.0, tvf=0.0, bc=None):
+        s = nl_fns.case(n)
+        s.dx = self.dx
+        s.h = self._kernel_fn.h
+        s.dt = float(dt)
+        s.dt_solver = self.dt
+        s.tvf = float(tvf)
+        s.c_ref = self.c_ref
+        s.eos = self.eos.kind
+        s.p_ref = float(self.eos.p_ref)
+        s.rho_ref = float(self.eos.rho_ref)
+        s.p_bg = float(self.eos.p_bg)
+        s.gamma = float(self.eos.gamma)
+        s.u_ref = float(self.eos.u_ref)
+        s.eta_limiter = self.eta_limiter
+        s.artificial_alpha = self.artificial_alpha
+        g = self.g_spec()
+        s.g_kind = g["kind"]
+        for d in range(3):
+            s.g[d] = g["g"][d]
+        s.g_band_lo, s.g_band_hi = g["band"]
+        bc = bc or dict(kind=_lib.BC_NONE, u_lid=(0.0, 0.0, 0.0))
+        s.bc_kind = bc["kind"]
+        for d in range(3):
+            s.u_lid[d] = bc["u_lid"][d]
+        return s
+
+    def engine(self, nl_fns, case):
+        key = (id(nl_fns), int(case.n))
+        e = self._engines.get(key)
+        if e is None:
+            if abs(nl_fns.r_cutoff - self._kernel_fn.cutoff) > 1e-12 * max(1.0, nl_fns.r_cutoff):
+                raise ValueError("neighbour-list cutoff differs from the kernel cutoff")
+            e = _lib.Engine(nl_fns.config(**self.solver_flags()), [case])
+            self._engines = {key: e}
+        elif bytes(e.cases[0]) != bytes(case):
+            e.update_cases([case])
+        return e
+
+    def _load(self, state, neighbors, case):
+        nl_fns = neighbors._fns
+        st = prepare_state(state, self.dim)
+        if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
+            st["g_ext"] = torch.as_tensor(self.g_ext_fn(st["r"])).to(
+                device=st["r"].device, dtype=torch.float32).contiguous()
+        if (self.solver == "RIE" or self.is_free_slip) and "nw" not in st:
+            st["nw"] = torch.zeros_like(st["r"])
+        e = self.engine(nl_fns, case)
+        e.set_state(st)
+        cap = neighbors.cell_list_capacity
+        e.nl_set_capacity(cap if cap is not None else 2 ** 31 - 1, neighbors.max_occupancy)
+        return e, st
+
+    @staticmethod
+    def _result(state, st, out):
+        res = dict(state)
+        for k, v in out.items():
+            res[k] = v
+        for k in ("tag", "mass", "eta"):
+            res[k] = state[k]
+        res["r"] = st["r"]
+        return res
+
+    # ---------------------------------------------------------------- API
+    def forward_wrapper(self):
+        """``forward(state, neighbors) -> state`` (solver.py:702-951)."""
+
+        def forward(state, neighbors):
+            nl_fns = neighbors._fns
+            r = torch.as_tensor(state["r"])
+            ref = torch.as_tensor(neighbors.reference_position).to(r.device, r.dtype)
+            if nl_fns.dr_threshold == 0.0 and not torch.equal(r, ref):
+                raise NotImplementedError(
+                    "forward with a neighbour list built on other positions: update the list first")
+            case = self.sph_case(nl_fns, r.shape[0])
+            e, st = self._load(state, neighbors, case)
+            e.forward()
+            out = empty_outputs(st)
+            e.get_state(out)
+            return self._result(state, st, out)
+
+        forward.__wcsph__ = self
+        return forward
+
+    def advance(self, dt, tvf, state, neighbors, bc_fn):
+        """One fused si_euler step on the GPU (integrator.py:22-56)."""
+        nl_fns = neighbors._fns
+        bc_spec = getattr(bc_fn, "spec", None)
+        case = self.sph_case(nl_fns, int(state["r"].shape[0]), dt=dt, tvf=tvf, bc=bc_spec)
+        if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
+            raise NotImplementedError(
+                "si_euler needs a g_ext_fn with a GPU spec (e.g. jaxsph_gb300.cases.GExt)")
+        e, st = self._load(state, neighbors, case)
+        e.read_status(clear=True)
+        e.step(1)
+        out = empty_outputs(st)
+        e.get_state(out)
+        code = e.read_status(clear=True)
+        if code & (_lib.ERR_INVALID_ARG | _lib.ERR_CUDA):
+            raise _lib.SphError(code, "step failed")
+        res = self._result(state, st, out)
+        if bc_fn is not None and bc_spec is None:
+            res = bc_fn(res)
+        if nl_fns.moved(res["r"], neighbors):
+            from .partition import NeighborList
+
+            nbrs = NeighborList(nl_fns, res["r"], neighbors.error.code | (code & 0xFF),
+                                neighbors.cell_list_capacity, neighbors.max_occupancy)
+        else:
+            nbrs = neighbors
+        return res, nbrs

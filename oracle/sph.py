@@ -1,0 +1,410 @@
+"""WCSPH forward pass and si_euler step restated from jax-sph (test oracle only).
+
+Restates ``jax_sph/kernel.py`` (quintic and Wendland C2 kernels),
+``jax_sph/eos.py``, ``jax_sph/solver.py`` (``WCSPH.forward``, SPH and RIE
+solvers, generalized wall BC, transport velocity, artificial viscosity) and
+``jax_sph/integrator.py`` (``si_euler``) as gather/``index_add_`` programs over
+the sparse edge list, exactly like the jitted JAX program. Kernel gradients are
+taken by autograd of ``w`` as ``BaseKernel.grad_w`` does (kernel.py:20-23), so
+the whole step is differentiable with torch autograd (used as the gradient
+oracle for the hand-written adjoint).
+"""
+
+import math
+
+import torch
+
+from . import space
+
+# jnp.finfo(float).eps (solver.py:21): float64 machine epsilon, used in every dtype
+EPS = 2.220446049250313e-16
+
+FLUID, SOLID_WALL, MOVING_WALL, DIRICHLET_WALL = 0, 1, 2, 3  # utils.py:22-29
+
+
+def _is_wall(tag):
+    return (tag == SOLID_WALL) | (tag == MOVING_WALL) | (tag == DIRICHLET_WALL)
+
+
+# ---------------------------------------------------------------- kernels
+class QuinticKernel:
+    """Morris quintic spline (kernel.py:51-72), cutoff 3h."""
+
+    def __init__(self, h, dim):
+        self.one_over_h = 1.0 / h
+        self.cutoff = 3.0 * h
+        self.sigma = {1: 1.0 / 120.0 * self.one_over_h,
+                      2: 7.0 / 478.0 / math.pi * self.one_over_h ** 2,
+                      3: 3.0 / 359.0 / math.pi * self.one_over_h ** 3}[dim]
+
+    def w(self, r):
+        q = r * self.one_over_h
+        z = torch.zeros_like(q)
+        q1 = torch.maximum(z, 1.0 - q)
+        q2 = torch.maximum(z, 2.0 - q)
+        q3 = torch.maximum(z, 3.0 - q)
+        return self.sigma * (q3 ** 5 - 6.0 * q2 ** 5 + 15.0 * q1 ** 5)
+
+
+class WendlandC2Kernel:
+    """Wendland C2 (kernel.py:75-103), cutoff 2h."""
+
+    def __init__(self, h, dim):
+        self.one_over_h = 1.0 / h
+        self.dim = dim
+        self.cutoff = 2.0 * h
+        self.sigma = {1: 5.0 / 8.0 * self.one_over_h,
+                      2: 7.0 / 4.0 / math.pi * self.one_over_h ** 2,
+                      3: 21.0 / 16.0 / math.pi * self.one_over_h ** 3}[dim]
+
+    def w(self, r):
+        q = r * self.one_over_h
+        q1 = torch.maximum(torch.zeros_like(q), 1.0 - 0.5 * q)
+        if self.dim == 1:
+            return self.sigma * (q1 ** 3 * (1.5 * q + 1.0))
+        return self.sigma * (q1 ** 4 * (2.0 * q + 1.0))
+
+
+def make_kernel(name, h, dim):
+    if name == "QSK":
+        return QuinticKernel(h, dim)
+    if name == "WC2K":
+        return WendlandC2Kernel(h, dim)
+    raise NotImplementedError(f"kernel {name} is outside the hot-path scope")
+
+
+def grad_w(kernel, r):
+    """dW/dr by autograd of ``w`` (kernel.py:20-23); keeps the graph for adjoints."""
+    with torch.enable_grad():
+        rr = r if r.requires_grad else r.detach().requires_grad_(True)
+        w = kernel.w(rr)
+        (g,) = torch.autograd.grad(w.sum(), rr, create_graph=True)
+    return g
+
+
+# ---------------------------------------------------------------- EOS
+class TaitEoS:
+    """eos.py:20-38."""
+
+    def __init__(self, p_ref, rho_ref, p_background, gamma):
+        self.p_ref, self.rho_ref, self.p_bg, self.gamma = p_ref, rho_ref, p_background, gamma
+
+    def p_fn(self, rho):
+        return self.p_ref * ((rho / self.rho_ref) ** self.gamma - 1) + self.p_bg
+
+    def rho_fn(self, p):
+        p_temp = p + self.p_ref - self.p_bg
+        return self.rho_ref * (p_temp / self.p_ref) ** (1 / self.gamma)
+
+
+class RIEMANNEoS:
+    """eos.py:41-57."""
+
+    def __init__(self, rho_ref, p_background, u_ref):
+        self.rho_ref, self.p_bg, self.u_ref = rho_ref, p_background, u_ref
+
+    def p_fn(self, rho):
+        return 100 * self.u_ref ** 2 * (rho - self.rho_ref) + self.p_bg
+
+    def rho_fn(self, p):
+        return (p - self.p_bg) / (100 * self.u_ref ** 2) + self.rho_ref
+
+
+# ---------------------------------------------------------------- helpers
+def seg(x, i_s, N):
+    """``ops.segment_sum(x, i_s, N)``."""
+    out = torch.zeros((N,) + tuple(x.shape[1:]), dtype=x.dtype)
+    return out.index_add(0, i_s, x)
+
+
+def dot(a, b):
+    return (a * b).sum(-1)
+
+
+# ---------------------------------------------------------------- solver
+class WCSPH:
+    """``WCSPH`` (solver.py:613-951) for the SPH and RIE solvers.
+
+    ``g_ext_fn(r)`` returns the external acceleration per particle (torch).
+    """
+
+    def __init__(self, box, eos, g_ext_fn, dx, dim, dt, c_ref, eta_limiter=3,
+                 solver="SPH", kernel="QSK", h_fac=1.0, is_bc_trick=False,
+                 is_rho_evol=False, artificial_alpha=0.0, is_free_slip=False):
+        if solver not in ("SPH", "RIE"):
+            raise NotImplementedError(f"solver {solver} is outside the hot-path scope")
+        self.box = box
+        self.eos = eos
+        self.g_ext_fn = g_ext_fn
+        self.dx, self.dim, self.dt, self.c_ref = dx, dim, dt, c_ref
+        self.eta_limiter = eta_limiter
+        self.solver = solver
+        self.kernel = make_kernel(kernel, h_fac * dx, dim)
+        self.is_bc_trick = is_bc_trick
+        self.is_rho_evol = is_rho_evol
+        self.artificial_alpha = artificial_alpha
+        self.is_free_slip = is_free_slip
+
+    # limiter_fn_wrapper (solver.py:574-588)
+    def beta_fn(self, u_L, u_R):
+        if self.eta_limiter == -1:
+            return torch.full_like(u_L, self.c_ref)
+        temp = self.eta_limiter * torch.maximum(u_L - u_R, torch.zeros_like(u_L))
+        return torch.minimum(temp, torch.full_like(temp, self.c_ref))
+
+    def forward(self, state, idx):
+        """``forward(state, neighbors)`` (solver.py:705-949)."""
+        side = torch.as_tensor(self.box, dtype=state["r"].dtype)
+        r, tag, mass, eta = state["r"], state["tag"], state["mass"], state["eta"]
+        u, v = state["u"], state["v"]
+        rho, drhodt, p = state["rho"], state["drhodt"], state["p"]
+        nw = state["nw"]
+        N = r.shape[0]
+        dtype = r.dtype
+
+        # pad with one dummy particle so that padding edges (index N) gather
+        # something; their contributions are dropped by the segment sum.
+        valid = idx[0] < N
+        i_s, j_s = idx[0][valid], idx[1][valid]
+
+        dr_i_j = space.periodic_displacement(side, r[i_s] - r[j_s])     # :723-725
+        dist = space.distance(dr_i_j)                                     # :726
+        w_dist = self.kernel.w(dist)                                      # :727
+        e_s = dr_i_j / (dist[:, None] + EPS)                              # :729
+        gw = grad_w(self.kernel, dist)                                    # :731
+        grad_w_dist = gw[:, None] * e_s                                   # :732
+
+        g_ext = self.g_ext_fn(r)                                          # :735
+        wall_mask = torch.where(_is_wall(tag), 1.0, 0.0).to(dtype)        # :738
+        fluid_mask = torch.where(tag == FLUID, 1.0, 0.0).to(dtype)       # :739
+
+        # Riemann velocity BCs (:742-745, gwbc_fn_riemann_wrapper :533-571)
+        if self.is_bc_trick and self.solver == "RIE" and not self.is_free_slip:
+            w_f = w_dist * fluid_mask[j_s]
+            nom = seg(w_f[:, None] * u[j_s], i_s, N)
+            den = seg(w_f, i_s, N)
+            u_tilde = nom / (den[:, None] + EPS)
+        else:
+            u_tilde = u
+
+        # density (:749-796)
+        if self.is_rho_evol and self.solver == "SPH":
+            # rho_evol_fn (:24-30)
+            v_j_s = (mass / rho)[j_s]
+            temp = v_j_s * ((u[i_s] - u[j_s]) * grad_w_dist).sum(axis=1)
+            drhodt = rho * seg(temp, i_s, N)
+            rho = rho + self.dt * drhodt
+        elif self.is_rho_evol and self.solver == "RIE":
+            temp = self._rho_evol_riemann(e_s, rho[i_s], rho[j_s], mass[j_s], u[i_s],
+                                          u[j_s], p[i_s], p[j_s], dr_i_j, dist,
+                                          tag[j_s], nw[j_s], g_ext[i_s], gw)
+            drhodt = seg(temp, i_s, N) * fluid_mask
+            rho = rho + self.dt * drhodt
+        else:
+            # rho_summation_fn (:176-178)
+            rho_ = mass * seg(w_dist, i_s, N)
+            rho = torch.where(fluid_mask > 0, rho_, rho)
+
+        p = self.eos.p_fn(rho)                                            # :801
+        p_bg_tvf = self.eos.p_fn(torch.zeros_like(p))                     # :802
+
+        if self.is_bc_trick and self.solver == "SPH":
+            p, rho, u, v = self._gwbc(rho, tag, u, v, p, g_ext, i_s, j_s, w_dist,
+                                      dr_i_j, nw, N)
+            mask = None
+        elif self.is_bc_trick and self.solver == "RIE":
+            mask = fluid_mask[i_s] if self.is_free_slip else torch.ones_like(i_s, dtype=dtype)
+        elif self.solver == "RIE":
+            mask = torch.ones_like(i_s, dtype=dtype)
+
+        if self.solver == "SPH":
+            out = self._acc_standard(dr_i_j, dist, rho[i_s], rho[j_s], u[i_s], u[j_s],
+                                     v[i_s], v[j_s], mass[i_s], mass[j_s], eta[i_s],
+                                     eta[j_s], p[i_s], p[j_s], gw)
+        else:
+            out = self._acc_riemann(e_s, dr_i_j, dist, rho[i_s], rho[j_s], mass[j_s],
+                                    mass[i_s], u[i_s], u[j_s], p[i_s], p[j_s],
+                                    eta[i_s], eta[j_s], tag[j_s], mask, nw[j_s],
+                                    g_ext[i_s], u_tilde[j_s], gw)
+        dudt = seg(out, i_s, N)
+
+        # acceleration_tvf_fn (:199-213, used :912-921)
+        m_i, m_j = mass[i_s], mass[j_s]
+        wv = ((m_i / rho[i_s]) ** 2 + (m_j / rho[j_s]) ** 2) / m_i
+        c = wv * gw / (dist + EPS)
+        out_tv = (c * 1.0 * p_bg_tvf[i_s])[:, None] * dr_i_j
+        dvdt = seg(out_tv, i_s, N)
+
+        if self.artificial_alpha != 0.0:                                  # :925-928
+            dudt = dudt + self._artificial_viscosity(rho, mass, u, tag, i_s, j_s,
+                                                     dr_i_j, dist, grad_w_dist, N)
+
+        out_state = dict(state)
+        out_state.update(u=u, v=v, drhodt=drhodt, dudt=dudt + g_ext, dvdt=dvdt,
+                         rho=rho, p=p)
+        return out_state
+
+    # rho_evol_riemann_fn (:108-164)
+    def _rho_evol_riemann(self, e_ij, rho_i, rho_j, m_j, u_i, u_j, p_i, p_j, r_ij, d_ij,
+                          tag_j, n_w_j, g_ext_i, gw):
+        kernel_grad = gw[:, None] * e_ij
+        wj = _is_wall(tag_j)
+        u_L = torch.where(wj, dot(u_i, -n_w_j), dot(u_i, -e_ij))
+        p_L, rho_L = p_i, rho_i
+        u_R = torch.where(wj, -u_L + 2 * dot(u_j, n_w_j), dot(u_j, -e_ij))
+        p_R = torch.where(wj, p_L + rho_L * dot(g_ext_i, -r_ij), p_j)
+        rho_R = torch.where(wj, self.eos.rho_fn(p_R), rho_j)
+        U_avg = (u_L + u_R) / 2
+        v_avg = (u_i + u_j) / 2
+        rho_avg = (rho_L + rho_R) / 2
+        U_star = U_avg + 0.5 * (p_L - p_R) / (rho_avg * self.c_ref)
+        v_star = U_star[:, None] * (-e_ij) + (v_avg - U_avg[:, None] * (-e_ij))
+        return 2 * rho_i * m_j / rho_j * dot(u_i - v_star, kernel_grad)
+
+    # acceleration_standard_fn (:221-256)
+    def _acc_standard(self, r_ij, d_ij, rho_i, rho_j, u_i, u_j, v_i, v_j, m_i, m_j,
+                      eta_i, eta_j, p_i, p_j, gw):
+        eta_ij = 2 * eta_i * eta_j / (eta_i + eta_j + EPS)
+        p_ij = (rho_j * p_i + rho_i * p_j) / (rho_i + rho_j)
+        wv = ((m_i / rho_i) ** 2 + (m_j / rho_j) ** 2) / m_i
+        c = wv * gw / (d_ij + EPS)
+        # tvf_stress_fn (:216-218): A = outer(rho*u, v-u); A @ r = rho*u*((v-u).r)
+        A_r = 0.5 * ((rho_i[:, None] * u_i) * dot(v_i - u_i, r_ij)[:, None]
+                     + (rho_j[:, None] * u_j) * dot(v_j - u_j, r_ij)[:, None])
+        u_ij = u_i - u_j
+        return c[:, None] * (-p_ij[:, None] * r_ij + A_r + eta_ij[:, None] * u_ij)
+
+    # acceleration_riemann_fn (:316-401)
+    def _acc_riemann(self, e_ij, r_ij, d_ij, rho_i, rho_j, m_j, m_i, u_i, u_j, p_i, p_j,
+                     eta_i, eta_j, tag_j, mask, n_w_j, g_ext_i, u_tilde_j, gw):
+        kernel_grad = gw[:, None] * e_ij
+        wj = _is_wall(tag_j)
+        u_L = torch.where(wj, dot(u_i, -n_w_j), dot(u_i, -e_ij))
+        p_L, rho_L = p_i, rho_i
+        u_R = torch.where(wj, -u_L + 2 * dot(u_j, n_w_j), dot(u_j, -e_ij))
+        p_R = torch.where(wj, p_L + rho_L * dot(g_ext_i, -r_ij), p_j)
+        rho_R = torch.where(wj, self.eos.rho_fn(p_R), rho_j)
+        P_avg = (p_L + p_R) / 2
+        rho_avg = (rho_L + rho_R) / 2
+        eta_ij = 2 * eta_i * eta_j / (eta_i + eta_j + EPS)
+        P_star = P_avg + 0.5 * rho_avg * (u_L - u_R) * self.beta_fn(u_L, u_R)
+        eq_9 = -2 * m_j[:, None] * (P_star / (rho_i * rho_j))[:, None] * kernel_grad
+        u_d = 2 * u_j - u_tilde_j
+        v_ij = torch.where(wj[:, None], u_i - u_d, u_i - u_j)
+        eq_6 = (2 * m_j * eta_ij / (rho_i * rho_j))[:, None] * v_ij / (d_ij + EPS)[:, None]
+        eq_6 = eq_6 * (gw * mask)[:, None]
+        # tvf stress with (u, u) is identically zero (:390-396)
+        return eq_9 + eq_6
+
+    # artificial_viscosity_fn (:404-428)
+    def _artificial_viscosity(self, rho, mass, u, tag, i_s, j_s, dr_i_j, dist,
+                              grad_w_dist, N):
+        h_ab = self.dx
+        c_ab = 10.0 * 1.0
+        rho_ab = (rho[i_s] + rho[j_s]) / 2
+        numerator = mass[j_s] * self.artificial_alpha * h_ab * c_ab
+        numerator = numerator * ((u[i_s] - u[j_s]) * dr_i_j).sum(axis=1)
+        numerator = numerator[:, None] * grad_w_dist
+        denominator = (rho_ab * (dist ** 2 + 0.01 * h_ab ** 2))[:, None]
+        mask_fluid = (tag == FLUID).to(rho.dtype)
+        mfe = mask_fluid[j_s] * mask_fluid[i_s]
+        return seg(mfe[:, None] * numerator / denominator, i_s, N)
+
+    # gwbc_fn (:431-530), heat conduction off
+    def _gwbc(self, rho, tag, u, v, p, g_ext, i_s, j_s, w_dist, dr_i_j, nw, N):
+        mask_bc = _is_wall(tag)
+        mask_j_fluid = (tag[j_s] == FLUID).to(rho.dtype)
+        w_f = w_dist * mask_j_fluid
+        w_sum = seg(w_f, i_s, N)
+
+        def no_slip(x):
+            x_wall = seg(w_f[:, None] * x[j_s], i_s, N) / (w_sum[:, None] + EPS)
+            return torch.where(mask_bc[:, None], 2 * x - x_wall, x)
+
+        def free_slip(x, n):
+            x_wall = seg(w_f[:, None] * x[j_s], i_s, N) / (w_sum[:, None] + EPS)
+            x_wall = n * (x_wall * n).sum(axis=1, keepdim=True)
+            return torch.where(mask_bc[:, None], 2 * x - x_wall, x)
+
+        if self.is_free_slip:
+            u, v = free_slip(u, -nw), free_slip(v, -nw)
+        else:
+            u, v = no_slip(u), no_slip(v)
+        p_unnorm = seg(w_f * p[j_s], i_s, N)
+        rho_wf = seg((rho[j_s] * w_f)[:, None] * dr_i_j, i_s, N)
+        p_ext = (g_ext * rho_wf).sum(axis=1)
+        p_wall = (p_unnorm + p_ext) / (w_sum + EPS)
+        p = torch.where(mask_bc, p_wall, p)
+        rho = self.eos.rho_fn(p)
+        return p, rho, u, v
+
+
+# ---------------------------------------------------------------- integrator
+def si_euler_advance(dt, tvf, state, nbrs, nl_fns, solver, bc_fn):
+    """``si_euler.advance`` (integrator.py:22-56); moving-wall normals are out of scope."""
+    side = torch.as_tensor(solver.box, dtype=state["r"].dtype)
+    st = dict(state)
+    st["u"] = st["u"] + 1.0 * dt * st["dudt"]
+    st["v"] = st["u"] + tvf * 0.5 * dt * st["dvdt"]
+    st["r"] = space.periodic_shift(side, st["r"], 1.0 * dt * st["v"])
+    nbrs = nl_fns.update(st["r"], nbrs)
+    st = solver.forward(st, nbrs.idx)
+    st = bc_fn(st)
+    return st, nbrs
+
+
+# ---------------------------------------------------------------- case callbacks
+def g_ext_zero(r):
+    """TGV / LDC ``_external_acceleration_fn`` (cases/tgv.py:53-54, cases/ldc.py:124-125)."""
+    return torch.zeros_like(r)
+
+
+def make_g_ext_db(g):
+    """DB: constant -g in y (cases/db.py:123-126)."""
+    def f(r):
+        res = torch.zeros_like(r)
+        res[:, 1] = -g
+        return res
+    return f
+
+
+def make_g_ext_pf(g, box_y, dxn):
+    """PF: body force g in x on the band dxn < y < box_y - dxn (cases/pf.py:122-131)."""
+    def f(r):
+        res = torch.zeros_like(r)
+        band = (r[:, 1] < box_y - dxn) & (r[:, 1] > dxn)
+        res[:, 0] = torch.where(band, torch.ones_like(r[:, 0]), torch.zeros_like(r[:, 0]))
+        return res * g
+    return f
+
+
+def bc_identity(state):
+    """TGV ``_boundary_conditions_fn`` (cases/tgv.py:56-57)."""
+    return state
+
+
+def bc_solid_zero(state, zero_p=False):
+    """DB / PF: zero u, v, dudt, dvdt on solid walls (cases/db.py:128-142, cases/pf.py:133-146)."""
+    st = dict(state)
+    m = (st["tag"] == SOLID_WALL)[:, None]
+    for k in ("u", "v", "dudt", "dvdt"):
+        st[k] = torch.where(m, torch.zeros_like(st[k]), st[k])
+    if zero_p:
+        st["p"] = torch.where(m[:, 0], torch.zeros_like(st["p"]), st["p"])
+    return st
+
+
+def make_bc_ldc(u_lid):
+    """LDC: walls at rest, lid at ``u_lid`` (cases/ldc.py:127-144)."""
+    def f(state):
+        st = dict(state)
+        m1 = (st["tag"] == SOLID_WALL)[:, None]
+        m2 = (st["tag"] == MOVING_WALL)[:, None]
+        lid = torch.as_tensor(u_lid, dtype=st["u"].dtype)
+        for k in ("u", "v"):
+            st[k] = torch.where(m1, torch.zeros_like(st[k]), st[k])
+            st[k] = torch.where(m2, lid.expand_as(st[k]), st[k])
+        for k in ("dudt", "dvdt"):
+            st[k] = torch.where(m1 | m2, torch.zeros_like(st[k]), st[k])
+        return st
+    return f

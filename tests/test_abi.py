@@ -1,0 +1,80 @@
+"""The C ABI: the library builds, loads, exports every symbol of include/sph_gb300.h,
+and the ctypes mirrors match the C struct layout (checked by compiling the header
+with gcc). No compute calls: these run without a GPU."""
+
+import ctypes
+import os
+import re
+import subprocess
+
+import pytest
+
+from jaxsph_gb300 import _build, _lib
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+HEADER = os.path.join(ROOT, "include", "sph_gb300.h")
+
+
+def header_functions():
+    src = open(HEADER).read()
+    return sorted(set(re.findall(r"^\s*(?:const\s+)?\w+\*?\s+\*?(sph_\w+)\s*\(", src, re.M)))
+
+
+@pytest.fixture(scope="module")
+def lib():
+    _build.build()
+    return ctypes.CDLL(_build.LIB_PATH)
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = header_functions()
+    assert len(names) >= 15
+    for name in names:
+        assert hasattr(lib, name), name
+    assert set(names) == set(_lib.EXPORTS)
+
+
+def test_abi_version_and_error_string(lib):
+    lib.sph_abi_version.restype = ctypes.c_int
+    assert lib.sph_abi_version() == 1
+    lib.sph_last_error.restype = ctypes.c_char_p
+    assert isinstance(lib.sph_last_error(), bytes)
+
+
+def test_create_rejects_bad_arguments_without_touching_the_gpu(lib):
+    lib.sph_create.restype = ctypes.c_int
+    cfg = _lib.SphConfig(dim=4)
+    case = _lib.SphCase(n=10)
+    h = ctypes.c_void_p()
+    rc = lib.sph_create(ctypes.byref(cfg), ctypes.byref(case), 1, ctypes.byref(h))
+    assert rc & _lib.ERR_INVALID_ARG and not h.value
+    lib.sph_last_error.restype = ctypes.c_char_p
+    assert b"dimension" in lib.sph_last_error()
+
+
+def test_struct_layout_matches_c(tmp_path):
+    prog = tmp_path / "layout.c"
+    fields = {
+        "SphConfig": [f[0] for f in _lib.SphConfig._fields_],
+        "SphCase": [f[0] for f in _lib.SphCase._fields_],
+        "SphStateView": [f[0] for f in _lib.SphStateView._fields_],
+        "SphNLCapacity": [f[0] for f in _lib.SphNLCapacity._fields_],
+    }
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "sph_gb300.h"',
+             "int main(void) {"]
+    for s, fs in fields.items():
+        lines.append(f'printf("{s} %zu\\n", sizeof({s}));')
+        for f in fs:
+            lines.append(f'printf("{s}.{f} %zu\\n", offsetof({s}, {f}));')
+    lines.append("return 0; }")
+    prog.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(prog), "-o", str(exe)],
+                   check=True)
+    out = subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout
+    c = dict(line.rsplit(" ", 1) for line in out.strip().splitlines())
+    for s, fs in fields.items():
+        cls = getattr(_lib, s)
+        assert int(c[s]) == ctypes.sizeof(cls), s
+        for f in fs:
+            assert int(c[f"{s}.{f}"]) == getattr(cls, f).offset, f"{s}.{f}"

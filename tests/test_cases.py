@@ -1,0 +1,77 @@
+"""Host-side case construction against the reference's setup code (no GPU)."""
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from jaxsph_gb300 import _lib, cases
+from oracle_setup import oracle_bc, oracle_g
+
+
+def test_tgv2d_lattice_layout():
+    s = cases.tgv(dim=2)
+    r = s.state["r"]
+    assert s.n == 2500 and r.dtype == torch.float32
+    # x fastest (meshgrid indexing="xy"), cell centres (i + 1/2) dx rounded in float32
+    assert r[1, 0] > r[0, 0] and r[1, 1] == r[0, 1]
+    assert r[0, 0].item() == np.float32(np.float32(0.5) * np.float32(0.02))
+    assert s.dt == pytest.approx(0.25 * 0.02 / 11)
+    assert s.p_ref == 100.0 and s.p_bg == 0.0
+
+
+def test_tgv3d_lattice_layout():
+    s = cases.tgv(dim=3)
+    r = s.state["r"]
+    assert s.n == 64 ** 3
+    # meshgrid(range(nx), range(ny), range(nz), indexing="xy"): z fastest, then x, then y
+    assert r[1, 2] > r[0, 2] and r[1, 0] == r[0, 0] and r[1, 1] == r[0, 1]
+    assert r[64, 0] > r[0, 0] and r[64, 1] == r[0, 1]
+    assert r[64 * 64, 1] > r[0, 1]
+    assert s.solver["kernel"] == "WC2K" and s.tvf == 1.0
+    assert s.viscosity == pytest.approx(1 / 1600)
+
+
+def test_dam_break_geometry():
+    s = cases.dam_break()
+    tag = s.state["tag"]
+    assert s.n == 88874 and int((tag == 1).sum()) == 8874 and int((tag == 0).sum()) == 80000
+    assert (tag[:8874] == 1).all()  # walls first in memory
+    assert np.allclose(s.box, [5.496, 2.13])
+    assert s.dt == pytest.approx(0.25 * 0.005 / (10 * np.sqrt(2) + np.sqrt(2)))
+    nw = s.state["nw"]
+    wall = tag == 1
+    assert torch.allclose(nw[wall].norm(dim=1), torch.ones(8874), atol=1e-5)
+    assert (nw[~wall] == 0).all()
+    assert (s.state["p"][wall] == 0).all()
+
+
+def test_lid_driven_cavity_tags():
+    s = cases.lid_driven_cavity()
+    tag = s.state["tag"]
+    assert s.n == 3136 and int((tag == 2).sum()) == 168 and int((tag == 0).sum()) == 2500
+    lid = s.state["u"][tag == 2]
+    assert torch.all(lid[:, 0] == 1.0)  # bc_fn applied at initialisation
+
+
+def test_poiseuille_band_force():
+    s = cases.poiseuille()
+    g = s.g_ext_fn(s.state["r"])
+    fluid = s.state["tag"] == 0
+    assert torch.all(g[fluid, 0] == 1000.0) and torch.all(g[~fluid, 0] == 0.0)
+
+
+@pytest.mark.parametrize("make", [lambda: cases.dam_break(dx=0.05),
+                                  lambda: cases.lid_driven_cavity(dx=0.05),
+                                  lambda: cases.poiseuille(dx=0.05)])
+def test_descriptors_match_oracle_callbacks(make):
+    s = make()
+    g = torch.Generator().manual_seed(0)
+    st = {k: (v + torch.randn(v.shape, generator=g) if v.is_floating_point() else v)
+          for k, v in s.state.items()}
+    st64 = {k: (v.double() if v.is_floating_point() else v.long()) for k, v in st.items()}
+    ours = s.bc_fn({k: v.double() if v.is_floating_point() else v for k, v in st.items()})
+    ref = oracle_bc(s)(st64)
+    for k in ("u", "v", "dudt", "dvdt", "p"):
+        assert torch.equal(ours[k], ref[k]), k
+    assert torch.equal(s.g_ext_fn(st64["r"]), oracle_g(s)(st64["r"]))

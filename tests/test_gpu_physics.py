@@ -1,0 +1,166 @@
+"""GPU forward pass and si_euler steps vs the CPU oracle (float64 and float32).
+
+Tolerances (GPU float32 vs the float64 oracle on identical float32 inputs):
+
+* density:        |rho - rho64|          <= 2e-6 * rho_ref
+* pressure:       |p - p64|              <= 2e-6 * rho_ref * c_ref^2
+* accelerations:  |a - a64|_inf          <= 1e-5 * F,  F = p_ref/(rho_ref*h) + |g|
+  (a pair's pressure term; lattice accelerations are residuals of cancelling
+  pair terms, so their own magnitude is no scale)
+* velocities:     |u - u64|_inf          <= 1e-5 * (u_ref + F*dt) after one step
+* positions:      |r - r64|_inf          <= 1e-6 * box after the steps run here
+and every error is also at most 10x the float32 oracle's own error (+ 1e-7 of
+the scale), i.e. the GPU is as accurate as a float32 evaluation of the same
+algorithm.
+"""
+
+import numpy as np
+import pytest
+import torch
+
+from jaxsph_gb300 import cases, integrator, partition, simulate, solver
+from oracle_setup import oracle_case, oracle_rollout
+import oracle
+
+pytestmark = pytest.mark.gpu
+
+
+def small_cases():
+    return {
+        "tgv2d_sph": lambda: cases.tgv(dim=2, dx=0.02),
+        "tgv3d_sph_tvf": lambda: cases.tgv(dim=3, dx=2 * np.pi / 20),
+        "tgv2d_rie": lambda: cases.tgv(dim=2, dx=0.04, solver_name="RIE"),
+        "db_rie": lambda: cases.dam_break(dx=0.04),
+        "db_rie_freeslip": lambda: cases.dam_break(dx=0.04, free_slip=True),
+        "ldc_sph": lambda: cases.lid_driven_cavity(dx=0.04),
+        "ldc_sph_tvf": lambda: cases.lid_driven_cavity(dx=0.04, tvf=1.0),
+        "pf_sph": lambda: cases.poiseuille(dx=0.05),
+        "pf_sph_evol": lambda: cases.poiseuille(dx=0.05, density_evolution=True),
+        "ldc_sph_freeslip_av": lambda: cases.lid_driven_cavity(dx=0.04, free_slip=True,
+                                                               artificial_alpha=0.1),
+    }
+
+
+def scales(setup):
+    g = max(abs(x) for x in setup.g_ext_fn.spec["g"])
+    F = setup.p_ref / (1.0 * setup.dx) + g
+    return F
+
+
+def err(a, b):
+    a = a.double().cpu()
+    b = b.double().cpu()
+    return (a - b).abs().max().item()
+
+
+def perturbed_state(setup, steps=3):
+    """A non-trivial float32 state: a few float64 oracle steps, rounded to float32."""
+    st = oracle_rollout(setup, steps, torch.float64)
+    return {k: (v.float() if v.is_floating_point() else v.int()) for k, v in st.items()}
+
+
+def gpu_solver(setup, kahan=False):
+    return simulate.make_solver(setup, kahan=kahan)
+
+
+@pytest.mark.parametrize("name", list(small_cases()))
+def test_forward_matches_oracle(name):
+    setup = small_cases()[name]()
+    st32 = perturbed_state(setup)
+    wc = gpu_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    dev = {k: v.cuda() for k, v in st32.items()}
+    nb = fns.allocate(dev["r"])
+    out = wc.forward_wrapper()(dev, nb)
+    res = {}
+    for dt_ in (torch.float64, torch.float32):
+        sol, ofns, _, ost = oracle_case(setup, dt_, state=st32)
+        onb = ofns.allocate(ost["r"])
+        res[dt_] = sol.forward(ost, onb.idx)
+    r64, r32 = res[torch.float64], res[torch.float32]
+    F = scales(setup)
+    prs = setup.c_ref ** 2
+    checks = [("rho", 2e-6), ("p", 2e-6 * prs), ("dudt", 1e-5 * F), ("dvdt", 1e-5 * F),
+              ("u", 1e-5), ("v", 1e-5), ("drhodt", 1e-5 * F)]
+    for key, tol in checks:
+        e_gpu = err(out[key], r64[key])
+        e_f32 = err(r32[key], r64[key])
+        assert e_gpu <= max(tol, 10 * e_f32 + 1e-7 * tol * 1e5), (key, e_gpu, e_f32, tol)
+
+
+@pytest.mark.parametrize("name", ["tgv2d_sph", "tgv3d_sph_tvf", "db_rie", "ldc_sph", "pf_sph"])
+def test_rollout_matches_oracle(name):
+    setup = small_cases()[name]()
+    steps = 20
+    sim = simulate.Simulation(setup)
+    code = sim.run(steps)
+    assert code & 0xF == 0
+    got = sim.state()[0]
+    ref = oracle_rollout(setup, steps, torch.float64)
+    box = float(np.max(setup.box))
+    F = scales(setup)
+    side = torch.as_tensor(setup.box, dtype=torch.float64)
+    dr = oracle.space.periodic_displacement(side, got["r"].double().cpu() - ref["r"])
+    assert dr.abs().max().item() <= 1e-6 * box
+    assert err(got["rho"], ref["rho"]) <= 2e-5
+    assert err(got["u"], ref["u"]) <= 1e-4 * (setup.u_ref + F * setup.dt)
+
+
+def test_drop_in_advance_equals_resident_rollout():
+    setup = cases.lid_driven_cavity(dx=0.04)
+    wc = gpu_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    disp, shift = setup.space()
+    adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
+    st = setup.to("cuda")
+    nb = fns.allocate(st["r"])
+    for _ in range(5):
+        st, nb = adv(setup.dt, st, nb)
+    sim = simulate.Simulation(setup)
+    sim.run(5)
+    got = sim.state()[0]
+    for k in ("r", "u", "v", "rho", "p", "dudt", "dvdt"):
+        assert torch.equal(st[k], got[k]), k
+
+
+def test_deterministic_and_graph_equals_eager():
+    setup = cases.tgv(dim=3, dx=2 * np.pi / 20)
+    a = simulate.Simulation(setup)
+    a.run(9)  # eager + graph replays
+    b = simulate.Simulation(setup)
+    for _ in range(9):
+        b.run(1)  # eager only
+    sa, sb = a.state()[0], b.state()[0]
+    for k in ("r", "u", "v", "rho", "p", "dudt", "dvdt"):
+        assert torch.equal(sa[k], sb[k]), k
+
+
+def test_forward_rejects_stale_neighbour_list():
+    setup = cases.tgv(dim=2, dx=0.05)
+    wc = gpu_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    st = setup.to("cuda")
+    nb = fns.allocate(st["r"])
+    st2 = dict(st)
+    st2["r"] = (st["r"] + 1e-3).contiguous()
+    with pytest.raises(NotImplementedError):
+        wc.forward_wrapper()(st2, nb)
+
+
+def test_diagnostics_float64():
+    setup = cases.dam_break(dx=0.04)
+    sim = simulate.Simulation(setup)
+    sim.run(10)
+    st = sim.state()[0]
+    d = sim.diagnostics()[0].cpu()
+    fluid = st["tag"] == 0
+    m = st["mass"].double()[fluid]
+    u = st["u"].double()[fluid]
+    v = st["v"].double()[fluid]
+    assert abs(d[0].item() - m.sum().item()) <= 1e-12 * m.sum().item()
+    mom = (m[:, None] * u).sum(0)
+    assert torch.allclose(d[1:3], mom.cpu(), rtol=1e-9, atol=1e-12)
+    ekin = 0.5 * (v ** 2).sum().item() * setup.dx ** 2
+    assert abs(d[4].item() - ekin) <= 1e-6 * max(ekin, 1e-30) + 1e-15
+    umax = st["u"].double().norm(dim=1).max().item()
+    assert abs(d[5].item() - umax) <= 1e-7 * max(umax, 1e-30)

@@ -1,0 +1,137 @@
+"""The CPU oracle pinned against the reference's own tests (no GPU needed).
+
+* neighbour lists: the four golden edge lists of the reference's
+  tests/test_neighbors.py:89-121, in float64 (the reference test enables x64)
+  and float32, allocate == update, no one-sided padding, self-edge rules;
+* kernels: tests/test_kernel.py:17-44 (1D half-integral 0.5, W >= 0, W' <= 0)
+  plus 2D/3D normalisation;
+* the product's closed-form kernel derivatives against the oracle's autograd.
+"""
+
+import json
+import math
+import os
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from jaxsph_gb300 import kernel as pk
+
+GOLDEN = os.path.join(os.path.dirname(__file__), "golden", "neighbors_golden.json")
+
+
+@pytest.mark.parametrize("dtype", [torch.float64, torch.float32])
+@pytest.mark.parametrize("case", range(4))
+def test_golden_neighbor_lists(case, dtype):
+    c = json.load(open(GOLDEN))["cases"][case]
+    r = torch.tensor(c["r"], dtype=dtype)
+    n = r.shape[0]
+    fns = oracle.partition.NeighborListFns(c["box_size"], c["cutoff"], dtype,
+                                           mask_self=c["mask_self"])
+    nb = fns.allocate(r)
+    nb2 = fns._build(r, nb.cell_list_capacity, nb.max_occupancy, 0)
+    assert not nb.did_buffer_overflow and not nb2.did_buffer_overflow
+    assert torch.equal(nb.idx, nb2.idx)
+    assert torch.equal(nb.idx[0] == n, nb.idx[1] == n)
+    real = nb.idx[:, nb.idx[0] < n]
+    selfe = real[0] == real[1]
+    if c["mask_self"]:
+        assert int(selfe.sum()) == 0
+    else:
+        assert len(torch.unique(real[0][selfe])) == n
+    assert oracle.partition.canonical_edges(nb.idx, n).tolist() == c["target"]
+
+
+def test_golden_fixture_is_the_reference_data():
+    d = json.load(open(GOLDEN))
+    assert len(d["cases"]) == 4
+    assert [c["mask_self"] for c in d["cases"]] == [False, True, False, True]
+
+
+@pytest.mark.parametrize("name,dx_factor", [("QSK", 1.0), ("WC2K", 1.3)])
+def test_kernel_1d_half_integral(name, dx_factor):
+    """tests/test_kernel.py:17-44 of the reference."""
+    N = 500
+    for h in (1.0, 0.1, 0.01):
+        k = oracle.sph.make_kernel(name, dx_factor * h, 1)
+        dx = k.cutoff / N
+        x = torch.linspace(dx / 2, k.cutoff + dx / 2, N, dtype=torch.float64)
+        w = k.w(x)
+        gw = oracle.sph.grad_w(k, x).detach()
+        assert abs(dx * w.sum().item() - 0.5) < 1e-2
+        assert (w >= 0).all() and (gw <= 0).all()
+
+
+@pytest.mark.parametrize("name", ["QSK", "WC2K"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_kernel_normalisation(name, dim):
+    k = oracle.sph.make_kernel(name, 1.0, dim)
+    r = torch.linspace(0, k.cutoff, 200001, dtype=torch.float64)
+    w = k.w(r)
+    shell = 2 * math.pi * r if dim == 2 else 4 * math.pi * r ** 2
+    integral = torch.trapezoid(w * shell, r).item()
+    if name == "QSK" and dim == 3:
+        # the reference's 3D quintic constant 3/(359 pi) (kernel.py:64) is 0.28 %
+        # above the exact 1/(120 pi); parity keeps the reference's value
+        assert abs(integral - 360.0 / 359.0) < 1e-6
+    else:
+        assert abs(integral - 1.0) < 1e-6
+
+
+@pytest.mark.parametrize("name", ["QSK", "WC2K"])
+@pytest.mark.parametrize("dim", [2, 3])
+def test_product_kernel_formulas_match_oracle_autograd(name, dim):
+    h = 0.037
+    k_o = oracle.sph.make_kernel(name, h, dim)
+    k_p = pk.make_kernel(name, h, dim)
+    assert k_p.cutoff == pytest.approx(k_o.cutoff)
+    r = torch.linspace(0, 1.1 * k_o.cutoff, 5001, dtype=torch.float64)
+    assert torch.allclose(k_p.w(r), k_o.w(r), rtol=1e-12, atol=1e-12 * k_o.sigma)
+    g_o = oracle.sph.grad_w(k_o, r).detach()
+    assert torch.allclose(k_p.grad_w(r), g_o, rtol=1e-10, atol=1e-10 * k_o.sigma / h)
+
+
+def test_jnp_mod_semantics():
+    side = torch.tensor(1.0, dtype=torch.float32)
+    x = torch.tensor([-1.5, -0.25, -0.0, 0.0, 0.25, 1.0, 1.75], dtype=torch.float32)
+    got = oracle.space.jnp_mod(x, side)
+    want = torch.tensor([0.5, 0.75, -0.0, 0.0, 0.25, 0.0, 0.75], dtype=torch.float32)
+    assert torch.equal(got, want)
+    # a value just below zero wraps to exactly the box length in float32
+    tiny = torch.tensor([-1e-9], dtype=torch.float32)
+    assert oracle.space.jnp_mod(tiny, side).item() == 1.0
+
+
+def test_oracle_step_conserves_mass_and_momentum():
+    from jaxsph_gb300 import cases
+    from oracle_setup import oracle_case
+
+    setup = cases.tgv(dim=2, dx=0.05)
+    solver, fns, bc, st = oracle_case(setup, torch.float64)
+    nb = fns.allocate(st["r"])
+    for _ in range(3):
+        st, nb = oracle.sph.si_euler_advance(setup.dt, 0.0, st, nb, fns, solver, bc)
+    # pairwise antisymmetric forces: total momentum change vanishes
+    mom_rate = (st["mass"][:, None] * st["dudt"]).sum(0)
+    assert mom_rate.abs().max().item() < 1e-9 * setup.p_ref
+    # density summation of a uniform lattice with periodic images is uniform
+    assert (st["rho"] - st["rho"].mean()).abs().max().item() < 1e-2
+
+
+def test_oracle_gradient_through_steps():
+    """torch autograd through the float64 oracle (the gradient oracle of the adjoint)."""
+    from jaxsph_gb300 import cases
+    from oracle_setup import oracle_case
+
+    setup = cases.tgv(dim=2, dx=0.1)
+    solver, fns, bc, st = oracle_case(setup, torch.float64)
+    nb = fns.allocate(st["r"])
+    u0 = st["u"].clone().requires_grad_(True)
+    s = dict(st, u=u0, v=u0)
+    for _ in range(2):
+        s, _ = oracle.sph.si_euler_advance(setup.dt, 0.0, s, nb, fns, solver, bc)
+    loss = (0.5 * s["u"] ** 2).sum()
+    (g,) = torch.autograd.grad(loss, u0)
+    assert torch.isfinite(g).all() and g.abs().max() > 0
