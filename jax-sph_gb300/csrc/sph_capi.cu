@@ -43,6 +43,8 @@ struct SphHandle {
   int *count = nullptr, *start = nullptr, *keyc = nullptr, *keys = nullptr;
   int *tsrc = nullptr, *tkey = nullptr, *tcell = nullptr, *scan_tmp = nullptr;
   int *rowcnt = nullptr, *rowoff = nullptr;
+  int *nbr = nullptr, *nbr_cnt = nullptr;
+  int kmax = kListSlots;  // neighbour-list slots per particle
   unsigned* status = nullptr;
   unsigned long long* edgecnt = nullptr;
   const float* g_arr = nullptr;
@@ -79,6 +81,9 @@ struct SphHandle {
     L.n_cases = n_cases;
     L.cases = dc;
     L.status = status;
+    L.nbr = nbr;
+    L.nbr_cnt = nbr_cnt;
+    L.kmax = kmax;
     L.launches = const_cast<int*>(&launch_count);
     L.ev = ev;
     return L;
@@ -183,6 +188,27 @@ int make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long lon
   c.g_lo = (float)in.g_band_lo;
   c.g_hi = (float)in.g_band_hi;
   c.bc_kind = in.bc_kind;
+  // Fast membership test. The minimum-image difference of two positions in
+  // [0, L] differs from the reference's float32 periodic displacement by at
+  // most ~3.3 ulp(L) per component, so their squared norms near the cutoff
+  // differ by at most ~20 ulp(L) * cutoff plus a few roundings of cutoff^2.
+  // Inside the band cut_sq * (1 +- rel) the reference metric decides.
+  bool fast = true;
+  float lmax = 0.f;
+  for (int d = 0; d < dim; ++d) {
+    fast = fast && nc[d] >= 5;
+    lmax = c.box[d] > lmax ? c.box[d] : lmax;
+    c.inv_box[d] = 1.0f / c.box[d];
+  }
+  const double rel = std::ldexp(24.0 * lmax / cut + 8.0, -23);
+  c.fast = fast && rel < 0.25;
+  if (c.fast) {
+    c.cut_lo = (float)(c.cutoff_sq * (1.0 - rel));
+    c.cut_hi = (float)(c.cutoff_sq * (1.0 + rel));
+  } else {  // every candidate takes the reference metric
+    c.cut_lo = -1.0f;
+    c.cut_hi = INFINITY;
+  }
   return 0;
 }
 
@@ -327,7 +353,8 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
     rc |= h->alloc(&h->count, h->C + 1) | h->alloc(&h->start, h->C + 1) |
           h->alloc(&h->keyc, N) | h->alloc(&h->keys, N) | h->alloc(&h->tsrc, N) |
           h->alloc(&h->tkey, N) | h->alloc(&h->tcell, N) | h->alloc(&h->rowcnt, N + 1) |
-          h->alloc(&h->rowoff, N + 1);
+          h->alloc(&h->rowoff, N + 1) | h->alloc(&h->nbr, (size_t)h->kmax * N) |
+          h->alloc(&h->nbr_cnt, N);
     long long m = h->C + 1 > N + 1 ? h->C + 1 : N + 1;
     rc |= h->alloc(&h->scan_tmp, scan_tmp_ints(m));
     rc |= h->alloc(&h->status, 1) | h->alloc(&h->edgecnt, n_cases) | h->alloc(&h->dc, n_cases) |
@@ -421,7 +448,13 @@ int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out
   if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   cudaStream_t st = (cudaStream_t)stream;
-  int rc = bin_static(h, st);
+  // allocation sizes the capacities from the data and never flags an overflow
+  for (auto& c : h->hc) {
+    c.cell_cap = INT_MAX;
+    c.edge_cap = LLONG_MAX;
+  }
+  int rc = upload_cases(h, st);
+  if (!rc) rc = bin_static(h, st);
   if (rc) return rc;
   LaunchCtx L = h->ctx(st);
   launch_row_counts(L, h->buf[h->cur], h->cellid, h->start, h->rowcnt);

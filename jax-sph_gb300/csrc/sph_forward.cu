@@ -1,20 +1,24 @@
-// WCSPH forward pass (jax_sph/solver.py:705-949) as three cell-tiled passes
-// over particles in cell-sorted order, one thread per receiving particle:
+// WCSPH forward pass (jax_sph/solver.py:705-949) as cell-tiled passes over
+// particles in cell-sorted order, one thread per receiving particle:
 //
-//   density pass  summation (solver.py:176-178) / SPH continuity (:24-30) /
-//                 Riemann continuity (:108-164), EOS (:801-802), Shepard wall
-//                 velocity for the Riemann wall BC (:547-552); counts edges.
-//   wall pass     generalized wall BC for the SPH solver (:431-530), wall
-//                 particles only, after every fluid pressure is known.
+//   density pass  walks the 3^d neighbour cells once, keeps exactly the
+//                 reference's edges (receiver i, sender j) with
+//                 metric(r_j, r_i) < cutoff_sq, records them in a per-step
+//                 neighbour list, and computes summation (solver.py:176-178) /
+//                 SPH continuity (:24-30) / Riemann continuity (:108-164)
+//                 density, EOS (:801-802) and the Shepard wall velocity of
+//                 the Riemann wall BC (:547-552); counts edges.
+//   wall pass     generalized wall BC of the SPH solver (:431-530) on wall
+//                 particles, after every fluid pressure is known.
 //   force pass    standard (:221-256) or Riemann (:316-401) acceleration,
 //                 transport-velocity acceleration (:199-213), artificial
 //                 viscosity (:404-428), g_ext (:936) and, in a step, bc_fn.
 //
-// Pairs are never materialised: each thread walks its 3^d neighbour cells and
-// keeps exactly the reference's edges (receiver i, sender j) with
-// metric(r_j, r_i) < cutoff_sq; the physics then uses dr_ij = disp(r_i, r_j)
-// as the reference does. Sums are accumulated per receiver in registers in a
-// fixed order (deterministic, no atomics on physics values).
+// The wall and force passes read the neighbour list; a particle with more
+// neighbours than the list holds walks the cells again instead. Pair sums are
+// accumulated per receiver in registers in a fixed order (deterministic, no
+// atomics on physics values). Self pairs contribute exactly zero to every
+// gradient sum (dW/dr(0) = 0), so the list omits them.
 #include "sph_internal.cuh"
 
 namespace sph {
@@ -30,6 +34,12 @@ __device__ __forceinline__ float3 f3(const float4& a) { return make_float3(a.x, 
 __device__ __forceinline__ float dot3(const float3& a, const float3& b) {
   return a.x * b.x + a.y * b.y + a.z * b.z;
 }
+
+struct NList {
+  int* nbr;   // [kmax][N] sender indices (k-major)
+  int* cnt;   // [N] neighbours without self (may exceed kmax)
+  int kmax;
+};
 
 // Per-case edge counter for the NEIGHBOR_LIST_OVERFLOW test: one reduction
 // and one atomic per case present in the warp (cases are contiguous, so
@@ -55,18 +65,66 @@ __device__ __forceinline__ void count_edges(int ci, int cnt, bool valid,
   }
 }
 
+// Visit the senders j of receiver i (self excluded): from the neighbour list,
+// or by walking the cells when the list overflowed for i.
+template <int DIM, typename F>
+__device__ __forceinline__ void for_each_neighbour(long long N, long long i, const float4& ri,
+                                                   const CaseDev& c, const float4* __restrict__ P4,
+                                                   const int* cellid, const int* start,
+                                                   const NList& L, F&& f) {
+  const int m = L.cnt[i];
+  if (m <= L.kmax) {
+    // software pipelined: the next sender's index and position are loaded
+    // while the current pair is evaluated
+    int jn = m > 0 ? L.nbr[i] : 0;
+    float4 rn = m > 0 ? __ldg(P4 + jn) : ri;
+    for (int k = 0; k < m; ++k) {
+      const int j = jn;
+      const float4 rj = rn;
+      if (k + 1 < m) {
+        jn = L.nbr[(long long)(k + 1) * N + i];
+        rn = __ldg(P4 + jn);
+      }
+      float3 dr;
+      float d2;
+      pair_dr<DIM>(ri, rj, c, dr, d2);
+      f(j, rj, dr, d2);
+    }
+    return;
+  }
+  for_each_range<DIM>(c, cellid[i] - c.cell_off, start, [&](int j0, int j1, float3 s) {
+    const float3 q = make_float3(ri.x - s.x, ri.y - s.y, ri.z - s.z);
+    for (int j = j0; j < j1; ++j) {
+      if (j == i) continue;
+      const float4 rj = __ldg(P4 + j);
+      float3 dr;
+      float d2;
+      if (edge_dr<DIM>(ri, rj, q, c, dr, d2)) f(j, rj, dr, d2);
+    }
+  });
+}
+
 // ------------------------------------------------------------------ density pass
+// Two phases per receiver i. (1) Walk the 3^d neighbour cells with the cheap
+// membership test and stage the senders in shared memory (k-major, bank
+// conflict free); the warp stays converged because the loop body is tiny.
+// (2) Loop over the staged senders -- the same count for most lanes -- to
+// evaluate the pair physics, copying the list to global memory (coalesced,
+// k-major) for the wall and force passes.
+//
 // MODE 0: summation (fluid receivers), 1: SPH continuity, 2: Riemann
 // continuity (fluid receivers). `rie_shepard`: wall receivers compute the
 // Shepard average of fluid velocities instead (gwbc_fn_riemann_wrapper,
 // solver.py:547-552); `sph_gwbc`: the SPH wall BC follows, which ends with
 // rho = EOS^-1(p) for every particle (solver.py:516).
 template <int DIM, int KER, int MODE, bool KAHAN>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 4)
 k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
           int mask_self, int rie_shepard, int sph_gwbc, const float* g_arr, float4* R4,
-          float4* UT4, unsigned long long* edgecnt, unsigned* status) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+          float4* UT4, NList nl, unsigned long long* edgecnt, unsigned* status) {
+  __shared__ int s_nbr[kListSlots][kBlock];
+  const int tid = threadIdx.x;
+  long long i = blockIdx.x * (long long)blockDim.x + tid;
   bool valid = i < N;
   int ci = 0, cnt = 0;
   if (valid) {
@@ -76,23 +134,50 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
     const int tag = tag_of(meta);
     const bool fluid = tag == FLUID;
     const float4 ri = b.P4[i];
+    // phase 1: candidate walk
+    int m = 0;
+    bool self_edge = false;
+    const int kmax = nl.kmax;
+    const float lo = c.cut_lo, hi = c.cut_hi;
+    const CaseDev* cp = cases + ci;
+    for_each_range<DIM>(c, cellid[i] - c.cell_off, start, [&](int j0, int j1, float3 s) {
+      const float3 q = make_float3(ri.x - s.x, ri.y - s.y, ri.z - s.z);
+      // two independent gathers per iteration; the body is branch-free
+      // (predicated count, unconditional shared-memory store)
+      for (int j = j0; j < j1; j += 2) {
+        const bool v1 = j + 1 < j1;
+        const float4 ra = __ldg(b.P4 + j);
+        const float4 rb = v1 ? __ldg(b.P4 + j + 1) : make_float4(3e30f, 3e30f, 3e30f, 0.f);
+        bool ea = edge_walk<DIM>(ri, ra, q, lo, hi, cp);
+        bool eb = v1 && edge_walk<DIM>(ri, rb, q, lo, hi, cp);
+        self_edge |= (ea && j == i) || (eb && j + 1 == i);
+        ea = ea && j != i;
+        eb = eb && j + 1 != i;
+        s_nbr[m < kmax ? m : kmax - 1][tid] = j;
+        m += ea;
+        s_nbr[m < kmax ? m : kmax - 1][tid] = j + 1;
+        m += eb;
+      }
+    });
+    const bool self_term = self_edge && !mask_self;
+    cnt = m + (self_term ? 1 : 0);
+    nl.cnt[i] = m;
+
+    // phase 2: pair physics over the senders
     const float4 Ui = b.U4[i];
     const float3 ui = f3(Ui);
     const float rho_i = Ui.w;
     const float p_i = b.V4[i].w;
     const bool shepard = rie_shepard && !fluid;
+    const bool need_pairs = MODE == 1 || fluid || shepard;
     float3 gi = make_float3(0.f, 0.f, 0.f);
     if (MODE == 2) gi = g_ext<DIM>(c, ri, g_arr, b.ORIG[i]);
     Acc<KAHAN> s0, sx, sy, sz;
-    for_each_candidate<DIM>(c, cellid[i] - c.cell_off, start, [&](int j) {
-      if (mask_self && j == i) return;
-      const float4 rj = b.P4[j];
-      if (!is_edge<DIM>(ri, rj, c)) return;
-      ++cnt;
-      if (MODE != 1 && !fluid && !shepard) return;
-      const float3 dr = pdisp3<DIM>(ri, rj, c);
-      const float d2 = sqd<DIM>(dr);
-      const float dist = d2 > 0.f ? __fsqrt_rn(d2) : 0.f;
+    // the self pair: W(0) in a summation; zero gradient elsewhere; a wall is
+    // not a fluid sender of its own Shepard average
+    if (MODE == 0 && fluid && self_term) s0.add(kw<KER>(0.f, c));
+    auto pair = [&](int j, const float4& rj, const float3& dr, float d2) {
+      const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
       if (shepard) {
         if (tag_of(b.META[j]) == FLUID) {
           const float w = kw<KER>(dist, c);
@@ -113,9 +198,9 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
       const float inv = 1.0f / (dist + kEps);
       const float gw = kdw<KER>(dist, c);
       if (MODE == 1) {
-        const float3 gv = make_float3(gw * dr.x * inv, gw * dr.y * inv, gw * dr.z * inv);
+        const float g = gw * inv;
         const float vj = rj.w / Uj.w;
-        s0.add(vj * ((ui.x - uj.x) * gv.x + (ui.y - uj.y) * gv.y + (ui.z - uj.z) * gv.z));
+        s0.add(vj * g * ((ui.x - uj.x) * dr.x + (ui.y - uj.y) * dr.y + (ui.z - uj.z) * dr.z));
         return;
       }
       // MODE 2, fluid receiver (rho_evol_riemann_fn, solver.py:108-164)
@@ -144,7 +229,41 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
                                        -Ustar * e.z + (0.5f * (ui.z + uj.z) + Uavg * e.z));
       const float3 dv = make_float3(ui.x - vstar.x, ui.y - vstar.y, ui.z - vstar.z);
       s0.add(2.0f * rho_i * rj.w / Uj.w * dot3(dv, kg));
-    });
+    };
+    if (m <= kmax) {
+      if (!need_pairs) {
+        for (int k = 0; k < m; ++k) nl.nbr[(long long)k * N + i] = s_nbr[k][tid];
+      } else {
+        int jn = m > 0 ? s_nbr[0][tid] : 0;
+        float4 rn = m > 0 ? __ldg(b.P4 + jn) : ri;
+        for (int k = 0; k < m; ++k) {
+          const int j = jn;
+          const float4 rj = rn;
+          if (k + 1 < m) {
+            jn = s_nbr[k + 1][tid];
+            rn = __ldg(b.P4 + jn);
+          }
+          nl.nbr[(long long)k * N + i] = j;
+          float3 dr;
+          float d2;
+          pair_dr<DIM>(ri, rj, c, dr, d2);
+          pair(j, rj, dr, d2);
+        }
+      }
+    } else if (need_pairs) {
+      // more senders than list slots: walk the cells again (the wall and
+      // force passes do the same for this receiver)
+      for_each_range<DIM>(c, cellid[i] - c.cell_off, start, [&](int j0, int j1, float3 s) {
+        const float3 q = make_float3(ri.x - s.x, ri.y - s.y, ri.z - s.z);
+        for (int j = j0; j < j1; ++j) {
+          if (j == i) continue;
+          const float4 rj = __ldg(b.P4 + j);
+          float3 dr;
+          float d2;
+          if (edge_dr<DIM>(ri, rj, q, c, dr, d2)) pair(j, rj, dr, d2);
+        }
+      });
+    }
     float rho_new = rho_i, drhodt = 0.f;
     if (MODE == 0) {
       if (fluid) rho_new = ri.w * s0.s;
@@ -165,7 +284,7 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
     }
     float p_new = eos_p(rho_new, c);
     if (sph_gwbc && fluid) rho_new = eos_rho(p_new, c);
-    R4[i] = make_float4(rho_new, p_new, drhodt, 0.f);
+    R4[i] = make_float4(rho_new, p_new, drhodt, b.ETA[i]);
     if (!isfinite(rho_new) || !isfinite(p_new)) atomicOr(status, SPH_ERR_NONFINITE);
   }
   count_edges(ci, cnt, valid, edgecnt, cases, status);
@@ -175,9 +294,9 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
 // gwbc_fn (solver.py:431-530) for wall receivers: Shepard sums over fluid
 // senders of u, v, p and rho*dr; writes u, v (U4/V4 xyz) and R4 (rho, p).
 template <int DIM, int KER, bool KAHAN>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 4)
 k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
-       int mask_self, int free_slip, const float* g_arr, float4* R4) {
+       int free_slip, const float* g_arr, float4* R4, NList nl) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= N) return;
   const int meta = b.META[i];
@@ -185,14 +304,10 @@ k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const in
   const CaseDev& c = cases[case_of(meta)];
   const float4 ri = b.P4[i];
   Acc<KAHAN> sw, su[3], sv[3], sp, sr[3];
-  for_each_candidate<DIM>(c, cellid[i] - c.cell_off, start, [&](int j) {
-    if (mask_self && j == i) return;
+  for_each_neighbour<DIM>(N, i, ri, c, b.P4, cellid, start, nl,
+                          [&](int j, const float4& rj, const float3& dr, float d2) {
     if (tag_of(b.META[j]) != FLUID) return;
-    const float4 rj = b.P4[j];
-    if (!is_edge<DIM>(ri, rj, c)) return;
-    const float3 dr = pdisp3<DIM>(ri, rj, c);
-    const float d2 = sqd<DIM>(dr);
-    const float dist = d2 > 0.f ? __fsqrt_rn(d2) : 0.f;
+    const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
     const float w = kw<KER>(dist, c);
     const float4 Uj = b.U4[j], Vj = b.V4[j], Rj = R4[j];
     sw.add(w);
@@ -217,17 +332,17 @@ k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const in
   b.V4[i] = make_float4(2.f * Vi.x - vw.x, 2.f * Vi.y - vw.y, 2.f * Vi.z - vw.z, Vi.w);
   const float3 gi = g_ext<DIM>(c, ri, g_arr, b.ORIG[i]);
   const float pw = (sp.s + (gi.x * sr[0].s + gi.y * sr[1].s + gi.z * sr[2].s)) / den;
-  const float drhodt = R4[i].z;
-  R4[i] = make_float4(eos_rho(pw, c), pw, drhodt, 0.f);
+  const float4 Ri = R4[i];
+  R4[i] = make_float4(eos_rho(pw, c), pw, Ri.z, Ri.w);
 }
 
 // ------------------------------------------------------------------ force pass
 // SOLVER 0: standard SPH with transport-velocity stress; 1: Riemann SPH.
 template <int DIM, int KER, int SOLVER, bool KAHAN>
-__global__ void __launch_bounds__(kBlock)
+__global__ void __launch_bounds__(kBlock, 3)
 k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
-        int mask_self, int bc_trick, int free_slip, const float* g_arr, const float4* R4,
-        const float4* UT4, bool apply_bc, unsigned* status) {
+        int bc_trick, int free_slip, const float* g_arr, const float4* R4, const float4* UT4,
+        NList nl, bool apply_bc, unsigned* status) {
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (i >= N) return;
   const int meta = b.META[i];
@@ -239,8 +354,7 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
   const float3 ui = f3(b.U4[i]);
   const float3 vi = f3(b.V4[i]);
   const float4 Ri = R4[i];
-  const float rho_i = Ri.x, p_i = Ri.y;
-  const float eta_i = b.ETA[i];
+  const float rho_i = Ri.x, p_i = Ri.y, eta_i = Ri.w;
   const float Vi = m_i / rho_i;
   const float Vi2 = Vi * Vi;
   const float inv_mi = 1.0f / m_i;
@@ -251,26 +365,22 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
   const bool av = c.av_alpha != 0.0f;
   const float mask_i = (SOLVER == 1 && bc_trick && free_slip) ? (fluid_i ? 1.f : 0.f) : 1.f;
   Acc<KAHAN> ax, ay, az, tx, ty, tz;
-  for_each_candidate<DIM>(c, cellid[i] - c.cell_off, start, [&](int j) {
-    if (mask_self && j == i) return;
-    const float4 rj = b.P4[j];
-    if (!is_edge<DIM>(ri, rj, c)) return;
-    const float3 dr = pdisp3<DIM>(ri, rj, c);
-    const float d2 = sqd<DIM>(dr);
-    const float dist = d2 > 0.f ? __fsqrt_rn(d2) : 0.f;
+  for_each_neighbour<DIM>(N, i, ri, c, b.P4, cellid, start, nl,
+                          [&](int j, const float4& rj, const float3& dr, float d2) {
+    const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
     const float gw = kdw<KER>(dist, c);
     const float inv_d = 1.0f / (dist + kEps);
     const float4 Rj = R4[j];
-    const float rho_j = Rj.x, p_j = Rj.y, m_j = rj.w;
+    const float rho_j = Rj.x, p_j = Rj.y, eta_j = Rj.w, m_j = rj.w;
     const float Vj = m_j / rho_j;
     const float cc = (Vi2 + Vj * Vj) * inv_mi * gw * inv_d;
     const float3 uj = f3(b.U4[j]);
-    const int tj = tag_of(b.META[j]);
+    const float eta_ij = 2.f * eta_i * eta_j / (eta_i + eta_j + kEps);
+    int tj = FLUID;
+    if (SOLVER == 1 || av) tj = tag_of(b.META[j]);
     float3 a;
     if (SOLVER == 0) {
       const float3 vj = f3(b.V4[j]);
-      const float eta_j = b.ETA[j];
-      const float eta_ij = 2.f * eta_i * eta_j / (eta_i + eta_j + kEps);
       const float p_ij = (rho_j * p_i + rho_i * p_j) / (rho_i + rho_j);
       const float ki = dot3(wi, dr);
       const float kj = dot3(make_float3(vj.x - uj.x, vj.y - uj.y, vj.z - uj.z), dr);
@@ -302,8 +412,6 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
       }
       const float P_avg = 0.5f * (p_i + pR);
       const float rho_avg = 0.5f * (rho_i + rhoR);
-      const float eta_j = b.ETA[j];
-      const float eta_ij = 2.f * eta_i * eta_j / (eta_i + eta_j + kEps);
       float beta;
       if (c.eta_limiter == -1.0f) {
         beta = c.c_ref;
@@ -360,11 +468,12 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
   const int rie_shepard = rie && L.bc_trick && !L.free_slip;
   const int sph_gwbc = !rie && L.bc_trick;
   float4* ut = rie ? UT4 : nullptr;
+  NList nl{L.nbr, L.nbr_cnt, L.kmax};
 #define SPH_DENSITY(MODE)                                                                 \
   k_density<DIM, KER, MODE, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,  \
                                                          L.mask_self, rie_shepard,        \
-                                                         sph_gwbc, g_arr, R4, ut, edgecnt, \
-                                                         L.status)
+                                                         sph_gwbc, g_arr, R4, ut, nl,     \
+                                                         edgecnt, L.status)
   if (!L.rho_evol)
     SPH_DENSITY(0);
   else if (rie)
@@ -375,19 +484,19 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
   count_launch(L);
   mark(L, 2);
   if (sph_gwbc && has_walls) {
-    k_wall<DIM, KER, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start, L.mask_self,
-                                                  L.free_slip, g_arr, R4);
+    k_wall<DIM, KER, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start, L.free_slip,
+                                                  g_arr, R4, nl);
     count_launch(L);
   }
   mark(L, 3);
   if (rie)
     k_force<DIM, KER, 1, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,
-                                                        L.mask_self, L.bc_trick, L.free_slip,
-                                                        g_arr, R4, UT4, apply_bc, L.status);
+                                                        L.bc_trick, L.free_slip, g_arr, R4, UT4,
+                                                        nl, apply_bc, L.status);
   else
     k_force<DIM, KER, 0, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,
-                                                        L.mask_self, L.bc_trick, L.free_slip,
-                                                        g_arr, R4, nullptr, apply_bc, L.status);
+                                                        L.bc_trick, L.free_slip, g_arr, R4,
+                                                        nullptr, nl, apply_bc, L.status);
   count_launch(L);
   mark(L, 4);
 }

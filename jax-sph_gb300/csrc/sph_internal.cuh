@@ -27,6 +27,11 @@ constexpr int kTagMask = 0xF;
 
 enum Tag { FLUID = 0, SOLID_WALL = 1, MOVING_WALL = 2, DIRICHLET_WALL = 3 };
 
+// Neighbour-list slots per particle. The density pass stages them in shared
+// memory (kListSlots * 256 threads * 4 B = 40 KB per block); a particle with
+// more neighbours makes the passes walk its cells instead.
+constexpr int kListSlots = 40;
+
 // Per-case constants, all rounded to float32 the way the reference's
 // float32 program sees them.
 struct CaseDev {
@@ -52,6 +57,12 @@ struct CaseDev {
   float g[3], g_lo, g_hi;
   int bc_kind;
   float u_lid[3];
+  // Fast membership test (every axis has >= 5 cells, so adjacent-cell images
+  // are minimum images): squared distances below cut_lo are edges, above
+  // cut_hi are not, and only the band between takes the reference metric.
+  int fast;
+  float cut_lo, cut_hi;
+  float inv_box[3];
 };
 
 struct Buffers {
@@ -240,6 +251,117 @@ __device__ __forceinline__ void for_each_candidate(const CaseDev& c, int cell_lo
   }
 }
 
+// Like for_each_candidate, but visits ranges [j0, j1) together with the
+// periodic shift s (per axis -L, 0 or +L) that maps the range's particles to
+// their image next to the receiving cell: f(j0, j1, s).
+template <int DIM, typename F>
+__device__ __forceinline__ void for_each_range(const CaseDev& c, int cell_local,
+                                               const int* __restrict__ start, F&& f) {
+  const int nx = c.nc[0], ny = c.nc[1], nz = (DIM == 3) ? c.nc[2] : 1;
+  const int cx = cell_local % nx;
+  const int t = cell_local / nx;
+  const int cy = t % ny;
+  const int cz = (DIM == 3) ? t / ny : 0;
+  const int* cs = start + c.cell_off;
+  const int zr = (DIM == 3 && nz >= 3) ? 1 : 0;
+  const int yr = (ny >= 3) ? 1 : 0;
+  for (int dz = -zr; dz <= zr; ++dz) {
+    int zz = cz + dz;
+    float sz = 0.f;
+    if (zz < 0) { zz += nz; sz = -c.box[2]; }
+    else if (zz >= nz) { zz -= nz; sz = c.box[2]; }
+    for (int dy = -yr; dy <= yr; ++dy) {
+      int yy = cy + dy;
+      float sy = 0.f;
+      if (yy < 0) { yy += ny; sy = -c.box[1]; }
+      else if (yy >= ny) { yy -= ny; sy = c.box[1]; }
+      const int row = (zz * ny + yy) * nx;
+      // up to two x-ranges per row (a second one where the row wraps); the
+      // visitor is instantiated once, inside the loop
+      int a0 = row, b0 = row + nx, a1 = row, b1 = row;
+      float s1 = 0.f;
+      if (nx >= 3) {
+        if (cx == 0) {
+          b0 = row + 2; a1 = row + nx - 1; b1 = row + nx; s1 = -c.box[0];
+        } else if (cx == nx - 1) {
+          a0 = row + nx - 2; a1 = row; b1 = row + 1; s1 = c.box[0];
+        } else {
+          a0 = row + cx - 1; b0 = row + cx + 2;
+        }
+      }
+#pragma unroll 1
+      for (int r = 0; r < 2; ++r) {
+        const int a = r ? a1 : a0, e = r ? b1 : b0;
+        if (e > a) f(cs[a], cs[e], make_float3(r ? s1 : 0.f, sy, sz));
+      }
+    }
+  }
+}
+
+// Membership of edge (receiver ri, sender rj) with the fast test when the
+// case allows it; q = ri - s for the sender's range shift s. On success
+// returns true and dr = r_i - r_j (minimum image) and its squared norm.
+template <int DIM>
+__device__ __forceinline__ bool edge_dr(const float4& ri, const float4& rj, const float3& q,
+                                        const CaseDev& c, float3& dr, float& d2) {
+  if (c.fast) {
+    dr.x = q.x - rj.x;
+    dr.y = q.y - rj.y;
+    dr.z = (DIM == 3) ? q.z - rj.z : 0.f;
+    d2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
+    if (d2 >= c.cut_hi) return false;
+    if (d2 > c.cut_lo && !is_edge<DIM>(ri, rj, c)) return false;
+    return true;
+  }
+  if (!is_edge<DIM>(ri, rj, c)) return false;
+  dr = pdisp3<DIM>(ri, rj, c);
+  d2 = sqd<DIM>(dr);
+  return true;
+}
+
+// The reference metric, out of line: only candidates in the narrow band
+// around the cutoff (or every candidate of a case without the fast test)
+// reach it, so the hot loop stays small.
+template <int DIM>
+__device__ __noinline__ bool exact_edge(float4 ri, float4 rj, const CaseDev* c) {
+  return is_edge<DIM>(ri, rj, *c);
+}
+
+// Branch-free membership for the candidate walk: d2 of the shifted
+// difference against the band [lo, hi) (lo = -1, hi = inf for a case
+// without the fast test), the reference metric inside the band.
+template <int DIM>
+__device__ __forceinline__ bool edge_walk(const float4& ri, const float4& rj, const float3& q,
+                                          float lo, float hi, const CaseDev* c) {
+  const float dx = q.x - rj.x, dy = q.y - rj.y;
+  float d2 = fmaf(dx, dx, dy * dy);
+  if (DIM == 3) {
+    const float dz = q.z - rj.z;
+    d2 = fmaf(dz, dz, d2);
+  }
+  bool in = d2 < lo;
+  if (!in && d2 < hi) in = exact_edge<DIM>(ri, rj, c);
+  return in;
+}
+
+// Minimum-image r_i - r_j of a pair already known to be an edge.
+template <int DIM>
+__device__ __forceinline__ void pair_dr(const float4& ri, const float4& rj, const CaseDev& c,
+                                        float3& dr, float& d2) {
+  if (c.fast) {
+    dr.x = ri.x - rj.x;
+    dr.y = ri.y - rj.y;
+    dr.z = (DIM == 3) ? ri.z - rj.z : 0.f;
+    dr.x = fmaf(-c.box[0], rintf(dr.x * c.inv_box[0]), dr.x);
+    dr.y = fmaf(-c.box[1], rintf(dr.y * c.inv_box[1]), dr.y);
+    if (DIM == 3) dr.z = fmaf(-c.box[2], rintf(dr.z * c.inv_box[2]), dr.z);
+    d2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
+  } else {
+    dr = pdisp3<DIM>(ri, rj, c);
+    d2 = sqd<DIM>(dr);
+  }
+}
+
 // Compensated accumulation (Kahan) selected at compile time.
 template <bool KAHAN>
 struct Acc {
@@ -267,6 +389,9 @@ struct LaunchCtx {
   int n_cases;
   const CaseDev* cases;   // device
   unsigned* status;       // device
+  int* nbr;               // per-step neighbour list [kmax][N]
+  int* nbr_cnt;           // neighbours per particle (self excluded)
+  int kmax;
   int* launches;          // optional host counter of kernel launches
   cudaEvent_t* ev;        // optional phase events: bin start, bin end, density end,
                           // wall end, force end

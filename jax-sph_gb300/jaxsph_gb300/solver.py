@@ -139,13 +139,12 @@ class WCSPH:
         return e, st
 
     @staticmethod
-    def _result(state, st, out):
+    def _result(state, out):
         res = dict(state)
         for k, v in out.items():
             res[k] = v
         for k in ("tag", "mass", "eta"):
             res[k] = state[k]
-        res["r"] = st["r"]
         return res
 
     # ---------------------------------------------------------------- API
@@ -164,7 +163,7 @@ class WCSPH:
             e.forward()
             out = empty_outputs(st)
             e.get_state(out)
-            return self._result(state, st, out)
+            return self._result(state, out)
 
         forward.__wcsph__ = self
         return forward
@@ -185,7 +184,7 @@ class WCSPH:
         code = e.read_status(clear=True)
         if code & (_lib.ERR_INVALID_ARG | _lib.ERR_CUDA):
             raise _lib.SphError(code, "step failed")
-        res = self._result(state, st, out)
+        res = self._result(state, out)
         if bc_fn is not None and bc_spec is None:
             res = bc_fn(res)
         if nl_fns.moved(res["r"], neighbors):
