@@ -200,6 +200,26 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream);
 /* Read (and optionally clear) the device status word. Synchronizes `stream`. */
 int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream);
 
+/* Allocation-free neighbour list (no counterpart in the reference: it exists
+ * for callers that cannot call cudaMalloc, such as a host framework that owns
+ * the whole device memory pool, or code that must not allocate after start-up).
+ * Same edges, order and padding as sph_nl_edges for `n` positions r (device,
+ * (n, dim) float32) in a periodic box with the reference's cutoff test; no
+ * handle and no allocation: all scratch lives in one fixed file-scope device
+ * array of about 4 MB, so n <= SPH_NOALLOC_MAX_PARTICLES and the cell grid
+ * must have <= SPH_NOALLOC_MAX_CELLS cells (larger inputs are rejected with
+ * SPH_ERR_INVALID_ARG before any GPU work). The array is shared by all calls
+ * on a device: calls that overlap on the GPU race and must be ordered by the
+ * caller. The first call on a device looks up the array's address
+ * (cudaGetSymbolAddress, with that device current) and should come before any
+ * stream capture. *count_dev receives the edge count; *status_dev (optional,
+ * device) the call's status bits. */
+#define SPH_NOALLOC_MAX_PARTICLES 65536
+#define SPH_NOALLOC_MAX_CELLS 65536
+int sph_nl_edges_noalloc(int32_t dim, const double* box, double r_cutoff, int32_t mask_self,
+                         const float* r, int64_t n, int32_t* idx, int64_t capacity,
+                         int64_t* count_dev, uint32_t* status_dev, void* stream);
+
 /* Float64 global diagnostics per case, computed on the GPU in double
  * precision: out[c*8 + k] = {mass, mom_x, mom_y, mom_z, E_kin, u_max, rho_min,
  * rho_max} of case c (fluid particles; E_kin follows jax_sph/utils.py:128-133).

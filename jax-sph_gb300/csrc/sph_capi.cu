@@ -90,11 +90,11 @@ struct SphHandle {
   }
 };
 
-namespace {
+void sph::set_last_error(const std::string& msg) { g_last_error = msg; }
 
 // Per-case float32 constants, rounded the way the reference's float32
 // program rounds its Python-float parameters (weak types become float32).
-int make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long long cell_off,
+int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long long cell_off,
               CaseDev& c, std::string& err) {
   std::memset(&c, 0, sizeof(c));
   const int dim = cfg.dim;
@@ -211,6 +211,8 @@ int make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long lon
   }
   return 0;
 }
+
+namespace {
 
 int upload_cases(SphHandle* h, cudaStream_t st) {
   cudaError_t e = cudaMemcpyAsync(h->dc, h->hc.data(), sizeof(CaseDev) * h->n_cases,

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <string>
+
 #include "../../include/sph_gb300.h"
 
 namespace sph {
@@ -206,6 +208,29 @@ __device__ __forceinline__ float3 bc_acc(float3 a, int tag, const CaseDev& c) {
 }
 __device__ __forceinline__ float bc_p(float p, int tag, const CaseDev& c) {
   return (c.bc_kind == SPH_BC_SOLID_ZERO_P && tag == SOLID_WALL) ? 0.0f : p;
+}
+
+// Cell of a position: hash = sum(int32(r / cell_size) * mult)
+// (jax_md/partition.py:367-368), axes with a single cell contribute 0.
+template <int DIM>
+__device__ __forceinline__ int cell_hash(const float4& r, const CaseDev& c, unsigned* status) {
+  float rr[3] = {r.x, r.y, r.z};
+  int h = 0;
+  bool finite = true;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    finite &= isfinite(rr[d]);
+    int ix = c.nc[d] > 1 ? __float2int_rz(__fdiv_rn(rr[d], c.cell_size[d])) : 0;
+    h += ix * c.mult[d];
+  }
+  if (!finite) {
+    atomicOr(status, SPH_ERR_NONFINITE);
+    h = 0;
+  } else if (h < 0 || h >= c.ncell) {
+    atomicOr(status, SPH_WARN_BOX_EDGE);
+    h = h < 0 ? 0 : c.ncell - 1;
+  }
+  return h;
 }
 
 // Visit every particle of the 3^d periodic neighbour cells of `cell_local`
@@ -427,5 +452,12 @@ void launch_forward(const LaunchCtx& L, Buffers b, const float4* R4, float4* R4w
                     const float* g_arr, bool apply_bc, bool has_walls);
 
 size_t scan_tmp_ints(long long n);
+
+// sph_capi.cu: per-case device constants from the ABI parameters; returns
+// non-zero and sets `err` on invalid input.
+int make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long long cell_off,
+              CaseDev& c, std::string& err);
+// sph_capi.cu: the message sph_last_error returns on this host thread.
+void set_last_error(const std::string& msg);
 
 }  // namespace sph

@@ -126,29 +126,6 @@ __device__ __forceinline__ void kick_drift(float4& r, float3& u, float3& v, cons
   }
 }
 
-// Cell of a position: hash = sum(int32(r / cell_size) * mult)
-// (jax_md/partition.py:367-368), axes with a single cell contribute 0.
-template <int DIM>
-__device__ __forceinline__ int cell_hash(const float4& r, const CaseDev& c, unsigned* status) {
-  float rr[3] = {r.x, r.y, r.z};
-  int h = 0;
-  bool finite = true;
-#pragma unroll
-  for (int d = 0; d < DIM; ++d) {
-    finite &= isfinite(rr[d]);
-    int ix = c.nc[d] > 1 ? __float2int_rz(__fdiv_rn(rr[d], c.cell_size[d])) : 0;
-    h += ix * c.mult[d];
-  }
-  if (!finite) {
-    atomicOr(status, SPH_ERR_NONFINITE);
-    h = 0;
-  } else if (h < 0 || h >= c.ncell) {
-    atomicOr(status, SPH_WARN_BOX_EDGE);
-    h = h < 0 ? 0 : c.ncell - 1;
-  }
-  return h;
-}
-
 template <int DIM>
 __global__ void k_hash_count(long long N, Buffers in, const float4* R4, const CaseDev* cases,
                              int* count, int* keyc, int* keys, unsigned* status, bool drift,

@@ -65,7 +65,7 @@ class SphNLCapacity(ctypes.Structure):
 EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sph_update_cases",
            "sph_set_state", "sph_get_state", "sph_nl_allocate", "sph_nl_set_capacity",
            "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_step_launch_count",
-           "sph_profile_step", "sph_read_status", "sph_diagnostics"]
+           "sph_profile_step", "sph_read_status", "sph_diagnostics", "sph_nl_edges_noalloc"]
 
 _LIB = None
 
@@ -99,6 +99,9 @@ def load(build_if_missing=True):
     lib.sph_profile_step.argtypes = [V, ctypes.c_int32, P(ctypes.c_float), V]
     lib.sph_read_status.argtypes = [V, P(ctypes.c_uint32), ctypes.c_int32, V]
     lib.sph_diagnostics.argtypes = [V, V, V]
+    lib.sph_nl_edges_noalloc.argtypes = [ctypes.c_int32, P(ctypes.c_double), ctypes.c_double,
+                                         ctypes.c_int32, V, ctypes.c_int64, V, ctypes.c_int64,
+                                         V, V, V]
     for name in EXPORTS:
         if name not in ("sph_abi_version", "sph_last_error"):
             getattr(lib, name).restype = I
