@@ -46,6 +46,12 @@ BIN_BYTES = 104           # binning + kick-drift: reads r,m,u,v,dudt,dvdt,eta,ta
 PHASES = ("binning+kick-drift", "density", "wall", "force")
 PHASE_KERNELS = ("k_hash_count/k_tile_scan/k_scatter/k_permute", "k_density", "k_wall", "k_force")
 PHASE_BYTES = (BIN_BYTES, DENSITY_BYTES, 0, FORCE_BYTES)
+# DRAM bytes per particle of one launch (dram__bytes_read.sum + dram__bytes_write.sum)
+# and FMA-pipe utilisation measured with ncu on the 128^3 case of the same kernels
+# (profiles/k_density_tgv3d_128.md, profiles/k_force_tgv3d_128.md); traffic grows
+# in proportion to the particle count, so it scales to 64^3 per particle.
+PHASE_TRAFFIC = (None, 153.4, None, 221.3)
+PHASE_FP32_PIPE = (None, 0.246, None, 0.267)
 
 
 def dist_env():
@@ -272,7 +278,9 @@ def gpu_arm(args, ws, rank, local):
         "roofline": {"bound": "hbm", "kernel": PHASE_KERNELS[dom], "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
                      "peak_source": peak_src, "alg_bytes_per_particle": PHASE_BYTES[dom],
-                     "traffic": None,
+                     "traffic": (PHASE_TRAFFIC[dom] * n if PHASE_TRAFFIC[dom] else None),
+                     "traffic_source": "ncu dram bytes per particle at 128^3, scaled to n",
+                     "fp32_pipe_frac": PHASE_FP32_PIPE[dom],
                      "step": {"alg_bytes_per_particle": STEP_BYTES, "achieved": step_achieved,
                               "frac": step_achieved / hbm}},
         "phases_ms": dict(zip(PHASES, phases)),
