@@ -222,6 +222,57 @@ def e2e_rate(setup, steps, device):
     return setup.n / t, h2d, d2h, t
 
 
+def timed_steps(sim, steps):
+    """Per-step CUDA-event times (ms) of a resident Simulation."""
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    torch.cuda.synchronize()
+    for k in range(steps):
+        starts[k].record()
+        sim.engine.step(1)
+        ends[k].record()
+    torch.cuda.synchronize()
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)]
+
+
+def batched_form(device, steps, n_instances=256):
+    """The batched form on its own workload: 256 cavity/channel instances with
+    log-uniform particle counts as one resident batch (one CUDA graph per step,
+    autotuned block size) versus the same instances run one after another on
+    the plain per-instance path."""
+    from jaxsph_gb300 import cases, simulate
+
+    batch = cases.cavity_channel_batch(n_instances, seed=0)
+    n_total = sum(s.n for s in batch)
+    sim = simulate.Simulation(batch, device=device, autotune=True)
+    sim.run(3, check_every=1)
+    ms = timed_steps(sim, steps)  # the batch state (~1 GB) exceeds L2
+    batched = n_total * steps / (sum(ms) * 1e-3)
+    plain_ms, plain_steps = 0.0, max(3, steps // 10)
+    diffs = []
+    for s in batch:
+        one = simulate.Simulation(s, device=device)
+        one.run(3, check_every=1)
+        plain_ms += sum(timed_steps(one, plain_steps)) / plain_steps
+        del one
+    # bit-for-bit agreement of batched and plain runs on a sample of instances
+    check = simulate.Simulation(batch, device=device)
+    check.run(5)
+    ref_states = check.state()
+    for k in (0, 1, n_instances // 2, n_instances - 1):
+        one = simulate.Simulation(batch[k], device=device)
+        one.run(5)
+        a, b = ref_states[k], one.state()[0]
+        diffs.append(max(float((a[x].double() - b[x].double()).abs().max()) for x in ("r", "u", "rho")))
+    per_instance = n_total / (plain_ms * 1e-3)
+    return {"workload": f"{n_instances} lid-driven cavities / Poiseuille channels (2D, QSK, SPH, "
+                        f"wall BC), fluid particles log-uniform 1e3-4e4, {n_total:,} particles",
+            "value": batched, "unit": UNIT, "steps": steps, "block_size": sim.block_size,
+            "per_instance_value": per_instance, "speedup_vs_per_instance": batched / per_instance,
+            "max_abs_diff_vs_per_instance": max(diffs),
+            "launches_per_step": sim.engine.launch_count()}
+
+
 def gpu_arm(args, ws, rank, local):
     from jaxsph_gb300 import cases, simulate
 
@@ -293,6 +344,8 @@ def gpu_arm(args, ws, rank, local):
         line["e2e"] = {"value": rate, "unit": UNIT, "h2d_bytes_per_step": h2d,
                        "d2h_bytes_per_step": d2h,
                        "path": "si_euler drop-in advance, pinned host state in/out every step"}
+    if rank == 0 and not args.no_forms:
+        line["forms"] = {"batched": batched_form(device, 100)}
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, steps, secs, n_cpu = cpu_oracle_rate(64, 2, 30.0, threads)
@@ -306,11 +359,13 @@ def gpu_arm(args, ws, rank, local):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=500)
+    ap.add_argument("--steps", type=int, default=2000)
     ap.add_argument("--warmup", type=int, default=10)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--no-cpu", action="store_true")
+    ap.add_argument("--no-forms", action="store_true",
+                    help="skip the batched/adjoint form measurements on their own workloads")
     ap.add_argument("--n-side", type=int, default=64,
                     help="particles per side of the 3D TGV lattice (64 = the benchmark case)")
     args = ap.parse_args()

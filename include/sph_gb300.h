@@ -189,6 +189,9 @@ int sph_forward(SphHandle* h, void* stream);
  * update (rebuilt every step), forward, bc_fn. Replays a CUDA graph. */
 int sph_step(SphHandle* h, int32_t nsteps, void* stream);
 
+/* Threads per block of the density, wall and force passes (a multiple of 32
+ * in [32, 256]; default 256). A tuning knob: results do not depend on it. */
+int sph_set_block_size(SphHandle* h, int32_t threads);
 /* Kernel launches issued by one si_euler step of this handle. */
 int sph_step_launch_count(SphHandle* h, int32_t* count);
 /* Run `nsteps` steps eagerly, timing their phases with CUDA events on

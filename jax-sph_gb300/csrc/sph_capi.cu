@@ -45,6 +45,7 @@ struct SphHandle {
   int *rowcnt = nullptr, *rowoff = nullptr;
   int *nbr = nullptr, *nbr_cnt = nullptr;
   int kmax = kListSlots;  // neighbour-list slots per particle
+  int block = 256;        // threads per block of the forward passes
   unsigned* status = nullptr;
   unsigned long long* edgecnt = nullptr;
   const float* g_arr = nullptr;
@@ -84,6 +85,7 @@ struct SphHandle {
     L.nbr = nbr;
     L.nbr_cnt = nbr_cnt;
     L.kmax = kmax;
+    L.block = block;
     L.launches = const_cast<int*>(&launch_count);
     L.ev = ev;
     return L;
@@ -553,6 +555,15 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream) {
     h->cur = 1 - h->cur;
     --nsteps;
   }
+  return 0;
+}
+
+int sph_set_block_size(SphHandle* h, int32_t threads) {
+  if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
+  if (threads < 32 || threads > 256 || threads % 32)
+    return fail((int)SPH_ERR_INVALID_ARG, "block size must be a multiple of 32 in [32, 256]");
+  h->block = threads;
+  drop_graph(h);
   return 0;
 }
 

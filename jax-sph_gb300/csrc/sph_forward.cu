@@ -122,8 +122,9 @@ __global__ void __launch_bounds__(kBlock, 4)
 k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
           int mask_self, int rie_shepard, int sph_gwbc, const float* g_arr, float4* R4,
           float4* UT4, NList nl, unsigned long long* edgecnt, unsigned* status) {
-  __shared__ int s_nbr[kListSlots][kBlock];
+  extern __shared__ int s_nbr[];  // [kListSlots][blockDim.x]
   const int tid = threadIdx.x;
+  const int bs = blockDim.x;
   long long i = blockIdx.x * (long long)blockDim.x + tid;
   bool valid = i < N;
   int ci = 0, cnt = 0;
@@ -153,9 +154,9 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
         self_edge |= (ea && j == i) || (eb && j + 1 == i);
         ea = ea && j != i;
         eb = eb && j + 1 != i;
-        s_nbr[m < kmax ? m : kmax - 1][tid] = j;
+        s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = j;
         m += ea;
-        s_nbr[m < kmax ? m : kmax - 1][tid] = j + 1;
+        s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = j + 1;
         m += eb;
       }
     });
@@ -232,15 +233,15 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
     };
     if (m <= kmax) {
       if (!need_pairs) {
-        for (int k = 0; k < m; ++k) nl.nbr[(long long)k * N + i] = s_nbr[k][tid];
+        for (int k = 0; k < m; ++k) nl.nbr[(long long)k * N + i] = s_nbr[k * bs + tid];
       } else {
-        int jn = m > 0 ? s_nbr[0][tid] : 0;
+        int jn = m > 0 ? s_nbr[tid] : 0;
         float4 rn = m > 0 ? __ldg(b.P4 + jn) : ri;
         for (int k = 0; k < m; ++k) {
           const int j = jn;
           const float4 rj = rn;
           if (k + 1 < m) {
-            jn = s_nbr[k + 1][tid];
+            jn = s_nbr[(k + 1) * bs + tid];
             rn = __ldg(b.P4 + jn);
           }
           nl.nbr[(long long)k * N + i] = j;
@@ -462,7 +463,9 @@ template <int DIM, int KER, bool KAHAN>
 void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int* cellid,
                const int* start, unsigned long long* edgecnt, const float* g_arr, bool apply_bc,
                bool has_walls) {
-  const int g = nblocks(L.N);
+  const int bt = L.block > 0 ? L.block : kBlock;
+  const int g = nblocks(L.N, bt);
+  const size_t smem = sizeof(int) * kListSlots * bt;
   cudaStream_t st = L.stream;
   const bool rie = L.solver == SPH_SOLVER_RIE;
   const int rie_shepard = rie && L.bc_trick && !L.free_slip;
@@ -470,7 +473,7 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
   float4* ut = rie ? UT4 : nullptr;
   NList nl{L.nbr, L.nbr_cnt, L.kmax};
 #define SPH_DENSITY(MODE)                                                                 \
-  k_density<DIM, KER, MODE, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,  \
+  k_density<DIM, KER, MODE, KAHAN><<<g, bt, smem, st>>>(L.N, b, L.cases, cellid, start,  \
                                                          L.mask_self, rie_shepard,        \
                                                          sph_gwbc, g_arr, R4, ut, nl,     \
                                                          edgecnt, L.status)
@@ -484,17 +487,17 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
   count_launch(L);
   mark(L, 2);
   if (sph_gwbc && has_walls) {
-    k_wall<DIM, KER, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start, L.free_slip,
+    k_wall<DIM, KER, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start, L.free_slip,
                                                   g_arr, R4, nl);
     count_launch(L);
   }
   mark(L, 3);
   if (rie)
-    k_force<DIM, KER, 1, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,
+    k_force<DIM, KER, 1, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
                                                         L.bc_trick, L.free_slip, g_arr, R4, UT4,
                                                         nl, apply_bc, L.status);
   else
-    k_force<DIM, KER, 0, KAHAN><<<g, kBlock, 0, st>>>(L.N, b, L.cases, cellid, start,
+    k_force<DIM, KER, 0, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
                                                         L.bc_trick, L.free_slip, g_arr, R4,
                                                         nullptr, nl, apply_bc, L.status);
   count_launch(L);

@@ -417,6 +417,7 @@ struct LaunchCtx {
   int* nbr;               // per-step neighbour list [kmax][N]
   int* nbr_cnt;           // neighbours per particle (self excluded)
   int kmax;
+  int block;              // threads per block of the forward passes (<= 256)
   int* launches;          // optional host counter of kernel launches
   cudaEvent_t* ev;        // optional phase events: bin start, bin end, density end,
                           // wall end, force end

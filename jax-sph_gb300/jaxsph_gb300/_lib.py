@@ -64,7 +64,8 @@ class SphNLCapacity(ctypes.Structure):
 
 EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sph_update_cases",
            "sph_set_state", "sph_get_state", "sph_nl_allocate", "sph_nl_set_capacity",
-           "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_step_launch_count",
+           "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_set_block_size",
+           "sph_step_launch_count",
            "sph_profile_step", "sph_read_status", "sph_diagnostics", "sph_nl_edges_noalloc"]
 
 _LIB = None
@@ -95,6 +96,7 @@ def load(build_if_missing=True):
     lib.sph_nl_edges.argtypes = [V, V, ctypes.c_int64, V, V]
     lib.sph_forward.argtypes = [V, V]
     lib.sph_step.argtypes = [V, ctypes.c_int32, V]
+    lib.sph_set_block_size.argtypes = [V, ctypes.c_int32]
     lib.sph_step_launch_count.argtypes = [V, P(ctypes.c_int32)]
     lib.sph_profile_step.argtypes = [V, ctypes.c_int32, P(ctypes.c_float), V]
     lib.sph_read_status.argtypes = [V, P(ctypes.c_uint32), ctypes.c_int32, V]
@@ -213,6 +215,9 @@ class Engine:
 
     def step(self, nsteps=1):
         _check(self.lib.sph_step(self.h, int(nsteps), _stream()))
+
+    def set_block_size(self, threads):
+        _check(self.lib.sph_set_block_size(self.h, int(threads)))
 
     def launch_count(self):
         c = ctypes.c_int32(0)

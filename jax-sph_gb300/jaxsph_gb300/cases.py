@@ -299,4 +299,33 @@ def poiseuille(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, g_ext_magni
                    g_ext=g, bc=BC(_lib.BC_SOLID_ZERO), dtype=dtype, **kw)
 
 
+def cavity_channel_batch(n_instances=256, seed=0, n_min=1000, n_max=40000, re_min=10.0,
+                         re_max=1000.0, dx_min=0.004, dx_max=0.02, dtype=np.float32, t_end=1.0):
+    """Independent lid-driven cavities and Poiseuille channels for the batched form.
+
+    Instances alternate LDC / PF. Fluid particle counts are drawn log-uniform
+    in [n_min, n_max] and set the lattice spacing (cavity: (1/dx)^2 fluid
+    particles, channel: 0.4/dx^2), clamped to [dx_min, dx_max]; Reynolds
+    numbers are uniform in [re_min, re_max]. Cavity: eta = u_lid/Re (lid
+    speed 1, side 1). Channel: u_max = 1.25, eta = u_max/Re and the Morris
+    body force g = 8 eta u_max / H^2 (H = 1). Every instance uses its own CFL
+    time step; all share the SPH solver, QSK kernel and the wall BC.
+    """
+    rng = np.random.default_rng(seed)
+    out = []
+    for k in range(n_instances):
+        n_target = float(np.exp(rng.uniform(np.log(n_min), np.log(n_max))))
+        re = float(rng.uniform(re_min, re_max))
+        if k % 2 == 0:
+            dx = float(np.clip(1.0 / np.sqrt(n_target), dx_min, dx_max))
+            out.append(lid_driven_cavity(dx=dx, viscosity=1.0 / re, dtype=dtype, t_end=t_end))
+        else:
+            dx = float(np.clip(np.sqrt(0.4 / n_target), dx_min, dx_max))
+            u_max = 1.25
+            eta = u_max / re
+            out.append(poiseuille(dx=dx, viscosity=eta, u_ref=u_max,
+                                  g_ext_magnitude=8.0 * eta * u_max, dtype=dtype, t_end=t_end))
+    return out
+
+
 CASES = {"tgv": tgv, "db": dam_break, "ldc": lid_driven_cavity, "pf": poiseuille}

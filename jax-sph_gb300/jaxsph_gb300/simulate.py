@@ -49,7 +49,7 @@ class Simulation:
     """
 
     def __init__(self, setups, kahan=False, mask_self=False, capacity_multiplier=1.25,
-                 device="cuda"):
+                 device="cuda", autotune=False, block_size=None):
         if not isinstance(setups, (list, tuple)):
             setups = [setups]
         _lib.require_cuda()
@@ -72,7 +72,16 @@ class Simulation:
         self.sizes = [s.n for s in self.setups]
         self.dim = self.setups[0].dim
         self.steps_done = 0
+        self.block_size = 256
         self.load([s.state for s in self.setups])
+        if block_size is not None:
+            self.engine.set_block_size(block_size)
+            self.block_size = int(block_size)
+        elif autotune:
+            from . import autotune as _at
+
+            self.block_size, self.tuning = _at.tune(self.engine)
+            self.load([s.state for s in self.setups])  # tuning ran steps: start over
 
     def load(self, states):
         parts = [prepare_state(st, self.dim, self.device) for st in states]

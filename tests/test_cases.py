@@ -61,6 +61,18 @@ def test_poiseuille_band_force():
     assert torch.all(g[fluid, 0] == 1000.0) and torch.all(g[~fluid, 0] == 0.0)
 
 
+def test_cavity_channel_batch_shapes():
+    batch = cases.cavity_channel_batch(8, seed=0)
+    ns = [s.n for s in batch]
+    assert [s.name for s in batch] == ["ldc", "pf"] * 4
+    assert min(ns) > 500 and max(ns) < 60000
+    for s in batch:
+        assert 0.004 - 1e-12 <= s.dx <= 0.02 + 1e-12
+    pf = batch[1]
+    eta = pf.viscosity
+    assert pf.g_ext_fn.spec["g"][0] == pytest.approx(8 * eta * 1.25)
+
+
 @pytest.mark.parametrize("make", [lambda: cases.dam_break(dx=0.05),
                                   lambda: cases.lid_driven_cavity(dx=0.05),
                                   lambda: cases.poiseuille(dx=0.05)])
