@@ -200,6 +200,22 @@ int sph_step_launch_count(SphHandle* h, int32_t* count);
  * Host-synchronous; the steps advance the state like sph_step. */
 int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream);
 
+/* Differentiable form: hand-written reverse of si_euler steps with the
+ * neighbour list frozen per step, the way the reference differentiates a
+ * rollout with jax.grad(..., allow_int=True) (notebooks/iclr24_grads.ipynb,
+ * notebooks/iclr24_inverse.ipynb). Covers one case of the SPH solver with
+ * density summation, tvf = 0, no wall BC and no artificial viscosity.
+ * sph_adjoint_init allocates a tape of `slots` steps. sph_tape_record saves
+ * the forward data of the step just taken by sph_step into a slot.
+ * sph_adjoint_step maps the adjoints (lam_r, lam_u, lam_a_in) of a recorded
+ * step's outputs r, u, dudt to those of its inputs (lam_r, lam_u updated in
+ * place, lam_a_out). Adjoint arrays are (n, dim) float32 device arrays in the
+ * original particle order; lam_a_in and lam_a_out must differ. */
+int sph_adjoint_init(SphHandle* h, int32_t slots);
+int sph_tape_record(SphHandle* h, int32_t slot, void* stream);
+int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u,
+                     const float* lam_a_in, float* lam_a_out, void* stream);
+
 /* Read (and optionally clear) the device status word. Synchronizes `stream`. */
 int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream);
 

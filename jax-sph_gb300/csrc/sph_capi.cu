@@ -55,6 +55,13 @@ struct SphHandle {
   const float* graph_g_arr = nullptr;
   int launch_count = 0;       // kernel launches of the last step
   cudaEvent_t* ev = nullptr;  // phase events while profiling
+  // adjoint tape: per recorded step the sorted order, P4, U4, R4 and the
+  // neighbour list of its forward pass
+  int tape_slots = 0;
+  int* t_orig = nullptr;
+  float4 *t_P4 = nullptr, *t_U4 = nullptr, *t_R4 = nullptr;
+  int *t_nbr = nullptr, *t_cnt = nullptr;
+  float* t_mu = nullptr;
   std::vector<void*> allocs;
 
   template <typename T>
@@ -596,6 +603,62 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) {
   }
   for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
   return rc;
+}
+
+int sph_adjoint_init(SphHandle* h, int32_t slots) {
+  if (!h || slots <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
+  const SphConfig& c = h->cfg;
+  if (c.solver != SPH_SOLVER_SPH || c.is_rho_evol || c.is_bc_trick || h->n_cases != 1)
+    return fail((int)SPH_ERR_INVALID_ARG,
+                "the adjoint covers one case of the SPH solver with density summation and "
+                "no wall boundary condition");
+  const CaseDev& cd = h->hc[0];
+  if (cd.cv != 0.0f || cd.av_alpha != 0.0f)
+    return fail((int)SPH_ERR_INVALID_ARG, "the adjoint needs tvf = 0 and no artificial viscosity");
+  if (h->tape_slots) return fail((int)SPH_ERR_INVALID_ARG, "adjoint tape already initialised");
+  const long long N = h->N;
+  int rc = h->alloc(&h->t_orig, (size_t)slots * N) | h->alloc(&h->t_P4, (size_t)slots * N) |
+           h->alloc(&h->t_U4, (size_t)slots * N) | h->alloc(&h->t_R4, (size_t)slots * N) |
+           h->alloc(&h->t_nbr, (size_t)slots * h->kmax * N) |
+           h->alloc(&h->t_cnt, (size_t)slots * N) | h->alloc(&h->t_mu, N);
+  if (rc) return rc;
+  h->tape_slots = slots;
+  return 0;
+}
+
+int sph_tape_record(SphHandle* h, int32_t slot, void* stream) {
+  if (!h || slot < 0 || slot >= h->tape_slots)
+    return fail((int)SPH_ERR_INVALID_ARG, "tape slot out of range");
+  if (!(h->from_forward && h->pending_bc))
+    return fail((int)SPH_ERR_INVALID_ARG, "record the tape right after sph_step");
+  cudaStream_t st = (cudaStream_t)stream;
+  const long long N = h->N;
+  const Buffers& b = h->buf[h->cur];
+  cudaError_t e = cudaSuccess;
+  auto cp = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+  };
+  cp(h->t_orig + slot * N, b.ORIG, sizeof(int) * N);
+  cp(h->t_P4 + slot * N, b.P4, sizeof(float4) * N);
+  cp(h->t_U4 + slot * N, b.U4, sizeof(float4) * N);
+  cp(h->t_R4 + slot * N, h->R4, sizeof(float4) * N);
+  cp(h->t_nbr + (size_t)slot * h->kmax * N, h->nbr, sizeof(int) * h->kmax * N);
+  cp(h->t_cnt + slot * N, h->nbr_cnt, sizeof(int) * N);
+  return cuda_check(e, "tape record");
+}
+
+int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u,
+                     const float* lam_a_in, float* lam_a_out, void* stream) {
+  if (!h || slot < 0 || slot >= h->tape_slots)
+    return fail((int)SPH_ERR_INVALID_ARG, "tape slot out of range");
+  if (!lam_r || !lam_u || !lam_a_in || !lam_a_out || lam_a_in == lam_a_out)
+    return fail((int)SPH_ERR_INVALID_ARG, "adjoint arrays missing or aliased");
+  const long long N = h->N;
+  LaunchCtx L = h->ctx((cudaStream_t)stream);
+  launch_adjoint(L, h->t_orig + slot * N, h->t_P4 + slot * N, h->t_U4 + slot * N,
+                 h->t_R4 + slot * N, h->t_nbr + (size_t)slot * h->kmax * N,
+                 h->t_cnt + slot * N, h->t_mu, lam_a_in, lam_a_out, lam_r, lam_u);
+  return launch_status("adjoint step");
 }
 
 int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream) {

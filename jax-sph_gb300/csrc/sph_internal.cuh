@@ -454,6 +454,11 @@ void launch_forward(const LaunchCtx& L, Buffers b, const float4* R4, float4* R4w
 
 size_t scan_tmp_ints(long long n);
 
+// sph_adjoint.cu: reverse of one recorded step (tape arrays of that step).
+void launch_adjoint(const LaunchCtx& L, const int* orig, const float4* P4, const float4* U4,
+                    const float4* R4, const int* nbr, const int* cnt, float* mu,
+                    const float* la_in, float* la_out, float* lr, float* lu);
+
 // sph_capi.cu: per-case device constants from the ABI parameters; returns
 // non-zero and sets `err` on invalid input.
 int make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long long cell_off,

@@ -65,8 +65,8 @@ class SphNLCapacity(ctypes.Structure):
 EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sph_update_cases",
            "sph_set_state", "sph_get_state", "sph_nl_allocate", "sph_nl_set_capacity",
            "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_set_block_size",
-           "sph_step_launch_count",
-           "sph_profile_step", "sph_read_status", "sph_diagnostics", "sph_nl_edges_noalloc"]
+           "sph_step_launch_count", "sph_profile_step", "sph_adjoint_init", "sph_tape_record",
+           "sph_adjoint_step", "sph_read_status", "sph_diagnostics", "sph_nl_edges_noalloc"]
 
 _LIB = None
 
@@ -99,6 +99,9 @@ def load(build_if_missing=True):
     lib.sph_set_block_size.argtypes = [V, ctypes.c_int32]
     lib.sph_step_launch_count.argtypes = [V, P(ctypes.c_int32)]
     lib.sph_profile_step.argtypes = [V, ctypes.c_int32, P(ctypes.c_float), V]
+    lib.sph_adjoint_init.argtypes = [V, ctypes.c_int32]
+    lib.sph_tape_record.argtypes = [V, ctypes.c_int32, V]
+    lib.sph_adjoint_step.argtypes = [V, ctypes.c_int32, V, V, V, V, V]
     lib.sph_read_status.argtypes = [V, P(ctypes.c_uint32), ctypes.c_int32, V]
     lib.sph_diagnostics.argtypes = [V, V, V]
     lib.sph_nl_edges_noalloc.argtypes = [ctypes.c_int32, P(ctypes.c_double), ctypes.c_double,
@@ -229,6 +232,19 @@ class Engine:
         ms = (ctypes.c_float * 4)()
         _check(self.lib.sph_profile_step(self.h, int(nsteps), ms, _stream()))
         return [float(x) for x in ms]
+
+    def adjoint_init(self, slots):
+        _check(self.lib.sph_adjoint_init(self.h, int(slots)))
+
+    def tape_record(self, slot):
+        _check(self.lib.sph_tape_record(self.h, int(slot), _stream()))
+
+    def adjoint_step(self, slot, lam_r, lam_u, lam_a_in, lam_a_out):
+        for t in (lam_r, lam_u, lam_a_in, lam_a_out):
+            if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float32):
+                raise ValueError("adjoint arrays must be contiguous float32 CUDA tensors")
+        _check(self.lib.sph_adjoint_step(self.h, int(slot), _ptr(lam_r), _ptr(lam_u),
+                                         _ptr(lam_a_in), _ptr(lam_a_out), _stream()))
 
     def read_status(self, clear=False):
         s = ctypes.c_uint32(0)

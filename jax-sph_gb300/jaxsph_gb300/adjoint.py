@@ -1,0 +1,112 @@
+"""Differentiable rollouts: hand-written adjoint with checkpointed recomputation.
+
+The reference differentiates whole rollouts with ``jax.grad`` (integer
+neighbour indices carry no gradient, so the list is frozen per step;
+``notebooks/iclr24_grads.ipynb``, ``notebooks/iclr24_inverse.ipynb``) and
+keeps the whole tape in memory. Here the forward rollout stores the state
+every ``checkpoint_every`` steps; the reverse sweep re-runs each segment
+forward (bit-identical to the original forward), records its steps on the
+GPU tape and applies the hand-written reverse step (``sph_adjoint_step``,
+``csrc/sph_adjoint.cu``) from the last step to the first. Memory is one
+segment of per-step data plus the checkpoints.
+
+``rollout`` wraps it as a ``torch.autograd.Function``: the gradient of any
+torch loss of the final positions flows back to the initial velocity.
+"""
+
+import torch
+
+from . import _lib
+from .simulate import Simulation
+
+
+class AdjointRollout:
+    """``steps`` si_euler steps of one case, differentiable w.r.t. the initial velocity.
+
+    The initial velocity enters as ``u = v = u0`` (the reference initialises
+    ``v`` with ``u``, case_setup.py:167-168) with ``dudt = 0``.
+    """
+
+    def __init__(self, setup, steps, checkpoint_every=10, device="cuda"):
+        if setup.tvf != 0.0:
+            raise NotImplementedError("the adjoint covers tvf = 0")
+        self.setup = setup
+        self.steps = int(steps)
+        self.k = int(checkpoint_every)
+        self.sim = Simulation(setup, device=device)
+        self.engine = self.sim.engine
+        self.engine.adjoint_init(self.k)
+        self.device = torch.device(device)
+        self.checkpoints = []
+
+    def _initial(self, u0):
+        st = {k: v.clone() for k, v in self.setup.state.items()}
+        u0 = u0.detach().to(device="cpu", dtype=st["u"].dtype)
+        st["u"] = u0.clone()
+        st["v"] = u0.clone()
+        st["dudt"] = torch.zeros_like(st["dudt"])
+        st["dvdt"] = torch.zeros_like(st["dvdt"])
+        return st
+
+    def forward(self, u0):
+        """Run the rollout from initial velocity ``u0``; returns the final positions."""
+        self.sim.load([self._initial(u0)])
+        self.checkpoints = []
+        done = 0
+        while done < self.steps:
+            self.checkpoints.append(self.sim.state(split=False))
+            n = min(self.k, self.steps - done)
+            code = self.sim.run(n)
+            if code & (_lib.ERR_NONFINITE | _lib.ERR_INVALID_ARG):
+                raise _lib.SphError(code, "rollout produced non-finite values")
+            done += n
+        return self.sim.state()[0]["r"].clone()
+
+    def backward(self, lam_r):
+        """Adjoints (d loss/d u0, d loss/d r0) for d loss/d r_T = ``lam_r``."""
+        shape = lam_r.shape
+        lr = lam_r.detach().to(self.device, torch.float32).contiguous().clone()
+        lu = torch.zeros_like(lr)
+        la = [torch.zeros_like(lr), torch.zeros_like(lr)]
+        cur = 0
+        for seg in reversed(range(len(self.checkpoints))):
+            ck = self.checkpoints[seg]
+            self.sim.load([ck])
+            n = min(self.k, self.steps - seg * self.k)
+            for t in range(n):
+                self.engine.step(1)
+                self.engine.tape_record(t)
+            for t in reversed(range(n)):
+                self.engine.adjoint_step(t, lr, lu, la[cur], la[1 - cur])
+                cur = 1 - cur
+        code = self.engine.read_status(clear=True)
+        if code & _lib.ERR_INVALID_ARG:
+            raise _lib.SphError(code, "a particle has more neighbours than the adjoint tape holds")
+        # u0 enters the first step as u; v0 = u0 does not reach the dynamics
+        # when tvf = 0, and dudt starts at zero
+        return lu.reshape(shape), lr.reshape(shape)
+
+
+class _RolloutFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, u0, roll):
+        ctx.roll = roll
+        return roll.forward(u0).to(u0.device)
+
+    @staticmethod
+    def backward(ctx, grad_r):
+        lu, _ = ctx.roll.backward(grad_r.contiguous())
+        return lu.to(grad_r.device), None
+
+
+def rollout(u0, roll):
+    """Final positions of ``roll`` started from ``u0``, differentiable in ``u0``."""
+    return _RolloutFn.apply(u0, roll)
+
+
+def position_mse(r, target, box):
+    """Mean over particles of the squared minimum-image distance to ``target``."""
+    side = torch.as_tensor(box, dtype=r.dtype, device=r.device)
+    d = r - target
+    d = d - side * torch.round(d / side)
+    return (d * d).sum(1).mean()

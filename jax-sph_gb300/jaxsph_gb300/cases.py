@@ -299,6 +299,46 @@ def poiseuille(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, g_ext_magni
                    g_ext=g, bc=BC(_lib.BC_SOLID_ZERO), dtype=dtype, **kw)
 
 
+def fourier_perturbation(r, sigma=0.1, kmax=8, seed=1):
+    """Divergence-free random velocity field on the periodic unit square.
+
+    Stream function psi = sum over integer wave vectors 0 < |k| <= kmax of
+    Gaussian coefficients times cos/sin(2 pi k.x); u = (d psi/dy, -d psi/dx),
+    scaled to an RMS speed of ``sigma`` over the given points.
+    """
+    rng = np.random.default_rng(seed)
+    x = np.asarray(r, dtype=np.float64)
+    u = np.zeros_like(x)
+    for kx in range(-kmax, kmax + 1):
+        for ky in range(0, kmax + 1):
+            if (kx, ky) == (0, 0) or kx * kx + ky * ky > kmax * kmax:
+                continue
+            if ky == 0 and kx < 0:
+                continue
+            a, b = rng.normal(size=2)
+            ph = 2 * np.pi * (kx * x[:, 0] + ky * x[:, 1])
+            dpsi = 2 * np.pi * (-a * np.sin(ph) + b * np.cos(ph))  # d psi / d phase
+            u[:, 0] += dpsi * ky
+            u[:, 1] -= dpsi * kx
+    rms = np.sqrt((u ** 2).sum(1).mean())
+    return u * (sigma / rms)
+
+
+def tgv_perturbed(n_side=128, sigma=0.1, kmax=8, seed=1, dtype=np.float32, **kw):
+    """2D periodic TGV (SPH, tvf = 0, QSK) whose initial velocity is the TGV field
+    plus a seeded divergence-free random Fourier perturbation: the workload of
+    the differentiable form (inverse problems on initial velocities)."""
+    s = tgv(dim=2, dx=1.0 / n_side, dtype=dtype, **kw)
+    r = s.state["r"].numpy()
+    pert = fourier_perturbation(r, sigma, kmax, seed)
+    u = s.state["u"].double().numpy() + pert
+    t = s.state["u"].dtype
+    s.state["u"] = torch.as_tensor(u, dtype=t)
+    s.state["v"] = s.state["u"].clone()
+    s.name = f"tgv2d_perturbed_seed{seed}"
+    return s
+
+
 def cavity_channel_batch(n_instances=256, seed=0, n_min=1000, n_max=40000, re_min=10.0,
                          re_max=1000.0, dx_min=0.004, dx_max=0.02, dtype=np.float32, t_end=1.0):
     """Independent lid-driven cavities and Poiseuille channels for the batched form.
