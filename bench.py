@@ -273,6 +273,43 @@ def batched_form(device, steps, n_instances=256):
             "launches_per_step": sim.engine.launch_count()}
 
 
+def adjoint_form(device, steps=100, checkpoint_every=10):
+    """The differentiable form on its own workload: gradient of the final
+    positions' mean squared distance to a target rollout (another seed) with
+    respect to the initial velocity of a 128^2 perturbed 2D TGV, through the
+    hand-written adjoint with checkpointing, versus the plain forward rollout."""
+    from jaxsph_gb300 import adjoint, cases, simulate
+
+    a = cases.tgv_perturbed(n_side=128, seed=1)
+    b = cases.tgv_perturbed(n_side=128, seed=2)
+    target = adjoint.AdjointRollout(b, steps, checkpoint_every).forward(b.state["u"].to(device))
+    roll = adjoint.AdjointRollout(a, steps, checkpoint_every, device=device)
+    u0 = a.state["u"].to(device)
+    roll.forward(u0)  # warm-up (graphs, allocation)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    u = u0.clone().requires_grad_(True)
+    loss = adjoint.position_mse(adjoint.rollout(u, roll), target, a.box)
+    (g,) = torch.autograd.grad(loss, u)
+    torch.cuda.synchronize()
+    t_grad = time.perf_counter() - t0
+    plain = simulate.Simulation(a, device=device)
+    plain.run(3)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    plain.run(steps)
+    torch.cuda.synchronize()
+    t_plain = time.perf_counter() - t0
+    return {"workload": f"2D TGV 128^2 = {a.n:,} particles, TGV + Fourier perturbation "
+                        f"(sigma 0.1, |k| <= 8), SPH tvf=0 QSK, {steps}-step rollout, "
+                        f"gradient of the final-position MSE w.r.t. the initial velocity",
+            "value": a.n * steps / t_grad, "unit": UNIT,
+            "note": "forward (with checkpoints) + reverse sweep, wall clock",
+            "checkpoint_every": checkpoint_every, "loss": float(loss),
+            "grad_norm": float(g.norm()), "plain_forward_value": a.n * steps / t_plain,
+            "ratio_vs_plain_forward": t_plain / t_grad}
+
+
 def gpu_arm(args, ws, rank, local):
     from jaxsph_gb300 import cases, simulate
 
@@ -345,7 +382,7 @@ def gpu_arm(args, ws, rank, local):
                        "d2h_bytes_per_step": d2h,
                        "path": "si_euler drop-in advance, pinned host state in/out every step"}
     if rank == 0 and not args.no_forms:
-        line["forms"] = {"batched": batched_form(device, 100)}
+        line["forms"] = {"batched": batched_form(device, 100), "adjoint": adjoint_form(device)}
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
         rate, steps, secs, n_cpu = cpu_oracle_rate(64, 2, 30.0, threads)

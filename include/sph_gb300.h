@@ -82,6 +82,8 @@ typedef struct SphConfig {
   int32_t is_free_slip;
   int32_t mask_self;      /* exclude self pairs from the neighbour list */
   int32_t kahan;          /* compensated (Kahan) pair sums */
+  int32_t fp64_positions; /* integrate positions in float64 (long rollouts); the
+                             passes read them rounded to float32 */
   double capacity_multiplier; /* neighbour/cell capacity factor (reference 1.25) */
 } SphConfig;
 

@@ -161,6 +161,8 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
   c.dt = (float)(1.0 * in.dt);
   c.cv = (float)(in.tvf * 0.5 * in.dt);
   c.dt_rho = (float)in.dt_solver;
+  c.dt64 = in.dt;
+  for (int d = 0; d < 3; ++d) c.box64[d] = (double)c.box[d];
   // EOS (eos.py)
   c.eos = in.eos;
   c.p_ref = (float)in.p_ref;
@@ -357,6 +359,7 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
           h->alloc(&b.A2, N) | h->alloc(&b.ETA, N) | h->alloc(&b.META, N) |
           h->alloc(&b.ORIG, N);
     if (need_nw) rc |= h->alloc(&b.NW4, N);
+    if (cfg->fp64_positions) rc |= h->alloc(&b.RD, N);
   }
   if (!rc) {
     rc |= h->alloc(&h->R4, N) | h->alloc(&h->cellid, N);

@@ -65,12 +65,14 @@ struct CaseDev {
   int fast;
   float cut_lo, cut_hi;
   float inv_box[3];
+  double dt64, box64[3];  // float64 drift of the precision form
 };
 
 struct Buffers {
   float4 *P4, *U4, *V4, *A4, *A2, *NW4;
   float* ETA;
   int *META, *ORIG;
+  double4* RD;  // float64 positions of the precision form (else null)
 };
 
 // ------------------------------------------------------------------ helpers

@@ -57,6 +57,7 @@ __global__ void k_pack(SphStateView s, int dim, Buffers o, const long long* case
   o.META[i] = (c << kTagBits) | (tag & kTagMask);
   o.ORIG[i] = (int)i;
   if (o.NW4) o.NW4[i] = s.nw ? ld4(s.nw, dim, i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  if (o.RD) o.RD[i] = make_double4(r.x, r.y, r.z, 0.0);
 }
 
 // The state a step or forward left behind: density/pressure from the density
@@ -126,6 +127,35 @@ __device__ __forceinline__ void kick_drift(float4& r, float3& u, float3& v, cons
   }
 }
 
+// Precision form: the same kick in float32, the drift accumulated in float64
+// (rd); the float32 position the passes read is rd rounded, kept below the
+// box length.
+__device__ __forceinline__ float drift_axis64(double& x, float v, double dt, double L, float Lf) {
+  double y = x + dt * (double)v;
+  if (y >= L) y -= L;
+  else if (y < 0.0) y += L;
+  x = y;
+  const float f = (float)y;
+  return f < Lf ? f : nextafterf(Lf, 0.f);
+}
+
+template <int DIM>
+__device__ __forceinline__ void kick_drift64(float4& r, double4& rd, float3& u, float3& v,
+                                             const float4& dudt, const float4& dvdt,
+                                             const CaseDev& c) {
+  u.x = __fadd_rn(u.x, __fmul_rn(c.dt, dudt.x));
+  u.y = __fadd_rn(u.y, __fmul_rn(c.dt, dudt.y));
+  v.x = __fadd_rn(u.x, __fmul_rn(c.cv, dvdt.x));
+  v.y = __fadd_rn(u.y, __fmul_rn(c.cv, dvdt.y));
+  r.x = drift_axis64(rd.x, v.x, c.dt64, c.box64[0], c.box[0]);
+  r.y = drift_axis64(rd.y, v.y, c.dt64, c.box64[1], c.box[1]);
+  if (DIM == 3) {
+    u.z = __fadd_rn(u.z, __fmul_rn(c.dt, dudt.z));
+    v.z = __fadd_rn(u.z, __fmul_rn(c.cv, dvdt.z));
+    r.z = drift_axis64(rd.z, v.z, c.dt64, c.box64[2], c.box[2]);
+  }
+}
+
 template <int DIM>
 __global__ void k_hash_count(long long N, Buffers in, const float4* R4, const CaseDev* cases,
                              int* count, int* keyc, int* keys, unsigned* status, bool drift,
@@ -140,7 +170,12 @@ __global__ void k_hash_count(long long N, Buffers in, const float4* R4, const Ca
     if (drift) {
       Final f = finalize(in, R4, k, c, tag_of(meta), from_forward, apply_bc);
       float3 u = f.u, v;
-      kick_drift<DIM>(r, u, v, in.A4[k], in.A2[k], c);
+      if (in.RD) {
+        double4 rd = in.RD[k];
+        kick_drift64<DIM>(r, rd, u, v, in.A4[k], in.A2[k], c);
+      } else {
+        kick_drift<DIM>(r, u, v, in.A4[k], in.A2[k], c);
+      }
     }
     cell = c.cell_off + cell_hash<DIM>(r, c, status);
   }
@@ -191,7 +226,13 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
     float4 r = in.P4[src];
     float4 A = in.A4[src], B = in.A2[src];
     float3 u = f.u, v = f.v;
-    if (drift) kick_drift<DIM>(r, u, v, A, B, c);
+    if (in.RD) {
+      double4 rd = in.RD[src];
+      if (drift) kick_drift64<DIM>(r, rd, u, v, A, B, c);
+      out.RD[dest] = rd;
+    } else if (drift) {
+      kick_drift<DIM>(r, u, v, A, B, c);
+    }
     out.P4[dest] = r;
     out.U4[dest] = make_float4(u.x, u.y, u.z, f.rho);
     out.V4[dest] = make_float4(v.x, v.y, v.z, f.p);

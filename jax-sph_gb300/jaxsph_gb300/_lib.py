@@ -34,7 +34,8 @@ class SphConfig(ctypes.Structure):
     _fields_ = [("dim", ctypes.c_int32), ("kernel", ctypes.c_int32), ("solver", ctypes.c_int32),
                 ("is_rho_evol", ctypes.c_int32), ("is_bc_trick", ctypes.c_int32),
                 ("is_free_slip", ctypes.c_int32), ("mask_self", ctypes.c_int32),
-                ("kahan", ctypes.c_int32), ("capacity_multiplier", ctypes.c_double)]
+                ("kahan", ctypes.c_int32), ("fp64_positions", ctypes.c_int32),
+                ("capacity_multiplier", ctypes.c_double)]
 
 
 class SphCase(ctypes.Structure):

@@ -56,10 +56,11 @@ class AdjointRollout:
         while done < self.steps:
             self.checkpoints.append(self.sim.state(split=False))
             n = min(self.k, self.steps - done)
-            code = self.sim.run(n)
-            if code & (_lib.ERR_NONFINITE | _lib.ERR_INVALID_ARG):
-                raise _lib.SphError(code, "rollout produced non-finite values")
+            self.engine.step(n)
             done += n
+        code = self.engine.read_status(clear=True)
+        if code & (_lib.ERR_NONFINITE | _lib.ERR_INVALID_ARG | _lib.ERR_CUDA):
+            raise _lib.SphError(code, "rollout failed")
         return self.sim.state()[0]["r"].clone()
 
     def backward(self, lam_r):
@@ -70,8 +71,7 @@ class AdjointRollout:
         la = [torch.zeros_like(lr), torch.zeros_like(lr)]
         cur = 0
         for seg in reversed(range(len(self.checkpoints))):
-            ck = self.checkpoints[seg]
-            self.sim.load([ck])
+            self.sim.restore(self.checkpoints[seg])
             n = min(self.k, self.steps - seg * self.k)
             for t in range(n):
                 self.engine.step(1)

@@ -288,15 +288,22 @@ def poiseuille(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, g_ext_magni
     dxn = n_walls * dx
     box = np.array([L, H + 2 * dxn])
     r_f = _add(pos_init_cartesian_2d(np.array([L, H]), dx, dtype), [0.0, dxn], dtype)
-    horiz = pos_init_cartesian_2d(np.array([L, dxn]), dx, dtype)
-    r_w = np.concatenate([horiz, _add(horiz, [0.0, H + dxn], dtype)])
+
+    def walls(ddx, nw_):  # PF._init_walls_2d (cases/pf.py:43-57)
+        hz = pos_init_cartesian_2d(np.array([L, ddx * nw_]), ddx, dtype)
+        return np.concatenate([hz, _add(hz, [0.0, H + ddx * nw_], dtype)])
+
+    r_w = walls(dx, n_walls)
     r = np.concatenate([r_w, r_f])
     tag = np.concatenate([np.full(len(r_w), SOLID_WALL), np.full(len(r_f), FLUID)])
     v = np.zeros_like(r, dtype=np.float64)
+    nw = None
+    if kw.get("solver_name") == "RIE" or kw.get("free_slip"):
+        nw = _nws_scipy(r, tag, dx, n_walls, np.array([0.0, dxn]), walls, dtype)
     g = GExt(_lib.GEXT_BAND_X, (g_ext_magnitude, 0.0, 0.0), (dxn, box[1] - dxn))
     return _finish("pf", 2, dx, box, r, tag, v, viscosity=viscosity, u_ref=u_ref,
                    g_ext_magnitude=g_ext_magnitude, is_bc_trick=True, t_end=t_end, dt=dt,
-                   g_ext=g, bc=BC(_lib.BC_SOLID_ZERO), dtype=dtype, **kw)
+                   g_ext=g, bc=BC(_lib.BC_SOLID_ZERO), nw=nw, dtype=dtype, **kw)
 
 
 def fourier_perturbation(r, sigma=0.1, kmax=8, seed=1):

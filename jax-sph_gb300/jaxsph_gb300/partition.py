@@ -166,6 +166,7 @@ class NeighborListFns:
         c.is_free_slip = int(solver.get("is_free_slip", 0))
         c.mask_self = int(self.mask_self)
         c.kahan = int(solver.get("kahan", 0))
+        c.fp64_positions = int(solver.get("fp64_positions", 0))
         c.capacity_multiplier = self.capacity_multiplier
         return c
 

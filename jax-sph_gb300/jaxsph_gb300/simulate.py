@@ -49,7 +49,7 @@ class Simulation:
     """
 
     def __init__(self, setups, kahan=False, mask_self=False, capacity_multiplier=1.25,
-                 device="cuda", autotune=False, block_size=None):
+                 device="cuda", autotune=False, block_size=None, fp64_positions=False):
         if not isinstance(setups, (list, tuple)):
             setups = [setups]
         _lib.require_cuda()
@@ -62,7 +62,7 @@ class Simulation:
         for v in self.solvers[1:]:
             if v.solver_flags() != flags or v.dim != self.solvers[0].dim:
                 raise ValueError("batched cases must share dimension, kernel, solver and BC treatment")
-        cfg = self.nl[0].config(**flags)
+        cfg = self.nl[0].config(**flags, fp64_positions=fp64_positions)
         self.cases = [v.sph_case(nl, s.n, dt=s.dt, tvf=s.tvf, bc=s.bc_fn.spec)
                       for s, v, nl in zip(self.setups, self.solvers, self.nl)]
         for v in self.solvers:
@@ -92,6 +92,12 @@ class Simulation:
         self.engine.set_state(full)
         self.capacity = self.engine.nl_allocate()
         self.engine.read_status(clear=True)
+
+    def restore(self, full):
+        """Reload a state saved with ``state(split=False)`` from this simulation,
+        keeping the capacities (no host synchronisation)."""
+        self._full = full
+        self.engine.set_state(full)
 
     def run(self, nsteps, check_every=None):
         """Advance every case by ``nsteps`` si_euler steps. Returns the status bits seen."""
