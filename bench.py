@@ -3,9 +3,11 @@
 
 Workload: 3D Taylor-Green vortex, 64^3 = 262,144 particles on the periodic
 (2 pi)^3 lattice, Wendland C2 kernel (h = dx, cutoff 2h), standard SPH with
-transport velocity (tvf = 1), Re = 1600, float32, neighbour list rebuilt every
-step. One step = one si_euler step (kick, drift, neighbour rebuild, WCSPH
-forward, bc_fn). Synthetic input: the reference's own initial condition
+transport velocity (tvf = 1), Re = 1600, float32, the reference's exact
+neighbour set every step. One step = one si_euler step (kick, drift,
+neighbour update, WCSPH forward, bc_fn). The neighbour update filters Verlet
+candidates (cutoff plus a skin, rebuilt on the GPU's own decision once a
+particle has moved half the skin) with the reference's membership test. Synthetic input: the reference's own initial condition
 (lattice + analytic velocity field), built by ``jaxsph_gb300.cases.tgv``.
 
 Default (our arm): resident rollout (``sph_step`` CUDA graphs), each timed step
@@ -37,14 +39,15 @@ METRIC = "particle-steps/s on 1 GB300: batched/adjoint vs plain at stated FP64 e
 UNIT = "particle-steps/s"
 WORKLOAD = ("3D Taylor-Green vortex 64^3 = 262,144 particles, periodic (2pi)^3, WC2K h=dx "
             "cutoff 2h, SPH + transport velocity (tvf=1), Re=1600, c0=10, float32, "
-            "neighbour rebuild every step")
+            "the reference's neighbour set every step")
 # Algorithmic bytes per particle (float32 / int32), the minimum unique state traffic
 STEP_BYTES = 128          # fused 3D TVF step: reads r,u,dudt,dvdt,m,eta,tag; writes r,u,v,dudt,dvdt,rho,p
 FORCE_BYTES = 76          # force pass: reads r,m,u,v,rho,p,eta (52 B); writes dudt,dvdt (24 B)
 DENSITY_BYTES = 24        # density pass: reads r,m (16 B); writes rho,p (8 B)
-BIN_BYTES = 104           # binning + kick-drift: reads r,m,u,v,dudt,dvdt,eta,tag (88 B -> 4+...)
-PHASES = ("binning+kick-drift", "density", "wall", "force")
-PHASE_KERNELS = ("k_hash_count/k_tile_scan/k_scatter/k_permute", "k_density", "k_wall", "k_force")
+BIN_BYTES = 104           # kick-drift + neighbour update: reads r,m,u,v,dudt,dvdt,eta,tag
+PHASES = ("kick+rebuild", "density", "wall", "force")
+PHASE_KERNELS = ("k_kick (+ k_hash_count/k_tile_scan/k_scatter/k_permute/k_verlet on rebuild)",
+                 "k_density", "k_wall", "k_force")
 PHASE_BYTES = (BIN_BYTES, DENSITY_BYTES, 0, FORCE_BYTES)
 # DRAM bytes per particle of one launch (dram__bytes_read.sum + dram__bytes_write.sum)
 # and FMA-pipe utilisation measured with ncu on the 128^3 case of the same kernels
@@ -256,11 +259,13 @@ def batched_form(device, steps, n_instances=256):
         plain_ms += sum(timed_steps(one, plain_steps)) / plain_steps
         del one
     # bit-for-bit agreement of batched and plain runs on a sample of instances
-    check = simulate.Simulation(batch, device=device)
+    # (canonical pair order: the batch rebuilds candidate lists when any of
+    # its cases needs it)
+    check = simulate.Simulation(batch, device=device, canonical_order=True)
     check.run(5)
     ref_states = check.state()
     for k in (0, 1, n_instances // 2, n_instances - 1):
-        one = simulate.Simulation(batch[k], device=device)
+        one = simulate.Simulation(batch[k], device=device, canonical_order=True)
         one.run(5)
         a, b = ref_states[k], one.state()[0]
         diffs.append(max(float((a[x].double() - b[x].double()).abs().max()) for x in ("r", "u", "rho")))
@@ -316,7 +321,7 @@ def gpu_arm(args, ws, rank, local):
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     setup = cases.tgv(dim=3, dx=2 * np.pi / args.n_side)
-    sim = simulate.Simulation(setup, device=device)
+    sim = simulate.Simulation(setup, device=device, skin=args.skin)
     # warm-up through run(): it polls the status word and re-allocates the
     # capacities on overflow, as the reference driver does
     sim.run(max(args.warmup, 3), check_every=1)
@@ -324,6 +329,7 @@ def gpu_arm(args, ws, rank, local):
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=device)
     starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
     ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    rebuilds0, per_rebuild = sim.engine.rebuild_stats()
     barrier(ws)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
@@ -337,7 +343,8 @@ def gpu_arm(args, ws, rank, local):
     step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_ms = max_over_ranks(float(np.sum(step_ms)), ws, device)
     status = sim.engine.read_status(clear=True)
-    launches = sim.engine.launch_count() * args.steps
+    rebuilds = sim.engine.rebuild_stats()[0] - rebuilds0
+    launches = sim.engine.launch_count() * args.steps + rebuilds * per_rebuild
     n = setup.n
     value = n * args.steps * ws / (total_ms / 1000.0)
     # phase times, measured with CUDA events on the launching stream
@@ -359,9 +366,10 @@ def gpu_arm(args, ws, rank, local):
         "warmup": max(args.warmup, 3), "ms_per_step": step_ms_mean, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (reference initial condition of the 3D TGV)",
-        "config": {"workload": WORKLOAD if args.n_side == 64 else
-                   WORKLOAD.replace("64^3 = 262,144", f"{args.n_side}^3 = {n:,}"),
+        "config": {"workload": (WORKLOAD if args.n_side == 64 else
+                                WORKLOAD.replace("64^3 = 262,144", f"{args.n_side}^3 = {n:,}")),
                    "n_particles": n, "parallelism": f"replicas x{ws}",
+                   "verlet_skin": args.skin, "candidate_rebuilds": rebuilds,
                    "l2": "flushed between timed steps (256 MiB write outside the events)"},
         "roofline": {"bound": "hbm", "kernel": PHASE_KERNELS[dom], "achieved": achieved,
                      "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
@@ -403,6 +411,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the batched/adjoint form measurements on their own workloads")
+    ap.add_argument("--skin", type=float, default=0.1,
+                    help="Verlet skin as a fraction of the cutoff (0: rebuild every step)")
     ap.add_argument("--n-side", type=int, default=64,
                     help="particles per side of the 3D TGV lattice (64 = the benchmark case)")
     args = ap.parse_args()

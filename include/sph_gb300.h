@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPH_ABI_VERSION 1
+#define SPH_ABI_VERSION 2
 
 /* Reference PartitionErrorCode bits (jax_sph/jax_md/partition.py:453-457). */
 #define SPH_NEIGHBOR_LIST_OVERFLOW 0x1u
@@ -85,6 +85,15 @@ typedef struct SphConfig {
   int32_t fp64_positions; /* integrate positions in float64 (long rollouts); the
                              passes read them rounded to float32 */
   double capacity_multiplier; /* neighbour/cell capacity factor (reference 1.25) */
+  double verlet_skin;     /* candidate-list skin as a fraction of the cutoff, in
+                             [0, 0.5]; 0 rebuilds the candidates every step. The
+                             neighbour set of every step is the reference's either
+                             way (each candidate takes the exact membership test) */
+  int32_t canonical_order; /* sum pairs in ascending original index: results then
+                              do not depend on the skin, the batching or when the
+                              candidates were rebuilt (slower rebuilds and gathers);
+                              0 sums in cell order, deterministic for a given run */
+  int32_t pad1;
 } SphConfig;
 
 /* Per-case parameters (all in the reference's units). */
@@ -194,12 +203,18 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream);
 /* Threads per block of the density, wall and force passes (a multiple of 32
  * in [32, 256]; default 256). A tuning knob: results do not depend on it. */
 int sph_set_block_size(SphHandle* h, int32_t threads);
-/* Kernel launches issued by one si_euler step of this handle. */
+/* Kernel launches issued by one si_euler step of this handle (without a
+ * candidate-list rebuild). */
 int sph_step_launch_count(SphHandle* h, int32_t* count);
+/* Candidate-list rebuilds run so far by this handle's steps and the kernel
+ * launches one rebuild adds to a step. Synchronizes `stream`. */
+int sph_rebuild_stats(SphHandle* h, int64_t* rebuilds, int32_t* kernels_per_rebuild,
+                      void* stream);
 /* Run `nsteps` steps eagerly, timing their phases with CUDA events on
- * `stream` (where the kernels run): ms[0] binning with the fused kick-drift,
- * ms[1] density pass, ms[2] wall pass, ms[3] force pass, averaged per step.
- * Host-synchronous; the steps advance the state like sph_step. */
+ * `stream` (where the kernels run): ms[0] kick-drift plus the candidate-list
+ * rebuilds that fell in the steps, ms[1] density pass, ms[2] wall pass,
+ * ms[3] force pass, averaged per step. Host-synchronous (the host reads the
+ * rebuild decision of each step); the steps advance the state like sph_step. */
 int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream);
 
 /* Differentiable form: hand-written reverse of si_euler steps with the
@@ -218,8 +233,14 @@ int sph_tape_record(SphHandle* h, int32_t slot, void* stream);
 int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u,
                      const float* lam_a_in, float* lam_a_out, void* stream);
 
-/* Read (and optionally clear) the device status word. Synchronizes `stream`. */
+/* Read (and optionally clear) the device status word. Synchronizes `stream`.
+ * sph_set_state clears the word. */
 int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream);
+/* Stream-ordered copy of the device status word into `status_dev` (a device
+ * uint32), optionally clearing it; no host synchronization. The way the
+ * reference keeps NeighborList.error as a device value until the caller
+ * tests it (jax_md/partition.py:460-499). */
+int sph_read_status_async(SphHandle* h, uint32_t* status_dev, int32_t clear, void* stream);
 
 /* Allocation-free neighbour list (no counterpart in the reference: it exists
  * for callers that cannot call cudaMalloc, such as a host framework that owns

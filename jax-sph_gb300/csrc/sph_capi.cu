@@ -35,8 +35,10 @@ struct SphHandle {
   CaseDev* dc = nullptr;
   long long* case_off_d = nullptr;
   long long N = 0, C = 0;
+  // buf[0] holds the state in the order of the last binning; buf[1] is the
+  // scratch copy a rebuild sorts from, so buffer addresses never change and
+  // one captured step serves every step
   Buffers buf[2]{};
-  int cur = 0;
   float4* R4 = nullptr;
   float4* UT4 = nullptr;
   int* cellid = nullptr;
@@ -45,13 +47,25 @@ struct SphHandle {
   int *rowcnt = nullptr, *rowoff = nullptr;
   int *nbr = nullptr, *nbr_cnt = nullptr;
   int kmax = kListSlots;  // neighbour-list slots per particle
+  int *vl = nullptr, *vcnt = nullptr;  // Verlet candidates
+  int kv = kVerletMinSlots;          // Verlet slots per particle
+  float4* rref = nullptr;              // positions at the last rebuild
+  int* cref_count = nullptr;           // per-step occupancy of the reference's cells
+  long long ref_cells = 0;
+  unsigned* vflag = nullptr;           // a rebuild is due
+  unsigned long long* rebuilds_d = nullptr;  // rebuilds run inside graph replays
+  long long rebuilds_h = 0;                  // rebuilds run eagerly
+  int rebuild_launches = 0;                  // kernels of one rebuild
   int block = 256;        // threads per block of the forward passes
   unsigned* status = nullptr;
   unsigned long long* edgecnt = nullptr;
   const float* g_arr = nullptr;
-  bool has_state = false, binned = false, from_forward = false, pending_bc = false;
-  cudaStream_t hs = nullptr;
-  cudaGraphExec_t gexec[2] = {nullptr, nullptr};  // one step from buffer parity 0 / 1
+  // binned: candidate lists valid for the current positions; fresh: the
+  // binning itself is of the current positions (no step since)
+  bool has_state = false, binned = false, fresh = false, from_forward = false,
+       pending_bc = false;
+  cudaStream_t hs = nullptr, hs2 = nullptr;  // capture streams (step, rebuild body)
+  cudaGraphExec_t gexec = nullptr;           // one steady step
   const float* graph_g_arr = nullptr;
   int launch_count = 0;       // kernel launches of the last step
   cudaEvent_t* ev = nullptr;  // phase events while profiling
@@ -92,6 +106,13 @@ struct SphHandle {
     L.nbr = nbr;
     L.nbr_cnt = nbr_cnt;
     L.kmax = kmax;
+    L.vl = vl;
+    L.vcnt = vcnt;
+    L.kv = kv;
+    L.rref = rref;
+    L.cref_count = cref_count;
+    L.vflag = vflag;
+    L.canonical = cfg.canonical_order;
     L.block = block;
     L.launches = const_cast<int*>(&launch_count);
     L.ev = ev;
@@ -104,7 +125,7 @@ void sph::set_last_error(const std::string& msg) { g_last_error = msg; }
 // Per-case float32 constants, rounded the way the reference's float32
 // program rounds its Python-float parameters (weak types become float32).
 int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long long cell_off,
-              CaseDev& c, std::string& err) {
+              CaseDev& c, std::string& err, bool fine_cells) {
   std::memset(&c, 0, sizeof(c));
   const int dim = cfg.dim;
   const float cut = (float)in.r_cutoff + 0.0f;
@@ -130,17 +151,79 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
     c.cell_size[d] = nc[d] > 1 ? box / cps : box;
   }
   c.use_cells = use_cells;
+  // Fast membership test. The minimum-image difference of two positions in
+  // [0, L] differs from the reference's float32 periodic displacement by at
+  // most ~3.3 ulp(L) per component, so their squared norms near the cutoff
+  // differ by at most ~20 ulp(L) * cutoff plus a few roundings of cutoff^2.
+  // Inside the band cut_sq * (1 +- rel) the reference metric decides.
+  bool fast = true;
+  float lmax = 0.f;
+  for (int d = 0; d < dim; ++d) {
+    fast = fast && nc[d] >= 5;
+    lmax = c.box[d] > lmax ? c.box[d] : lmax;
+    c.inv_box[d] = 1.0f / c.box[d];
+  }
+  const double rel = std::ldexp(24.0 * lmax / cut + 8.0, -23);
+  c.fast = fast && rel < 0.25;
+  c.cutoff_sq = cut * cut;
+  if (c.fast) {
+    c.cut_lo = (float)(c.cutoff_sq * (1.0 - rel));
+    c.cut_hi = (float)(c.cutoff_sq * (1.0 + rel));
+    // rows are trimmed to a sphere a little larger than the band's outer edge
+    c.trim_r2 = (float)(c.cutoff_sq * (1.0 + rel) * (1.0 + std::ldexp(1.0, -20)));
+    c.trim_m = (float)std::ldexp((double)lmax, -17);
+  } else {  // every candidate takes the reference metric
+    c.cut_lo = -1.0f;
+    c.cut_hi = INFINITY;
+  }
+  // Fast cases are binned into half-size cells (fewer candidates per
+  // receiver: the walk covers +-2 half cells with trimmed rows instead of
+  // +-1 reference cell).
   long long ncell = 1;
   for (int d = 0; d < 3; ++d) {
-    c.nc[d] = nc[d];
+    const int sub = (fine_cells && c.fast && nc[d] > 1) ? 2 : 1;
+    c.sub[d] = sub;
+    c.nc[d] = nc[d] * sub;
+    c.rad[d] = nc[d] > 1 ? sub : 0;
+    if (sub == 2) c.cell_size[d] = c.cell_size[d] * 0.5f;
+    c.inv_cs[d] = 1.0f / c.cell_size[d];
     c.mult[d] = (int)ncell;
-    ncell *= nc[d];
+    ncell *= c.nc[d];
   }
   if (ncell > INT_MAX / 2) {
     err = "too many cells";
     return -1;
   }
   c.ncell = (int)ncell;
+  c.ncref = (int)(ncell / ((long long)c.sub[0] * c.sub[1] * c.sub[2]));
+  // Verlet candidate list. Without a skin (or without the fast test) the list
+  // holds the senders within the band's outer edge (the reference's edges in
+  // a case without the fast test) and any motion triggers a rebuild. With a
+  // skin s the list radius is rv = r_hi (1 + s), r_hi the band's outer
+  // radius; a rebuild is due once some particle moved farther than
+  // dmax = (rv - r_hi) / 2 less margins, so until then two particles within
+  // the cutoff were within rv of each other at the last rebuild.
+  const double skin = cfg.verlet_skin;
+  for (int d = 0; d < 3; ++d) c.vrad[d] = c.rad[d];
+  c.v_r2 = c.fast ? c.trim_r2 : INFINITY;
+  c.v_dmax2 = 0.0f;
+  if (c.fast && skin > 0.0) {
+    const double r_hi = std::sqrt((double)c.trim_r2);
+    const double rv = r_hi * (1.0 + skin);
+    const double dmax = 0.5 * (rv - r_hi) - 4.0 * (double)c.trim_m;
+    bool ok = dmax > 0.0;
+    int vr[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) {
+      if (c.nc[d] <= 1) continue;
+      vr[d] = (int)std::ceil((rv + 2.0 * (double)c.trim_m) / (double)c.cell_size[d]);
+      ok = ok && c.nc[d] >= 2 * vr[d] + 1;  // every cell visited once
+    }
+    if (ok) {
+      for (int d = 0; d < 3; ++d) c.vrad[d] = vr[d];
+      c.v_r2 = (float)(rv * rv);
+      c.v_dmax2 = (float)(dmax * dmax);
+    }
+  }
   c.cell_off = (int)cell_off;
   c.p_off = (int)p_off;
   c.n = (int)in.n;
@@ -199,27 +282,6 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
   c.g_lo = (float)in.g_band_lo;
   c.g_hi = (float)in.g_band_hi;
   c.bc_kind = in.bc_kind;
-  // Fast membership test. The minimum-image difference of two positions in
-  // [0, L] differs from the reference's float32 periodic displacement by at
-  // most ~3.3 ulp(L) per component, so their squared norms near the cutoff
-  // differ by at most ~20 ulp(L) * cutoff plus a few roundings of cutoff^2.
-  // Inside the band cut_sq * (1 +- rel) the reference metric decides.
-  bool fast = true;
-  float lmax = 0.f;
-  for (int d = 0; d < dim; ++d) {
-    fast = fast && nc[d] >= 5;
-    lmax = c.box[d] > lmax ? c.box[d] : lmax;
-    c.inv_box[d] = 1.0f / c.box[d];
-  }
-  const double rel = std::ldexp(24.0 * lmax / cut + 8.0, -23);
-  c.fast = fast && rel < 0.25;
-  if (c.fast) {
-    c.cut_lo = (float)(c.cutoff_sq * (1.0 - rel));
-    c.cut_hi = (float)(c.cutoff_sq * (1.0 + rel));
-  } else {  // every candidate takes the reference metric
-    c.cut_lo = -1.0f;
-    c.cut_hi = INFINITY;
-  }
   return 0;
 }
 
@@ -233,72 +295,170 @@ int upload_cases(SphHandle* h, cudaStream_t st) {
 }
 
 void drop_graph(SphHandle* h) {
-  for (int k = 0; k < 2; ++k) {
-    if (h->gexec[k]) cudaGraphExecDestroy(h->gexec[k]);
-    h->gexec[k] = nullptr;
-  }
+  if (h->gexec) cudaGraphExecDestroy(h->gexec);
+  h->gexec = nullptr;
 }
 
 int launch_status(const char* what) { return cuda_check(cudaGetLastError(), what); }
 
-// Re-bin the current positions without moving them; folds a pending forward
-// result / bc_fn into the state buffers.
-int bin_static(SphHandle* h, cudaStream_t st) {
-  LaunchCtx L = h->ctx(st);
-  Buffers in = h->buf[h->cur], out = h->buf[1 - h->cur];
-  launch_bin(L, in, out, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc,
-             h->tkey, h->tcell, h->scan_tmp, h->C, false, h->from_forward, h->pending_bc);
-  h->cur = 1 - h->cur;
-  h->binned = true;
-  h->from_forward = false;
-  h->pending_bc = false;
-  return launch_status("bin");
+// Sets the conditional of the rebuild node of a captured step from the flag
+// the kick raised, and clears the flag.
+__global__ void k_decide(unsigned* vflag, unsigned long long* rebuilds,
+                         cudaGraphConditionalHandle cond) {
+  const unsigned v = *vflag;
+  *vflag = 0u;
+  if (v) *rebuilds += 1ull;
+  cudaGraphSetConditional(cond, v ? 1u : 0u);
 }
 
-// One si_euler step (integrator.py:22-56): kick-drift fused into the binning,
-// forward pass, bc_fn (applied to accelerations in the force pass and folded
-// into the state by the next binning / readback).
+// Rebuild: copy the state to the scratch set, sort it back into the resident
+// set by cell (folding a pending forward result / bc_fn on the way, and
+// keeping the positions as the new rebuild reference), then build the
+// candidate lists. Stream-ordered and allocation-free (capturable).
+int rebuild(SphHandle* h, cudaStream_t st, bool from_forward, bool apply_bc) {
+  LaunchCtx L = h->ctx(st);
+  const Buffers& A = h->buf[0];
+  const Buffers& B = h->buf[1];
+  const size_t N = (size_t)h->N;
+  cudaError_t e = cudaSuccess;
+  auto cp = [&](void* dst, const void* src, size_t bytes) {
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
+  };
+  cp(B.P4, A.P4, sizeof(float4) * N);
+  cp(B.U4, A.U4, sizeof(float4) * N);
+  cp(B.V4, A.V4, sizeof(float4) * N);
+  cp(B.A4, A.A4, sizeof(float4) * N);
+  cp(B.A2, A.A2, sizeof(float4) * N);
+  cp(B.ETA, A.ETA, sizeof(float) * N);
+  cp(B.META, A.META, sizeof(int) * N);
+  cp(B.ORIG, A.ORIG, sizeof(int) * N);
+  if (A.NW4) cp(B.NW4, A.NW4, sizeof(float4) * N);
+  if (A.RD) cp(B.RD, A.RD, sizeof(double4) * N);
+  if (e != cudaSuccess) return cuda_check(e, "rebuild copy");
+  launch_bin(L, B, A, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc, h->tkey,
+             h->tcell, h->scan_tmp, h->C, false, from_forward, apply_bc, h->rref);
+  launch_verlet(L, A, h->cellid, h->start);
+  return launch_status("rebuild");
+}
+
+// Re-bin the current positions without moving them (neighbour-list
+// allocate / update, a forward pass on a loaded state).
+int bin_static(SphHandle* h, cudaStream_t st) {
+  int base = h->launch_count;
+  int rc = rebuild(h, st, h->from_forward, h->pending_bc);
+  h->launch_count = base;
+  h->binned = h->fresh = true;
+  h->from_forward = false;
+  h->pending_bc = false;
+  return rc;
+}
+
+// One si_euler step (integrator.py:22-56), eagerly: kick-drift in place, a
+// rebuild of the candidate lists when the kick found one due (the host reads
+// the flag) or no lists exist yet, forward pass, bc_fn (applied to the
+// accelerations in the force pass and folded into the state on the next read).
 int step_once(SphHandle* h, cudaStream_t st) {
   h->launch_count = 0;
   LaunchCtx L = h->ctx(st);
-  Buffers in = h->buf[h->cur], out = h->buf[1 - h->cur];
-  launch_bin(L, in, out, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc,
-             h->tkey, h->tcell, h->scan_tmp, h->C, true, h->from_forward, h->pending_bc);
-  h->cur = 1 - h->cur;
-  launch_forward(L, out, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
-                 true);
+  mark(L, 0);
+  launch_kick(L, h->buf[0], h->R4, h->ref_cells, h->from_forward, h->pending_bc);
+  mark(L, 5);
+  bool rb = !h->binned;
+  cudaError_t e = cudaSuccess;
+  if (!rb) {
+    unsigned v = 0;
+    e = cudaMemcpyAsync(&v, h->vflag, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    rb = v != 0u;
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, sizeof(unsigned), st);
+  if (e != cudaSuccess) return cuda_check(e, "rebuild flag");
+  mark(L, 6);
+  if (rb) {
+    const int base = h->launch_count;
+    int rc = rebuild(h, st, false, false);
+    if (rc) return rc;
+    h->rebuild_launches = h->launch_count - base;
+    h->launch_count = base;
+    ++h->rebuilds_h;
+  }
+  mark(L, 1);
+  launch_forward(L, h->buf[0], h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr,
+                 true, true);
   h->binned = true;
+  h->fresh = rb;
   h->from_forward = true;
   h->pending_bc = true;
   return launch_status("step");
 }
 
-bool steady(const SphHandle* h) { return h->from_forward && h->pending_bc; }
+bool steady(const SphHandle* h) { return h->binned && h->from_forward && h->pending_bc; }
 
-// Capture one step starting from the current buffer parity. Capture only
-// records the launches; the host-side parity flip it performs is undone.
+// Capture one steady step: kick, decide, a conditional node whose body is the
+// rebuild, forward pass. The rebuild runs on the device's own decision, so a
+// replay never waits for the host.
+int capture_step(SphHandle* h, cudaStream_t st) {
+  h->launch_count = 0;
+  LaunchCtx L = h->ctx(st);
+  launch_kick(L, h->buf[0], h->R4, h->ref_cells, true, true);
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t g = nullptr;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaError_t e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return cuda_check(e, "capture info");
+  cudaGraphConditionalHandle cond;
+  e = cudaGraphConditionalHandleCreate(&cond, g, 0u, 0u);
+  if (e != cudaSuccess) return cuda_check(e, "conditional handle");
+  k_decide<<<1, 1, 0, st>>>(h->vflag, h->rebuilds_d, cond);
+  count_launch(L);
+  e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
+  if (e != cudaSuccess) return cuda_check(e, "capture info");
+  cudaGraphNodeParams p = {};
+  p.type = cudaGraphNodeTypeConditional;
+  p.conditional.handle = cond;
+  p.conditional.type = cudaGraphCondTypeIf;
+  p.conditional.size = 1;
+  cudaGraphNode_t node;
+  e = cudaGraphAddNode(&node, g, deps, nullptr, nd, &p);
+  if (e != cudaSuccess) return cuda_check(e, "conditional node");
+  e = cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1, cudaStreamSetCaptureDependencies);
+  if (e != cudaSuccess) return cuda_check(e, "capture dependencies");
+  cudaGraph_t body = p.conditional.phGraph_out[0];
+  e = cudaStreamBeginCaptureToGraph(h->hs2, body, nullptr, nullptr, 0,
+                                    cudaStreamCaptureModeThreadLocal);
+  if (e != cudaSuccess) return cuda_check(e, "capture rebuild");
+  const int base = h->launch_count;
+  int rc = rebuild(h, h->hs2, false, false);
+  h->rebuild_launches = h->launch_count - base;
+  h->launch_count = base;
+  e = cudaStreamEndCapture(h->hs2, &body);
+  if (rc) return rc;
+  if (e != cudaSuccess) return cuda_check(e, "end rebuild capture");
+  launch_forward(L, h->buf[0], h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr,
+                 true, true);
+  return launch_status("step capture");
+}
+
 int capture_graph(SphHandle* h) {
-  const int parity = h->cur;
-  if (h->gexec[parity]) {
-    cudaGraphExecDestroy(h->gexec[parity]);
-    h->gexec[parity] = nullptr;
-  }
-  if (!h->hs) {
-    cudaError_t e = cudaStreamCreateWithFlags(&h->hs, cudaStreamNonBlocking);
-    if (e != cudaSuccess) return cuda_check(e, "stream create");
+  drop_graph(h);
+  for (cudaStream_t* s : {&h->hs, &h->hs2}) {
+    if (!*s) {
+      cudaError_t e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+      if (e != cudaSuccess) return cuda_check(e, "stream create");
+    }
   }
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamBeginCapture(h->hs, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_check(e, "begin capture");
-  int rc = step_once(h, h->hs);
+  int rc = capture_step(h, h->hs);
   e = cudaStreamEndCapture(h->hs, &graph);
-  h->cur = parity;
   if (rc) {
     if (graph) cudaGraphDestroy(graph);
     return rc;
   }
   if (e != cudaSuccess) return cuda_check(e, "end capture");
-  e = cudaGraphInstantiate(&h->gexec[parity], graph, 0);
+  e = cudaGraphInstantiate(&h->gexec, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_check(e, "graph instantiate");
   h->graph_g_arr = h->g_arr;
@@ -324,13 +484,15 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
   if (cfg->solver != SPH_SOLVER_SPH && cfg->solver != SPH_SOLVER_RIE)
     return fail((int)SPH_ERR_INVALID_ARG, "solver must be SPH or RIE");
   if (n_cases >= (1 << 26)) return fail((int)SPH_ERR_INVALID_ARG, "too many cases");
+  if (!(cfg->verlet_skin >= 0.0 && cfg->verlet_skin <= 0.5))
+    return fail((int)SPH_ERR_INVALID_ARG, "verlet_skin must lie in [0, 0.5]");
   SphHandle* h = new SphHandle();
   h->cfg = *cfg;
   h->n_cases = n_cases;
   h->cases.assign(cases, cases + n_cases);
   h->hc.resize(n_cases);
   std::vector<long long> off(n_cases + 1, 0);
-  long long cells = 0;
+  long long cells = 0, ref_cells = 0;
   for (int i = 0; i < n_cases; ++i) {
     if (cases[i].n <= 0) {
       delete h;
@@ -341,11 +503,30 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
       delete h;
       return fail((int)SPH_ERR_INVALID_ARG, "case " + std::to_string(i) + ": " + err);
     }
+    h->hc[i].cref_off = (int)ref_cells;
     cells += h->hc[i].ncell;
+    ref_cells += h->hc[i].ncref;
     off[i + 1] = off[i] + cases[i].n;
   }
   h->N = off[n_cases];
   h->C = cells;
+  h->ref_cells = ref_cells;
+  // Verlet slots: the candidates a particle of a case at lattice spacing dx
+  // expects (sphere of the list radius over dx^d), times 1.5, plus 8
+  {
+    double est = 0.0;
+    for (int i = 0; i < n_cases; ++i) {
+      const CaseDev& c = h->hc[i];
+      const double rv = c.fast ? std::sqrt((double)c.v_r2) : std::sqrt((double)c.cutoff_sq);
+      const double q = cases[i].dx > 0.0 ? rv / cases[i].dx : 1e6;  // no spacing: most slots
+      const double v = cfg->dim == 3 ? 4.0 / 3.0 * M_PI * q * q * q : M_PI * q * q;
+      est = v > est ? v : est;
+    }
+    long long kv = (long long)std::ceil(1.5 * est) + 8;
+    kv = (kv + 7) / 8 * 8;
+    kv = kv < kVerletMinSlots ? kVerletMinSlots : (kv > kVerletMaxSlots ? kVerletMaxSlots : kv);
+    h->kv = (int)kv;
+  }
   if (h->N >= INT_MAX / 2 || h->C >= INT_MAX / 2) {
     delete h;
     return fail((int)SPH_ERR_INVALID_ARG, "problem too large for 32-bit indices");
@@ -368,13 +549,20 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
           h->alloc(&h->keyc, N) | h->alloc(&h->keys, N) | h->alloc(&h->tsrc, N) |
           h->alloc(&h->tkey, N) | h->alloc(&h->tcell, N) | h->alloc(&h->rowcnt, N + 1) |
           h->alloc(&h->rowoff, N + 1) | h->alloc(&h->nbr, (size_t)h->kmax * N) |
-          h->alloc(&h->nbr_cnt, N);
+          h->alloc(&h->nbr_cnt, N) | h->alloc(&h->vl, (size_t)h->kv * N) |
+          h->alloc(&h->vcnt, N) | h->alloc(&h->rref, N) |
+          h->alloc(&h->cref_count, h->ref_cells + 1) | h->alloc(&h->vflag, 1) |
+          h->alloc(&h->rebuilds_d, 1);
     long long m = h->C + 1 > N + 1 ? h->C + 1 : N + 1;
     rc |= h->alloc(&h->scan_tmp, scan_tmp_ints(m));
     rc |= h->alloc(&h->status, 1) | h->alloc(&h->edgecnt, n_cases) | h->alloc(&h->dc, n_cases) |
           h->alloc(&h->case_off_d, n_cases + 1);
   }
   if (!rc) rc = cuda_check(cudaMemset(h->status, 0, sizeof(unsigned)), "memset");
+  if (!rc) rc = cuda_check(cudaMemset(h->vflag, 0, sizeof(unsigned)), "memset");
+  if (!rc) rc = cuda_check(cudaMemset(h->rebuilds_d, 0, sizeof(unsigned long long)), "memset");
+  if (!rc) rc = cuda_check(cudaMemset(h->rref, 0, sizeof(float4) * N), "memset");
+  if (!rc) rc = cuda_check(prepare_kernels(h->kv), "kernel attributes");
   if (!rc)
     rc = cuda_check(cudaMemcpy(h->case_off_d, off.data(), sizeof(long long) * (n_cases + 1),
                                cudaMemcpyHostToDevice),
@@ -393,6 +581,7 @@ int sph_destroy(SphHandle* h) {
   if (!h) return 0;
   drop_graph(h);
   if (h->hs) cudaStreamDestroy(h->hs);
+  if (h->hs2) cudaStreamDestroy(h->hs2);
   for (void* p : h->allocs) cudaFree(p);
   delete h;
   return 0;
@@ -413,6 +602,7 @@ int sph_update_cases(SphHandle* h, const SphCase* cases, int32_t n_cases) {
       return fail((int)SPH_ERR_INVALID_ARG, "case " + std::to_string(i) + ": " + err);
     next[i].cell_cap = h->hc[i].cell_cap;
     next[i].edge_cap = h->hc[i].edge_cap;
+    next[i].cref_off = h->hc[i].cref_off;
   }
   h->cases.assign(cases, cases + n_cases);
   h->hc = next;
@@ -433,11 +623,11 @@ int sph_set_state(SphHandle* h, const SphStateView* s, void* stream) {
   if (garr && !s->g_ext)
     return fail((int)SPH_ERR_INVALID_ARG, "g_ext array required by SPH_GEXT_ARRAY");
   cudaStream_t st = (cudaStream_t)stream;
-  h->cur = 0;
+  cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);  // a new state starts clean
   launch_pack(h->ctx(st), *s, h->buf[0], h->case_off_d);
   h->g_arr = s->g_ext;
   h->has_state = true;
-  h->binned = h->from_forward = h->pending_bc = false;
+  h->binned = h->fresh = h->from_forward = h->pending_bc = false;
   return launch_status("set_state");
 }
 
@@ -447,7 +637,7 @@ int sph_get_state(SphHandle* h, SphStateView* s, void* stream) {
   if (s->n != h->N) return fail((int)SPH_ERR_INVALID_ARG, "state has the wrong particle count");
   if (!s->r || !s->u || !s->v || !s->dudt || !s->dvdt || !s->rho || !s->p)
     return fail((int)SPH_ERR_INVALID_ARG, "missing state field");
-  launch_unpack(h->ctx((cudaStream_t)stream), h->buf[h->cur], h->R4, *s, h->from_forward,
+  launch_unpack(h->ctx((cudaStream_t)stream), h->buf[0], h->R4, *s, h->from_forward,
                 h->pending_bc);
   return launch_status("get_state");
 }
@@ -471,7 +661,7 @@ int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out
   if (!rc) rc = bin_static(h, st);
   if (rc) return rc;
   LaunchCtx L = h->ctx(st);
-  launch_row_counts(L, h->buf[h->cur], h->cellid, h->start, h->rowcnt);
+  launch_row_counts(L, h->buf[0], h->cellid, h->start, h->rowcnt);
   if ((rc = launch_status("row counts"))) return rc;
   std::vector<int> start(h->C + 1), rows(h->N);
   cudaError_t e = cudaMemcpyAsync(start.data(), h->start, sizeof(int) * (h->C + 1),
@@ -485,9 +675,16 @@ int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out
   for (int i = 0; i < h->n_cases; ++i) {
     CaseDev& c = h->hc[i];
     long long maxocc = 0, occ = 0;
-    for (int k = 0; k < c.ncell; ++k) {
-      long long o = start[c.cell_off + k + 1] - start[c.cell_off + k];
-      maxocc = o > maxocc ? o : maxocc;
+    {
+      // occupancy of the reference's cells: sums over their fine cells
+      const int rx = c.nc[0] / c.sub[0], ry = c.nc[1] / c.sub[1];
+      std::vector<long long> ref((size_t)c.ncell / (c.sub[0] * c.sub[1] * c.sub[2]), 0);
+      for (int k = 0; k < c.ncell; ++k) {
+        const int x = k % c.nc[0], y = (k / c.nc[0]) % c.nc[1], z = k / (c.nc[0] * c.nc[1]);
+        const size_t r = ((size_t)(z / c.sub[2]) * ry + y / c.sub[1]) * rx + x / c.sub[0];
+        ref[r] += start[c.cell_off + k + 1] - start[c.cell_off + k];
+      }
+      for (long long o : ref) maxocc = o > maxocc ? o : maxocc;
     }
     for (int k = 0; k < c.n; ++k) occ += rows[c.p_off + k];
     // _estimate_cell_capacity (jax_md/partition.py:195-199) + extra capacity
@@ -513,6 +710,12 @@ int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out
 
 int sph_nl_set_capacity(SphHandle* h, const SphNLCapacity* cap) {
   if (!h || !cap) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+  if (cap->cell_capacity < 0 || cap->cell_capacity > INT_MAX || cap->max_occupancy < 0)
+    return fail((int)SPH_ERR_INVALID_ARG, "capacity out of range");
+  bool same = true;
+  for (const auto& c : h->hc)
+    same = same && c.cell_cap == (int)cap->cell_capacity && c.edge_cap == cap->max_occupancy;
+  if (same) return 0;  // nothing to upload (a drop-in step sets them on every call)
   for (auto& c : h->hc) {
     c.cell_cap = (int)cap->cell_capacity;
     c.edge_cap = cap->max_occupancy;
@@ -526,8 +729,13 @@ int sph_nl_edges(SphHandle* h, int32_t* idx, int64_t capacity, int64_t* count_de
   if (!h || !idx || !count_dev || capacity < 0)
     return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (!h->binned) return fail((int)SPH_ERR_INVALID_ARG, "neighbour list not built");
+  // the edges come from a binning of the current positions
+  if (!h->fresh) {
+    int rc = bin_static(h, (cudaStream_t)stream);
+    if (rc) return rc;
+  }
   LaunchCtx L = h->ctx((cudaStream_t)stream);
-  launch_edges(L, h->buf[h->cur], h->cellid, h->start, h->rowcnt, h->rowoff, h->scan_tmp, idx,
+  launch_edges(L, h->buf[0], h->cellid, h->start, h->rowcnt, h->rowoff, h->scan_tmp, idx,
                capacity, (long long*)count_dev);
   return launch_status("edges");
 }
@@ -539,7 +747,7 @@ int sph_forward(SphHandle* h, void* stream) {
   int rc = 0;
   if (!h->binned || h->from_forward) rc = bin_static(h, st);
   if (rc) return rc;
-  launch_forward(h->ctx(st), h->buf[h->cur], h->R4, h->R4, h->UT4, h->cellid, h->start,
+  launch_forward(h->ctx(st), h->buf[0], h->R4, h->R4, h->UT4, h->cellid, h->start,
                  h->edgecnt, h->g_arr, false, true);
   h->from_forward = true;
   h->pending_bc = false;
@@ -553,16 +761,17 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream) {
   cudaStream_t st = (cudaStream_t)stream;
   int rc = 0;
   // the first step after loading a state runs eagerly (it folds the loaded
-  // state in); every later step replays the graph of its buffer parity
+  // state in and builds the first candidate lists); every later step replays
+  // the captured steady step
   if (nsteps > 0 && !steady(h)) {
     if ((rc = step_once(h, st))) return rc;
     --nsteps;
   }
   if (h->graph_g_arr != h->g_arr) drop_graph(h);
   while (nsteps > 0) {
-    if (!h->gexec[h->cur] && (rc = capture_graph(h))) return rc;
-    if ((rc = cuda_check(cudaGraphLaunch(h->gexec[h->cur], st), "graph launch"))) return rc;
-    h->cur = 1 - h->cur;
+    if (!h->gexec && (rc = capture_graph(h))) return rc;
+    if ((rc = cuda_check(cudaGraphLaunch(h->gexec, st), "graph launch"))) return rc;
+    h->fresh = false;
     --nsteps;
   }
   return 0;
@@ -587,8 +796,10 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) {
   if (!h || !ms || nsteps <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   cudaStream_t st = (cudaStream_t)stream;
-  cudaEvent_t ev[5];
-  for (int k = 0; k < 5; ++k) cudaEventCreate(&ev[k]);
+  // events: 0 step start, 5 kick end, 6 rebuild start (after the host read
+  // the flag), 1 rebuild end, 2 density end, 3 wall end, 4 force end
+  cudaEvent_t ev[7];
+  for (int k = 0; k < 7; ++k) cudaEventCreate(&ev[k]);
   for (int k = 0; k < 4; ++k) ms[k] = 0.f;
   int rc = 0;
   for (int i = 0; i < nsteps && !rc; ++i) {
@@ -598,13 +809,16 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) {
     if (rc) break;
     cudaError_t e = cudaEventSynchronize(ev[4]);
     if ((rc = cuda_check(e, "profile sync"))) break;
-    for (int k = 0; k < 4; ++k) {
-      float t = 0.f;
+    float t = 0.f, t2 = 0.f;
+    cudaEventElapsedTime(&t, ev[0], ev[5]);
+    cudaEventElapsedTime(&t2, ev[6], ev[1]);
+    ms[0] += (t + t2) / nsteps;  // kick + rebuild, without the host's read
+    for (int k = 1; k < 4; ++k) {
       cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
       ms[k] += t / nsteps;
     }
   }
-  for (int k = 0; k < 5; ++k) cudaEventDestroy(ev[k]);
+  for (int k = 0; k < 7; ++k) cudaEventDestroy(ev[k]);
   return rc;
 }
 
@@ -636,7 +850,7 @@ int sph_tape_record(SphHandle* h, int32_t slot, void* stream) {
     return fail((int)SPH_ERR_INVALID_ARG, "record the tape right after sph_step");
   cudaStream_t st = (cudaStream_t)stream;
   const long long N = h->N;
-  const Buffers& b = h->buf[h->cur];
+  const Buffers& b = h->buf[0];
   cudaError_t e = cudaSuccess;
   auto cp = [&](void* dst, const void* src, size_t bytes) {
     if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
@@ -676,10 +890,31 @@ int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream)
   return rc;
 }
 
+int sph_rebuild_stats(SphHandle* h, int64_t* rebuilds, int32_t* kernels_per_rebuild,
+                      void* stream) {
+  if (!h || !rebuilds || !kernels_per_rebuild) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  unsigned long long v = 0;
+  cudaError_t e = cudaMemcpyAsync(&v, h->rebuilds_d, sizeof(v), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  *rebuilds = (int64_t)v + h->rebuilds_h;
+  *kernels_per_rebuild = h->rebuild_launches;
+  return cuda_check(e, "rebuild stats");
+}
+
+int sph_read_status_async(SphHandle* h, uint32_t* status_dev, int32_t clear, void* stream) {
+  if (!h || !status_dev) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaError_t e = cudaMemcpyAsync(status_dev, h->status, sizeof(unsigned),
+                                  cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess && clear) e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
+  return cuda_check(e, "read status async");
+}
+
 int sph_diagnostics(SphHandle* h, double* out, void* stream) {
   if (!h || !out) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
-  launch_diagnostics(h->ctx((cudaStream_t)stream), h->buf[h->cur], h->R4, h->from_forward,
+  launch_diagnostics(h->ctx((cudaStream_t)stream), h->buf[0], h->R4, h->from_forward,
                      h->pending_bc, out);
   return launch_status("diagnostics");
 }

@@ -39,6 +39,10 @@ struct NList {
   int* nbr;   // [kmax][N] sender indices (k-major)
   int* cnt;   // [N] neighbours without self (may exceed kmax)
   int kmax;
+  const int* vl;   // [kv][N] Verlet candidates, ascending original index
+  const int* vcnt; // [N] candidates (may exceed kv)
+  int kv;
+  const float4* rref;  // positions at the last rebuild
 };
 
 // Per-case edge counter for the NEIGHBOR_LIST_OVERFLOW test: one reduction
@@ -65,11 +69,49 @@ __device__ __forceinline__ void count_edges(int ci, int cnt, bool valid,
   }
 }
 
-// Visit the senders j of receiver i (self excluded): from the neighbour list,
-// or by walking the cells when the list overflowed for i.
+// Visit the senders j of receiver i (self excluded) that are edges at the
+// current positions, from its Verlet candidates (ascending original index),
+// or -- a receiver with more candidates than the list holds -- by walking the
+// cells of the last binning around its position at that binning: every
+// sender now within the cutoff was within the Verlet radius of it then.
+template <int DIM, typename F>
+__device__ __forceinline__ void for_each_edge_slow(long long N, long long i, const float4& ri,
+                                                   const CaseDev& c, const CaseDev* cp,
+                                                   const float4* __restrict__ P4,
+                                                   const int* cellid, const int* start,
+                                                   const NList& L, F&& f) {
+  const float lo = c.cut_lo, hi = c.cut_hi;
+  auto test = [&](int j) {
+    const float4 rj = __ldg(P4 + j);
+    if (edge_mi<DIM>(ri, rj, lo, hi, c, cp)) {
+      float3 dr;
+      float d2;
+      pair_dr<DIM>(ri, rj, c, dr, d2);
+      f(j, rj, dr, d2);
+    }
+  };
+  const int vc = L.vcnt[i];
+  if (vc <= L.kv) {
+    for (int k = 0; k < vc; ++k) test(L.vl[(long long)k * N + i]);
+    return;
+  }
+  const float4 r0 = L.rref[i];
+  auto visit = [&](int j0, int j1, float3) {
+    for (int j = j0; j < j1; ++j)
+      if (j != i) test(j);
+  };
+  if (c.fast)
+    walk_rows<DIM, true>(c, cellid[i] - c.cell_off, r0, start, c.vrad, c.v_r2, visit);
+  else
+    walk_rows<DIM, false>(c, cellid[i] - c.cell_off, r0, start, c.vrad, 0.f, visit);
+}
+
+// Visit the senders j of receiver i (self excluded): from the step's
+// neighbour list, or the slow way when it overflowed for i.
 template <int DIM, typename F>
 __device__ __forceinline__ void for_each_neighbour(long long N, long long i, const float4& ri,
-                                                   const CaseDev& c, const float4* __restrict__ P4,
+                                                   const CaseDev& c, const CaseDev* cp,
+                                                   const float4* __restrict__ P4,
                                                    const int* cellid, const int* start,
                                                    const NList& L, F&& f) {
   const int m = L.cnt[i];
@@ -92,16 +134,70 @@ __device__ __forceinline__ void for_each_neighbour(long long N, long long i, con
     }
     return;
   }
-  for_each_range<DIM>(c, cellid[i] - c.cell_off, start, [&](int j0, int j1, float3 s) {
-    const float3 q = make_float3(ri.x - s.x, ri.y - s.y, ri.z - s.z);
-    for (int j = j0; j < j1; ++j) {
-      if (j == i) continue;
-      const float4 rj = __ldg(P4 + j);
-      float3 dr;
-      float d2;
-      if (edge_dr<DIM>(ri, rj, q, c, dr, d2)) f(j, rj, dr, d2);
+  for_each_edge_slow<DIM>(N, i, ri, c, cp, P4, cellid, start, L, f);
+}
+
+// ------------------------------------------------------------------ Verlet lists
+// Candidate senders of every receiver at the current binning: the particles
+// within the Verlet radius (shifted squared distance < v_r2; in a case
+// without the fast test, the reference's own edges), self excluded. SORT
+// stages them in shared memory in ascending original index (insertion while
+// walking), so that every pair sum built on them runs in an order that depends
+// neither on the binning nor on when it was rebuilt; otherwise they are
+// written in walk order (cell order), straight to the list.
+template <int DIM, bool SORT>
+__global__ void __launch_bounds__(256)
+k_verlet(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
+         int* vl, int* vcnt, int kv) {
+  extern __shared__ int s_v[];  // SORT: keys [kv][blockDim], senders [kv][blockDim]
+  const int tid = threadIdx.x, bs = blockDim.x;
+  int* keys = s_v;
+  int* js = s_v + kv * bs;
+  const long long i = blockIdx.x * (long long)bs + tid;
+  if (i >= N) return;
+  const CaseDev& c = cases[case_of(b.META[i])];
+  const float4 ri = b.P4[i];
+  int m = 0;
+  auto add = [&](int j) {
+    if (m < kv) {
+      if (SORT) {
+        const int key = b.ORIG[j];
+        int p = m;
+        while (p > 0 && keys[(p - 1) * bs + tid] > key) {
+          keys[p * bs + tid] = keys[(p - 1) * bs + tid];
+          js[p * bs + tid] = js[(p - 1) * bs + tid];
+          --p;
+        }
+        keys[p * bs + tid] = key;
+        js[p * bs + tid] = j;
+      } else {
+        vl[(long long)m * N + i] = j;
+      }
     }
-  });
+    ++m;
+  };
+  const int cell = cellid[i] - c.cell_off;
+  if (c.fast) {
+    const float r2 = c.v_r2;
+    walk_rows<DIM, true>(c, cell, ri, start, c.vrad, r2, [&](int j0, int j1, float3 s) {
+      const float qx = ri.x - s.x, qy = ri.y - s.y, qz = ri.z - s.z;
+      for (int j = j0; j < j1; ++j) {
+        const float4 rj = __ldg(b.P4 + j);
+        const float dx = qx - rj.x, dy = qy - rj.y, dz = (DIM == 3) ? qz - rj.z : 0.f;
+        if (j != i && dx * dx + dy * dy + dz * dz < r2) add(j);
+      }
+    });
+  } else {
+    walk_rows<DIM, false>(c, cell, ri, start, c.vrad, 0.f, [&](int j0, int j1, float3) {
+      for (int j = j0; j < j1; ++j)
+        if (j != i && is_edge<DIM>(ri, __ldg(b.P4 + j), c)) add(j);
+    });
+  }
+  vcnt[i] = m;
+  if (SORT) {
+    const int e = m < kv ? m : kv;
+    for (int k = 0; k < e; ++k) vl[(long long)k * N + i] = js[k * bs + tid];
+  }
 }
 
 // ------------------------------------------------------------------ density pass
@@ -135,32 +231,55 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
     const int tag = tag_of(meta);
     const bool fluid = tag == FLUID;
     const float4 ri = b.P4[i];
-    // phase 1: candidate walk
+    // the self pair is always an edge (metric(r, r) = 0 < cutoff^2)
+    const bool self_term = !mask_self;
+    Acc<KAHAN> s0, sx, sy, sz;
+    // the self pair: W(0) in a summation; zero gradient elsewhere; a wall is
+    // not a fluid sender of its own Shepard average
+    if (MODE == 0 && fluid && self_term) s0.add(kw<KER>(0.f, c));
+    // a summation needs only W(|r_ij|): it is accumulated while filtering,
+    // in the same order as a second pass would
+    const bool sum_here = MODE == 0 && fluid;
+    // phase 1: filter the Verlet candidates (ascending original index)
     int m = 0;
-    bool self_edge = false;
     const int kmax = nl.kmax;
     const float lo = c.cut_lo, hi = c.cut_hi;
     const CaseDev* cp = cases + ci;
-    for_each_range<DIM>(c, cellid[i] - c.cell_off, start, [&](int j0, int j1, float3 s) {
-      const float3 q = make_float3(ri.x - s.x, ri.y - s.y, ri.z - s.z);
-      // two independent gathers per iteration; the body is branch-free
-      // (predicated count, unconditional shared-memory store)
-      for (int j = j0; j < j1; j += 2) {
-        const bool v1 = j + 1 < j1;
-        const float4 ra = __ldg(b.P4 + j);
-        const float4 rb = v1 ? __ldg(b.P4 + j + 1) : make_float4(3e30f, 3e30f, 3e30f, 0.f);
-        bool ea = edge_walk<DIM>(ri, ra, q, lo, hi, cp);
-        bool eb = v1 && edge_walk<DIM>(ri, rb, q, lo, hi, cp);
-        self_edge |= (ea && j == i) || (eb && j + 1 == i);
-        ea = ea && j != i;
-        eb = eb && j + 1 != i;
-        s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = j;
+    const int vc = nl.vcnt[i];
+    if (vc <= nl.kv) {
+      // two independent gathers per iteration, the next two candidate
+      // indices loaded ahead; predicated count and an unconditional
+      // shared-memory store
+      const int* vli = nl.vl + i;
+      int jan = vc > 0 ? vli[0] : 0;
+      int jbn = vc > 1 ? vli[N] : jan;
+      for (int k = 0; k < vc; k += 2) {
+        const bool v1 = k + 1 < vc;
+        const int ja = jan, jb = jbn;
+        if (k + 2 < vc) jan = vli[(long long)(k + 2) * N];
+        jbn = k + 3 < vc ? vli[(long long)(k + 3) * N] : jan;
+        const float4 ra = __ldg(b.P4 + ja);
+        const float4 rb = __ldg(b.P4 + jb);
+        float d2a, d2b;
+        const bool ea = edge_mi_d2<DIM>(ri, ra, lo, hi, c, cp, d2a);
+        const bool eb = v1 && edge_mi_d2<DIM>(ri, rb, lo, hi, c, cp, d2b);
+        if (sum_here) {
+          if (ea) s0.add(kw<KER>(d2a > 0.f ? sqrtf(d2a) : 0.f, c));
+          if (eb) s0.add(kw<KER>(d2b > 0.f ? sqrtf(d2b) : 0.f, c));
+        }
+        s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = ja;
         m += ea;
-        s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = j + 1;
+        s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = jb;
         m += eb;
       }
-    });
-    const bool self_term = self_edge && !mask_self;
+    } else {
+      for_each_edge_slow<DIM>(N, i, ri, c, cp, b.P4, cellid, start, nl,
+                              [&](int j, const float4&, const float3&, float d2) {
+                                if (sum_here) s0.add(kw<KER>(d2 > 0.f ? sqrtf(d2) : 0.f, c));
+                                s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = j;
+                                ++m;
+                              });
+    }
     cnt = m + (self_term ? 1 : 0);
     nl.cnt[i] = m;
 
@@ -170,13 +289,9 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
     const float rho_i = Ui.w;
     const float p_i = b.V4[i].w;
     const bool shepard = rie_shepard && !fluid;
-    const bool need_pairs = MODE == 1 || fluid || shepard;
+    const bool need_pairs = MODE == 1 || (fluid && MODE != 0) || shepard;
     float3 gi = make_float3(0.f, 0.f, 0.f);
     if (MODE == 2) gi = g_ext<DIM>(c, ri, g_arr, b.ORIG[i]);
-    Acc<KAHAN> s0, sx, sy, sz;
-    // the self pair: W(0) in a summation; zero gradient elsewhere; a wall is
-    // not a fluid sender of its own Shepard average
-    if (MODE == 0 && fluid && self_term) s0.add(kw<KER>(0.f, c));
     auto pair = [&](int j, const float4& rj, const float3& dr, float d2) {
       const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
       if (shepard) {
@@ -188,10 +303,6 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
           sy.add(w * Uj.y);
           sz.add(w * Uj.z);
         }
-        return;
-      }
-      if (MODE == 0) {
-        s0.add(kw<KER>(dist, c));
         return;
       }
       const float4 Uj = b.U4[j];
@@ -252,18 +363,9 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
         }
       }
     } else if (need_pairs) {
-      // more senders than list slots: walk the cells again (the wall and
-      // force passes do the same for this receiver)
-      for_each_range<DIM>(c, cellid[i] - c.cell_off, start, [&](int j0, int j1, float3 s) {
-        const float3 q = make_float3(ri.x - s.x, ri.y - s.y, ri.z - s.z);
-        for (int j = j0; j < j1; ++j) {
-          if (j == i) continue;
-          const float4 rj = __ldg(b.P4 + j);
-          float3 dr;
-          float d2;
-          if (edge_dr<DIM>(ri, rj, q, c, dr, d2)) pair(j, rj, dr, d2);
-        }
-      });
+      // more senders than list slots: filter the candidates again (the wall
+      // and force passes do the same for this receiver)
+      for_each_edge_slow<DIM>(N, i, ri, c, cp, b.P4, cellid, start, nl, pair);
     }
     float rho_new = rho_i, drhodt = 0.f;
     if (MODE == 0) {
@@ -305,7 +407,7 @@ k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const in
   const CaseDev& c = cases[case_of(meta)];
   const float4 ri = b.P4[i];
   Acc<KAHAN> sw, su[3], sv[3], sp, sr[3];
-  for_each_neighbour<DIM>(N, i, ri, c, b.P4, cellid, start, nl,
+  for_each_neighbour<DIM>(N, i, ri, c, cases + case_of(meta), b.P4, cellid, start, nl,
                           [&](int j, const float4& rj, const float3& dr, float d2) {
     if (tag_of(b.META[j]) != FLUID) return;
     const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
@@ -339,6 +441,10 @@ k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const in
 
 // ------------------------------------------------------------------ force pass
 // SOLVER 0: standard SPH with transport-velocity stress; 1: Riemann SPH.
+// The per-pair quotients use the fast division intrinsic (at most 2 ulp, for
+// denominators far inside its range): the correctly rounded division is a
+// multi-instruction sequence that cost a quarter of this pass, and the
+// float32 tolerances against the float64 oracle hold either way.
 template <int DIM, int KER, int SOLVER, bool KAHAN>
 __global__ void __launch_bounds__(kBlock, 3)
 k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
@@ -366,23 +472,23 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
   const bool av = c.av_alpha != 0.0f;
   const float mask_i = (SOLVER == 1 && bc_trick && free_slip) ? (fluid_i ? 1.f : 0.f) : 1.f;
   Acc<KAHAN> ax, ay, az, tx, ty, tz;
-  for_each_neighbour<DIM>(N, i, ri, c, b.P4, cellid, start, nl,
+  for_each_neighbour<DIM>(N, i, ri, c, cases + case_of(meta), b.P4, cellid, start, nl,
                           [&](int j, const float4& rj, const float3& dr, float d2) {
     const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
     const float gw = kdw<KER>(dist, c);
-    const float inv_d = 1.0f / (dist + kEps);
+    const float inv_d = __fdividef(1.0f, dist + kEps);
     const float4 Rj = R4[j];
     const float rho_j = Rj.x, p_j = Rj.y, eta_j = Rj.w, m_j = rj.w;
-    const float Vj = m_j / rho_j;
+    const float Vj = __fdividef(m_j, rho_j);
     const float cc = (Vi2 + Vj * Vj) * inv_mi * gw * inv_d;
     const float3 uj = f3(b.U4[j]);
-    const float eta_ij = 2.f * eta_i * eta_j / (eta_i + eta_j + kEps);
+    const float eta_ij = __fdividef(2.f * eta_i * eta_j, eta_i + eta_j + kEps);
     int tj = FLUID;
     if (SOLVER == 1 || av) tj = tag_of(b.META[j]);
     float3 a;
     if (SOLVER == 0) {
       const float3 vj = f3(b.V4[j]);
-      const float p_ij = (rho_j * p_i + rho_i * p_j) / (rho_i + rho_j);
+      const float p_ij = __fdividef(rho_j * p_i + rho_i * p_j, rho_i + rho_j);
       const float ki = dot3(wi, dr);
       const float kj = dot3(make_float3(vj.x - uj.x, vj.y - uj.y, vj.z - uj.z), dr);
       const float3 Ar = make_float3(0.5f * (Ai.x * ki + rho_j * uj.x * kj),
@@ -421,8 +527,8 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
       }
       const float Pstar = P_avg + 0.5f * rho_avg * (uL - uR) * beta;
       const float rr = rho_i * rho_j;
-      const float k9 = -2.f * m_j * (Pstar / rr);
-      const float k6 = 2.f * m_j * eta_ij / rr * inv_d * gw * mask_i;
+      const float k9 = -2.f * m_j * __fdividef(Pstar, rr);
+      const float k6 = 2.f * m_j * __fdividef(eta_ij, rr) * inv_d * gw * mask_i;
       a = make_float3(k9 * kg.x + k6 * (ui.x - ud.x), k9 * kg.y + k6 * (ui.y - ud.y),
                       k9 * kg.z + k6 * (ui.z - ud.z));
     }
@@ -471,7 +577,7 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
   const int rie_shepard = rie && L.bc_trick && !L.free_slip;
   const int sph_gwbc = !rie && L.bc_trick;
   float4* ut = rie ? UT4 : nullptr;
-  NList nl{L.nbr, L.nbr_cnt, L.kmax};
+  NList nl{L.nbr, L.nbr_cnt, L.kmax, L.vl, L.vcnt, L.kv, L.rref};
 #define SPH_DENSITY(MODE)                                                                 \
   k_density<DIM, KER, MODE, KAHAN><<<g, bt, smem, st>>>(L.N, b, L.cases, cellid, start,  \
                                                          L.mask_self, rie_shepard,        \
@@ -515,6 +621,38 @@ void forward_k(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
 }
 
 }  // namespace
+
+cudaError_t prepare_kernels(int kv) {
+  const int smem = 2 * (int)sizeof(int) * kv * verlet_block(kv);
+  cudaError_t e =
+      cudaFuncSetAttribute(k_verlet<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_verlet<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  return e;
+}
+
+void launch_verlet(const LaunchCtx& L, Buffers b, const int* cellid, const int* start) {
+  if (L.canonical) {
+    const int bt = verlet_block(L.kv);
+    const int g = nblocks(L.N, bt);
+    const size_t smem = 2 * sizeof(int) * L.kv * bt;
+    if (L.dim == 3)
+      k_verlet<3, true><<<g, bt, smem, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl, L.vcnt,
+                                                   L.kv);
+    else
+      k_verlet<2, true><<<g, bt, smem, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl, L.vcnt,
+                                                   L.kv);
+  } else {
+    const int g = nblocks(L.N, kBlock);
+    if (L.dim == 3)
+      k_verlet<3, false><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl,
+                                                     L.vcnt, L.kv);
+    else
+      k_verlet<2, false><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl,
+                                                     L.vcnt, L.kv);
+  }
+  count_launch(L);
+}
 
 void launch_forward(const LaunchCtx& L, Buffers b, const float4* /*R4*/, float4* R4w, float4* UT4,
                     const int* cellid, const int* start, unsigned long long* edgecnt,

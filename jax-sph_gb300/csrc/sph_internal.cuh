@@ -34,12 +34,29 @@ enum Tag { FLUID = 0, SOLID_WALL = 1, MOVING_WALL = 2, DIRICHLET_WALL = 3 };
 // more neighbours makes the passes walk its cells instead.
 constexpr int kListSlots = 40;
 
+// Verlet candidate slots per particle: sized per handle from the expected
+// candidate count (the volume of the Verlet sphere over dx^d, times 1.5, plus
+// 8), between these bounds; a particle with more walks its cells instead.
+constexpr int kVerletMinSlots = 32;
+constexpr int kVerletMaxSlots = 384;
+// Threads per block of the candidate-list build for kv slots (its shared
+// memory, 8 kv bytes per thread, stays under 100 KB).
+inline int verlet_block(int kv) { return kv <= 96 ? 128 : (kv <= 192 ? 64 : 32); }
+
 // Per-case constants, all rounded to float32 the way the reference's
 // float32 program sees them.
+//
+// The particles are binned into cells of the reference's cell size divided by
+// sub (1 or 2) along each axis. With sub = 2 the fine size is exactly half the
+// reference's (a power-of-two split), so fl(r / (s/2)) = 2 fl(r / s) and the
+// reference's cell index is the fine index >> 1: the reference's cell
+// occupancy is the sum over its 2^d fine cells.
 struct CaseDev {
   float box[3], half[3];
-  float cell_size[3];
-  int nc[3];          // cells per side (1 along an axis with fewer than 3 cells)
+  float cell_size[3];  // binned (fine) cell size
+  int nc[3];          // fine cells per side (1 along an axis with fewer than 3 reference cells)
+  int sub[3];         // fine cells per reference cell along each axis
+  int rad[3];         // cells walked on each side of the receiver's cell (0: whole axis)
   int mult[3];        // hash multipliers (1, nx, nx*ny)
   int use_cells;      // reference builds a cell list (cells >= 3 on every axis)
   int cell_off, ncell;
@@ -65,6 +82,20 @@ struct CaseDev {
   int fast;
   float cut_lo, cut_hi;
   float inv_box[3];
+  // Row trimming of the walk (fast cases): a (y, z) row of cells is skipped
+  // when its nearest point is farther than sqrt(trim_r2), and its x extent is
+  // cut to the chord of that sphere; trim_m (64 ulp of the largest side)
+  // absorbs every rounding of the bounds and of the hash.
+  float trim_r2, trim_m;
+  float inv_cs[3];
+  // Verlet candidate list: the senders within sqrt(v_r2) of the receiver at
+  // the last rebuild, found by walking vrad cells on each side; a rebuild is
+  // due once some particle has moved farther than sqrt(v_dmax2) since (half
+  // the skin, less rounding margins), so every sender within the cutoff stays
+  // in the list until then. Without a skin v_dmax2 = 0: any motion rebuilds.
+  int vrad[3];
+  float v_r2, v_dmax2;
+  int cref_off, ncref;  // this case's reference cells in the per-step occupancy count
   double dt64, box64[3];  // float64 drift of the precision form
 };
 
@@ -235,86 +266,76 @@ __device__ __forceinline__ int cell_hash(const float4& r, const CaseDev& c, unsi
   return h;
 }
 
-// Visit every particle of the 3^d periodic neighbour cells of `cell_local`
-// (the candidate set of jax_md/partition.py:832-856, as a set). Cells along x
-// are contiguous in the sorted order, so each (y, z) row is one or two ranges.
-template <int DIM, typename F>
-__device__ __forceinline__ void for_each_candidate(const CaseDev& c, int cell_local,
-                                                   const int* __restrict__ start, F&& f) {
+// Visit the candidate senders of a receiver in cell `cell_local` at ri as
+// ranges [j0, j1) of the cell-sorted order, f(j0, j1, s), where s (per axis
+// -L, 0 or +L) is the periodic shift that maps the range's particles to their
+// image next to the receiver. The walk covers rad[d] cells on each side of the
+// receiver's cell along every axis (the whole axis where rad = 0): with
+// c.rad, a superset of the reference's 3^d-cell candidates that are within
+// the cutoff (jax_md/partition.py:832-856); with c.vrad, of those within the
+// Verlet radius. Cells along x are contiguous in the sorted order, so each
+// (y, z) row is one range, or two where it wraps.
+// TRIM (fast cases): a row whose nearest point lies beyond sqrt(trim_r2) is
+// skipped and the x extent of the others is cut to the sphere's chord; the
+// bounds are lowered by trim_m, so no particle within that sphere is ever
+// left out.
+template <int DIM, bool TRIM, typename F>
+__device__ __forceinline__ void walk_rows(const CaseDev& c, int cell_local, const float4& ri,
+                                          const int* __restrict__ start, const int* rad,
+                                          float trim_r2, F&& f) {
   const int nx = c.nc[0], ny = c.nc[1], nz = (DIM == 3) ? c.nc[2] : 1;
   const int cx = cell_local % nx;
   const int t = cell_local / nx;
   const int cy = t % ny;
   const int cz = (DIM == 3) ? t / ny : 0;
   const int* cs = start + c.cell_off;
-  const int zr = (DIM == 3 && nz >= 3) ? 1 : 0;
-  const int yr = (ny >= 3) ? 1 : 0;
-  for (int dz = -zr; dz <= zr; ++dz) {
-    int zz = cz + dz;
-    zz = zz < 0 ? zz + nz : (zz >= nz ? zz - nz : zz);
-    for (int dy = -yr; dy <= yr; ++dy) {
-      int yy = cy + dy;
-      yy = yy < 0 ? yy + ny : (yy >= ny ? yy - ny : yy);
-      const int row = (zz * ny + yy) * nx;
-      int a0, b0, a1 = 0, b1 = -1;  // inclusive cell ranges
-      if (nx >= 3) {
-        if (cx == 0) {
-          a0 = row; b0 = row + 1; a1 = row + nx - 1; b1 = row + nx - 1;
-        } else if (cx == nx - 1) {
-          a0 = row + nx - 2; b0 = row + nx - 1; a1 = row; b1 = row;
-        } else {
-          a0 = row + cx - 1; b0 = row + cx + 1;
-        }
-      } else {
-        a0 = row; b0 = row + nx - 1;
-      }
-      const int e0 = cs[b0 + 1];
-      for (int j = cs[a0]; j < e0; ++j) f(j);
-      if (b1 >= a1) {
-        const int e1 = cs[b1 + 1];
-        for (int j = cs[a1]; j < e1; ++j) f(j);
-      }
-    }
-  }
-}
-
-// Like for_each_candidate, but visits ranges [j0, j1) together with the
-// periodic shift s (per axis -L, 0 or +L) that maps the range's particles to
-// their image next to the receiving cell: f(j0, j1, s).
-template <int DIM, typename F>
-__device__ __forceinline__ void for_each_range(const CaseDev& c, int cell_local,
-                                               const int* __restrict__ start, F&& f) {
-  const int nx = c.nc[0], ny = c.nc[1], nz = (DIM == 3) ? c.nc[2] : 1;
-  const int cx = cell_local % nx;
-  const int t = cell_local / nx;
-  const int cy = t % ny;
-  const int cz = (DIM == 3) ? t / ny : 0;
-  const int* cs = start + c.cell_off;
-  const int zr = (DIM == 3 && nz >= 3) ? 1 : 0;
-  const int yr = (ny >= 3) ? 1 : 0;
-  for (int dz = -zr; dz <= zr; ++dz) {
+  const int rx = rad[0], ry = rad[1];
+  const int rz = (DIM == 3) ? rad[2] : 0;
+  for (int dz = -rz; dz <= rz; ++dz) {
     int zz = cz + dz;
     float sz = 0.f;
     if (zz < 0) { zz += nz; sz = -c.box[2]; }
     else if (zz >= nz) { zz -= nz; sz = c.box[2]; }
-    for (int dy = -yr; dy <= yr; ++dy) {
+    float gz2 = 0.f;
+    if (TRIM && DIM == 3 && dz != 0) {
+      const float g = (dz > 0 ? (float)(cz + dz) * c.cell_size[2] - ri.z
+                              : ri.z - (float)(cz + dz + 1) * c.cell_size[2]) - c.trim_m;
+      gz2 = g > 0.f ? g * g : 0.f;
+    }
+    for (int dy = -ry; dy <= ry; ++dy) {
       int yy = cy + dy;
       float sy = 0.f;
       if (yy < 0) { yy += ny; sy = -c.box[1]; }
       else if (yy >= ny) { yy -= ny; sy = c.box[1]; }
       const int row = (zz * ny + yy) * nx;
-      // up to two x-ranges per row (a second one where the row wraps); the
-      // visitor is instantiated once, inside the loop
-      int a0 = row, b0 = row + nx, a1 = row, b1 = row;
-      float s1 = 0.f;
-      if (nx >= 3) {
-        if (cx == 0) {
-          b0 = row + 2; a1 = row + nx - 1; b1 = row + nx; s1 = -c.box[0];
-        } else if (cx == nx - 1) {
-          a0 = row + nx - 2; a1 = row; b1 = row + 1; s1 = c.box[0];
-        } else {
-          a0 = row + cx - 1; b0 = row + cx + 2;
+      // x cells [xa, xb] of this row, unwrapped
+      int xa = cx - rx, xb = cx + rx;
+      if (TRIM) {
+        float g2 = gz2;
+        if (dy != 0) {
+          const float g = (dy > 0 ? (float)(cy + dy) * c.cell_size[1] - ri.y
+                                  : ri.y - (float)(cy + dy + 1) * c.cell_size[1]) - c.trim_m;
+          if (g > 0.f) g2 += g * g;
         }
+        if (g2 >= trim_r2) continue;
+        const float w = sqrtf(trim_r2 - g2) + c.trim_m;
+        const int lo = (int)floorf((ri.x - w) * c.inv_cs[0]);
+        const int hi = (int)floorf((ri.x + w) * c.inv_cs[0]);
+        xa = lo > xa ? lo : xa;
+        xb = hi < xb ? hi : xb;
+      }
+      // up to two ranges (the second where the row wraps); the visitor is
+      // instantiated once, inside the loop
+      int a0, b0, a1 = row, b1 = row;
+      float s1 = 0.f;
+      if (rx == 0) {
+        a0 = row; b0 = row + nx;
+      } else if (xa < 0) {
+        a0 = row; b0 = row + xb + 1; a1 = row + xa + nx; b1 = row + nx; s1 = -c.box[0];
+      } else if (xb >= nx) {
+        a0 = row + xa; b0 = row + nx; a1 = row; b1 = row + xb - nx + 1; s1 = c.box[0];
+      } else {
+        a0 = row + xa; b0 = row + xb + 1;
       }
 #pragma unroll 1
       for (int r = 0; r < 2; ++r) {
@@ -325,26 +346,58 @@ __device__ __forceinline__ void for_each_range(const CaseDev& c, int cell_local,
   }
 }
 
-// Membership of edge (receiver ri, sender rj) with the fast test when the
-// case allows it; q = ri - s for the sender's range shift s. On success
-// returns true and dr = r_i - r_j (minimum image) and its squared norm.
+// Occupancy of the reference's cell that contains fine cell `cell_local`:
+// the sum over its sub[0] x sub[1] x sub[2] fine cells.
 template <int DIM>
-__device__ __forceinline__ bool edge_dr(const float4& ri, const float4& rj, const float3& q,
-                                        const CaseDev& c, float3& dr, float& d2) {
-  if (c.fast) {
-    dr.x = q.x - rj.x;
-    dr.y = q.y - rj.y;
-    dr.z = (DIM == 3) ? q.z - rj.z : 0.f;
-    d2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
-    if (d2 >= c.cut_hi) return false;
-    if (d2 > c.cut_lo && !is_edge<DIM>(ri, rj, c)) return false;
-    return true;
-  }
-  if (!is_edge<DIM>(ri, rj, c)) return false;
-  dr = pdisp3<DIM>(ri, rj, c);
-  d2 = sqd<DIM>(dr);
-  return true;
+__device__ __forceinline__ int ref_cell_occupancy(const CaseDev& c, int cell_local,
+                                                  const int* __restrict__ start) {
+  const int* cs = start + c.cell_off;
+  const int nx = c.nc[0], ny = c.nc[1];
+  const int cx = cell_local % nx;
+  const int t = cell_local / nx;
+  const int cy = t % ny;
+  const int cz = (DIM == 3) ? t / ny : 0;
+  const int bx = cx - cx % c.sub[0], by = cy - cy % c.sub[1];
+  const int sz = (DIM == 3) ? c.sub[2] : 1;
+  const int bz = cz - cz % sz;
+  int occ = 0;
+  for (int oz = 0; oz < sz; ++oz)
+    for (int oy = 0; oy < c.sub[1]; ++oy) {
+      const int row = ((bz + oz) * ny + by + oy) * nx + bx;
+      occ += cs[row + c.sub[0]] - cs[row];
+    }
+  return occ;
 }
+
+// Index of the reference's cell of r within its case (the reference's hash,
+// jax_md/partition.py:367-368): the binned cell coordinates divided by sub,
+// clamped into the grid. Returns -1 for a non-finite position.
+template <int DIM>
+__device__ __forceinline__ int ref_cell_hash(const float4& r, const CaseDev& c) {
+  const float rr[3] = {r.x, r.y, r.z};
+  int h = 0, mult = 1;
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    if (!isfinite(rr[d])) return -1;
+    const int n = c.nc[d] / c.sub[d];
+    int ix = c.nc[d] > 1 ? __float2int_rz(__fdiv_rn(rr[d], c.cell_size[d])) / c.sub[d] : 0;
+    ix = ix < 0 ? 0 : (ix >= n ? n - 1 : ix);
+    h += ix * mult;
+    mult *= n;
+  }
+  return h;
+}
+
+// Every candidate sender (untrimmed walk), one at a time.
+template <int DIM, typename F>
+__device__ __forceinline__ void for_each_candidate(const CaseDev& c, int cell_local,
+                                                   const int* __restrict__ start, F&& f) {
+  walk_rows<DIM, false>(c, cell_local, make_float4(0.f, 0.f, 0.f, 0.f), start, c.rad, 0.f,
+                        [&](int j0, int j1, float3) {
+                          for (int j = j0; j < j1; ++j) f(j);
+                        });
+}
+
 
 // The reference metric, out of line: only candidates in the narrow band
 // around the cutoff (or every candidate of a case without the fast test)
@@ -352,23 +405,6 @@ __device__ __forceinline__ bool edge_dr(const float4& ri, const float4& rj, cons
 template <int DIM>
 __device__ __noinline__ bool exact_edge(float4 ri, float4 rj, const CaseDev* c) {
   return is_edge<DIM>(ri, rj, *c);
-}
-
-// Branch-free membership for the candidate walk: d2 of the shifted
-// difference against the band [lo, hi) (lo = -1, hi = inf for a case
-// without the fast test), the reference metric inside the band.
-template <int DIM>
-__device__ __forceinline__ bool edge_walk(const float4& ri, const float4& rj, const float3& q,
-                                          float lo, float hi, const CaseDev* c) {
-  const float dx = q.x - rj.x, dy = q.y - rj.y;
-  float d2 = fmaf(dx, dx, dy * dy);
-  if (DIM == 3) {
-    const float dz = q.z - rj.z;
-    d2 = fmaf(dz, dz, d2);
-  }
-  bool in = d2 < lo;
-  if (!in && d2 < hi) in = exact_edge<DIM>(ri, rj, c);
-  return in;
 }
 
 // Minimum-image r_i - r_j of a pair already known to be an edge.
@@ -387,6 +423,37 @@ __device__ __forceinline__ void pair_dr(const float4& ri, const float4& rj, cons
     dr = pdisp3<DIM>(ri, rj, c);
     d2 = sqd<DIM>(dr);
   }
+}
+
+// Membership of edge (receiver ri, sender rj) for a candidate whose periodic
+// image is not known from a walk (Verlet list, walk of a past binning): the
+// minimum-image squared distance against the band [lo, hi), the reference
+// metric inside it. That distance differs from the reference metric by no
+// more than the shifted one does, so the band of the fast test holds. A case
+// without the fast test takes the reference metric for every candidate.
+template <int DIM>
+__device__ __forceinline__ bool edge_mi(const float4& ri, const float4& rj, float lo, float hi,
+                                        const CaseDev& c, const CaseDev* cp) {
+  if (!c.fast) return exact_edge<DIM>(ri, rj, cp);
+  float3 dr;
+  float d2;
+  pair_dr<DIM>(ri, rj, c, dr, d2);
+  bool in = d2 < lo;
+  if (!in && d2 < hi) in = exact_edge<DIM>(ri, rj, cp);
+  return in;
+}
+
+// edge_mi that also returns the squared distance pair_dr gives the pair.
+template <int DIM>
+__device__ __forceinline__ bool edge_mi_d2(const float4& ri, const float4& rj, float lo,
+                                           float hi, const CaseDev& c, const CaseDev* cp,
+                                           float& d2) {
+  float3 dr;
+  pair_dr<DIM>(ri, rj, c, dr, d2);
+  if (!c.fast) return exact_edge<DIM>(ri, rj, cp);
+  bool in = d2 < lo;
+  if (!in && d2 < hi) in = exact_edge<DIM>(ri, rj, cp);
+  return in;
 }
 
 // Compensated accumulation (Kahan) selected at compile time.
@@ -419,6 +486,13 @@ struct LaunchCtx {
   int* nbr;               // per-step neighbour list [kmax][N]
   int* nbr_cnt;           // neighbours per particle (self excluded)
   int kmax;
+  int* vl;                // Verlet candidates [kv][N], ascending original index
+  int* vcnt;              // candidates per particle (may exceed kv)
+  int kv;
+  float4* rref;           // positions at the last rebuild
+  int* cref_count;        // per-step occupancy of the reference's cells
+  unsigned* vflag;        // a rebuild is due
+  int canonical;          // candidate lists in ascending original index
   int block;              // threads per block of the forward passes (<= 256)
   int* launches;          // optional host counter of kernel launches
   cudaEvent_t* ev;        // optional phase events: bin start, bin end, density end,
@@ -439,7 +513,11 @@ void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateVie
 void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,
                 int* count, int* start, int* keyc, int* keys, int* tsrc, int* tkey, int* tcell,
                 int* scan_tmp, long long total_cells, bool drift, bool from_forward,
-                bool apply_bc);
+                bool apply_bc, float4* rref);
+// In-place kick-drift of a step on the resident buffers, with the per-step
+// reference-cell occupancy test and the rebuild test.
+void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_cells,
+                 bool from_forward, bool apply_bc);
 int launch_scan(cudaStream_t st, const int* in, int* out, long long n, int* tmp);
 void launch_edges(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
                   int* rowcnt, int* rowoff, int* scan_tmp, int32_t* idx, long long capacity,
@@ -450,6 +528,10 @@ void launch_diagnostics(const LaunchCtx& L, Buffers b, const float4* R4, bool fr
                         bool apply_bc, double* out);
 
 // sph_forward.cu
+// Verlet candidate lists of the current binning.
+void launch_verlet(const LaunchCtx& L, Buffers b, const int* cellid, const int* start);
+// One-time kernel attributes (shared-memory opt-in); returns a CUDA error.
+cudaError_t prepare_kernels(int kv);
 void launch_forward(const LaunchCtx& L, Buffers b, const float4* R4, float4* R4w, float4* UT4,
                     const int* cellid, const int* start, unsigned long long* edgecnt,
                     const float* g_arr, bool apply_bc, bool has_walls);
@@ -464,7 +546,7 @@ void launch_adjoint(const LaunchCtx& L, const int* orig, const float4* P4, const
 // sph_capi.cu: per-case device constants from the ABI parameters; returns
 // non-zero and sets `err` on invalid input.
 int make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long long cell_off,
-              CaseDev& c, std::string& err);
+              CaseDev& c, std::string& err, bool fine_cells = true);
 // sph_capi.cu: the message sph_last_error returns on this host thread.
 void set_last_error(const std::string& msg);
 

@@ -165,7 +165,7 @@ int sph_nl_edges_noalloc(int32_t dim, const double* box, double r_cutoff, int32_
   sc.eta_limiter = -1.0;
   CaseDev c;
   std::string err;
-  if (make_case(cfg, sc, 0, 0, c, err)) return fail((int)SPH_ERR_INVALID_ARG, err.c_str());
+  if (make_case(cfg, sc, 0, 0, c, err, false)) return fail((int)SPH_ERR_INVALID_ARG, err.c_str());
   if (c.ncell > kMaxC)
     return fail((int)SPH_ERR_INVALID_ARG, "cell count above SPH_NOALLOC_MAX_CELLS (65536)");
   unsigned char* base = nullptr;

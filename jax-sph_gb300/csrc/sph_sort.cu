@@ -208,7 +208,7 @@ template <int DIM>
 __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4,
                           const CaseDev* cases, const int* start, const int* tsrc,
                           const int* tkey, const int* tcell, int* cellid, unsigned* status,
-                          bool drift, bool from_forward, bool apply_bc) {
+                          bool drift, bool from_forward, bool apply_bc, float4* rref) {
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   bool over = false;
   if (q < N) {
@@ -243,9 +243,71 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
     out.ORIG[dest] = key;
     if (out.NW4) out.NW4[dest] = in.NW4[src];
     cellid[dest] = cell;
-    over = c.use_cells && (e - a) > c.cell_cap;
+    if (rref) rref[dest] = r;
+    // one test per occupied cell, against the reference's cell
+    if (c.use_cells && q == a)
+      over = ref_cell_occupancy<DIM>(c, cell - c.cell_off, start) > c.cell_cap;
   }
   if (__any_sync(kFull, over) && (threadIdx.x & 31) == 0) atomicOr(status, SPH_CELL_LIST_OVERFLOW);
+}
+
+// One si_euler kick-drift (integrator.py:22-56) in place on the resident
+// buffers, with the state folded in first (forward result, bc_fn). Two tests
+// per particle ride along:
+//  * the reference's cell-list capacity test of this step's update
+//    (jax_md/partition.py:385-392): occupancy of the reference's cells,
+//    counted with one atomic per cell present in a warp;
+//  * the rebuild test: a rebuild of the candidate lists is due once the
+//    minimum-image displacement since the last rebuild exceeds sqrt(v_dmax2).
+template <int DIM>
+__global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* cases,
+                       const float4* rref, int* cref_count, unsigned* vflag, unsigned* status,
+                       bool from_forward, bool apply_bc) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int lane = threadIdx.x & 31;
+  bool rebuild = false, over = false;
+  int key = -1, cap = 0;
+  if (i < N) {
+    const int meta = b.META[i];
+    const CaseDev& c = cases[case_of(meta)];
+    const Final f = finalize(b, R4, i, c, tag_of(meta), from_forward, apply_bc);
+    float4 r = b.P4[i];
+    float3 u = f.u, v;
+    const float4 A = b.A4[i], B = b.A2[i];
+    if (b.RD) {
+      double4 rd = b.RD[i];
+      kick_drift64<DIM>(r, rd, u, v, A, B, c);
+      b.RD[i] = rd;
+    } else {
+      kick_drift<DIM>(r, u, v, A, B, c);
+    }
+    b.P4[i] = r;
+    b.U4[i] = make_float4(u.x, u.y, u.z, f.rho);
+    b.V4[i] = make_float4(v.x, v.y, v.z, f.p);
+    const float4 q = rref[i];
+    float dx = r.x - q.x, dy = r.y - q.y, dz = (DIM == 3) ? r.z - q.z : 0.f;
+    dx = fmaf(-c.box[0], rintf(dx * c.inv_box[0]), dx);
+    dy = fmaf(-c.box[1], rintf(dy * c.inv_box[1]), dy);
+    if (DIM == 3) dz = fmaf(-c.box[2], rintf(dz * c.inv_box[2]), dz);
+    rebuild = !(dx * dx + dy * dy + dz * dz <= c.v_dmax2);  // NaN rebuilds too
+    if (c.use_cells) {
+      key = ref_cell_hash<DIM>(r, c);
+      if (key < 0) atomicOr(status, SPH_ERR_NONFINITE);
+      else key += c.cref_off;
+      cap = c.cell_cap;
+    }
+  }
+  if (__any_sync(0xffffffffu, rebuild) && lane == 0) atomicOr(vflag, 1u);
+  const unsigned m = __ballot_sync(0xffffffffu, key >= 0);
+  if (key >= 0) {
+    const unsigned peers = __match_any_sync(m, key);
+    const int leader = __ffs(peers) - 1;
+    if (lane == leader) {
+      const int n = __popc(peers);
+      over = atomicAdd(&cref_count[key], n) + n > cap;
+    }
+  }
+  if (__any_sync(0xffffffffu, over) && lane == 0) atomicOr(status, SPH_CELL_LIST_OVERFLOW);
 }
 
 // ------------------------------------------------------------------ scan
@@ -462,8 +524,7 @@ void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateVie
 void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,
                 int* count, int* start, int* keyc, int* keys, int* tsrc, int* tkey, int* tcell,
                 int* scan_tmp, long long total_cells, bool drift, bool from_forward,
-                bool apply_bc) {
-  mark(L, 0);
+                bool apply_bc, float4* rref) {
   cudaMemsetAsync(count, 0, sizeof(int) * (total_cells + 1), L.stream);
   int g = nblocks(L.N);
   if (L.dim == 3)
@@ -477,12 +538,24 @@ void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, i
   if (L.dim == 3)
     k_permute<3><<<g, kBlock, 0, L.stream>>>(L.N, in, out, R4, L.cases, start, tsrc, tkey,
                                               tcell, cellid, L.status, drift, from_forward,
-                                              apply_bc);
+                                              apply_bc, rref);
   else
     k_permute<2><<<g, kBlock, 0, L.stream>>>(L.N, in, out, R4, L.cases, start, tsrc, tkey,
                                               tcell, cellid, L.status, drift, from_forward,
-                                              apply_bc);
-  mark(L, 1);
+                                              apply_bc, rref);
+}
+
+void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_cells,
+                 bool from_forward, bool apply_bc) {
+  if (ref_cells > 0) cudaMemsetAsync(L.cref_count, 0, sizeof(int) * ref_cells, L.stream);
+  int g = nblocks(L.N);
+  if (L.dim == 3)
+    k_kick<3><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, L.rref, L.cref_count, L.vflag,
+                                          L.status, from_forward, apply_bc);
+  else
+    k_kick<2><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, L.rref, L.cref_count, L.vflag,
+                                          L.status, from_forward, apply_bc);
+  count_launch(L);
 }
 
 void launch_row_counts(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,

@@ -35,7 +35,8 @@ class SphConfig(ctypes.Structure):
                 ("is_rho_evol", ctypes.c_int32), ("is_bc_trick", ctypes.c_int32),
                 ("is_free_slip", ctypes.c_int32), ("mask_self", ctypes.c_int32),
                 ("kahan", ctypes.c_int32), ("fp64_positions", ctypes.c_int32),
-                ("capacity_multiplier", ctypes.c_double)]
+                ("capacity_multiplier", ctypes.c_double), ("verlet_skin", ctypes.c_double),
+                ("canonical_order", ctypes.c_int32), ("pad1", ctypes.c_int32)]
 
 
 class SphCase(ctypes.Structure):
@@ -67,7 +68,8 @@ EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sp
            "sph_set_state", "sph_get_state", "sph_nl_allocate", "sph_nl_set_capacity",
            "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_set_block_size",
            "sph_step_launch_count", "sph_profile_step", "sph_adjoint_init", "sph_tape_record",
-           "sph_adjoint_step", "sph_read_status", "sph_diagnostics", "sph_nl_edges_noalloc"]
+           "sph_adjoint_step", "sph_read_status", "sph_read_status_async", "sph_diagnostics",
+           "sph_nl_edges_noalloc", "sph_rebuild_stats"]
 
 _LIB = None
 
@@ -104,6 +106,8 @@ def load(build_if_missing=True):
     lib.sph_tape_record.argtypes = [V, ctypes.c_int32, V]
     lib.sph_adjoint_step.argtypes = [V, ctypes.c_int32, V, V, V, V, V]
     lib.sph_read_status.argtypes = [V, P(ctypes.c_uint32), ctypes.c_int32, V]
+    lib.sph_read_status_async.argtypes = [V, V, ctypes.c_int32, V]
+    lib.sph_rebuild_stats.argtypes = [V, P(ctypes.c_int64), P(ctypes.c_int32), V]
     lib.sph_diagnostics.argtypes = [V, V, V]
     lib.sph_nl_edges_noalloc.argtypes = [ctypes.c_int32, P(ctypes.c_double), ctypes.c_double,
                                          ctypes.c_int32, V, ctypes.c_int64, V, ctypes.c_int64,
@@ -111,7 +115,7 @@ def load(build_if_missing=True):
     for name in EXPORTS:
         if name not in ("sph_abi_version", "sph_last_error"):
             getattr(lib, name).restype = I
-    if lib.sph_abi_version() != 1:
+    if lib.sph_abi_version() != 2:
         raise RuntimeError("libsph_gb300 ABI version mismatch")
     _LIB = lib
     return lib
@@ -251,6 +255,18 @@ class Engine:
         s = ctypes.c_uint32(0)
         _check(self.lib.sph_read_status(self.h, ctypes.byref(s), int(bool(clear)), _stream()))
         return int(s.value)
+
+    def rebuild_stats(self):
+        """(candidate-list rebuilds so far, kernels per rebuild); synchronises."""
+        n, k = ctypes.c_int64(0), ctypes.c_int32(0)
+        _check(self.lib.sph_rebuild_stats(self.h, ctypes.byref(n), ctypes.byref(k), _stream()))
+        return int(n.value), int(k.value)
+
+    def read_status_async(self, clear=False):
+        """The status word as a 0-d int32 device tensor (stream-ordered, no sync)."""
+        out = torch.empty((), dtype=torch.int32, device="cuda")
+        _check(self.lib.sph_read_status_async(self.h, _ptr(out), int(bool(clear)), _stream()))
+        return out
 
     def diagnostics(self, device):
         out = torch.empty((len(self.cases), 8), dtype=torch.float64, device=device)

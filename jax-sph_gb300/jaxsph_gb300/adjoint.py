@@ -33,7 +33,10 @@ class AdjointRollout:
         self.setup = setup
         self.steps = int(steps)
         self.k = int(checkpoint_every)
-        self.sim = Simulation(setup, device=device)
+        # canonical order: a segment recomputed from its checkpoint (which
+        # rebuilds the candidate lists at other steps) equals the forward
+        # rollout bit for bit
+        self.sim = Simulation(setup, device=device, canonical_order=True)
         self.engine = self.sim.engine
         self.engine.adjoint_init(self.k)
         self.device = torch.device(device)

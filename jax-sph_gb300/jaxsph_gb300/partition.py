@@ -53,10 +53,32 @@ OrderedSparse = NeighborListFormat.OrderedSparse
 
 
 class PartitionError:
-    """``PartitionError`` (jax_md/partition.py:460-499): an error-code bitfield."""
+    """``PartitionError`` (jax_md/partition.py:460-499): an error-code bitfield.
+
+    The code is a Python int or, straight out of a GPU step, a 0-d integer
+    device tensor that is read (one synchronisation) the first time ``code``
+    is asked for -- as the reference's code stays a device array until the
+    caller tests ``did_buffer_overflow``.
+    """
 
     def __init__(self, code=0):
-        self.code = int(code) & 0xFF
+        if isinstance(code, torch.Tensor):
+            self._dev, self._code = code, None
+        else:
+            self._dev, self._code = None, int(code) & 0xFF
+
+    @property
+    def code(self):
+        if self._code is None:
+            self._code = int(self._dev.item()) & 0xFF
+            self._dev = None
+        return self._code
+
+    def merged(self, status, moved):
+        """This code OR the low bits of a device ``status`` where ``moved`` (device
+        bool), without a host synchronisation."""
+        base = self._dev if self._code is None else torch.full_like(status, self._code)
+        return PartitionError(torch.where(moved, base | (status & 0xFF), base))
 
     def update(self, bit, pred):
         return PartitionError(self.code | (int(bit) if pred else 0))
@@ -168,6 +190,8 @@ class NeighborListFns:
         c.kahan = int(solver.get("kahan", 0))
         c.fp64_positions = int(solver.get("fp64_positions", 0))
         c.capacity_multiplier = self.capacity_multiplier
+        c.verlet_skin = float(solver.get("verlet_skin", 0.0))
+        c.canonical_order = int(solver.get("canonical_order", 0))
         return c
 
     def case(self, n):
@@ -237,6 +261,13 @@ class NeighborListFns:
         ref = _as_device_f32(neighbors.reference_position)
         d2 = square_distance(self._metric(r, ref))
         return bool((d2 > self.threshold_sq).any().item())
+
+    def moved_dev(self, position, neighbors):
+        """``moved`` as a 0-d bool device tensor (no host synchronisation)."""
+        r = _as_device_f32(position)
+        ref = _as_device_f32(neighbors.reference_position)
+        d2 = square_distance(self._metric(r, ref))
+        return (d2 > self.threshold_sq).any()
 
     def update(self, position, neighbors, **kwargs):
         """Rebuild with fixed capacities if any particle moved beyond the threshold."""

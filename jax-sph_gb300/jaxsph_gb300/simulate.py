@@ -45,11 +45,18 @@ class Simulation:
 
     ``setups`` is a ``CaseSetup`` or a list of them sharing dimension, kernel,
     solver and boundary treatment. States are given and returned per case in
-    the reference's particle order.
+    the reference's particle order. ``skin`` (a fraction of the cutoff) sets
+    how far particles may move before the candidate lists are rebuilt; the
+    neighbour set of every step is the reference's whatever its value. Pair
+    sums run in cell order (deterministic for a given run); with
+    ``canonical_order`` they run in ascending original index, so that results
+    are bit for bit independent of the skin, the batching and checkpoint
+    restores.
     """
 
     def __init__(self, setups, kahan=False, mask_self=False, capacity_multiplier=1.25,
-                 device="cuda", autotune=False, block_size=None, fp64_positions=False):
+                 device="cuda", autotune=False, block_size=None, fp64_positions=False,
+                 skin=0.1, canonical_order=False):
         if not isinstance(setups, (list, tuple)):
             setups = [setups]
         _lib.require_cuda()
@@ -62,7 +69,8 @@ class Simulation:
         for v in self.solvers[1:]:
             if v.solver_flags() != flags or v.dim != self.solvers[0].dim:
                 raise ValueError("batched cases must share dimension, kernel, solver and BC treatment")
-        cfg = self.nl[0].config(**flags, fp64_positions=fp64_positions)
+        cfg = self.nl[0].config(**flags, fp64_positions=fp64_positions, verlet_skin=skin,
+                                canonical_order=canonical_order)
         self.cases = [v.sph_case(nl, s.n, dt=s.dt, tvf=s.tvf, bc=s.bc_fn.spec)
                       for s, v, nl in zip(self.setups, self.solvers, self.nl)]
         for v in self.solvers:

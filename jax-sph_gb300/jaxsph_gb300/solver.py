@@ -177,21 +177,24 @@ class WCSPH:
             raise NotImplementedError(
                 "si_euler needs a g_ext_fn with a GPU spec (e.g. jaxsph_gb300.cases.GExt)")
         e, st = self._load(state, neighbors, case)
-        e.read_status(clear=True)
         e.step(1)
         out = empty_outputs(st)
         e.get_state(out)
-        code = e.read_status(clear=True)
-        if code & (_lib.ERR_INVALID_ARG | _lib.ERR_CUDA):
-            raise _lib.SphError(code, "step failed")
+        # no host synchronisation: the status stays a device value inside the
+        # returned list's error code until the caller tests it (host-side
+        # failures raise from the calls above)
+        status = e.read_status_async(clear=True)
         res = self._result(state, out)
         if bc_fn is not None and bc_spec is None:
             res = bc_fn(res)
-        if nl_fns.moved(res["r"], neighbors):
-            from .partition import NeighborList
+        from .partition import NeighborList
 
-            nbrs = NeighborList(nl_fns, res["r"], neighbors.error.code | (code & 0xFF),
-                                neighbors.cell_list_capacity, neighbors.max_occupancy)
-        else:
-            nbrs = neighbors
+        # the reference rebuilds inside the step only when a particle moved
+        # (jax_md/partition.py:1010-1018); the new list's reference position
+        # and error code are selected on the device
+        mv = nl_fns.moved_dev(res["r"], neighbors)
+        ref = torch.where(mv, res["r"], torch.as_tensor(neighbors.reference_position).to(
+            res["r"].device, res["r"].dtype))
+        nbrs = NeighborList(nl_fns, ref, neighbors.error.merged(status, mv),
+                            neighbors.cell_list_capacity, neighbors.max_occupancy)
         return res, nbrs
