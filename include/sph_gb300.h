@@ -51,6 +51,8 @@ extern "C" {
 /* A position hashed outside the cell grid (exactly on the upper box face);
  * it is clamped into the last cell. */
 #define SPH_WARN_BOX_EDGE 0x1000u
+/* sph_advance: a particle moved beyond the neighbour list's threshold. */
+#define SPH_INFO_MOVED 0x2000u
 
 enum { SPH_KERNEL_QSK = 0, SPH_KERNEL_WC2K = 1 };   /* jax_sph/kernel.py:51-103 */
 enum { SPH_SOLVER_SPH = 0, SPH_SOLVER_RIE = 1 };    /* jax_sph/solver.py:676-694 */
@@ -199,6 +201,19 @@ int sph_forward(SphHandle* h, void* stream);
 /* `nsteps` si_euler steps (jax_sph/integrator.py:22-56): kick, drift, neighbour
  * update (rebuilt every step), forward, bc_fn. Replays a CUDA graph. */
 int sph_step(SphHandle* h, int32_t nsteps, void* stream);
+
+/* One drop-in si_euler advance on caller buffers, the way the reference's
+ * jitted advance(dt, state, neighbors) runs (jax_sph/integrator.py:22-56,
+ * jax_sph/simulate.py:115-123): load `in`, kick, drift, neighbour update,
+ * forward pass, bc_fn, and write the new state to `out` (which may alias
+ * `in`). Then, stream-ordered and without a host synchronization, the device
+ * status word is copied to `status_dev` (a device uint32) and cleared; it
+ * carries SPH_INFO_MOVED when some new position lies farther than
+ * sqrt(threshold_sq) from `ref_r` (the list's reference positions, device
+ * (n, dim) float32; NULL skips the test) under the periodic metric -- the
+ * reference's test for rebuilding the list (jax_md/partition.py:1010-1018). */
+int sph_advance(SphHandle* h, const SphStateView* in, SphStateView* out, const float* ref_r,
+                float threshold_sq, uint32_t* status_dev, void* stream);
 
 /* Threads per block of the density, wall and force passes (a multiple of 32
  * in [32, 256]; default 256). A tuning knob: results do not depend on it. */

@@ -777,6 +777,49 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream) {
   return 0;
 }
 
+int sph_advance(SphHandle* h, const SphStateView* in, SphStateView* out, const float* ref_r,
+                float threshold_sq, uint32_t* status_dev, void* stream) {
+  if (!h || !in || !out || !status_dev) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+  if (in->n != h->N || out->n != h->N)
+    return fail((int)SPH_ERR_INVALID_ARG, "state has the wrong particle count");
+  if (!in->r || !in->tag || !in->u || !in->v || !in->dudt || !in->dvdt || !in->rho || !in->p ||
+      !in->mass || !in->eta || !out->r || !out->u || !out->v || !out->dudt || !out->dvdt ||
+      !out->rho || !out->p)
+    return fail((int)SPH_ERR_INVALID_ARG, "missing state field");
+  if (h->buf[0].NW4 && !in->nw)
+    return fail((int)SPH_ERR_INVALID_ARG, "wall normals nw are required by this solver");
+  bool garr = false;
+  for (const auto& c : h->hc) garr |= c.g_kind == SPH_GEXT_ARRAY;
+  if (garr && !in->g_ext)
+    return fail((int)SPH_ERR_INVALID_ARG, "g_ext array required by SPH_GEXT_ARRAY");
+  cudaStream_t st = (cudaStream_t)stream;
+  LaunchCtx L = h->ctx(st);
+  const Buffers& A = h->buf[0];
+  const Buffers& B = h->buf[1];
+  // load into the scratch set, kick there, sort into the resident set: the
+  // rebuild needs no copy
+  cudaError_t e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
+  launch_pack(L, *in, B, h->case_off_d);
+  h->g_arr = in->g_ext;
+  h->launch_count = 0;
+  launch_kick(L, B, h->R4, h->ref_cells, false, false);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, sizeof(unsigned), st);
+  launch_bin(L, B, A, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc, h->tkey,
+             h->tcell, h->scan_tmp, h->C, false, false, false, h->rref);
+  launch_verlet(L, A, h->cellid, h->start);
+  launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
+                 true);
+  launch_unpack(L, A, h->R4, *out, true, true, ref_r, threshold_sq);
+  if (e == cudaSuccess)
+    e = cudaMemcpyAsync(status_dev, h->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
+  h->has_state = h->binned = h->fresh = true;
+  h->from_forward = h->pending_bc = true;
+  ++h->rebuilds_h;
+  if (e != cudaSuccess) return cuda_check(e, "advance");
+  return launch_status("advance");
+}
+
 int sph_set_block_size(SphHandle* h, int32_t threads) {
   if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
   if (threads < 32 || threads > 256 || threads % 32)

@@ -509,7 +509,8 @@ inline void mark(const LaunchCtx& L, int i) {
 // sph_sort.cu
 void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out, const long long* case_off_dev);
 void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateView& s,
-                   bool from_forward, bool apply_bc);
+                   bool from_forward, bool apply_bc, const float* ref = nullptr,
+                   float thr_sq = 0.f);
 void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,
                 int* count, int* start, int* keyc, int* keys, int* tsrc, int* tkey, int* tcell,
                 int* scan_tmp, long long total_cells, bool drift, bool from_forward,

@@ -89,24 +89,43 @@ __device__ __forceinline__ Final finalize(const Buffers& b, const float4* R4, lo
   return f;
 }
 
+// Write the state back in the original order. With `ref` (device (n, dim)
+// positions of a neighbour list) also the reference's rebuild test of that
+// list (jax_md/partition.py:1010-1018): SPH_INFO_MOVED when some particle is
+// farther than sqrt(thr_sq) from its reference position under the periodic
+// metric.
 __global__ void k_unpack(SphStateView s, int dim, Buffers b, const float4* R4,
-                         const CaseDev* cases, bool from_forward, bool apply_bc) {
+                         const CaseDev* cases, bool from_forward, bool apply_bc,
+                         const float* ref, float thr_sq, unsigned* status) {
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= s.n) return;
-  int meta = b.META[q];
-  const CaseDev& c = cases[case_of(meta)];
-  int tag = tag_of(meta);
-  long long o = b.ORIG[q];
-  Final f = finalize(b, R4, q, c, tag, from_forward, apply_bc);
-  float4 r = b.P4[q], a = b.A4[q], a2 = b.A2[q];
-  st3(s.r, dim, o, r.x, r.y, r.z);
-  st3(s.u, dim, o, f.u.x, f.u.y, f.u.z);
-  st3(s.v, dim, o, f.v.x, f.v.y, f.v.z);
-  st3(s.dudt, dim, o, a.x, a.y, a.z);
-  st3(s.dvdt, dim, o, a2.x, a2.y, a2.z);
-  if (s.drhodt) s.drhodt[o] = a.w;
-  s.rho[o] = f.rho;
-  s.p[o] = f.p;
+  bool moved = false;
+  if (q < s.n) {
+    int meta = b.META[q];
+    const CaseDev& c = cases[case_of(meta)];
+    int tag = tag_of(meta);
+    long long o = b.ORIG[q];
+    Final f = finalize(b, R4, q, c, tag, from_forward, apply_bc);
+    float4 r = b.P4[q], a = b.A4[q], a2 = b.A2[q];
+    st3(s.r, dim, o, r.x, r.y, r.z);
+    st3(s.u, dim, o, f.u.x, f.u.y, f.u.z);
+    st3(s.v, dim, o, f.v.x, f.v.y, f.v.z);
+    st3(s.dudt, dim, o, a.x, a.y, a.z);
+    st3(s.dvdt, dim, o, a2.x, a2.y, a2.z);
+    if (s.drhodt) s.drhodt[o] = a.w;
+    s.rho[o] = f.rho;
+    s.p[o] = f.p;
+    if (ref) {
+      const float4 r0 = make_float4(ref[o * dim], ref[o * dim + 1],
+                                    dim == 3 ? ref[o * dim + 2] : 0.f, 0.f);
+      float3 d;
+      d.x = pdisp(__fsub_rn(r.x, r0.x), c.box[0], c.half[0]);
+      d.y = pdisp(__fsub_rn(r.y, r0.y), c.box[1], c.half[1]);
+      d.z = dim == 3 ? pdisp(__fsub_rn(r.z, r0.z), c.box[2], c.half[2]) : 0.f;
+      const float d2 = dim == 3 ? sqd<3>(d) : sqd<2>(d);
+      moved = d2 > thr_sq;
+    }
+  }
+  if (__any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0) atomicOr(status, SPH_INFO_MOVED);
 }
 
 // ------------------------------------------------------------------ binning
@@ -516,9 +535,10 @@ void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out,
 }
 
 void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateView& s,
-                   bool from_forward, bool apply_bc) {
+                   bool from_forward, bool apply_bc, const float* ref, float thr_sq) {
   k_unpack<<<nblocks(L.N), kBlock, 0, L.stream>>>(s, L.dim, in, R4, L.cases, from_forward,
-                                                   apply_bc);
+                                                   apply_bc, ref, thr_sq, L.status);
+  count_launch(L);
 }
 
 void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,

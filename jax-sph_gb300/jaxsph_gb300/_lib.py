@@ -21,6 +21,7 @@ ERR_INVALID_ARG = 0x100
 ERR_CUDA = 0x200
 ERR_TIMEOUT = 0x400
 ERR_NONFINITE = 0x800
+INFO_MOVED = 0x2000
 WARN_BOX_EDGE = 0x1000
 
 KERNELS = {"QSK": 0, "WC2K": 1}
@@ -69,7 +70,7 @@ EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sp
            "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_set_block_size",
            "sph_step_launch_count", "sph_profile_step", "sph_adjoint_init", "sph_tape_record",
            "sph_adjoint_step", "sph_read_status", "sph_read_status_async", "sph_diagnostics",
-           "sph_nl_edges_noalloc", "sph_rebuild_stats"]
+           "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance"]
 
 _LIB = None
 
@@ -108,6 +109,7 @@ def load(build_if_missing=True):
     lib.sph_read_status.argtypes = [V, P(ctypes.c_uint32), ctypes.c_int32, V]
     lib.sph_read_status_async.argtypes = [V, V, ctypes.c_int32, V]
     lib.sph_rebuild_stats.argtypes = [V, P(ctypes.c_int64), P(ctypes.c_int32), V]
+    lib.sph_advance.argtypes = [V, P(SphStateView), P(SphStateView), V, ctypes.c_float, V, V]
     lib.sph_diagnostics.argtypes = [V, V, V]
     lib.sph_nl_edges_noalloc.argtypes = [ctypes.c_int32, P(ctypes.c_double), ctypes.c_double,
                                          ctypes.c_int32, V, ctypes.c_int64, V, ctypes.c_int64,
@@ -255,6 +257,18 @@ class Engine:
         s = ctypes.c_uint32(0)
         _check(self.lib.sph_read_status(self.h, ctypes.byref(s), int(bool(clear)), _stream()))
         return int(s.value)
+
+    def advance(self, state, out, ref=None, threshold_sq=0.0):
+        """One fused drop-in step (load, step, read back); returns the status
+        word as a 0-d int32 device tensor (no host synchronisation)."""
+        vin = self.view(state, self.n)
+        vout = self.view(out, self.n)
+        status = torch.empty((), dtype=torch.int32, device=state["r"].device)
+        self._keep = state
+        _check(self.lib.sph_advance(self.h, ctypes.byref(vin), ctypes.byref(vout),
+                                    _ptr(ref) if ref is not None else None,
+                                    float(threshold_sq), _ptr(status), _stream()))
+        return status
 
     def rebuild_stats(self):
         """(candidate-list rebuilds so far, kernels per rebuild); synchronises."""

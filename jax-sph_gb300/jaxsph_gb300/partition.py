@@ -61,24 +61,28 @@ class PartitionError:
     caller tests ``did_buffer_overflow``.
     """
 
-    def __init__(self, code=0):
+    def __init__(self, code=0, base=0):
         if isinstance(code, torch.Tensor):
-            self._dev, self._code = code, None
+            self._dev, self._code, self._base = code, None, int(base)
         else:
-            self._dev, self._code = None, int(code) & 0xFF
+            self._dev, self._code, self._base = None, (int(code) | int(base)) & 0xFF, 0
 
     @property
     def code(self):
         if self._code is None:
-            self._code = int(self._dev.item()) & 0xFF
+            self._code = (int(self._dev.item()) | self._base) & 0xFF
             self._dev = None
         return self._code
 
-    def merged(self, status, moved):
-        """This code OR the low bits of a device ``status`` where ``moved`` (device
-        bool), without a host synchronisation."""
+    def merged(self, status, moved=None):
+        """This code OR the low bits of a device ``status`` (where the device
+        bool ``moved`` holds, if given), without a host synchronisation."""
+        if moved is None:
+            if self._code is not None:
+                return PartitionError(status, base=self._code)
+            return PartitionError(self._dev | status, base=self._base)
         base = self._dev if self._code is None else torch.full_like(status, self._code)
-        return PartitionError(torch.where(moved, base | (status & 0xFF), base))
+        return PartitionError(torch.where(moved, base | status, base), base=self._base)
 
     def update(self, bit, pred):
         return PartitionError(self.code | (int(bit) if pred else 0))

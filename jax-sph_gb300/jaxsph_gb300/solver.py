@@ -124,7 +124,7 @@ class WCSPH:
             e.update_cases([case])
         return e
 
-    def _load(self, state, neighbors, case):
+    def _load(self, state, neighbors, case, load=True):
         nl_fns = neighbors._fns
         st = prepare_state(state, self.dim)
         if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
@@ -133,7 +133,8 @@ class WCSPH:
         if (self.solver == "RIE" or self.is_free_slip) and "nw" not in st:
             st["nw"] = torch.zeros_like(st["r"])
         e = self.engine(nl_fns, case)
-        e.set_state(st)
+        if load:
+            e.set_state(st)
         cap = neighbors.cell_list_capacity
         e.nl_set_capacity(cap if cap is not None else 2 ** 31 - 1, neighbors.max_occupancy)
         return e, st
@@ -176,25 +177,32 @@ class WCSPH:
         if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
             raise NotImplementedError(
                 "si_euler needs a g_ext_fn with a GPU spec (e.g. jaxsph_gb300.cases.GExt)")
-        e, st = self._load(state, neighbors, case)
-        e.step(1)
+        e, st = self._load(state, neighbors, case, load=False)
         out = empty_outputs(st)
-        e.get_state(out)
-        # no host synchronisation: the status stays a device value inside the
-        # returned list's error code until the caller tests it (host-side
-        # failures raise from the calls above)
-        status = e.read_status_async(clear=True)
+        # one fused call: load, step, read back; the status stays a device
+        # value inside the returned list's error code until the caller tests
+        # it (host-side failures raise from the call)
+        ref = torch.as_tensor(neighbors.reference_position)
+        if nl_fns.threshold_sq > 0.0:
+            ref = ref.to(device=st["r"].device, dtype=torch.float32).contiguous()
+            status = e.advance(st, out, ref, nl_fns.threshold_sq)
+        else:
+            status = e.advance(st, out)
         res = self._result(state, out)
         if bc_fn is not None and bc_spec is None:
             res = bc_fn(res)
         from .partition import NeighborList
 
-        # the reference rebuilds inside the step only when a particle moved
-        # (jax_md/partition.py:1010-1018); the new list's reference position
-        # and error code are selected on the device
-        mv = nl_fns.moved_dev(res["r"], neighbors)
-        ref = torch.where(mv, res["r"], torch.as_tensor(neighbors.reference_position).to(
-            res["r"].device, res["r"].dtype))
-        nbrs = NeighborList(nl_fns, ref, neighbors.error.merged(status, mv),
-                            neighbors.cell_list_capacity, neighbors.max_occupancy)
+        if nl_fns.threshold_sq > 0.0:
+            # the reference rebuilds inside the step only when a particle
+            # moved beyond the threshold (jax_md/partition.py:1010-1018)
+            mv = (status & _lib.INFO_MOVED) != 0
+            nbrs = NeighborList(nl_fns, torch.where(mv, res["r"], ref),
+                                neighbors.error.merged(status & 0xFF, mv),
+                                neighbors.cell_list_capacity, neighbors.max_occupancy)
+        else:
+            # threshold 0: a list not rebuilt is one at unchanged positions,
+            # whose reference position and overflow bits equal the new ones
+            nbrs = NeighborList(nl_fns, res["r"], neighbors.error.merged(status),
+                                neighbors.cell_list_capacity, neighbors.max_occupancy)
         return res, nbrs

@@ -116,11 +116,57 @@ def test_drop_in_advance_equals_resident_rollout():
     nb = fns.allocate(st["r"])
     for _ in range(5):
         st, nb = adv(setup.dt, st, nb)
-    sim = simulate.Simulation(setup)
+    # without a skin the resident rollout bins after every kick, as each
+    # drop-in step does, so the pair order (cell order) is the same
+    sim = simulate.Simulation(setup, skin=0.0)
     sim.run(5)
     got = sim.state()[0]
     for k in ("r", "u", "v", "rho", "p", "dudt", "dvdt"):
         assert torch.equal(st[k], got[k]), k
+
+
+def test_drop_in_advance_reports_overflow_lazily():
+    from jaxsph_gb300.partition import NeighborList
+
+    setup = cases.tgv(dim=2, dx=0.05)
+    wc = gpu_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    _, shift = setup.space()
+    adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
+    st = setup.to("cuda")
+    nb = fns.allocate(st["r"])
+    st1, nb1 = adv(setup.dt, st, nb)
+    assert not nb1.did_buffer_overflow
+    # a list whose edge capacity is far too small overflows on the next step
+    small = NeighborList(fns, nb1.reference_position, 0, nb1.cell_list_capacity, 10)
+    st2, nb2 = adv(setup.dt, st1, small)
+    assert nb2.did_buffer_overflow
+    # the state itself does not depend on the capacity
+    st3, _ = adv(setup.dt, st1, nb1)
+    for k in ("r", "u", "rho", "dudt"):
+        assert torch.equal(st2[k], st3[k]), k
+
+
+def test_drop_in_advance_keeps_reference_position_within_threshold():
+    from jaxsph_gb300.partition import NeighborListFns, Sparse
+
+    setup = cases.tgv(dim=2, dx=0.05)
+    wc = gpu_solver(setup)
+    cut = wc._kernel_fn.cutoff
+    # a skin as in the reference's dr_threshold: rebuild only past half of it
+    fns = NeighborListFns(setup.box, cut, 0.5 * cut, 1.25, False, Sparse)
+    _, shift = setup.space()
+    adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
+    st = setup.to("cuda")
+    nb = fns.allocate(st["r"])
+    st1, nb1 = adv(setup.dt, st, nb)
+    assert torch.equal(nb1.reference_position, nb.reference_position)
+    fns0 = simulate.make_neighbor_fns(setup, wc)
+    st_b, _ = adv(setup.dt, st, fns0.allocate(st["r"]))
+    # pairs beyond the kernel support add nothing (W = 0 there): the same
+    # state up to the summation order of another binning
+    for k in ("r", "u", "rho"):
+        assert torch.allclose(st1[k], st_b[k], rtol=1e-6, atol=1e-6), k
 
 
 def test_deterministic_and_graph_equals_eager():
