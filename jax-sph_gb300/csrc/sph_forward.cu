@@ -472,22 +472,21 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
   const bool av = c.av_alpha != 0.0f;
   const float mask_i = (SOLVER == 1 && bc_trick && free_slip) ? (fluid_i ? 1.f : 0.f) : 1.f;
   Acc<KAHAN> ax, ay, az, tx, ty, tz;
-  for_each_neighbour<DIM>(N, i, ri, c, cases + case_of(meta), b.P4, cellid, start, nl,
-                          [&](int j, const float4& rj, const float3& dr, float d2) {
+  auto pair = [&](int j, const float4& rj, const float4& Uj4, const float4& Vj4,
+                  const float4& Rj, const float3& dr, float d2) {
     const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
     const float gw = kdw<KER>(dist, c);
     const float inv_d = __fdividef(1.0f, dist + kEps);
-    const float4 Rj = R4[j];
     const float rho_j = Rj.x, p_j = Rj.y, eta_j = Rj.w, m_j = rj.w;
     const float Vj = __fdividef(m_j, rho_j);
     const float cc = (Vi2 + Vj * Vj) * inv_mi * gw * inv_d;
-    const float3 uj = f3(b.U4[j]);
+    const float3 uj = f3(Uj4);
     const float eta_ij = __fdividef(2.f * eta_i * eta_j, eta_i + eta_j + kEps);
     int tj = FLUID;
     if (SOLVER == 1 || av) tj = tag_of(b.META[j]);
     float3 a;
     if (SOLVER == 0) {
-      const float3 vj = f3(b.V4[j]);
+      const float3 vj = f3(Vj4);
       const float p_ij = __fdividef(rho_j * p_i + rho_i * p_j, rho_i + rho_j);
       const float ki = dot3(wi, dr);
       const float kj = dot3(make_float3(vj.x - uj.x, vj.y - uj.y, vj.z - uj.z), dr);
@@ -549,7 +548,37 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
     tx.add(ct * dr.x);
     ty.add(ct * dr.y);
     tz.add(ct * dr.z);
-  });
+  };
+  const int m = nl.cnt[i];
+  if (m <= nl.kmax) {
+    // the next sender's four records are loaded while the current pair is
+    // evaluated, and its index one step earlier still
+    const int* nbi = nl.nbr + i;
+    int j = m > 0 ? nbi[0] : (int)i;
+    int jn = m > 1 ? nbi[N] : j;
+    float4 rj = __ldg(b.P4 + j), uj = __ldg(b.U4 + j), vj = __ldg(b.V4 + j), Rj = __ldg(R4 + j);
+    for (int k = 0; k < m; ++k) {
+      const int jc = j;
+      const float4 rc = rj, uc = uj, vc = vj, Rc = Rj;
+      j = jn;
+      if (k + 2 < m) jn = nbi[(long long)(k + 2) * N];
+      if (k + 1 < m) {
+        rj = __ldg(b.P4 + j);
+        uj = __ldg(b.U4 + j);
+        vj = __ldg(b.V4 + j);
+        Rj = __ldg(R4 + j);
+      }
+      float3 dr;
+      float d2;
+      pair_dr<DIM>(ri, rc, c, dr, d2);
+      pair(jc, rc, uc, vc, Rc, dr, d2);
+    }
+  } else {
+    for_each_edge_slow<DIM>(N, i, ri, c, cases + case_of(meta), b.P4, cellid, start, nl,
+                            [&](int j, const float4& rj, const float3& dr, float d2) {
+                              pair(j, rj, b.U4[j], b.V4[j], R4[j], dr, d2);
+                            });
+  }
   float3 dudt = make_float3(ax.s + gi.x, ay.s + gi.y, az.s + gi.z);
   float3 dvdt = make_float3(tx.s, ty.s, tz.s);
   if (DIM == 2) {
