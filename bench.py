@@ -190,8 +190,10 @@ def reference_arm(args, ws, rank):
 
 # ------------------------------------------------------------------ GPU arm
 def e2e_rate(setup, steps, device):
-    """The public drop-in API with host buffers: per step H2D of the state,
-    ``si_euler`` advance, D2H of the resulting state."""
+    """The public drop-in API with host buffers: every step the ``si_euler``
+    advance takes its state from pinned host memory and returns the new state
+    in pinned host memory (DMA copies in and out inside the one library
+    call, which returns once the result is in host memory)."""
     from jaxsph_gb300 import integrator, simulate
 
     wc = simulate.make_solver(setup)
@@ -199,30 +201,32 @@ def e2e_rate(setup, steps, device):
     _, shift = setup.space()
     adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
     keys_in = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
-    host = {k: setup.state[k].contiguous().pin_memory() for k in keys_in}
     keys_out = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
-    host_out = {k: torch.empty_like(host[k]).pin_memory() for k in keys_out}
+    host = {k: setup.state[k].to(torch.int32 if k == "tag" else torch.float32)
+            .contiguous().pin_memory() for k in keys_in}
     h2d = sum(host[k].numel() * host[k].element_size() for k in keys_in)
-    d2h = sum(host_out[k].numel() * host_out[k].element_size() for k in keys_out)
-    dev = {k: v.to(device, non_blocking=True) for k, v in host.items()}
-    nb = fns.allocate(dev["r"])
-    st = dev
-    for _ in range(2):  # warm-up (engine creation, graph capture)
+    d2h = sum(host[k].numel() * host[k].element_size() for k in keys_out)
+    nb = fns.allocate(host["r"])
+    st = host
+    for _ in range(3):  # warm-up (engine creation, pinned output blocks)
         st, nb = adv(setup.dt, st, nb)
     torch.cuda.synchronize()
-    times = []
+    assert all(st[k].device.type == "cpu" and st[k].is_pinned() for k in keys_out)
+    times, redone = [], 0
     for _ in range(steps):
         t0 = time.perf_counter()
-        dev = {k: v.to(device, non_blocking=True) for k, v in host.items()}
-        out, nb = adv(setup.dt, dev, nb)
-        for k in keys_out:
-            host_out[k].copy_(out[k], non_blocking=True)
+        st_new, nb_new = adv(setup.dt, st, nb)
+        if nb_new.did_buffer_overflow:
+            # the reference driver's protocol (simulate.py:118-128): allocate
+            # at the step's input positions and redo the step
+            nb = fns.allocate(st["r"])
+            st_new, nb_new = adv(setup.dt, st, nb)
+            redone += 1
+        st, nb = st_new, nb_new
         torch.cuda.synchronize()
         times.append(time.perf_counter() - t0)
-        for k in keys_out:  # next step's host inputs
-            host[k].copy_(host_out[k])
     t = float(np.mean(times))
-    return setup.n / t, h2d, d2h, t
+    return setup.n / t, h2d, d2h, t, redone
 
 
 def timed_steps(sim, steps):
@@ -385,10 +389,11 @@ def gpu_arm(args, ws, rank, local):
         "clocks": clocks.summary(),
     }
     if rank == 0 and ws == 1 and not args.no_e2e:
-        rate, h2d, d2h, t = e2e_rate(setup, min(args.steps, 30), device)
+        rate, h2d, d2h, t, redone = e2e_rate(setup, min(args.steps, 30), device)
         line["e2e"] = {"value": rate, "unit": UNIT, "h2d_bytes_per_step": h2d,
-                       "d2h_bytes_per_step": d2h,
-                       "path": "si_euler drop-in advance, pinned host state in/out every step"}
+                       "d2h_bytes_per_step": d2h, "steps_redone_on_overflow": redone,
+                       "path": "si_euler drop-in advance on a pinned host state: each step "
+                               "reads its inputs from and writes its result to host memory"}
     if rank == 0 and not args.no_forms:
         line["forms"] = {"batched": batched_form(device, 100), "adjoint": adjoint_form(device)}
     if rank == 0 and ws == 1 and not args.no_cpu:

@@ -206,7 +206,9 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream);
  * jitted advance(dt, state, neighbors) runs (jax_sph/integrator.py:22-56,
  * jax_sph/simulate.py:115-123): load `in`, kick, drift, neighbour update,
  * forward pass, bc_fn, and write the new state to `out` (which may alias
- * `in`). Then, stream-ordered and without a host synchronization, the device
+ * `in`). Arrays may be device memory or pinned host memory (copied by DMA
+ * through device staging the handle allocates on the first such call);
+ * pageable host memory is rejected. Then, stream-ordered and without a host synchronization, the device
  * status word is copied to `status_dev` (a device uint32) and cleared; it
  * carries SPH_INFO_MOVED when some new position lies farther than
  * sqrt(threshold_sq) from `ref_r` (the list's reference positions, device

@@ -56,6 +56,8 @@ struct SphHandle {
   unsigned long long* rebuilds_d = nullptr;  // rebuilds run inside graph replays
   long long rebuilds_h = 0;                  // rebuilds run eagerly
   int rebuild_launches = 0;                  // kernels of one rebuild
+  unsigned char* stage = nullptr;  // device copies of pinned host fields (sph_advance)
+  size_t stage_slot = 0;
   int block = 256;        // threads per block of the forward passes
   unsigned* status = nullptr;
   unsigned long long* edgecnt = nullptr;
@@ -777,9 +779,104 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream) {
   return 0;
 }
 
-int sph_advance(SphHandle* h, const SphStateView* in, SphStateView* out, const float* ref_r,
+}  // extern "C"
+
+namespace {
+// Where a caller array lives: device memory (used in place) or pinned
+// (page-locked) host memory (copied by DMA to and from a device staging
+// slot). Anything else -- pageable memory -- is rejected before any work.
+int pinned_host(const void* p, const char* name, bool* host) {
+  *host = false;
+  if (!p) return 0;
+  cudaPointerAttributes a;
+  cudaError_t e = cudaPointerGetAttributes(&a, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return fail((int)SPH_ERR_INVALID_ARG, std::string(name) + ": unknown pointer");
+  }
+  if (a.type == cudaMemoryTypeDevice || a.type == cudaMemoryTypeManaged) return 0;
+  if (a.type == cudaMemoryTypeHost) {
+    *host = true;
+    return 0;
+  }
+  return fail((int)SPH_ERR_INVALID_ARG,
+              std::string(name) + ": host arrays must be pinned (page-locked) memory");
+}
+}  // namespace
+
+extern "C" {
+
+int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const float* ref_r_,
                 float threshold_sq, uint32_t* status_dev, void* stream) {
-  if (!h || !in || !out || !status_dev) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+  if (!h || !in_ || !out_ || !status_dev) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+  SphStateView vin = *in_, vout = *out_;
+  const SphStateView* in = &vin;
+  SphStateView* out = &vout;
+  cudaStream_t st = (cudaStream_t)stream;
+  // fields in pinned host memory go through device staging slots: one DMA
+  // copy per field in, one per result field out
+  const size_t N = (size_t)h->N;
+  const size_t vec = sizeof(float) * (size_t)h->cfg.dim * N, sc = sizeof(float) * N;
+  struct Field {
+    const char* name;
+    void** in;
+    void** out;
+    size_t bytes;
+  };
+  Field fields[] = {
+      {"r", (void**)&vin.r, (void**)&vout.r, vec},
+      {"tag", (void**)&vin.tag, nullptr, sizeof(int32_t) * N},
+      {"u", (void**)&vin.u, (void**)&vout.u, vec},
+      {"v", (void**)&vin.v, (void**)&vout.v, vec},
+      {"dudt", (void**)&vin.dudt, (void**)&vout.dudt, vec},
+      {"dvdt", (void**)&vin.dvdt, (void**)&vout.dvdt, vec},
+      {"drhodt", (void**)&vin.drhodt, (void**)&vout.drhodt, sc},
+      {"rho", (void**)&vin.rho, (void**)&vout.rho, sc},
+      {"p", (void**)&vin.p, (void**)&vout.p, sc},
+      {"mass", (void**)&vin.mass, nullptr, sc},
+      {"eta", (void**)&vin.eta, nullptr, sc},
+      {"nw", (void**)&vin.nw, nullptr, vec},
+      {"g_ext", (void**)&vin.g_ext, nullptr, vec},
+  };
+  constexpr int kFields = sizeof(fields) / sizeof(fields[0]);
+  bool hin[kFields], hout[kFields], href = false, hst = false;
+  bool any = false;
+  for (int k = 0; k < kFields; ++k) {
+    int rc = pinned_host(*fields[k].in, fields[k].name, &hin[k]);
+    hout[k] = false;
+    if (!rc && fields[k].out) rc = pinned_host(*fields[k].out, fields[k].name, &hout[k]);
+    if (rc) return rc;
+    any = any || hin[k] || hout[k];
+  }
+  int vrc = pinned_host(ref_r_, "ref_r", &href);
+  if (!vrc) vrc = pinned_host(status_dev, "status", &hst);
+  if (vrc) return vrc;
+  any = any || href;
+  if (any && !h->stage) {  // allocated once, on the first call with host arrays
+    h->stage_slot = (vec + 255) / 256 * 256;
+    if (h->alloc(&h->stage, h->stage_slot * (kFields + 1))) return SPH_ERR_CUDA;
+  }
+  cudaError_t e = cudaSuccess;
+  void* host_dst[kFields] = {};
+  for (int k = 0; k < kFields; ++k) {
+    void* slot = h->stage ? h->stage + h->stage_slot * k : nullptr;
+    if (hin[k]) {
+      if (e == cudaSuccess)
+        e = cudaMemcpyAsync(slot, *fields[k].in, fields[k].bytes, cudaMemcpyHostToDevice, st);
+      *fields[k].in = slot;
+    }
+    if (hout[k]) {  // the result goes to the slot, then to the host array
+      host_dst[k] = *fields[k].out;
+      *fields[k].out = slot;
+    }
+  }
+  const float* ref_r = ref_r_;
+  if (href) {
+    void* slot = h->stage + h->stage_slot * kFields;
+    if (e == cudaSuccess) e = cudaMemcpyAsync(slot, ref_r_, vec, cudaMemcpyHostToDevice, st);
+    ref_r = (const float*)slot;
+  }
+  if (e != cudaSuccess) return cuda_check(e, "advance input copy");
   if (in->n != h->N || out->n != h->N)
     return fail((int)SPH_ERR_INVALID_ARG, "state has the wrong particle count");
   if (!in->r || !in->tag || !in->u || !in->v || !in->dudt || !in->dvdt || !in->rho || !in->p ||
@@ -792,13 +889,12 @@ int sph_advance(SphHandle* h, const SphStateView* in, SphStateView* out, const f
   for (const auto& c : h->hc) garr |= c.g_kind == SPH_GEXT_ARRAY;
   if (garr && !in->g_ext)
     return fail((int)SPH_ERR_INVALID_ARG, "g_ext array required by SPH_GEXT_ARRAY");
-  cudaStream_t st = (cudaStream_t)stream;
   LaunchCtx L = h->ctx(st);
   const Buffers& A = h->buf[0];
   const Buffers& B = h->buf[1];
   // load into the scratch set, kick there, sort into the resident set: the
   // rebuild needs no copy
-  cudaError_t e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
+  e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
   launch_pack(L, *in, B, h->case_off_d);
   h->g_arr = in->g_ext;
   h->launch_count = 0;
@@ -810,8 +906,13 @@ int sph_advance(SphHandle* h, const SphStateView* in, SphStateView* out, const f
   launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
                  true);
   launch_unpack(L, A, h->R4, *out, true, true, ref_r, threshold_sq);
+  for (int k = 0; k < kFields; ++k)
+    if (host_dst[k] && e == cudaSuccess)
+      e = cudaMemcpyAsync(host_dst[k], h->stage + h->stage_slot * k, fields[k].bytes,
+                          cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(status_dev, h->status, sizeof(unsigned), cudaMemcpyDeviceToDevice, st);
+    e = cudaMemcpyAsync(status_dev, h->status, sizeof(unsigned),
+                        hst ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
   h->has_state = h->binned = h->fresh = true;
   h->from_forward = h->pending_bc = true;

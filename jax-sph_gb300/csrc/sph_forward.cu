@@ -140,39 +140,36 @@ __device__ __forceinline__ void for_each_neighbour(long long N, long long i, con
 // ------------------------------------------------------------------ Verlet lists
 // Candidate senders of every receiver at the current binning: the particles
 // within the Verlet radius (shifted squared distance < v_r2; in a case
-// without the fast test, the reference's own edges), self excluded. SORT
-// stages them in shared memory in ascending original index (insertion while
-// walking), so that every pair sum built on them runs in an order that depends
-// neither on the binning nor on when it was rebuilt; otherwise they are
-// written in walk order (cell order), straight to the list.
+// without the fast test, the reference's own edges), self excluded, staged in
+// shared memory and written out k-major (coalesced). SORT keeps them in
+// ascending original index (insertion while walking), so that every pair sum
+// built on them runs in an order that depends neither on the binning nor on
+// when it was rebuilt; otherwise they stay in walk (cell) order.
 template <int DIM, bool SORT>
-__global__ void __launch_bounds__(256)
+__global__ void __launch_bounds__(128)
 k_verlet(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
          int* vl, int* vcnt, int kv) {
-  extern __shared__ int s_v[];  // SORT: keys [kv][blockDim], senders [kv][blockDim]
+  // staging: senders [kv][blockDim] (SORT: and their keys [kv][blockDim])
+  extern __shared__ int s_v[];
   const int tid = threadIdx.x, bs = blockDim.x;
-  int* keys = s_v;
-  int* js = s_v + kv * bs;
+  int* js = s_v;
+  int* keys = s_v + kv * bs;
   const long long i = blockIdx.x * (long long)bs + tid;
   if (i >= N) return;
   const CaseDev& c = cases[case_of(b.META[i])];
   const float4 ri = b.P4[i];
   int m = 0;
-  auto add = [&](int j) {
+  auto insert = [&](int j) {  // SORT: insertion by original index
     if (m < kv) {
-      if (SORT) {
-        const int key = b.ORIG[j];
-        int p = m;
-        while (p > 0 && keys[(p - 1) * bs + tid] > key) {
-          keys[p * bs + tid] = keys[(p - 1) * bs + tid];
-          js[p * bs + tid] = js[(p - 1) * bs + tid];
-          --p;
-        }
-        keys[p * bs + tid] = key;
-        js[p * bs + tid] = j;
-      } else {
-        vl[(long long)m * N + i] = j;
+      const int key = b.ORIG[j];
+      int p = m;
+      while (p > 0 && keys[(p - 1) * bs + tid] > key) {
+        keys[p * bs + tid] = keys[(p - 1) * bs + tid];
+        js[p * bs + tid] = js[(p - 1) * bs + tid];
+        --p;
       }
+      keys[p * bs + tid] = key;
+      js[p * bs + tid] = j;
     }
     ++m;
   };
@@ -181,23 +178,47 @@ k_verlet(long long N, Buffers b, const CaseDev* cases, const int* cellid, const 
     const float r2 = c.v_r2;
     walk_rows<DIM, true>(c, cell, ri, start, c.vrad, r2, [&](int j0, int j1, float3 s) {
       const float qx = ri.x - s.x, qy = ri.y - s.y, qz = ri.z - s.z;
-      for (int j = j0; j < j1; ++j) {
-        const float4 rj = __ldg(b.P4 + j);
-        const float dx = qx - rj.x, dy = qy - rj.y, dz = (DIM == 3) ? qz - rj.z : 0.f;
-        if (j != i && dx * dx + dy * dy + dz * dz < r2) add(j);
+      if (SORT) {
+        for (int j = j0; j < j1; ++j) {
+          const float4 rj = __ldg(b.P4 + j);
+          const float dx = qx - rj.x, dy = qy - rj.y, dz = (DIM == 3) ? qz - rj.z : 0.f;
+          if (j != i && dx * dx + dy * dy + dz * dz < r2) insert(j);
+        }
+      } else {
+        // two gathers per iteration, predicated count, unconditional store
+        for (int j = j0; j < j1; j += 2) {
+          const bool v1 = j + 1 < j1;
+          const float4 ra = __ldg(b.P4 + j);
+          const float4 rb = v1 ? __ldg(b.P4 + j + 1) : make_float4(3e30f, 3e30f, 3e30f, 0.f);
+          float dx = qx - ra.x, dy = qy - ra.y, dz = (DIM == 3) ? qz - ra.z : 0.f;
+          const bool ea = j != i && dx * dx + dy * dy + dz * dz < r2;
+          dx = qx - rb.x;
+          dy = qy - rb.y;
+          dz = (DIM == 3) ? qz - rb.z : 0.f;
+          const bool eb = v1 && j + 1 != i && dx * dx + dy * dy + dz * dz < r2;
+          js[(m < kv ? m : kv - 1) * bs + tid] = j;
+          m += ea;
+          js[(m < kv ? m : kv - 1) * bs + tid] = j + 1;
+          m += eb;
+        }
       }
     });
   } else {
     walk_rows<DIM, false>(c, cell, ri, start, c.vrad, 0.f, [&](int j0, int j1, float3) {
-      for (int j = j0; j < j1; ++j)
-        if (j != i && is_edge<DIM>(ri, __ldg(b.P4 + j), c)) add(j);
+      for (int j = j0; j < j1; ++j) {
+        if (j == i || !is_edge<DIM>(ri, __ldg(b.P4 + j), c)) continue;
+        if (SORT) {
+          insert(j);
+        } else {
+          if (m < kv) js[m * bs + tid] = j;
+          ++m;
+        }
+      }
     });
   }
   vcnt[i] = m;
-  if (SORT) {
-    const int e = m < kv ? m : kv;
-    for (int k = 0; k < e; ++k) vl[(long long)k * N + i] = js[k * bs + tid];
-  }
+  const int e = m < kv ? m : kv;
+  for (int k = 0; k < e; ++k) vl[(long long)k * N + i] = js[k * bs + tid];
 }
 
 // ------------------------------------------------------------------ density pass
@@ -651,20 +672,29 @@ void forward_k(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
 
 }  // namespace
 
-cudaError_t prepare_kernels(int kv) {
-  const int smem = 2 * (int)sizeof(int) * kv * verlet_block(kv);
-  cudaError_t e =
-      cudaFuncSetAttribute(k_verlet<3, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+cudaError_t prepare_kernels(int /*kv*/) {
+  // the attribute belongs to the kernel, not to a handle: allow the largest
+  // staging any handle uses (kv * verlet_block(kv) <= 96 * 128 for every kv)
+  const int most = 96 * 128 * (int)sizeof(int);
+  cudaError_t e = cudaFuncSetAttribute(k_verlet<3, true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, 2 * most);
   if (e == cudaSuccess)
-    e = cudaFuncSetAttribute(k_verlet<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    e = cudaFuncSetAttribute(k_verlet<2, true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             2 * most);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_verlet<3, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             most);
+  if (e == cudaSuccess)
+    e = cudaFuncSetAttribute(k_verlet<2, false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             most);
   return e;
 }
 
 void launch_verlet(const LaunchCtx& L, Buffers b, const int* cellid, const int* start) {
+  const int bt = verlet_block(L.kv);
+  const int g = nblocks(L.N, bt);
+  const size_t smem = (L.canonical ? 2 : 1) * sizeof(int) * L.kv * bt;
   if (L.canonical) {
-    const int bt = verlet_block(L.kv);
-    const int g = nblocks(L.N, bt);
-    const size_t smem = 2 * sizeof(int) * L.kv * bt;
     if (L.dim == 3)
       k_verlet<3, true><<<g, bt, smem, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl, L.vcnt,
                                                    L.kv);
@@ -672,13 +702,12 @@ void launch_verlet(const LaunchCtx& L, Buffers b, const int* cellid, const int* 
       k_verlet<2, true><<<g, bt, smem, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl, L.vcnt,
                                                    L.kv);
   } else {
-    const int g = nblocks(L.N, kBlock);
     if (L.dim == 3)
-      k_verlet<3, false><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl,
-                                                     L.vcnt, L.kv);
+      k_verlet<3, false><<<g, bt, smem, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl, L.vcnt,
+                                                    L.kv);
     else
-      k_verlet<2, false><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl,
-                                                     L.vcnt, L.kv);
+      k_verlet<2, false><<<g, bt, smem, L.stream>>>(L.N, b, L.cases, cellid, start, L.vl, L.vcnt,
+                                                    L.kv);
   }
   count_launch(L);
 }

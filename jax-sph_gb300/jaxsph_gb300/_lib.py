@@ -177,16 +177,19 @@ class Engine:
         self.cases = cases
 
     @staticmethod
-    def view(state, n):
-        """SphStateView over a dict of contiguous float32/int32 CUDA tensors."""
+    def view(state, n, pinned_ok=False):
+        """SphStateView over a dict of contiguous float32/int32 CUDA tensors
+        (or pinned host tensors, where ``pinned_ok``)."""
         v = SphStateView()
         v.n = n
         for k in ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta",
                   "nw", "g_ext"):
             t = state.get(k)
             if t is not None:
-                if not t.is_cuda or not t.is_contiguous():
-                    raise ValueError(f"state['{k}'] must be a contiguous CUDA tensor")
+                ok = t.is_cuda or (pinned_ok and t.device.type == "cpu" and t.is_pinned())
+                if not ok or not t.is_contiguous():
+                    raise ValueError(f"state['{k}'] must be a contiguous CUDA tensor"
+                                     + (" or pinned host tensor" if pinned_ok else ""))
                 want = torch.int32 if k == "tag" else torch.float32
                 if t.dtype != want:
                     raise ValueError(f"state['{k}'] must be {want}, got {t.dtype}")
@@ -261,9 +264,9 @@ class Engine:
     def advance(self, state, out, ref=None, threshold_sq=0.0):
         """One fused drop-in step (load, step, read back); returns the status
         word as a 0-d int32 device tensor (no host synchronisation)."""
-        vin = self.view(state, self.n)
-        vout = self.view(out, self.n)
-        status = torch.empty((), dtype=torch.int32, device=state["r"].device)
+        vin = self.view(state, self.n, pinned_ok=True)
+        vout = self.view(out, self.n, pinned_ok=True)
+        status = torch.empty((), dtype=torch.int32, device="cuda")
         self._keep = state
         _check(self.lib.sph_advance(self.h, ctypes.byref(vin), ctypes.byref(vout),
                                     _ptr(ref) if ref is not None else None,

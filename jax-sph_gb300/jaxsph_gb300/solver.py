@@ -41,8 +41,31 @@ def prepare_state(state, dim, device="cuda"):
     return out
 
 
+OUT_KEYS = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
+
+
 def empty_outputs(st):
-    return {k: torch.empty_like(st[k]) for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")}
+    return {k: torch.empty_like(st[k]) for k in OUT_KEYS}
+
+
+def pinned_state(state, dim, need_nw):
+    """The state's own tensors when every field is a contiguous, pinned host
+    tensor of the kernels' dtype (float32, int32 tags) and shape; else None."""
+    out = {}
+    for k in STATE_KEYS:
+        t = state.get(k)
+        if t is None:
+            if k == "nw" and not need_nw:
+                continue
+            return None
+        if not isinstance(t, torch.Tensor) or t.device.type != "cpu" or not t.is_pinned():
+            return None
+        if t.dtype != (torch.int32 if k == "tag" else torch.float32) or not t.is_contiguous():
+            return None
+        if k in _VEC and (t.ndim != 2 or t.shape[1] != dim):
+            return None
+        out[k] = t
+    return out
 
 
 class WCSPH:
@@ -170,36 +193,63 @@ class WCSPH:
         return forward
 
     def advance(self, dt, tvf, state, neighbors, bc_fn):
-        """One fused si_euler step on the GPU (integrator.py:22-56)."""
+        """One fused si_euler step on the GPU (integrator.py:22-56).
+
+        A state of pinned (page-locked) host tensors is copied to the GPU and
+        its result back inside the one library call (DMA, one copy per
+        field), and the call returns once the result is in host memory. Any
+        other state goes to the GPU first and stays there.
+        """
         nl_fns = neighbors._fns
         bc_spec = getattr(bc_fn, "spec", None)
         case = self.sph_case(nl_fns, int(state["r"].shape[0]), dt=dt, tvf=tvf, bc=bc_spec)
         if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
             raise NotImplementedError(
                 "si_euler needs a g_ext_fn with a GPU spec (e.g. jaxsph_gb300.cases.GExt)")
-        e, st = self._load(state, neighbors, case, load=False)
-        out = empty_outputs(st)
+        st = pinned_state(state, self.dim, self.solver == "RIE" or self.is_free_slip)
+        host = st is not None
+        if host:
+            e = self.engine(nl_fns, case)
+            cap = neighbors.cell_list_capacity
+            e.nl_set_capacity(cap if cap is not None else 2 ** 31 - 1, neighbors.max_occupancy)
+            out = {k: torch.empty(st[k].shape, dtype=st[k].dtype, pin_memory=True)
+                   for k in OUT_KEYS}
+        else:
+            e, st = self._load(state, neighbors, case, load=False)
+            out = empty_outputs(st)
         # one fused call: load, step, read back; the status stays a device
         # value inside the returned list's error code until the caller tests
         # it (host-side failures raise from the call)
+        thr = nl_fns.threshold_sq
         ref = torch.as_tensor(neighbors.reference_position)
-        if nl_fns.threshold_sq > 0.0:
-            ref = ref.to(device=st["r"].device, dtype=torch.float32).contiguous()
-            status = e.advance(st, out, ref, nl_fns.threshold_sq)
+        if thr > 0.0:
+            if host and not (ref.device.type == "cpu" and ref.is_pinned()):
+                ref = ref.to(torch.float32).contiguous().pin_memory()
+            elif not host:
+                ref = ref.to(device=st["r"].device, dtype=torch.float32).contiguous()
+            status = e.advance(st, out, ref, thr)
         else:
             status = e.advance(st, out)
+        if host:
+            torch.cuda.current_stream().synchronize()
         res = self._result(state, out)
         if bc_fn is not None and bc_spec is None:
             res = bc_fn(res)
         from .partition import NeighborList
 
-        if nl_fns.threshold_sq > 0.0:
+        if thr > 0.0:
             # the reference rebuilds inside the step only when a particle
             # moved beyond the threshold (jax_md/partition.py:1010-1018)
-            mv = (status & _lib.INFO_MOVED) != 0
-            nbrs = NeighborList(nl_fns, torch.where(mv, res["r"], ref),
-                                neighbors.error.merged(status & 0xFF, mv),
-                                neighbors.cell_list_capacity, neighbors.max_occupancy)
+            if host:
+                moved = bool(int(status.item()) & _lib.INFO_MOVED)
+                nbrs = NeighborList(nl_fns, res["r"] if moved else ref,
+                                    neighbors.error.update(int(status.item()) & 0xFF, moved),
+                                    neighbors.cell_list_capacity, neighbors.max_occupancy)
+            else:
+                mv = (status & _lib.INFO_MOVED) != 0
+                nbrs = NeighborList(nl_fns, torch.where(mv, res["r"], ref),
+                                    neighbors.error.merged(status & 0xFF, mv),
+                                    neighbors.cell_list_capacity, neighbors.max_occupancy)
         else:
             # threshold 0: a list not rebuilt is one at unchanged positions,
             # whose reference position and overflow bits equal the new ones

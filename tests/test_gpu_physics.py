@@ -210,3 +210,53 @@ def test_diagnostics_float64():
     assert abs(d[4].item() - ekin) <= 1e-6 * max(ekin, 1e-30) + 1e-15
     umax = st["u"].double().norm(dim=1).max().item()
     assert abs(d[5].item() - umax) <= 1e-7 * max(umax, 1e-30)
+
+
+def test_drop_in_advance_on_pinned_host_state():
+    # a pinned host state goes to the GPU and back inside the call: the
+    # same result as on device tensors, bit for bit
+    setup = cases.tgv(dim=3, dx=2 * np.pi / 12)
+    wc = gpu_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    _, shift = setup.space()
+    adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
+    keys = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
+    host = {k: setup.state[k].to(torch.int32 if k == "tag" else torch.float32)
+            .contiguous().pin_memory() for k in keys}
+    dev = {k: v.cuda() for k, v in host.items()}
+    hs, hn = host, fns.allocate(host["r"])
+    ds, dn = dev, fns.allocate(dev["r"])
+    for _ in range(4):
+        hs, hn = adv(setup.dt, hs, hn)
+        ds, dn = adv(setup.dt, ds, dn)
+    for k in ("r", "u", "v", "rho", "p", "dudt", "dvdt"):
+        assert hs[k].device.type == "cpu" and hs[k].is_pinned(), k
+        assert torch.equal(hs[k], ds[k].cpu()), k
+    assert not hn.did_buffer_overflow
+
+
+def test_drop_in_advance_rejects_pageable_host_arrays():
+    setup = cases.tgv(dim=2, dx=0.05)
+    wc = gpu_solver(setup)
+    e = wc.engine(simulate.make_neighbor_fns(setup, wc), wc.sph_case(
+        simulate.make_neighbor_fns(setup, wc), setup.n))
+    keys = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
+    st = {k: setup.state[k].to(torch.int32 if k == "tag" else torch.float32).contiguous()
+          for k in keys}
+    out = {k: torch.empty_like(st[k]) for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")}
+    with pytest.raises(Exception, match="pinned"):
+        e.advance(st, out)  # refused by the binding
+    # and by the library itself, before any launch
+    from jaxsph_gb300 import _lib
+    import ctypes
+    vin, vout = _lib.SphStateView(), _lib.SphStateView()
+    vin.n = vout.n = setup.n
+    for k in keys:
+        setattr(vin, k, st[k].data_ptr())
+    for k in out:
+        setattr(vout, k, out[k].data_ptr())
+    status = torch.zeros((), dtype=torch.int32, device="cuda")
+    rc = e.lib.sph_advance(e.h, ctypes.byref(vin), ctypes.byref(vout), None, 0.0,
+                           status.data_ptr(), None)
+    assert rc & _lib.ERR_INVALID_ARG
+    assert b"pinned" in e.lib.sph_last_error()
