@@ -51,10 +51,11 @@ PHASE_KERNELS = ("k_kick (+ k_hash_count/k_tile_scan/k_scatter/k_permute/k_verle
 PHASE_BYTES = (BIN_BYTES, DENSITY_BYTES, 0, FORCE_BYTES)
 # DRAM bytes per particle of one launch (dram__bytes_read.sum + dram__bytes_write.sum)
 # and FMA-pipe utilisation measured with ncu on the 128^3 case of the same kernels
-# (profiles/k_density_tgv3d_128.md, profiles/k_force_tgv3d_128.md); traffic grows
-# in proportion to the particle count, so it scales to 64^3 per particle.
-PHASE_TRAFFIC = (None, 153.4, None, 221.3)
-PHASE_FP32_PIPE = (None, 0.246, None, 0.267)
+# (profiles/k_kick_tgv3d_128.md, k_density_tgv3d_128.md, k_force_tgv3d_128.md); traffic
+# grows in proportion to the particle count, so it scales to 64^3 per particle. The
+# kick phase's figure is the kick alone (the rebuild kernels run every few steps).
+PHASE_TRAFFIC = (131.5, 289.8, None, 220.6)
+PHASE_FP32_PIPE = (0.157, 0.193, None, 0.409)
 
 
 def dist_env():

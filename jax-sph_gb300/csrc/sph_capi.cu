@@ -61,6 +61,7 @@ struct SphHandle {
   int block = 256;        // threads per block of the forward passes
   unsigned* status = nullptr;
   unsigned long long* edgecnt = nullptr;
+  int* case_max = nullptr;  // allocate: largest reference-cell occupancy per case
   const float* g_arr = nullptr;
   // binned: candidate lists valid for the current positions; fresh: the
   // binning itself is of the current positions (no step since)
@@ -557,7 +558,8 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
           h->alloc(&h->rebuilds_d, 1);
     long long m = h->C + 1 > N + 1 ? h->C + 1 : N + 1;
     rc |= h->alloc(&h->scan_tmp, scan_tmp_ints(m));
-    rc |= h->alloc(&h->status, 1) | h->alloc(&h->edgecnt, n_cases) | h->alloc(&h->dc, n_cases) |
+    rc |= h->alloc(&h->status, 1) | h->alloc(&h->edgecnt, n_cases) |
+          h->alloc(&h->case_max, n_cases) | h->alloc(&h->dc, n_cases) |
           h->alloc(&h->case_off_d, n_cases + 1);
   }
   if (!rc) rc = cuda_check(cudaMemset(h->status, 0, sizeof(unsigned)), "memset");
@@ -664,31 +666,22 @@ int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out
   if (rc) return rc;
   LaunchCtx L = h->ctx(st);
   launch_row_counts(L, h->buf[0], h->cellid, h->start, h->rowcnt);
-  if ((rc = launch_status("row counts"))) return rc;
-  std::vector<int> start(h->C + 1), rows(h->N);
-  cudaError_t e = cudaMemcpyAsync(start.data(), h->start, sizeof(int) * (h->C + 1),
+  launch_alloc_stats(L, h->buf[0], h->cellid, h->start, h->rowcnt, h->case_max, h->edgecnt);
+  if ((rc = launch_status("allocate stats"))) return rc;
+  std::vector<int> maxocc_c(h->n_cases);
+  std::vector<unsigned long long> occ_c(h->n_cases);
+  cudaError_t e = cudaMemcpyAsync(maxocc_c.data(), h->case_max, sizeof(int) * h->n_cases,
                                   cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess)
-    e = cudaMemcpyAsync(rows.data(), h->rowcnt, sizeof(int) * h->N, cudaMemcpyDeviceToHost, st);
+    e = cudaMemcpyAsync(occ_c.data(), h->edgecnt, sizeof(unsigned long long) * h->n_cases,
+                        cudaMemcpyDeviceToHost, st);
   if (e == cudaSuccess) e = cudaStreamSynchronize(st);
   if ((rc = cuda_check(e, "allocate readback"))) return rc;
   const double mult = h->cfg.capacity_multiplier;
   const int nb = h->cfg.dim == 3 ? 27 : 9;
   for (int i = 0; i < h->n_cases; ++i) {
     CaseDev& c = h->hc[i];
-    long long maxocc = 0, occ = 0;
-    {
-      // occupancy of the reference's cells: sums over their fine cells
-      const int rx = c.nc[0] / c.sub[0], ry = c.nc[1] / c.sub[1];
-      std::vector<long long> ref((size_t)c.ncell / (c.sub[0] * c.sub[1] * c.sub[2]), 0);
-      for (int k = 0; k < c.ncell; ++k) {
-        const int x = k % c.nc[0], y = (k / c.nc[0]) % c.nc[1], z = k / (c.nc[0] * c.nc[1]);
-        const size_t r = ((size_t)(z / c.sub[2]) * ry + y / c.sub[1]) * rx + x / c.sub[0];
-        ref[r] += start[c.cell_off + k + 1] - start[c.cell_off + k];
-      }
-      for (long long o : ref) maxocc = o > maxocc ? o : maxocc;
-    }
-    for (int k = 0; k < c.n; ++k) occ += rows[c.p_off + k];
+    const long long maxocc = maxocc_c[i], occ = (long long)occ_c[i];
     // _estimate_cell_capacity (jax_md/partition.py:195-199) + extra capacity
     c.cell_cap = (int)(maxocc * mult) + (int)extra_capacity;
     // max_occupancy = int(occupancy * multiplier + N * extra) (:956-971)
@@ -706,7 +699,7 @@ int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out
       cap_out->max_cell_occupancy = maxocc;
     }
   }
-  drop_graph(h);
+  // the captured step reads the capacities from device memory: no re-capture
   return upload_cases(h, st);
 }
 
@@ -722,7 +715,6 @@ int sph_nl_set_capacity(SphHandle* h, const SphNLCapacity* cap) {
     c.cell_cap = (int)cap->cell_capacity;
     c.edge_cap = cap->max_occupancy;
   }
-  drop_graph(h);
   return upload_cases(h, 0);
 }
 

@@ -525,6 +525,9 @@ void launch_edges(const LaunchCtx& L, Buffers b, const int* cellid, const int* s
                   long long* count_dev);
 void launch_row_counts(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
                        int* rowcnt);
+// Per case: largest reference-cell occupancy and edge count of the binning.
+void launch_alloc_stats(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
+                        const int* rowcnt, int* case_max, unsigned long long* case_edges);
 void launch_diagnostics(const LaunchCtx& L, Buffers b, const float4* R4, bool from_forward,
                         bool apply_bc, double* out);
 

@@ -578,6 +578,43 @@ void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_
   count_launch(L);
 }
 
+// Capacities of an allocate (jax_md/partition.py:195-199, :956-971), per
+// case: the largest occupancy of a reference cell (every occupied cell has a
+// particle that sees it) and the number of edges (row counts, indexed by
+// original particle). One atomic per case present in a warp.
+__global__ void k_alloc_stats(long long N, Buffers b, const CaseDev* cases, const int* cellid,
+                              const int* start, const int* rowcnt, int dim, int* case_max,
+                              unsigned long long* case_edges) {
+  const long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const bool valid = s < N;
+  int ci = 0, occ = 0, rows = 0;
+  if (valid) {
+    ci = case_of(b.META[s]);
+    const CaseDev& c = cases[ci];
+    const int cell = cellid[s] - c.cell_off;
+    occ = dim == 3 ? ref_cell_occupancy<3>(c, cell, start) : ref_cell_occupancy<2>(c, cell, start);
+    rows = rowcnt[b.ORIG[s]];
+  }
+  const unsigned mask = __ballot_sync(kFull, valid);
+  if (!valid) return;
+  const unsigned peers = __match_any_sync(mask, ci);
+  const int lane = threadIdx.x & 31, leader = __ffs(peers) - 1;
+  const int m = __reduce_max_sync(peers, occ);
+  const unsigned t = __reduce_add_sync(peers, (unsigned)rows);
+  if (lane == leader) {
+    atomicMax(&case_max[ci], m);
+    atomicAdd(&case_edges[ci], (unsigned long long)t);
+  }
+}
+
+void launch_alloc_stats(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
+                        const int* rowcnt, int* case_max, unsigned long long* case_edges) {
+  cudaMemsetAsync(case_max, 0, sizeof(int) * L.n_cases, L.stream);
+  cudaMemsetAsync(case_edges, 0, sizeof(unsigned long long) * L.n_cases, L.stream);
+  k_alloc_stats<<<nblocks(L.N), kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, rowcnt,
+                                                       L.dim, case_max, case_edges);
+}
+
 void launch_row_counts(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
                        int* rowcnt) {
   int g = nblocks(L.N);

@@ -245,15 +245,17 @@ class NeighborListFns:
 
     # -- reference API
     def allocate(self, position, extra_capacity=0, **kwargs):
-        """Build a list and size its capacities from the data (host-synchronous)."""
-        e, r = self._load(position)
-        e.read_status(clear=True)
+        """Build a list and size its capacities from the data (host-synchronous).
+
+        The edge array ``idx`` is emitted when first read (the same array the
+        reference's allocate returns); a fused si_euler step never reads it.
+        """
+        e, _ = self._load(position)  # loading clears the status word
         cap = e.nl_allocate(extra_capacity)
-        idx, count = e.nl_edges(cap.max_occupancy, r.device)
         code = e.read_status(clear=True) & 0xFF
         cell_cap = int(cap.cell_capacity) if self._uses_cells() else None
-        return NeighborList(self, position, code, cell_cap, cap.max_occupancy, idx=idx,
-                            occupancy=int(count.item()))
+        return NeighborList(self, position, code, cell_cap, cap.max_occupancy,
+                            occupancy=int(cap.occupancy))
 
     def _uses_cells(self):
         box32 = self.box.astype(np.float32)
