@@ -58,10 +58,15 @@ struct SphHandle {
   int rebuild_launches = 0;                  // kernels of one rebuild
   unsigned char* stage = nullptr;  // device copies of pinned host fields (sph_advance)
   size_t stage_slot = 0;
+  // the staging copies are spread over a few streams (several copy engines)
+  static constexpr int kCopyStreams = 4;
+  cudaStream_t cs[kCopyStreams] = {};
+  cudaEvent_t fork = nullptr, join[kCopyStreams] = {};
   int block = 256;        // threads per block of the forward passes
   unsigned* status = nullptr;
   unsigned long long* edgecnt = nullptr;
   int* case_max = nullptr;  // allocate: largest reference-cell occupancy per case
+  int* inv = nullptr;       // sorted position of each original index (valid once binned)
   const float* g_arr = nullptr;
   // binned: candidate lists valid for the current positions; fresh: the
   // binning itself is of the current positions (no step since)
@@ -116,6 +121,7 @@ struct SphHandle {
     L.cref_count = cref_count;
     L.vflag = vflag;
     L.canonical = cfg.canonical_order;
+    L.inv = inv;
     L.block = block;
     L.launches = const_cast<int*>(&launch_count);
     L.ev = ev;
@@ -336,7 +342,7 @@ int rebuild(SphHandle* h, cudaStream_t st, bool from_forward, bool apply_bc) {
   cp(B.META, A.META, sizeof(int) * N);
   cp(B.ORIG, A.ORIG, sizeof(int) * N);
   if (A.NW4) cp(B.NW4, A.NW4, sizeof(float4) * N);
-  if (A.RD) cp(B.RD, A.RD, sizeof(double4) * N);
+  if (A.RD) cp(B.RD, A.RD, sizeof(double4_32a) * N);
   if (e != cudaSuccess) return cuda_check(e, "rebuild copy");
   launch_bin(L, B, A, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc, h->tkey,
              h->tcell, h->scan_tmp, h->C, false, from_forward, apply_bc, h->rref);
@@ -553,7 +559,7 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
           h->alloc(&h->tkey, N) | h->alloc(&h->tcell, N) | h->alloc(&h->rowcnt, N + 1) |
           h->alloc(&h->rowoff, N + 1) | h->alloc(&h->nbr, (size_t)h->kmax * N) |
           h->alloc(&h->nbr_cnt, N) | h->alloc(&h->vl, (size_t)h->kv * N) |
-          h->alloc(&h->vcnt, N) | h->alloc(&h->rref, N) |
+          h->alloc(&h->vcnt, N) | h->alloc(&h->rref, N) | h->alloc(&h->inv, N) |
           h->alloc(&h->cref_count, h->ref_cells + 1) | h->alloc(&h->vflag, 1) |
           h->alloc(&h->rebuilds_d, 1);
     long long m = h->C + 1 > N + 1 ? h->C + 1 : N + 1;
@@ -584,6 +590,11 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
 int sph_destroy(SphHandle* h) {
   if (!h) return 0;
   drop_graph(h);
+  for (int k = 0; k < SphHandle::kCopyStreams; ++k) {
+    if (h->cs[k]) cudaStreamDestroy(h->cs[k]);
+    if (h->join[k]) cudaEventDestroy(h->join[k]);
+  }
+  if (h->fork) cudaEventDestroy(h->fork);
   if (h->hs) cudaStreamDestroy(h->hs);
   if (h->hs2) cudaStreamDestroy(h->hs2);
   for (void* p : h->allocs) cudaFree(p);
@@ -641,8 +652,9 @@ int sph_get_state(SphHandle* h, SphStateView* s, void* stream) {
   if (s->n != h->N) return fail((int)SPH_ERR_INVALID_ARG, "state has the wrong particle count");
   if (!s->r || !s->u || !s->v || !s->dudt || !s->dvdt || !s->rho || !s->p)
     return fail((int)SPH_ERR_INVALID_ARG, "missing state field");
+  // after a binning the read-back runs per original index (coalesced writes)
   launch_unpack(h->ctx((cudaStream_t)stream), h->buf[0], h->R4, *s, h->from_forward,
-                h->pending_bc);
+                h->pending_bc, nullptr, 0.f, h->binned ? h->inv : nullptr);
   return launch_status("get_state");
 }
 
@@ -847,14 +859,38 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   if (any && !h->stage) {  // allocated once, on the first call with host arrays
     h->stage_slot = (vec + 255) / 256 * 256;
     if (h->alloc(&h->stage, h->stage_slot * (kFields + 1))) return SPH_ERR_CUDA;
+    cudaError_t e0 = cudaEventCreateWithFlags(&h->fork, cudaEventDisableTiming);
+    for (int k = 0; k < SphHandle::kCopyStreams && e0 == cudaSuccess; ++k) {
+      e0 = cudaStreamCreateWithFlags(&h->cs[k], cudaStreamNonBlocking);
+      if (e0 == cudaSuccess) e0 = cudaEventCreateWithFlags(&h->join[k], cudaEventDisableTiming);
+    }
+    if (e0 != cudaSuccess) return cuda_check(e0, "copy streams");
   }
-  cudaError_t e = cudaSuccess;
+  // fork: the copy streams start after the work already on `st`; join: `st`
+  // continues after all of them
+  auto fork = [&]() {
+    cudaError_t r = cudaEventRecord(h->fork, st);
+    for (int k = 0; k < SphHandle::kCopyStreams && r == cudaSuccess; ++k)
+      r = cudaStreamWaitEvent(h->cs[k], h->fork, 0);
+    return r;
+  };
+  auto join = [&]() {
+    cudaError_t r = cudaSuccess;
+    for (int k = 0; k < SphHandle::kCopyStreams && r == cudaSuccess; ++k) {
+      r = cudaEventRecord(h->join[k], h->cs[k]);
+      if (r == cudaSuccess) r = cudaStreamWaitEvent(st, h->join[k], 0);
+    }
+    return r;
+  };
+  cudaError_t e = any ? fork() : cudaSuccess;
+  int ncopy = 0;
   void* host_dst[kFields] = {};
   for (int k = 0; k < kFields; ++k) {
     void* slot = h->stage ? h->stage + h->stage_slot * k : nullptr;
     if (hin[k]) {
       if (e == cudaSuccess)
-        e = cudaMemcpyAsync(slot, *fields[k].in, fields[k].bytes, cudaMemcpyHostToDevice, st);
+        e = cudaMemcpyAsync(slot, *fields[k].in, fields[k].bytes, cudaMemcpyHostToDevice,
+                            h->cs[ncopy++ % SphHandle::kCopyStreams]);
       *fields[k].in = slot;
     }
     if (hout[k]) {  // the result goes to the slot, then to the host array
@@ -865,9 +901,12 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   const float* ref_r = ref_r_;
   if (href) {
     void* slot = h->stage + h->stage_slot * kFields;
-    if (e == cudaSuccess) e = cudaMemcpyAsync(slot, ref_r_, vec, cudaMemcpyHostToDevice, st);
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(slot, ref_r_, vec, cudaMemcpyHostToDevice,
+                          h->cs[ncopy++ % SphHandle::kCopyStreams]);
     ref_r = (const float*)slot;
   }
+  if (any && e == cudaSuccess) e = join();
   if (e != cudaSuccess) return cuda_check(e, "advance input copy");
   if (in->n != h->N || out->n != h->N)
     return fail((int)SPH_ERR_INVALID_ARG, "state has the wrong particle count");
@@ -897,11 +936,16 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   launch_verlet(L, A, h->cellid, h->start);
   launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
                  true);
-  launch_unpack(L, A, h->R4, *out, true, true, ref_r, threshold_sq);
+  launch_unpack(L, A, h->R4, *out, true, true, ref_r, threshold_sq, h->inv);
+  bool any_out = false;
+  for (int k = 0; k < kFields; ++k) any_out = any_out || host_dst[k];
+  if (any_out && e == cudaSuccess) e = fork();
+  ncopy = 0;
   for (int k = 0; k < kFields; ++k)
     if (host_dst[k] && e == cudaSuccess)
       e = cudaMemcpyAsync(host_dst[k], h->stage + h->stage_slot * k, fields[k].bytes,
-                          cudaMemcpyDeviceToHost, st);
+                          cudaMemcpyDeviceToHost, h->cs[ncopy++ % SphHandle::kCopyStreams]);
+  if (any_out && e == cudaSuccess) e = join();
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(status_dev, h->status, sizeof(unsigned),
                         hst ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st);

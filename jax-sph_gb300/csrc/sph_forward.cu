@@ -268,19 +268,18 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
     const CaseDev* cp = cases + ci;
     const int vc = nl.vcnt[i];
     if (vc <= nl.kv) {
-      // two independent gathers per iteration, the next two candidate
-      // indices loaded ahead; predicated count and an unconditional
-      // shared-memory store
+      // two candidates per iteration, software pipelined: the next pair's
+      // positions and the pair after's indices are in flight while a pair
+      // is tested; predicated count and an unconditional shared-memory store
       const int* vli = nl.vl + i;
-      int jan = vc > 0 ? vli[0] : 0;
-      int jbn = vc > 1 ? vli[N] : jan;
+      auto cand = [&](int k, int dflt) { return k < vc ? vli[(long long)k * N] : dflt; };
+      int ja = cand(0, (int)i), jb = cand(1, ja);
+      int jc = cand(2, ja), jd = cand(3, jc);
+      float4 ra = __ldg(b.P4 + ja), rb = __ldg(b.P4 + jb);
       for (int k = 0; k < vc; k += 2) {
         const bool v1 = k + 1 < vc;
-        const int ja = jan, jb = jbn;
-        if (k + 2 < vc) jan = vli[(long long)(k + 2) * N];
-        jbn = k + 3 < vc ? vli[(long long)(k + 3) * N] : jan;
-        const float4 ra = __ldg(b.P4 + ja);
-        const float4 rb = __ldg(b.P4 + jb);
+        const float4 rc = __ldg(b.P4 + jc), rd = __ldg(b.P4 + jd);
+        const int je = cand(k + 4, jc), jf = cand(k + 5, je);
         float d2a, d2b;
         const bool ea = edge_mi_d2<DIM>(ri, ra, lo, hi, c, cp, d2a);
         const bool eb = v1 && edge_mi_d2<DIM>(ri, rb, lo, hi, c, cp, d2b);
@@ -292,6 +291,12 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
         m += ea;
         s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = jb;
         m += eb;
+        ja = jc;
+        jb = jd;
+        ra = rc;
+        rb = rd;
+        jc = je;
+        jd = jf;
       }
     } else {
       for_each_edge_slow<DIM>(N, i, ri, c, cp, b.P4, cellid, start, nl,

@@ -103,7 +103,7 @@ struct Buffers {
   float4 *P4, *U4, *V4, *A4, *A2, *NW4;
   float* ETA;
   int *META, *ORIG;
-  double4* RD;  // float64 positions of the precision form (else null)
+  double4_32a* RD;  // float64 positions of the precision form (else null)
 };
 
 // ------------------------------------------------------------------ helpers
@@ -493,6 +493,7 @@ struct LaunchCtx {
   int* cref_count;        // per-step occupancy of the reference's cells
   unsigned* vflag;        // a rebuild is due
   int canonical;          // candidate lists in ascending original index
+  int* inv;               // sorted position of every original index (last binning)
   int block;              // threads per block of the forward passes (<= 256)
   int* launches;          // optional host counter of kernel launches
   cudaEvent_t* ev;        // optional phase events: bin start, bin end, density end,
@@ -508,9 +509,12 @@ inline void mark(const LaunchCtx& L, int i) {
 
 // sph_sort.cu
 void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out, const long long* case_off_dev);
+// Write the state back in original order; with `inv` (the binning's inverse
+// permutation) by original index, gathering from the sorted buffers and
+// writing coalesced.
 void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateView& s,
                    bool from_forward, bool apply_bc, const float* ref = nullptr,
-                   float thr_sq = 0.f);
+                   float thr_sq = 0.f, const int* inv = nullptr);
 void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,
                 int* count, int* start, int* keyc, int* keys, int* tsrc, int* tkey, int* tcell,
                 int* scan_tmp, long long total_cells, bool drift, bool from_forward,

@@ -57,7 +57,7 @@ __global__ void k_pack(SphStateView s, int dim, Buffers o, const long long* case
   o.META[i] = (c << kTagBits) | (tag & kTagMask);
   o.ORIG[i] = (int)i;
   if (o.NW4) o.NW4[i] = s.nw ? ld4(s.nw, dim, i) : make_float4(0.f, 0.f, 0.f, 0.f);
-  if (o.RD) o.RD[i] = make_double4(r.x, r.y, r.z, 0.0);
+  if (o.RD) o.RD[i] = make_double4_32a(r.x, r.y, r.z, 0.0);
 }
 
 // The state a step or forward left behind: density/pressure from the density
@@ -96,14 +96,17 @@ __device__ __forceinline__ Final finalize(const Buffers& b, const float4* R4, lo
 // metric.
 __global__ void k_unpack(SphStateView s, int dim, Buffers b, const float4* R4,
                          const CaseDev* cases, bool from_forward, bool apply_bc,
-                         const float* ref, float thr_sq, unsigned* status) {
-  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+                         const float* ref, float thr_sq, unsigned* status, const int* inv) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   bool moved = false;
-  if (q < s.n) {
+  if (t < s.n) {
+    // thread per original index (coalesced writes) when the inverse
+    // permutation is known, else per sorted position
+    const long long q = inv ? inv[t] : t;
     int meta = b.META[q];
     const CaseDev& c = cases[case_of(meta)];
     int tag = tag_of(meta);
-    long long o = b.ORIG[q];
+    long long o = inv ? t : b.ORIG[q];
     Final f = finalize(b, R4, q, c, tag, from_forward, apply_bc);
     float4 r = b.P4[q], a = b.A4[q], a2 = b.A2[q];
     st3(s.r, dim, o, r.x, r.y, r.z);
@@ -159,7 +162,7 @@ __device__ __forceinline__ float drift_axis64(double& x, float v, double dt, dou
 }
 
 template <int DIM>
-__device__ __forceinline__ void kick_drift64(float4& r, double4& rd, float3& u, float3& v,
+__device__ __forceinline__ void kick_drift64(float4& r, double4_32a& rd, float3& u, float3& v,
                                              const float4& dudt, const float4& dvdt,
                                              const CaseDev& c) {
   u.x = __fadd_rn(u.x, __fmul_rn(c.dt, dudt.x));
@@ -190,7 +193,7 @@ __global__ void k_hash_count(long long N, Buffers in, const float4* R4, const Ca
       Final f = finalize(in, R4, k, c, tag_of(meta), from_forward, apply_bc);
       float3 u = f.u, v;
       if (in.RD) {
-        double4 rd = in.RD[k];
+        double4_32a rd = in.RD[k];
         kick_drift64<DIM>(r, rd, u, v, in.A4[k], in.A2[k], c);
       } else {
         kick_drift<DIM>(r, u, v, in.A4[k], in.A2[k], c);
@@ -227,7 +230,8 @@ template <int DIM>
 __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4,
                           const CaseDev* cases, const int* start, const int* tsrc,
                           const int* tkey, const int* tcell, int* cellid, unsigned* status,
-                          bool drift, bool from_forward, bool apply_bc, float4* rref) {
+                          bool drift, bool from_forward, bool apply_bc, float4* rref,
+                          int* inv) {
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   bool over = false;
   if (q < N) {
@@ -246,7 +250,7 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
     float4 A = in.A4[src], B = in.A2[src];
     float3 u = f.u, v = f.v;
     if (in.RD) {
-      double4 rd = in.RD[src];
+      double4_32a rd = in.RD[src];
       if (drift) kick_drift64<DIM>(r, rd, u, v, A, B, c);
       out.RD[dest] = rd;
     } else if (drift) {
@@ -263,6 +267,7 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
     if (out.NW4) out.NW4[dest] = in.NW4[src];
     cellid[dest] = cell;
     if (rref) rref[dest] = r;
+    if (inv) inv[key] = dest;
     // one test per occupied cell, against the reference's cell
     if (c.use_cells && q == a)
       over = ref_cell_occupancy<DIM>(c, cell - c.cell_off, start) > c.cell_cap;
@@ -294,7 +299,7 @@ __global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* 
     float3 u = f.u, v;
     const float4 A = b.A4[i], B = b.A2[i];
     if (b.RD) {
-      double4 rd = b.RD[i];
+      double4_32a rd = b.RD[i];
       kick_drift64<DIM>(r, rd, u, v, A, B, c);
       b.RD[i] = rd;
     } else {
@@ -535,9 +540,10 @@ void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out,
 }
 
 void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateView& s,
-                   bool from_forward, bool apply_bc, const float* ref, float thr_sq) {
+                   bool from_forward, bool apply_bc, const float* ref, float thr_sq,
+                   const int* inv) {
   k_unpack<<<nblocks(L.N), kBlock, 0, L.stream>>>(s, L.dim, in, R4, L.cases, from_forward,
-                                                   apply_bc, ref, thr_sq, L.status);
+                                                   apply_bc, ref, thr_sq, L.status, inv);
   count_launch(L);
 }
 
@@ -558,11 +564,11 @@ void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, i
   if (L.dim == 3)
     k_permute<3><<<g, kBlock, 0, L.stream>>>(L.N, in, out, R4, L.cases, start, tsrc, tkey,
                                               tcell, cellid, L.status, drift, from_forward,
-                                              apply_bc, rref);
+                                              apply_bc, rref, L.inv);
   else
     k_permute<2><<<g, kBlock, 0, L.stream>>>(L.N, in, out, R4, L.cases, start, tsrc, tkey,
                                               tcell, cellid, L.status, drift, from_forward,
-                                              apply_bc, rref);
+                                              apply_bc, rref, L.inv);
 }
 
 void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_cells,

@@ -186,7 +186,8 @@ class Engine:
                   "nw", "g_ext"):
             t = state.get(k)
             if t is not None:
-                ok = t.is_cuda or (pinned_ok and t.device.type == "cpu" and t.is_pinned())
+                # host tensors: the library itself refuses pageable memory
+                ok = t.is_cuda or (pinned_ok and t.device.type == "cpu")
                 if not ok or not t.is_contiguous():
                     raise ValueError(f"state['{k}'] must be a contiguous CUDA tensor"
                                      + (" or pinned host tensor" if pinned_ok else ""))

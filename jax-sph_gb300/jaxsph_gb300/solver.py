@@ -48,9 +48,10 @@ def empty_outputs(st):
     return {k: torch.empty_like(st[k]) for k in OUT_KEYS}
 
 
-def pinned_state(state, dim, need_nw):
-    """The state's own tensors when every field is a contiguous, pinned host
-    tensor of the kernels' dtype (float32, int32 tags) and shape; else None."""
+def host_state(state, dim, need_nw):
+    """The state's own tensors when every field is a contiguous host tensor of
+    the kernels' dtype (float32, int32 tags) and shape; else None. (Whether
+    they are pinned the library checks itself, before any work.)"""
     out = {}
     for k in STATE_KEYS:
         t = state.get(k)
@@ -58,7 +59,7 @@ def pinned_state(state, dim, need_nw):
             if k == "nw" and not need_nw:
                 continue
             return None
-        if not isinstance(t, torch.Tensor) or t.device.type != "cpu" or not t.is_pinned():
+        if not isinstance(t, torch.Tensor) or t.device.type != "cpu":
             return None
         if t.dtype != (torch.int32 if k == "tag" else torch.float32) or not t.is_contiguous():
             return None
@@ -206,7 +207,10 @@ class WCSPH:
         if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
             raise NotImplementedError(
                 "si_euler needs a g_ext_fn with a GPU spec (e.g. jaxsph_gb300.cases.GExt)")
-        st = pinned_state(state, self.dim, self.solver == "RIE" or self.is_free_slip)
+        st = host_state(state, self.dim, self.solver == "RIE" or self.is_free_slip)
+        thr = nl_fns.threshold_sq
+        ref = torch.as_tensor(neighbors.reference_position)
+        status = None
         host = st is not None
         if host:
             e = self.engine(nl_fns, case)
@@ -214,22 +218,23 @@ class WCSPH:
             e.nl_set_capacity(cap if cap is not None else 2 ** 31 - 1, neighbors.max_occupancy)
             out = {k: torch.empty(st[k].shape, dtype=st[k].dtype, pin_memory=True)
                    for k in OUT_KEYS}
-        else:
+            if thr > 0.0 and not (ref.device.type == "cpu" and ref.is_pinned()):
+                ref = ref.to(torch.float32).contiguous().pin_memory()
+            try:
+                status = e.advance(st, out, ref if thr > 0.0 else None, thr)
+            except _lib.SphError as err:
+                if "pinned" not in str(err):
+                    raise
+                host = False  # pageable host arrays: go through device copies instead
+        if not host:
             e, st = self._load(state, neighbors, case, load=False)
             out = empty_outputs(st)
-        # one fused call: load, step, read back; the status stays a device
-        # value inside the returned list's error code until the caller tests
-        # it (host-side failures raise from the call)
-        thr = nl_fns.threshold_sq
-        ref = torch.as_tensor(neighbors.reference_position)
-        if thr > 0.0:
-            if host and not (ref.device.type == "cpu" and ref.is_pinned()):
-                ref = ref.to(torch.float32).contiguous().pin_memory()
-            elif not host:
+            if thr > 0.0:
                 ref = ref.to(device=st["r"].device, dtype=torch.float32).contiguous()
-            status = e.advance(st, out, ref, thr)
-        else:
-            status = e.advance(st, out)
+            # one fused call: load, step, read back; the status stays a device
+            # value inside the returned list's error code until the caller
+            # tests it (host-side failures raise from the call)
+            status = e.advance(st, out, ref if thr > 0.0 else None, thr)
         if host:
             torch.cuda.current_stream().synchronize()
         res = self._result(state, out)

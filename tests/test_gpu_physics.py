@@ -245,8 +245,14 @@ def test_drop_in_advance_rejects_pageable_host_arrays():
           for k in keys}
     out = {k: torch.empty_like(st[k]) for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")}
     with pytest.raises(Exception, match="pinned"):
-        e.advance(st, out)  # refused by the binding
-    # and by the library itself, before any launch
+        e.advance(st, out)  # refused by the library, before any launch
+    # the drop-in advance then falls back to device copies
+    fns = simulate.make_neighbor_fns(setup, wc)
+    _, shift = setup.space()
+    adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
+    res, _ = adv(setup.dt, st, fns.allocate(st["r"].cuda()))
+    assert res["r"].is_cuda
+    # the raw call, as a C caller makes it
     from jaxsph_gb300 import _lib
     import ctypes
     vin, vout = _lib.SphStateView(), _lib.SphStateView()
