@@ -96,6 +96,7 @@ class WCSPH:
         self.is_free_slip = bool(is_free_slip)
         self.kahan = bool(kahan)
         self._engines = {}
+        self._step_cases = {}
 
     # ---------------------------------------------------------------- engine
     def solver_flags(self):
@@ -203,10 +204,20 @@ class WCSPH:
         """
         nl_fns = neighbors._fns
         bc_spec = getattr(bc_fn, "spec", None)
-        case = self.sph_case(nl_fns, int(state["r"].shape[0]), dt=dt, tvf=tvf, bc=bc_spec)
-        if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
-            raise NotImplementedError(
-                "si_euler needs a g_ext_fn with a GPU spec (e.g. jaxsph_gb300.cases.GExt)")
+        # the step's parameters, built once per (list, size, dt, tvf, bc)
+        key = (id(nl_fns), int(state["r"].shape[0]), float(dt), float(tvf), id(bc_spec))
+        hit = self._step_cases.get(key)
+        case = hit[0] if hit else None
+        if case is None:
+            if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
+                raise NotImplementedError(
+                    "si_euler needs a g_ext_fn with a GPU spec (e.g. jaxsph_gb300.cases.GExt)")
+            case = self.sph_case(nl_fns, key[1], dt=dt, tvf=tvf, bc=bc_spec)
+            if len(self._step_cases) > 16:
+                self._step_cases.clear()
+            # the entry holds the list functions and the bc spec, so their ids
+            # in the key cannot be reused by other objects
+            self._step_cases[key] = (case, nl_fns, bc_spec)
         st = host_state(state, self.dim, self.solver == "RIE" or self.is_free_slip)
         thr = nl_fns.threshold_sq
         ref = torch.as_tensor(neighbors.reference_position)
