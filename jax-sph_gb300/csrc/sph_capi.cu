@@ -52,7 +52,7 @@ struct SphHandle {
   float4* rref = nullptr;              // positions at the last rebuild
   int* cref_count = nullptr;           // per-step occupancy of the reference's cells
   long long ref_cells = 0;
-  unsigned* vflag = nullptr;           // a rebuild is due
+  unsigned* vflag = nullptr;           // [0] a rebuild is due, [1] sph_advance: positions changed
   unsigned long long* rebuilds_d = nullptr;  // rebuilds run inside graph replays
   long long rebuilds_h = 0;                  // rebuilds run eagerly
   int rebuild_launches = 0;                  // kernels of one rebuild
@@ -560,7 +560,7 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
           h->alloc(&h->rowoff, N + 1) | h->alloc(&h->nbr, (size_t)h->kmax * N) |
           h->alloc(&h->nbr_cnt, N) | h->alloc(&h->vl, (size_t)h->kv * N) |
           h->alloc(&h->vcnt, N) | h->alloc(&h->rref, N) | h->alloc(&h->inv, N) |
-          h->alloc(&h->cref_count, h->ref_cells + 1) | h->alloc(&h->vflag, 1) |
+          h->alloc(&h->cref_count, h->ref_cells + 1) | h->alloc(&h->vflag, 2) |
           h->alloc(&h->rebuilds_d, 1);
     long long m = h->C + 1 > N + 1 ? h->C + 1 : N + 1;
     rc |= h->alloc(&h->scan_tmp, scan_tmp_ints(m));
@@ -569,7 +569,7 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
           h->alloc(&h->case_off_d, n_cases + 1);
   }
   if (!rc) rc = cuda_check(cudaMemset(h->status, 0, sizeof(unsigned)), "memset");
-  if (!rc) rc = cuda_check(cudaMemset(h->vflag, 0, sizeof(unsigned)), "memset");
+  if (!rc) rc = cuda_check(cudaMemset(h->vflag, 0, 2 * sizeof(unsigned)), "memset");
   if (!rc) rc = cuda_check(cudaMemset(h->rebuilds_d, 0, sizeof(unsigned long long)), "memset");
   if (!rc) rc = cuda_check(cudaMemset(h->rref, 0, sizeof(float4) * N), "memset");
   if (!rc) rc = cuda_check(prepare_kernels(h->kv), "kernel attributes");
@@ -933,17 +933,39 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   LaunchCtx L = h->ctx(st);
   const Buffers& A = h->buf[0];
   const Buffers& B = h->buf[1];
-  // load into the scratch set, kick there, sort into the resident set: the
-  // rebuild needs no copy
   e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
-  launch_pack(L, *in, B, h->case_off_d);
   h->g_arr = in->g_ext;
   h->launch_count = 0;
-  launch_kick(L, B, h->R4, h->ref_cells, false, false);
-  if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, sizeof(unsigned), st);
-  launch_bin(L, B, A, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc, h->tkey,
-             h->tcell, h->scan_tmp, h->C, false, false, false, h->rref);
-  launch_verlet(L, A, h->cellid, h->start);
+  if (h->binned) {
+    // warm: the state goes to the sorted slots of the binning the handle
+    // holds; when no position differs from the one there (the caller passed
+    // back the last result) the binning and candidate lists still fit, and
+    // only the skin test decides on a rebuild -- the host reads both flags
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, 2 * sizeof(unsigned), st);
+    launch_pack(L, *in, A, h->case_off_d, h->inv, h->vflag + 1);
+    launch_kick(L, A, h->R4, h->ref_cells, false, false);
+    unsigned f[2] = {0u, 0u};
+    if (e == cudaSuccess)
+      e = cudaMemcpyAsync(f, h->vflag, sizeof(f), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, 2 * sizeof(unsigned), st);
+    if (e != cudaSuccess) return cuda_check(e, "advance flags");
+    if (f[0] || f[1]) {
+      int rc = rebuild(h, st, false, false);
+      if (rc) return rc;
+      ++h->rebuilds_h;
+    }
+  } else {
+    // cold: load into the scratch set, kick there, sort into the resident
+    // set (the rebuild needs no copy)
+    launch_pack(L, *in, B, h->case_off_d);
+    launch_kick(L, B, h->R4, h->ref_cells, false, false);
+    if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, sizeof(unsigned), st);
+    launch_bin(L, B, A, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc,
+               h->tkey, h->tcell, h->scan_tmp, h->C, false, false, false, h->rref);
+    launch_verlet(L, A, h->cellid, h->start);
+    ++h->rebuilds_h;
+  }
   launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
                  true);
   launch_unpack(L, A, h->R4, *out, true, true, ref_r, threshold_sq, h->inv);
@@ -960,9 +982,9 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     e = cudaMemcpyAsync(status_dev, h->status, sizeof(unsigned),
                         hst ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
-  h->has_state = h->binned = h->fresh = true;
+  h->has_state = h->binned = true;
+  h->fresh = false;  // the binning may predate the kick
   h->from_forward = h->pending_bc = true;
-  ++h->rebuilds_h;
   if (e != cudaSuccess) return cuda_check(e, "advance");
   return launch_status("advance");
 }

@@ -508,7 +508,11 @@ inline void mark(const LaunchCtx& L, int i) {
 }
 
 // sph_sort.cu
-void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out, const long long* case_off_dev);
+// Load a state given in original order (into a binning's sorted slots with
+// `inv`, raising `changed` when a position differs from the one there).
+void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out,
+                 const long long* case_off_dev, const int* inv = nullptr,
+                 unsigned* changed = nullptr);
 // Write the state back in original order; with `inv` (the binning's inverse
 // permutation) by original index, gathering from the sorted buffers and
 // writing coalesced.

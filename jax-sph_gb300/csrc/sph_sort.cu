@@ -31,33 +31,50 @@ __device__ __forceinline__ void st3(float* p, int dim, long long i, float x, flo
 }
 
 // ------------------------------------------------------------------ pack / unpack
+// Load a state given in original order. With `inv` (the inverse permutation
+// of the binning the buffers hold) every particle goes to its sorted slot, and
+// `changed` is raised when a position differs (bitwise) from the one already
+// there: the binning and candidate lists then still fit unless it is raised.
+// A position that did not change keeps its float64 copy (precision form).
 __global__ void k_pack(SphStateView s, int dim, Buffers o, const long long* case_off, int n_cases,
-                       unsigned* status) {
-  long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (i >= s.n) return;
-  int c = 0;
-  while (c + 1 < n_cases && i >= case_off[c + 1]) ++c;
-  int tag = s.tag[i];
-  if (tag < 0 || tag > 3) atomicOr(status, SPH_ERR_INVALID_ARG);
-  float4 r = ld4(s.r, dim, i);
-  r.w = s.mass[i];
-  float4 u = ld4(s.u, dim, i);
-  u.w = s.rho[i];
-  float4 v = ld4(s.v, dim, i);
-  v.w = s.p[i];
-  float4 a = ld4(s.dudt, dim, i);
-  a.w = s.drhodt ? s.drhodt[i] : 0.0f;
-  float4 b = ld4(s.dvdt, dim, i);
-  o.P4[i] = r;
-  o.U4[i] = u;
-  o.V4[i] = v;
-  o.A4[i] = a;
-  o.A2[i] = b;
-  o.ETA[i] = s.eta[i];
-  o.META[i] = (c << kTagBits) | (tag & kTagMask);
-  o.ORIG[i] = (int)i;
-  if (o.NW4) o.NW4[i] = s.nw ? ld4(s.nw, dim, i) : make_float4(0.f, 0.f, 0.f, 0.f);
-  if (o.RD) o.RD[i] = make_double4_32a(r.x, r.y, r.z, 0.0);
+                       unsigned* status, const int* inv, unsigned* changed) {
+  const long long i0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  bool moved = false;
+  if (i0 < s.n) {
+    const long long i = i0;
+    const long long q = inv ? inv[i] : i;
+    int c = 0;
+    while (c + 1 < n_cases && i >= case_off[c + 1]) ++c;
+    int tag = s.tag[i];
+    if (tag < 0 || tag > 3) atomicOr(status, SPH_ERR_INVALID_ARG);
+    float4 r = ld4(s.r, dim, i);
+    r.w = s.mass[i];
+    float4 u = ld4(s.u, dim, i);
+    u.w = s.rho[i];
+    float4 v = ld4(s.v, dim, i);
+    v.w = s.p[i];
+    float4 a = ld4(s.dudt, dim, i);
+    a.w = s.drhodt ? s.drhodt[i] : 0.0f;
+    float4 b = ld4(s.dvdt, dim, i);
+    if (inv) {
+      const float4 old = o.P4[q];
+      moved = __float_as_uint(old.x) != __float_as_uint(r.x) ||
+              __float_as_uint(old.y) != __float_as_uint(r.y) ||
+              (dim == 3 && __float_as_uint(old.z) != __float_as_uint(r.z));
+    }
+    o.P4[q] = r;
+    o.U4[q] = u;
+    o.V4[q] = v;
+    o.A4[q] = a;
+    o.A2[q] = b;
+    o.ETA[q] = s.eta[i];
+    o.META[q] = (c << kTagBits) | (tag & kTagMask);
+    o.ORIG[q] = (int)i;
+    if (o.NW4) o.NW4[q] = s.nw ? ld4(s.nw, dim, i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (o.RD && (!inv || moved)) o.RD[q] = make_double4_32a(r.x, r.y, r.z, 0.0);
+  }
+  if (changed && __any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0)
+    atomicOr(changed, 1u);
 }
 
 // The state a step or forward left behind: density/pressure from the density
@@ -535,8 +552,10 @@ int launch_scan(cudaStream_t st, const int* in, int* out, long long n, int* tmp)
 }
 
 void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out,
-                 const long long* case_off_dev) {
-  k_pack<<<nblocks(L.N), kBlock, 0, L.stream>>>(s, L.dim, out, case_off_dev, L.n_cases, L.status);
+                 const long long* case_off_dev, const int* inv, unsigned* changed) {
+  k_pack<<<nblocks(L.N), kBlock, 0, L.stream>>>(s, L.dim, out, case_off_dev, L.n_cases, L.status,
+                                                inv, changed);
+  count_launch(L);
 }
 
 void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateView& s,

@@ -143,7 +143,9 @@ class WCSPH:
         if e is None:
             if abs(nl_fns.r_cutoff - self._kernel_fn.cutoff) > 1e-12 * max(1.0, nl_fns.r_cutoff):
                 raise ValueError("neighbour-list cutoff differs from the kernel cutoff")
-            e = _lib.Engine(nl_fns.config(**self.solver_flags()), [case])
+            # a skin lets consecutive drop-in steps keep their candidate lists
+            # (the neighbour set of every step is exact either way)
+            e = _lib.Engine(nl_fns.config(**self.solver_flags(), verlet_skin=0.1), [case])
             self._engines = {key: e}
         elif bytes(e.cases[0]) != bytes(case):
             e.update_cases([case])
