@@ -306,6 +306,35 @@ def poiseuille(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, g_ext_magni
                    g_ext=g, bc=BC(_lib.BC_SOLID_ZERO), nw=nw, dtype=dtype, **kw)
 
 
+def couette(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, u_x_wall=1.25,
+            dtype=np.float32, t_end=0.01, dt=None, **kw):
+    """2D Couette flow (cases/cf.py, cases/cf.yaml): the Poiseuille channel
+    L=0.4, H=1 without body force, its top wall moving at u_x_wall."""
+    L, H = 0.4, 1.0
+    dxn = n_walls * dx
+    box = np.array([L, H + 2 * dxn])
+    r_f = _add(pos_init_cartesian_2d(np.array([L, H]), dx, dtype), [0.0, dxn], dtype)
+
+    def walls(ddx, nw_):  # CF._init_walls_2d (cases/cf.py:50-63)
+        hz = pos_init_cartesian_2d(np.array([L, ddx * nw_]), ddx, dtype)
+        return np.concatenate([hz, _add(hz, [0.0, H + ddx * nw_], dtype)])
+
+    r_w = walls(dx, n_walls)
+    r = np.concatenate([r_w, r_f])
+    tag = np.concatenate([np.full(len(r_w), SOLID_WALL), np.full(len(r_f), FLUID)])
+    # the top wall moves (cases/cf.py:101-104)
+    tag = np.where(r[:, 1].astype(np.float64) > box[1] - n_walls * dx, MOVING_WALL, tag)
+    v = np.zeros_like(r, dtype=np.float64)
+    nw = None
+    if kw.get("solver_name") == "RIE" or kw.get("free_slip"):
+        nw = _nws_scipy(r, tag, dx, n_walls, np.array([0.0, dxn]), walls, dtype)
+    # walls at rest, the moving wall at u_wall, no wall acceleration
+    # (cases/cf.py:156-171): the lid boundary condition
+    return _finish("cf", 2, dx, box, r, tag, v, viscosity=viscosity, u_ref=u_ref,
+                   is_bc_trick=True, t_end=t_end, dt=dt,
+                   bc=BC(_lib.BC_LID, (u_x_wall, 0.0, 0.0)), nw=nw, dtype=dtype, **kw)
+
+
 def fourier_perturbation(r, sigma=0.1, kmax=8, seed=1):
     """Divergence-free random velocity field on the periodic unit square.
 

@@ -61,6 +61,17 @@ def test_poiseuille_band_force():
     assert torch.all(g[fluid, 0] == 1000.0) and torch.all(g[~fluid, 0] == 0.0)
 
 
+def test_couette_geometry_and_wall_speed():
+    # cases/cf.py: the Poiseuille channel, top wall layers moving at 1.25
+    s = cases.couette(dx=0.0333333)
+    tag = s.state["tag"]
+    assert s.n == 432 and int((tag == 0).sum()) == 360
+    assert int((tag == 1).sum()) == 36 and int((tag == 2).sum()) == 36
+    assert torch.all(s.state["r"][tag == 2][:, 1] > s.state["r"][tag == 0][:, 1].max())
+    assert torch.all(s.state["u"][tag == 2][:, 0] == 1.25)
+    assert torch.all(s.g_ext_fn(s.state["r"]) == 0.0)
+
+
 def test_cavity_channel_batch_shapes():
     batch = cases.cavity_channel_batch(8, seed=0)
     ns = [s.n for s in batch]
@@ -75,7 +86,8 @@ def test_cavity_channel_batch_shapes():
 
 @pytest.mark.parametrize("make", [lambda: cases.dam_break(dx=0.05),
                                   lambda: cases.lid_driven_cavity(dx=0.05),
-                                  lambda: cases.poiseuille(dx=0.05)])
+                                  lambda: cases.poiseuille(dx=0.05),
+                                  lambda: cases.couette(dx=0.05)])
 def test_descriptors_match_oracle_callbacks(make):
     s = make()
     g = torch.Generator().manual_seed(0)
