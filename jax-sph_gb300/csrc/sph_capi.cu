@@ -68,9 +68,10 @@ struct SphHandle {
   int* case_max = nullptr;  // allocate: largest reference-cell occupancy per case
   int* inv = nullptr;       // sorted position of each original index (valid once binned)
   const float* g_arr = nullptr;
-  // binned: candidate lists valid for the current positions; fresh: the
-  // binning itself is of the current positions (no step since)
-  bool has_state = false, binned = false, fresh = false, from_forward = false,
+  // binned: a binning (order, cells, inverse permutation) exists; lists: the
+  // candidate lists fit the current positions; fresh: the binning itself is
+  // of the current positions (no step since)
+  bool has_state = false, binned = false, lists = false, fresh = false, from_forward = false,
        pending_bc = false;
   cudaStream_t hs = nullptr, hs2 = nullptr;  // capture streams (step, rebuild body)
   cudaGraphExec_t gexec = nullptr;           // one steady step
@@ -324,7 +325,8 @@ __global__ void k_decide(unsigned* vflag, unsigned long long* rebuilds,
 // set by cell (folding a pending forward result / bc_fn on the way, and
 // keeping the positions as the new rebuild reference), then build the
 // candidate lists. Stream-ordered and allocation-free (capturable).
-int rebuild(SphHandle* h, cudaStream_t st, bool from_forward, bool apply_bc) {
+int rebuild(SphHandle* h, cudaStream_t st, bool from_forward, bool apply_bc,
+            bool lists = true) {
   LaunchCtx L = h->ctx(st);
   const Buffers& A = h->buf[0];
   const Buffers& B = h->buf[1];
@@ -346,17 +348,18 @@ int rebuild(SphHandle* h, cudaStream_t st, bool from_forward, bool apply_bc) {
   if (e != cudaSuccess) return cuda_check(e, "rebuild copy");
   launch_bin(L, B, A, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc, h->tkey,
              h->tcell, h->scan_tmp, h->C, false, from_forward, apply_bc, h->rref);
-  launch_verlet(L, A, h->cellid, h->start);
+  if (lists) launch_verlet(L, A, h->cellid, h->start);
   return launch_status("rebuild");
 }
 
 // Re-bin the current positions without moving them (neighbour-list
 // allocate / update, a forward pass on a loaded state).
-int bin_static(SphHandle* h, cudaStream_t st) {
+int bin_static(SphHandle* h, cudaStream_t st, bool lists = true) {
   int base = h->launch_count;
-  int rc = rebuild(h, st, h->from_forward, h->pending_bc);
+  int rc = rebuild(h, st, h->from_forward, h->pending_bc, lists);
   h->launch_count = base;
   h->binned = h->fresh = true;
+  h->lists = lists;
   h->from_forward = false;
   h->pending_bc = false;
   return rc;
@@ -372,7 +375,7 @@ int step_once(SphHandle* h, cudaStream_t st) {
   mark(L, 0);
   launch_kick(L, h->buf[0], h->R4, h->ref_cells, h->from_forward, h->pending_bc);
   mark(L, 5);
-  bool rb = !h->binned;
+  bool rb = !h->lists;
   cudaError_t e = cudaSuccess;
   if (!rb) {
     unsigned v = 0;
@@ -394,14 +397,14 @@ int step_once(SphHandle* h, cudaStream_t st) {
   mark(L, 1);
   launch_forward(L, h->buf[0], h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr,
                  true, true);
-  h->binned = true;
+  h->binned = h->lists = true;
   h->fresh = rb;
   h->from_forward = true;
   h->pending_bc = true;
   return launch_status("step");
 }
 
-bool steady(const SphHandle* h) { return h->binned && h->from_forward && h->pending_bc; }
+bool steady(const SphHandle* h) { return h->lists && h->from_forward && h->pending_bc; }
 
 // Capture one steady step: kick, decide, a conditional node whose body is the
 // rebuild, forward pass. The rebuild runs on the device's own decision, so a
@@ -642,7 +645,7 @@ int sph_set_state(SphHandle* h, const SphStateView* s, void* stream) {
   launch_pack(h->ctx(st), *s, h->buf[0], h->case_off_d);
   h->g_arr = s->g_ext;
   h->has_state = true;
-  h->binned = h->fresh = h->from_forward = h->pending_bc = false;
+  h->binned = h->lists = h->fresh = h->from_forward = h->pending_bc = false;
   return launch_status("set_state");
 }
 
@@ -674,7 +677,7 @@ int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out
     c.edge_cap = LLONG_MAX;
   }
   int rc = upload_cases(h, st);
-  if (!rc) rc = bin_static(h, st);
+  if (!rc) rc = bin_static(h, st, false);  // the capacities need no candidate lists
   if (rc) return rc;
   LaunchCtx L = h->ctx(st);
   launch_row_counts(L, h->buf[0], h->cellid, h->start, h->rowcnt);
@@ -737,7 +740,7 @@ int sph_nl_edges(SphHandle* h, int32_t* idx, int64_t capacity, int64_t* count_de
   if (!h->binned) return fail((int)SPH_ERR_INVALID_ARG, "neighbour list not built");
   // the edges come from a binning of the current positions
   if (!h->fresh) {
-    int rc = bin_static(h, (cudaStream_t)stream);
+    int rc = bin_static(h, (cudaStream_t)stream, h->lists);
     if (rc) return rc;
   }
   LaunchCtx L = h->ctx((cudaStream_t)stream);
@@ -751,7 +754,7 @@ int sph_forward(SphHandle* h, void* stream) {
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   cudaStream_t st = (cudaStream_t)stream;
   int rc = 0;
-  if (!h->binned || h->from_forward) rc = bin_static(h, st);
+  if (!h->lists || h->from_forward) rc = bin_static(h, st);
   if (rc) return rc;
   launch_forward(h->ctx(st), h->buf[0], h->R4, h->R4, h->UT4, h->cellid, h->start,
                  h->edgecnt, h->g_arr, false, true);
@@ -950,7 +953,7 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, 2 * sizeof(unsigned), st);
     if (e != cudaSuccess) return cuda_check(e, "advance flags");
-    if (f[0] || f[1]) {
+    if (f[0] || f[1] || !h->lists) {
       int rc = rebuild(h, st, false, false);
       if (rc) return rc;
       ++h->rebuilds_h;
@@ -966,23 +969,44 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     launch_verlet(L, A, h->cellid, h->start);
     ++h->rebuilds_h;
   }
+  bool any_out = false;
+  for (int k = 0; k < kFields; ++k) any_out = any_out || host_dst[k];
+  // copy the result fields in [k0, k1) of `fields` back to host memory
+  ncopy = 0;
+  auto copy_back = [&](int k0, int k1) {
+    if (e == cudaSuccess) e = fork();
+    for (int k = k0; k < k1; ++k)
+      if (host_dst[k] && e == cudaSuccess)
+        e = cudaMemcpyAsync(host_dst[k], h->stage + h->stage_slot * k, fields[k].bytes,
+                            cudaMemcpyDeviceToHost, h->cs[ncopy++ % SphHandle::kCopyStreams]);
+  };
+  // r, u and v are final after the kick unless the SPH wall BC pass rewrites
+  // wall velocities: then they go back to host memory while the forward
+  // pass runs (fields 0..3 of the list: r, tag, u, v)
+  const bool early = any_out && !(h->cfg.is_bc_trick && h->cfg.solver == SPH_SOLVER_SPH);
+  if (early) {
+    SphStateView first{};
+    first.n = out->n;
+    first.r = out->r;
+    first.u = out->u;
+    first.v = out->v;
+    launch_unpack(L, A, h->R4, first, false, true, ref_r, threshold_sq, h->inv);
+    copy_back(0, 4);
+    out->r = out->u = out->v = nullptr;
+    ref_r = nullptr;
+  }
   launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
                  true);
   launch_unpack(L, A, h->R4, *out, true, true, ref_r, threshold_sq, h->inv);
-  bool any_out = false;
-  for (int k = 0; k < kFields; ++k) any_out = any_out || host_dst[k];
-  if (any_out && e == cudaSuccess) e = fork();
-  ncopy = 0;
-  for (int k = 0; k < kFields; ++k)
-    if (host_dst[k] && e == cudaSuccess)
-      e = cudaMemcpyAsync(host_dst[k], h->stage + h->stage_slot * k, fields[k].bytes,
-                          cudaMemcpyDeviceToHost, h->cs[ncopy++ % SphHandle::kCopyStreams]);
-  if (any_out && e == cudaSuccess) e = join();
+  if (any_out) {
+    copy_back(early ? 4 : 0, kFields);
+    if (e == cudaSuccess) e = join();
+  }
   if (e == cudaSuccess)
     e = cudaMemcpyAsync(status_dev, h->status, sizeof(unsigned),
                         hst ? cudaMemcpyDeviceToHost : cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess) e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
-  h->has_state = h->binned = true;
+  h->has_state = h->binned = h->lists = true;
   h->fresh = false;  // the binning may predate the kick
   h->from_forward = h->pending_bc = true;
   if (e != cudaSuccess) return cuda_check(e, "advance");

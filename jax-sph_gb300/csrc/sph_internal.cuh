@@ -388,17 +388,6 @@ __device__ __forceinline__ int ref_cell_hash(const float4& r, const CaseDev& c) 
   return h;
 }
 
-// Every candidate sender (untrimmed walk), one at a time.
-template <int DIM, typename F>
-__device__ __forceinline__ void for_each_candidate(const CaseDev& c, int cell_local,
-                                                   const int* __restrict__ start, F&& f) {
-  walk_rows<DIM, false>(c, cell_local, make_float4(0.f, 0.f, 0.f, 0.f), start, c.rad, 0.f,
-                        [&](int j0, int j1, float3) {
-                          for (int j = j0; j < j1; ++j) f(j);
-                        });
-}
-
-
 // The reference metric, out of line: only candidates in the narrow band
 // around the cutoff (or every candidate of a case without the fast test)
 // reach it, so the hot loop stays small.

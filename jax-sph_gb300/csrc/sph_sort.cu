@@ -25,6 +25,7 @@ __device__ __forceinline__ float4 ld4(const float* p, int dim, long long i) {
   return r;
 }
 __device__ __forceinline__ void st3(float* p, int dim, long long i, float x, float y, float z) {
+  if (!p) return;  // a field the caller does not read back
   p[i * dim] = x;
   p[i * dim + 1] = y;
   if (dim == 3) p[i * dim + 2] = z;
@@ -132,8 +133,8 @@ __global__ void k_unpack(SphStateView s, int dim, Buffers b, const float4* R4,
     st3(s.dudt, dim, o, a.x, a.y, a.z);
     st3(s.dvdt, dim, o, a2.x, a2.y, a2.z);
     if (s.drhodt) s.drhodt[o] = a.w;
-    s.rho[o] = f.rho;
-    s.p[o] = f.p;
+    if (s.rho) s.rho[o] = f.rho;
+    if (s.p) s.p[o] = f.p;
     if (ref) {
       const float4 r0 = make_float4(ref[o * dim], ref[o * dim + 1],
                                     dim == 3 ? ref[o * dim + 2] : 0.f, 0.f);
@@ -420,8 +421,38 @@ __global__ void k_tile_scan(const int* in, long long n, int* out, const int* til
 }
 
 // ------------------------------------------------------------------ edges
-// Per-sender edge count: edge (receiver c, sender s) iff
-// metric(r[s], r[c]) < cutoff_sq (jax_md/partition.py:885-909).
+// The receivers c of sender s, i.e. the edges (c, s) with
+// metric(r[s], r[c]) < cutoff_sq (jax_md/partition.py:885-909): the walk of
+// the sender's cells (rows trimmed in fast cases) with the band test of the
+// passes -- the shifted squared distance decides outside the band, the
+// reference metric inside it (every candidate without the fast test).
+template <int DIM, typename F>
+__device__ __forceinline__ void for_each_receiver(const CaseDev& c, const CaseDev* cp, int cell,
+                                                  const float4& rs, long long s, int mask_self,
+                                                  const int* start, const float4* P4, F&& f) {
+  auto visit = [&](int j0, int j1, float3 sh) {
+    const float qx = rs.x - sh.x, qy = rs.y - sh.y, qz = rs.z - sh.z;
+    for (int j = j0; j < j1; ++j) {
+      if (mask_self && j == s) continue;
+      const float4 rc = P4[j];
+      bool e;
+      if (c.fast) {
+        const float dx = qx - rc.x, dy = qy - rc.y, dz = (DIM == 3) ? qz - rc.z : 0.f;
+        const float d2 = dx * dx + dy * dy + dz * dz;
+        e = d2 < c.cut_lo || (d2 < c.cut_hi && exact_edge<DIM>(rc, rs, cp));
+      } else {
+        e = is_edge<DIM>(rc, rs, c);
+      }
+      if (e) f(j);
+    }
+  };
+  if (c.fast)
+    walk_rows<DIM, true>(c, cell, rs, start, c.rad, c.trim_r2, visit);
+  else
+    walk_rows<DIM, false>(c, cell, rs, start, c.rad, 0.f, visit);
+}
+
+// Per-sender edge count.
 template <int DIM>
 __global__ void k_row_counts(long long N, Buffers b, const CaseDev* cases, const int* cellid,
                              const int* start, int mask_self, int* rowcnt) {
@@ -431,11 +462,8 @@ __global__ void k_row_counts(long long N, Buffers b, const CaseDev* cases, const
   const CaseDev& c = cases[case_of(meta)];
   float4 rs = b.P4[s];
   int cnt = 0;
-  for_each_candidate<DIM>(c, cellid[s] - c.cell_off, start, [&](int j) {
-    if (mask_self && j == s) return;
-    float4 rc = b.P4[j];
-    cnt += is_edge<DIM>(rc, rs, c);
-  });
+  for_each_receiver<DIM>(c, cases + case_of(meta), cellid[s] - c.cell_off, rs, s, mask_self,
+                         start, b.P4, [&](int) { ++cnt; });
   rowcnt[b.ORIG[s]] = cnt;
 }
 
@@ -451,17 +479,14 @@ __global__ void k_emit(long long N, Buffers b, const CaseDev* cases, const int* 
   int sender = b.ORIG[s];
   long long off = rowoff[sender];
   long long k = off;
-  for_each_candidate<DIM>(c, cellid[s] - c.cell_off, start, [&](int j) {
-    if (mask_self && j == s) return;
-    float4 rc = b.P4[j];
-    if (is_edge<DIM>(rc, rs, c)) {
-      if (k < capacity) {
-        idx[k] = b.ORIG[j];
-        idx[capacity + k] = sender;
-      }
-      ++k;
-    }
-  });
+  for_each_receiver<DIM>(c, cases + case_of(meta), cellid[s] - c.cell_off, rs, s, mask_self,
+                         start, b.P4, [&](int j) {
+                           if (k < capacity) {
+                             idx[k] = b.ORIG[j];
+                             idx[capacity + k] = sender;
+                           }
+                           ++k;
+                         });
   // receivers ascending per sender (insertion sort of the owned segment)
   long long end = k < capacity ? k : capacity;
   for (long long x = off + 1; x < end; ++x) {

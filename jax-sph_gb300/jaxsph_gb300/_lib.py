@@ -262,17 +262,28 @@ class Engine:
         _check(self.lib.sph_read_status(self.h, ctypes.byref(s), int(bool(clear)), _stream()))
         return int(s.value)
 
-    def advance(self, state, out, ref=None, threshold_sq=0.0):
+    def advance(self, state, out, ref=None, threshold_sq=0.0, vin=None):
         """One fused drop-in step (load, step, read back); returns the status
-        word as a 0-d int32 device tensor (no host synchronisation)."""
-        vin = self.view(state, self.n, pinned_ok=True)
+        word as a 0-d int32 device tensor (no host synchronisation). ``vin``:
+        a view of ``state`` already built (see ``next_view``)."""
+        vin = vin if vin is not None else self.view(state, self.n, pinned_ok=True)
         vout = self.view(out, self.n, pinned_ok=True)
+        self._views = (vin, vout)
         status = torch.empty((), dtype=torch.int32, device="cuda")
         self._keep = state
         _check(self.lib.sph_advance(self.h, ctypes.byref(vin), ctypes.byref(vout),
                                     _ptr(ref) if ref is not None else None,
                                     float(threshold_sq), _ptr(status), _stream()))
         return status
+
+    def next_view(self):
+        """The input view of a state made of the last advance's outputs and its
+        inputs' other fields (tag, mass, eta, nw, g_ext)."""
+        vin, vout = self._views
+        v = SphStateView.from_buffer_copy(vin)
+        for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p"):
+            setattr(v, k, getattr(vout, k))
+        return v
 
     def rebuild_stats(self):
         """(candidate-list rebuilds so far, kernels per rebuild); synchronises."""

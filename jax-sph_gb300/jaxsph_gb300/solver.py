@@ -97,6 +97,7 @@ class WCSPH:
         self.kahan = bool(kahan)
         self._engines = {}
         self._step_cases = {}
+        self._last_host = None
 
     # ---------------------------------------------------------------- engine
     def solver_flags(self):
@@ -220,7 +221,16 @@ class WCSPH:
             # the entry holds the list functions and the bc spec, so their ids
             # in the key cannot be reused by other objects
             self._step_cases[key] = (case, nl_fns, bc_spec)
-        st = host_state(state, self.dim, self.solver == "RIE" or self.is_free_slip)
+        # the state returned by the last host-buffer step, passed back as it was:
+        # its fields are known to be valid and its view is already built
+        last = self._last_host
+        vin = None
+        if (last is not None and last[0] is state and last[3] is self.engine(nl_fns, case)
+                and all(state.get(k) is t for k, t in last[1].items())):
+            st, vin = last[1], last[2]
+        else:
+            st = host_state(state, self.dim, self.solver == "RIE" or self.is_free_slip)
+        self._last_host = None
         thr = nl_fns.threshold_sq
         ref = torch.as_tensor(neighbors.reference_position)
         status = None
@@ -234,7 +244,7 @@ class WCSPH:
             if thr > 0.0 and not (ref.device.type == "cpu" and ref.is_pinned()):
                 ref = ref.to(torch.float32).contiguous().pin_memory()
             try:
-                status = e.advance(st, out, ref if thr > 0.0 else None, thr)
+                status = e.advance(st, out, ref if thr > 0.0 else None, thr, vin=vin)
             except _lib.SphError as err:
                 if "pinned" not in str(err):
                     raise
@@ -251,6 +261,9 @@ class WCSPH:
         if host:
             torch.cuda.current_stream().synchronize()
         res = self._result(state, out)
+        if host:
+            fields = {k: res[k] for k in STATE_KEYS if res.get(k) is not None}
+            self._last_host = (res, fields, e.next_view(), e)
         if bc_fn is not None and bc_spec is None:
             res = bc_fn(res)
         from .partition import NeighborList
