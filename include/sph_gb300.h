@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPH_ABI_VERSION 2
+#define SPH_ABI_VERSION 3
 
 /* Reference PartitionErrorCode bits (jax_sph/jax_md/partition.py:453-457). */
 #define SPH_NEIGHBOR_LIST_OVERFLOW 0x1u
@@ -55,7 +55,9 @@ extern "C" {
 #define SPH_INFO_MOVED 0x2000u
 
 enum { SPH_KERNEL_QSK = 0, SPH_KERNEL_WC2K = 1 };   /* jax_sph/kernel.py:51-103 */
-enum { SPH_SOLVER_SPH = 0, SPH_SOLVER_RIE = 1 };    /* jax_sph/solver.py:676-694 */
+/* jax_sph/solver.py:676-694; DELTA: the standard SPH acceleration plus the
+ * delta-SPH diffusive term (solver.py:259-313), with summation density */
+enum { SPH_SOLVER_SPH = 0, SPH_SOLVER_RIE = 1, SPH_SOLVER_DELTA = 2 };
 enum { SPH_EOS_TAIT = 0, SPH_EOS_RIEMANN = 1 };     /* jax_sph/eos.py:20-57 */
 
 /* External acceleration g_ext_fn(r) of the cases on the path. */
@@ -119,6 +121,8 @@ typedef struct SphCase {
   double g[3];            /* SPH_GEXT_CONST / BAND_X magnitude vector */
   double g_band_lo, g_band_hi;
   double u_lid[3];
+  double diff_alpha;      /* delta-SPH acceleration diffusion (DELTA solver) */
+  double diff_delta;      /* delta-SPH density diffusion (not on the GPU path) */
 } SphCase;
 
 /* Caller-owned device arrays in the reference state-dict layout

@@ -284,6 +284,9 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
   c.av_hab = (float)in.dx;
   c.av_cab = 10.0f;
   c.av_eps = (float)(0.01 * in.dx * in.dx);
+  // acceleration_delta_fn_wrapper(kernel, alpha, support = h, c_ref, rho_ref)
+  // (solver.py:259-313, :682-689)
+  c.delta_coef = (float)(in.diff_alpha * in.h * in.c_ref * in.rho_ref);
   c.g_kind = in.g_kind;
   for (int d = 0; d < 3; ++d) {
     c.g[d] = (float)in.g[d];
@@ -493,8 +496,12 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
     return fail((int)SPH_ERR_INVALID_ARG, "Cell list spatial dimension must be 2 or 3");
   if (cfg->kernel != SPH_KERNEL_QSK && cfg->kernel != SPH_KERNEL_WC2K)
     return fail((int)SPH_ERR_INVALID_ARG, "kernel must be QSK or WC2K");
-  if (cfg->solver != SPH_SOLVER_SPH && cfg->solver != SPH_SOLVER_RIE)
-    return fail((int)SPH_ERR_INVALID_ARG, "solver must be SPH or RIE");
+  if (cfg->solver != SPH_SOLVER_SPH && cfg->solver != SPH_SOLVER_RIE &&
+      cfg->solver != SPH_SOLVER_DELTA)
+    return fail((int)SPH_ERR_INVALID_ARG, "solver must be SPH, RIE or DELTA");
+  if (cfg->solver == SPH_SOLVER_DELTA && cfg->is_rho_evol)
+    return fail((int)SPH_ERR_INVALID_ARG,
+                "DELTA with density evolution (rho_evol_fn_delta) is not on the GPU path");
   if (n_cases >= (1 << 26)) return fail((int)SPH_ERR_INVALID_ARG, "too many cases");
   if (!(cfg->verlet_skin >= 0.0 && cfg->verlet_skin <= 0.5))
     return fail((int)SPH_ERR_INVALID_ARG, "verlet_skin must lie in [0, 0.5]");
@@ -980,10 +987,10 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
         e = cudaMemcpyAsync(host_dst[k], h->stage + h->stage_slot * k, fields[k].bytes,
                             cudaMemcpyDeviceToHost, h->cs[ncopy++ % SphHandle::kCopyStreams]);
   };
-  // r, u and v are final after the kick unless the SPH wall BC pass rewrites
-  // wall velocities: then they go back to host memory while the forward
-  // pass runs (fields 0..3 of the list: r, tag, u, v)
-  const bool early = any_out && !(h->cfg.is_bc_trick && h->cfg.solver == SPH_SOLVER_SPH);
+  // r, u and v are final after the kick unless the wall BC pass of the SPH
+  // and DELTA solvers rewrites wall velocities: then they go back to host
+  // memory while the forward pass runs (fields 0..3 of the list: r, tag, u, v)
+  const bool early = any_out && !(h->cfg.is_bc_trick && h->cfg.solver != SPH_SOLVER_RIE);
   if (early) {
     SphStateView first{};
     first.n = out->n;

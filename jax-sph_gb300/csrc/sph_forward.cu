@@ -466,7 +466,8 @@ k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const in
 }
 
 // ------------------------------------------------------------------ force pass
-// SOLVER 0: standard SPH with transport-velocity stress; 1: Riemann SPH.
+// SOLVER 0: standard SPH with transport-velocity stress; 1: Riemann SPH;
+// 2: delta-SPH (standard plus the diffusive term).
 // The per-pair quotients use the fast division intrinsic (at most 2 ulp, for
 // denominators far inside its range): the correctly rounded division is a
 // multi-instruction sequence that cost a quarter of this pass, and the
@@ -509,9 +510,9 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
     const float3 uj = f3(Uj4);
     const float eta_ij = __fdividef(2.f * eta_i * eta_j, eta_i + eta_j + kEps);
     int tj = FLUID;
-    if (SOLVER == 1 || av) tj = tag_of(b.META[j]);
+    if (SOLVER != 0 || av) tj = tag_of(b.META[j]);
     float3 a;
-    if (SOLVER == 0) {
+    if (SOLVER != 1) {
       const float3 vj = f3(Vj4);
       const float p_ij = __fdividef(rho_j * p_i + rho_i * p_j, rho_i + rho_j);
       const float ki = dot3(wi, dr);
@@ -522,6 +523,16 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
       a = make_float3(cc * (-p_ij * dr.x + Ar.x + eta_ij * (ui.x - uj.x)),
                       cc * (-p_ij * dr.y + Ar.y + eta_ij * (ui.y - uj.y)),
                       cc * (-p_ij * dr.z + Ar.z + eta_ij * (ui.z - uj.z)));
+      if (SOLVER == 2 && tj == FLUID) {
+        // delta-SPH diffusion (solver.py:293-309): V_j pi_ij W'(d) e_ij
+        // alpha h c_ref rho_ref / rho_i, pi_ij = (u_j - u_i).(-r_ij) / (d + eps)^2
+        const float pi_ij = ((uj.x - ui.x) * -dr.x + (uj.y - ui.y) * -dr.y +
+                             (uj.z - ui.z) * -dr.z) * inv_d * inv_d;
+        const float k = Vj * pi_ij * gw * inv_d * __fdividef(c.delta_coef, rho_i);
+        a.x += k * dr.x;
+        a.y += k * dr.y;
+        a.z += k * dr.z;
+      }
     } else {
       const float3 e = make_float3(dr.x * inv_d, dr.y * inv_d, dr.z * inv_d);
       const float3 kg = make_float3(gw * e.x, gw * e.y, gw * e.z);
@@ -657,6 +668,10 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
     k_force<DIM, KER, 1, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
                                                         L.bc_trick, L.free_slip, g_arr, R4, UT4,
                                                         nl, apply_bc, L.status);
+  else if (L.solver == SPH_SOLVER_DELTA)
+    k_force<DIM, KER, 2, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
+                                                        L.bc_trick, L.free_slip, g_arr, R4,
+                                                        nullptr, nl, apply_bc, L.status);
   else
     k_force<DIM, KER, 0, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
                                                         L.bc_trick, L.free_slip, g_arr, R4,

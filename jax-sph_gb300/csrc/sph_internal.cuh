@@ -72,6 +72,7 @@ struct CaseDev {
   float p_bg_tvf;     // eos.p_fn(0)
   float c_ref, eta_limiter;
   float av_alpha, av_hab, av_cab, av_eps;
+  float delta_coef;   // diff_alpha * h * c_ref * rho_ref (DELTA diffusive acceleration)
   int g_kind;
   float g[3], g_lo, g_hi;
   int bc_kind;

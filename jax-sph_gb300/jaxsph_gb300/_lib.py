@@ -25,7 +25,7 @@ INFO_MOVED = 0x2000
 WARN_BOX_EDGE = 0x1000
 
 KERNELS = {"QSK": 0, "WC2K": 1}
-SOLVERS = {"SPH": 0, "RIE": 1}
+SOLVERS = {"SPH": 0, "RIE": 1, "DELTA": 2}
 EOS_TAIT, EOS_RIEMANN = 0, 1
 GEXT_ZERO, GEXT_CONST, GEXT_BAND_X, GEXT_ARRAY = 0, 1, 2, 3
 BC_NONE, BC_SOLID_ZERO, BC_SOLID_ZERO_P, BC_LID = 0, 1, 2, 3
@@ -51,7 +51,8 @@ class SphCase(ctypes.Structure):
                 ("u_ref", ctypes.c_double), ("eta_limiter", ctypes.c_double),
                 ("artificial_alpha", ctypes.c_double), ("g", ctypes.c_double * 3),
                 ("g_band_lo", ctypes.c_double), ("g_band_hi", ctypes.c_double),
-                ("u_lid", ctypes.c_double * 3)]
+                ("u_lid", ctypes.c_double * 3), ("diff_alpha", ctypes.c_double),
+                ("diff_delta", ctypes.c_double)]
 
 
 class SphStateView(ctypes.Structure):
@@ -117,7 +118,7 @@ def load(build_if_missing=True):
     for name in EXPORTS:
         if name not in ("sph_abi_version", "sph_last_error"):
             getattr(lib, name).restype = I
-    if lib.sph_abi_version() != 2:
+    if lib.sph_abi_version() != 3:
         raise RuntimeError("libsph_gb300 ABI version mismatch")
     _LIB = lib
     return lib

@@ -145,7 +145,8 @@ def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref
             c_ref_factor=10.0, gamma=1.0, p_bg_factor=0.0, g_ext_magnitude=0.0, cfl=0.25,
             dt=None, t_end=1.0, solver_name="SPH", kernel="QSK", h_fac=1.0, tvf=0.0,
             is_bc_trick=False, density_evolution=False, artificial_alpha=0.0,
-            free_slip=False, eta_limiter=3, g_ext=None, bc=None, nw=None, dtype=np.float32):
+            free_slip=False, eta_limiter=3, g_ext=None, bc=None, nw=None, dtype=np.float32,
+            diff_alpha=0.01, diff_delta=0.1):
     """The common part of ``initialize`` (case_setup.py:71-231)."""
     c_ref = c_ref_factor * u_ref
     p_ref = rho_ref * c_ref ** 2 / gamma
@@ -184,7 +185,8 @@ def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref
     state = bc(state)  # case_setup.py:203
     solver = dict(solver=solver_name, kernel=kernel, h_fac=h_fac, is_bc_trick=is_bc_trick,
                   is_rho_evol=density_evolution, artificial_alpha=artificial_alpha,
-                  is_free_slip=free_slip, eta_limiter=eta_limiter)
+                  is_free_slip=free_slip, eta_limiter=eta_limiter,
+                  diff_alpha=diff_alpha, diff_delta=diff_delta)  # defaults.py:96-99
     return CaseSetup(name, dim, dx, np.asarray(box, dtype=np.float64), state, dt,
                      sequence_length, c_ref, p_ref, p_bg, u_ref, viscosity, eos, g_ext, bc,
                      solver, tvf)

@@ -79,9 +79,9 @@ class _SlabEngines:
         self.device = torch.device(device)
         self.cutoff = float(self.solver._kernel_fn.cutoff)
         # cutoff levels a particle's step reaches: force <- neighbour density
-        # <- its neighbours; the SPH wall BC adds wall pressure <- fluid
-        # pressure (solver.py:431-530)
-        self.levels = 3 if (self.solver.solver == "SPH" and self.solver.is_bc_trick) else 2
+        # <- its neighbours; the wall BC of SPH and DELTA adds wall pressure
+        # <- fluid pressure (solver.py:431-530)
+        self.levels = 3 if (self.solver.solver != "RIE" and self.solver.is_bc_trick) else 2
         self.cv = float(setup.tvf) * 0.5 * float(setup.dt)
         self._engines = {}
         if self.solver.g_spec()["kind"] == _lib.GEXT_ARRAY:

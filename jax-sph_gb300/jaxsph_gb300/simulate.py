@@ -28,7 +28,8 @@ def make_solver(setup, kahan=False):
     disp, _ = setup.space()
     s = setup.solver
     return WCSPH(disp, setup.eos, setup.g_ext_fn, setup.dx, setup.dim, setup.dt, setup.c_ref,
-                 eta_limiter=s.get("eta_limiter", 3), solver=s["solver"], kernel=s["kernel"],
+                 eta_limiter=s.get("eta_limiter", 3), diff_delta=s.get("diff_delta", 0.1),
+                 diff_alpha=s.get("diff_alpha", 0.01), solver=s["solver"], kernel=s["kernel"],
                  h_fac=s.get("h_fac", 1.0), is_bc_trick=s["is_bc_trick"],
                  is_rho_evol=s["is_rho_evol"], artificial_alpha=s["artificial_alpha"],
                  is_free_slip=s["is_free_slip"], kahan=kahan)

@@ -79,7 +79,10 @@ class WCSPH:
                  kahan=False):
         if solver not in _lib.SOLVERS:
             raise NotImplementedError(
-                f"solver {solver!r}: the GPU hot path implements SPH and RIE")
+                f"solver {solver!r}: the GPU hot path implements SPH, RIE and DELTA")
+        if solver == "DELTA" and is_rho_evol:
+            raise NotImplementedError(
+                "DELTA with density evolution (rho_evol_fn_delta) is not on the GPU path")
         if is_rho_renorm or is_heat_conduction:
             raise NotImplementedError("density renormalisation and heat conduction are not on the path")
         self.displacement_fn = displacement_fn
@@ -87,6 +90,7 @@ class WCSPH:
         self.g_ext_fn = g_ext_fn
         self.dx, self.dim, self.dt, self.c_ref = float(dx), int(dim), float(dt), float(c_ref)
         self.eta_limiter = float(eta_limiter)
+        self.diff_delta, self.diff_alpha = float(diff_delta), float(diff_alpha)
         self.solver = solver
         self.kernel = kernel
         self._kernel_fn = make_kernel(kernel, h_fac * dx, dim)
@@ -127,6 +131,8 @@ class WCSPH:
         s.u_ref = float(self.eos.u_ref)
         s.eta_limiter = self.eta_limiter
         s.artificial_alpha = self.artificial_alpha
+        s.diff_alpha = self.diff_alpha
+        s.diff_delta = self.diff_delta
         g = self.g_spec()
         s.g_kind = g["kind"]
         for d in range(3):

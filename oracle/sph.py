@@ -123,16 +123,20 @@ def dot(a, b):
 
 # ---------------------------------------------------------------- solver
 class WCSPH:
-    """``WCSPH`` (solver.py:613-951) for the SPH and RIE solvers.
+    """``WCSPH`` (solver.py:613-951) for the SPH, RIE and DELTA solvers
+    (DELTA with density summation).
 
     ``g_ext_fn(r)`` returns the external acceleration per particle (torch).
     """
 
     def __init__(self, box, eos, g_ext_fn, dx, dim, dt, c_ref, eta_limiter=3,
                  solver="SPH", kernel="QSK", h_fac=1.0, is_bc_trick=False,
-                 is_rho_evol=False, artificial_alpha=0.0, is_free_slip=False):
-        if solver not in ("SPH", "RIE"):
+                 is_rho_evol=False, artificial_alpha=0.0, is_free_slip=False,
+                 diff_alpha=0.1):
+        if solver not in ("SPH", "RIE", "DELTA"):
             raise NotImplementedError(f"solver {solver} is outside the hot-path scope")
+        if solver == "DELTA" and is_rho_evol:
+            raise NotImplementedError("rho_evol_fn_delta is outside the hot-path scope")
         self.box = box
         self.eos = eos
         self.g_ext_fn = g_ext_fn
@@ -144,6 +148,9 @@ class WCSPH:
         self.is_rho_evol = is_rho_evol
         self.artificial_alpha = artificial_alpha
         self.is_free_slip = is_free_slip
+        # acceleration_delta_fn_wrapper(kernel, alpha, support=h_fac*dx, c_ref,
+        # rho_ref) (solver.py:684-690)
+        self.delta_coef = diff_alpha * h_fac * dx * c_ref * eos.rho_ref
 
     # limiter_fn_wrapper (solver.py:574-588)
     def beta_fn(self, u_L, u_R):
@@ -208,7 +215,7 @@ class WCSPH:
         p = self.eos.p_fn(rho)                                            # :801
         p_bg_tvf = self.eos.p_fn(torch.zeros_like(p))                     # :802
 
-        if self.is_bc_trick and self.solver == "SPH":
+        if self.is_bc_trick and self.solver in ("SPH", "DELTA"):          # :796
             p, rho, u, v = self._gwbc(rho, tag, u, v, p, g_ext, i_s, j_s, w_dist,
                                       dr_i_j, nw, N)
             mask = None
@@ -217,10 +224,13 @@ class WCSPH:
         elif self.solver == "RIE":
             mask = torch.ones_like(i_s, dtype=dtype)
 
-        if self.solver == "SPH":
+        if self.solver in ("SPH", "DELTA"):
             out = self._acc_standard(dr_i_j, dist, rho[i_s], rho[j_s], u[i_s], u[j_s],
                                      v[i_s], v[j_s], mass[i_s], mass[j_s], eta[i_s],
                                      eta[j_s], p[i_s], p[j_s], gw)
+            if self.solver == "DELTA":
+                out = out + self._acc_delta_diff(dr_i_j, dist, rho[i_s], rho[j_s], u[i_s],
+                                                 u[j_s], mass[j_s], gw, fluid_mask[j_s])
         else:
             out = self._acc_riemann(e_s, dr_i_j, dist, rho[i_s], rho[j_s], mass[j_s],
                                     mass[i_s], u[i_s], u[j_s], p[i_s], p[j_s],
@@ -273,6 +283,14 @@ class WCSPH:
                      + (rho_j[:, None] * u_j) * dot(v_j - u_j, r_ij)[:, None])
         u_ij = u_i - u_j
         return c[:, None] * (-p_ij[:, None] * r_ij + A_r + eta_ij[:, None] * u_ij)
+
+    # the diffusive term of acceleration_delta_fn (:293-309)
+    def _acc_delta_diff(self, r_ij, d_ij, rho_i, rho_j, u_i, u_j, m_j, gw, fluid_j):
+        e_ij = r_ij / (d_ij[:, None] + EPS)
+        V_j = m_j / rho_j
+        pi_ij = dot(u_j - u_i, -r_ij) / (d_ij + EPS) ** 2
+        k = V_j * pi_ij * gw * self.delta_coef / rho_i * fluid_j
+        return k[:, None] * e_ij
 
     # acceleration_riemann_fn (:316-401)
     def _acc_riemann(self, e_ij, r_ij, d_ij, rho_i, rho_j, m_j, m_i, u_i, u_j, p_i, p_j,

@@ -28,7 +28,8 @@ def u_series_couette(y, t, n_max=10):
     return res
 
 
-@pytest.mark.parametrize("tvf,solver", [(0.0, "SPH"), (1.0, "SPH"), (0.0, "RIE")])
+@pytest.mark.parametrize("tvf,solver", [(0.0, "SPH"), (1.0, "SPH"), (0.0, "RIE"),
+                                        (0.0, "DELTA")])
 def test_couette_matches_series(tvf, solver):
     import torch
 

@@ -38,6 +38,11 @@ def small_cases():
         "pf_sph_evol": lambda: cases.poiseuille(dx=0.05, density_evolution=True),
         "ldc_sph_freeslip_av": lambda: cases.lid_driven_cavity(dx=0.04, free_slip=True,
                                                                artificial_alpha=0.1),
+        # delta-SPH: the reference runs it with density summation (pf.yaml, cf.yaml)
+        "tgv2d_delta": lambda: cases.tgv(dim=2, dx=0.02, solver_name="DELTA", diff_alpha=0.5),
+        "pf_delta": lambda: cases.poiseuille(dx=0.05, solver_name="DELTA"),
+        "ldc_delta_tvf": lambda: cases.lid_driven_cavity(dx=0.04, tvf=1.0,
+                                                         solver_name="DELTA"),
     }
 
 

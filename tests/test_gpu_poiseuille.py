@@ -50,7 +50,8 @@ def interpolate_u(st, dx, box, targets):
     return ((wt * u[:, 0][None, :]).sum(1) / wt.sum(1)).numpy()
 
 
-@pytest.mark.parametrize("tvf,solver", [(0.0, "SPH"), (1.0, "SPH"), (0.0, "RIE")])
+@pytest.mark.parametrize("tvf,solver", [(0.0, "SPH"), (1.0, "SPH"), (0.0, "RIE"),
+                                        (0.0, "DELTA")])
 def test_poiseuille_matches_series(tvf, solver):
     dx, dt = 0.0333333, 0.000002
     setup = cases.poiseuille(dx=dx, dt=dt, t_end=0.005, tvf=tvf, solver_name=solver)
