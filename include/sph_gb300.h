@@ -56,7 +56,8 @@ extern "C" {
 
 enum { SPH_KERNEL_QSK = 0, SPH_KERNEL_WC2K = 1 };   /* jax_sph/kernel.py:51-103 */
 /* jax_sph/solver.py:676-694; DELTA: the standard SPH acceleration plus the
- * delta-SPH diffusive term (solver.py:259-313), with summation density */
+ * delta-SPH diffusive term (solver.py:259-313), with summation density or the
+ * delta-SPH density evolution (solver.py:33-105) */
 enum { SPH_SOLVER_SPH = 0, SPH_SOLVER_RIE = 1, SPH_SOLVER_DELTA = 2 };
 enum { SPH_EOS_TAIT = 0, SPH_EOS_RIEMANN = 1 };     /* jax_sph/eos.py:20-57 */
 
@@ -97,7 +98,8 @@ typedef struct SphConfig {
                               do not depend on the skin, the batching or when the
                               candidates were rebuilt (slower rebuilds and gathers);
                               0 sums in cell order, deterministic for a given run */
-  int32_t pad1;
+  int32_t is_rho_renorm;  /* density renormalisation after density evolution
+                             (rho_renorm_fn, solver.py:167-173, :755-793) */
 } SphConfig;
 
 /* Per-case parameters (all in the reference's units). */
@@ -122,7 +124,7 @@ typedef struct SphCase {
   double g_band_lo, g_band_hi;
   double u_lid[3];
   double diff_alpha;      /* delta-SPH acceleration diffusion (DELTA solver) */
-  double diff_delta;      /* delta-SPH density diffusion (not on the GPU path) */
+  double diff_delta;      /* delta-SPH density diffusion (DELTA, density evolution) */
 } SphCase;
 
 /* Caller-owned device arrays in the reference state-dict layout

@@ -41,6 +41,8 @@ struct SphHandle {
   Buffers buf[2]{};
   float4* R4 = nullptr;
   float4* UT4 = nullptr;
+  float4* R4e = nullptr;   // evolved density before renormalisation
+  float4* dscr = nullptr;  // delta-SPH density scratch (5 planes of N)
   int* cellid = nullptr;
   int *count = nullptr, *start = nullptr, *keyc = nullptr, *keys = nullptr;
   int *tsrc = nullptr, *tkey = nullptr, *tcell = nullptr, *scan_tmp = nullptr;
@@ -123,6 +125,9 @@ struct SphHandle {
     L.vflag = vflag;
     L.canonical = cfg.canonical_order;
     L.inv = inv;
+    L.rho_renorm = cfg.is_rho_renorm;
+    L.R4e = R4e;
+    L.dscr = dscr;
     L.block = block;
     L.launches = const_cast<int*>(&launch_count);
     L.ev = ev;
@@ -287,6 +292,8 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
   // acceleration_delta_fn_wrapper(kernel, alpha, support = h, c_ref, rho_ref)
   // (solver.py:259-313, :682-689)
   c.delta_coef = (float)(in.diff_alpha * in.h * in.c_ref * in.rho_ref);
+  // rho_evol_fn_delta_wrapper(delta, support = h, c_ref) (solver.py:33-105, :693)
+  c.delta_rho_coef = (float)(in.c_ref * in.diff_delta * in.h);
   c.g_kind = in.g_kind;
   for (int d = 0; d < 3; ++d) {
     c.g[d] = (float)in.g[d];
@@ -499,9 +506,6 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
   if (cfg->solver != SPH_SOLVER_SPH && cfg->solver != SPH_SOLVER_RIE &&
       cfg->solver != SPH_SOLVER_DELTA)
     return fail((int)SPH_ERR_INVALID_ARG, "solver must be SPH, RIE or DELTA");
-  if (cfg->solver == SPH_SOLVER_DELTA && cfg->is_rho_evol)
-    return fail((int)SPH_ERR_INVALID_ARG,
-                "DELTA with density evolution (rho_evol_fn_delta) is not on the GPU path");
   if (n_cases >= (1 << 26)) return fail((int)SPH_ERR_INVALID_ARG, "too many cases");
   if (!(cfg->verlet_skin >= 0.0 && cfg->verlet_skin <= 0.5))
     return fail((int)SPH_ERR_INVALID_ARG, "verlet_skin must lie in [0, 0.5]");
@@ -564,6 +568,9 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
   if (!rc) {
     rc |= h->alloc(&h->R4, N) | h->alloc(&h->cellid, N);
     if (cfg->solver == SPH_SOLVER_RIE) rc |= h->alloc(&h->UT4, N);
+    if (cfg->is_rho_evol && cfg->is_rho_renorm) rc |= h->alloc(&h->R4e, N);
+    if (cfg->is_rho_evol && cfg->solver == SPH_SOLVER_DELTA)
+      rc |= h->alloc(&h->dscr, 5 * (size_t)N);
     rc |= h->alloc(&h->count, h->C + 1) | h->alloc(&h->start, h->C + 1) |
           h->alloc(&h->keyc, N) | h->alloc(&h->keys, N) | h->alloc(&h->tsrc, N) |
           h->alloc(&h->tkey, N) | h->alloc(&h->tcell, N) | h->alloc(&h->rowcnt, N + 1) |

@@ -19,7 +19,7 @@
 // accumulated per receiver in registers in a fixed order (deterministic, no
 // atomics on physics values). Self pairs contribute exactly zero to every
 // gradient sum (dW/dr(0) = 0), so the list omits them.
-#include "sph_internal.cuh"
+#include "sph_pairs.cuh"
 
 namespace sph {
 
@@ -29,21 +29,6 @@ constexpr int kBlock = 256;
 constexpr unsigned kFull = 0xffffffffu;
 
 inline int nblocks(long long n, int b = kBlock) { return (int)((n + b - 1) / b); }
-
-__device__ __forceinline__ float3 f3(const float4& a) { return make_float3(a.x, a.y, a.z); }
-__device__ __forceinline__ float dot3(const float3& a, const float3& b) {
-  return a.x * b.x + a.y * b.y + a.z * b.z;
-}
-
-struct NList {
-  int* nbr;   // [kmax][N] sender indices (k-major)
-  int* cnt;   // [N] neighbours without self (may exceed kmax)
-  int kmax;
-  const int* vl;   // [kv][N] Verlet candidates, ascending original index
-  const int* vcnt; // [N] candidates (may exceed kv)
-  int kv;
-  const float4* rref;  // positions at the last rebuild
-};
 
 // Per-case edge counter for the NEIGHBOR_LIST_OVERFLOW test: one reduction
 // and one atomic per case present in the warp (cases are contiguous, so
@@ -67,74 +52,6 @@ __device__ __forceinline__ void count_edges(int ci, int cnt, bool valid,
     }
     remaining &= ~grp;
   }
-}
-
-// Visit the senders j of receiver i (self excluded) that are edges at the
-// current positions, from its Verlet candidates (ascending original index),
-// or -- a receiver with more candidates than the list holds -- by walking the
-// cells of the last binning around its position at that binning: every
-// sender now within the cutoff was within the Verlet radius of it then.
-template <int DIM, typename F>
-__device__ __forceinline__ void for_each_edge_slow(long long N, long long i, const float4& ri,
-                                                   const CaseDev& c, const CaseDev* cp,
-                                                   const float4* __restrict__ P4,
-                                                   const int* cellid, const int* start,
-                                                   const NList& L, F&& f) {
-  const float lo = c.cut_lo, hi = c.cut_hi;
-  auto test = [&](int j) {
-    const float4 rj = __ldg(P4 + j);
-    if (edge_mi<DIM>(ri, rj, lo, hi, c, cp)) {
-      float3 dr;
-      float d2;
-      pair_dr<DIM>(ri, rj, c, dr, d2);
-      f(j, rj, dr, d2);
-    }
-  };
-  const int vc = L.vcnt[i];
-  if (vc <= L.kv) {
-    for (int k = 0; k < vc; ++k) test(L.vl[(long long)k * N + i]);
-    return;
-  }
-  const float4 r0 = L.rref[i];
-  auto visit = [&](int j0, int j1, float3) {
-    for (int j = j0; j < j1; ++j)
-      if (j != i) test(j);
-  };
-  if (c.fast)
-    walk_rows<DIM, true>(c, cellid[i] - c.cell_off, r0, start, c.vrad, c.v_r2, visit);
-  else
-    walk_rows<DIM, false>(c, cellid[i] - c.cell_off, r0, start, c.vrad, 0.f, visit);
-}
-
-// Visit the senders j of receiver i (self excluded): from the step's
-// neighbour list, or the slow way when it overflowed for i.
-template <int DIM, typename F>
-__device__ __forceinline__ void for_each_neighbour(long long N, long long i, const float4& ri,
-                                                   const CaseDev& c, const CaseDev* cp,
-                                                   const float4* __restrict__ P4,
-                                                   const int* cellid, const int* start,
-                                                   const NList& L, F&& f) {
-  const int m = L.cnt[i];
-  if (m <= L.kmax) {
-    // software pipelined: the next sender's index and position are loaded
-    // while the current pair is evaluated
-    int jn = m > 0 ? L.nbr[i] : 0;
-    float4 rn = m > 0 ? __ldg(P4 + jn) : ri;
-    for (int k = 0; k < m; ++k) {
-      const int j = jn;
-      const float4 rj = rn;
-      if (k + 1 < m) {
-        jn = L.nbr[(long long)(k + 1) * N + i];
-        rn = __ldg(P4 + jn);
-      }
-      float3 dr;
-      float d2;
-      pair_dr<DIM>(ri, rj, c, dr, d2);
-      f(j, rj, dr, d2);
-    }
-    return;
-  }
-  for_each_edge_slow<DIM>(N, i, ri, c, cp, P4, cellid, start, L, f);
 }
 
 // ------------------------------------------------------------------ Verlet lists
@@ -230,7 +147,8 @@ k_verlet(long long N, Buffers b, const CaseDev* cases, const int* cellid, const 
 // k-major) for the wall and force passes.
 //
 // MODE 0: summation (fluid receivers), 1: SPH continuity, 2: Riemann
-// continuity (fluid receivers). `rie_shepard`: wall receivers compute the
+// continuity (fluid receivers), 3: the neighbour list only (delta-SPH
+// density evolution follows). `rie_shepard`: wall receivers compute the
 // Shepard average of fluid velocities instead (gwbc_fn_riemann_wrapper,
 // solver.py:547-552); `sph_gwbc`: the SPH wall BC follows, which ends with
 // rho = EOS^-1(p) for every particle (solver.py:516).
@@ -315,7 +233,7 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
     const float rho_i = Ui.w;
     const float p_i = b.V4[i].w;
     const bool shepard = rie_shepard && !fluid;
-    const bool need_pairs = MODE == 1 || (fluid && MODE != 0) || shepard;
+    const bool need_pairs = MODE == 1 || (fluid && MODE == 2) || shepard;
     float3 gi = make_float3(0.f, 0.f, 0.f);
     if (MODE == 2) gi = g_ext<DIM>(c, ri, g_arr, b.ORIG[i]);
     auto pair = [&](int j, const float4& rj, const float3& dr, float d2) {
@@ -393,28 +311,32 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
       // and force passes do the same for this receiver)
       for_each_edge_slow<DIM>(N, i, ri, c, cp, b.P4, cellid, start, nl, pair);
     }
-    float rho_new = rho_i, drhodt = 0.f;
-    if (MODE == 0) {
-      if (fluid) rho_new = ri.w * s0.s;
-    } else if (MODE == 1) {
-      drhodt = rho_i * s0.s;
-      rho_new = rho_i + c.dt_rho * drhodt;
-    } else {
-      if (fluid) drhodt = s0.s;
-      rho_new = rho_i + c.dt_rho * drhodt;
-    }
-    if (UT4) {
-      if (shepard) {
-        const float den = s0.s + kEps;
-        UT4[i] = make_float4(sx.s / den, sy.s / den, sz.s / den, 0.f);
+    // MODE 3 writes the neighbour list only: the delta-SPH passes compute
+    // the density
+    if constexpr (MODE != 3) {
+      float rho_new = rho_i, drhodt = 0.f;
+      if (MODE == 0) {
+        if (fluid) rho_new = ri.w * s0.s;
+      } else if (MODE == 1) {
+        drhodt = rho_i * s0.s;
+        rho_new = rho_i + c.dt_rho * drhodt;
       } else {
-        UT4[i] = make_float4(ui.x, ui.y, ui.z, 0.f);
+        if (fluid) drhodt = s0.s;
+        rho_new = rho_i + c.dt_rho * drhodt;
       }
+      if (UT4) {
+        if (shepard) {
+          const float den = s0.s + kEps;
+          UT4[i] = make_float4(sx.s / den, sy.s / den, sz.s / den, 0.f);
+        } else {
+          UT4[i] = make_float4(ui.x, ui.y, ui.z, 0.f);
+        }
+      }
+      float p_new = eos_p(rho_new, c);
+      if (sph_gwbc && fluid) rho_new = eos_rho(p_new, c);
+      R4[i] = make_float4(rho_new, p_new, drhodt, b.ETA[i]);
+      if (!isfinite(rho_new) || !isfinite(p_new)) atomicOr(status, SPH_ERR_NONFINITE);
     }
-    float p_new = eos_p(rho_new, c);
-    if (sph_gwbc && fluid) rho_new = eos_rho(p_new, c);
-    R4[i] = make_float4(rho_new, p_new, drhodt, b.ETA[i]);
-    if (!isfinite(rho_new) || !isfinite(p_new)) atomicOr(status, SPH_ERR_NONFINITE);
   }
   count_edges(ci, cnt, valid, edgecnt, cases, status);
 }
@@ -644,19 +566,29 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
   const int sph_gwbc = !rie && L.bc_trick;
   float4* ut = rie ? UT4 : nullptr;
   NList nl{L.nbr, L.nbr_cnt, L.kmax, L.vl, L.vcnt, L.kv, L.rref};
+  // with renormalisation the evolved density goes to R4e first; the wall
+  // BC's rho = EOS^-1(p) then follows the renormalisation
+  const bool renorm = L.rho_evol && L.rho_renorm;
+  float4* Rd = renorm ? L.R4e : R4;
+  const int gw_d = renorm ? 0 : sph_gwbc;
 #define SPH_DENSITY(MODE)                                                                 \
   k_density<DIM, KER, MODE, KAHAN><<<g, bt, smem, st>>>(L.N, b, L.cases, cellid, start,  \
                                                          L.mask_self, rie_shepard,        \
-                                                         sph_gwbc, g_arr, R4, ut, nl,     \
+                                                         gw_d, g_arr, Rd, ut, nl,         \
                                                          edgecnt, L.status)
   if (!L.rho_evol)
     SPH_DENSITY(0);
   else if (rie)
     SPH_DENSITY(2);
+  else if (L.solver == SPH_SOLVER_DELTA)
+    SPH_DENSITY(3);
   else
     SPH_DENSITY(1);
 #undef SPH_DENSITY
   count_launch(L);
+  if (L.rho_evol && L.solver == SPH_SOLVER_DELTA)
+    launch_delta_density(L, b, Rd, cellid, start, gw_d);
+  if (renorm) launch_renorm(L, b, Rd, R4, cellid, start, sph_gwbc);
   mark(L, 2);
   if (sph_gwbc && has_walls) {
     k_wall<DIM, KER, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start, L.free_slip,

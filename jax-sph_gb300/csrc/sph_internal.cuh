@@ -73,6 +73,7 @@ struct CaseDev {
   float c_ref, eta_limiter;
   float av_alpha, av_hab, av_cab, av_eps;
   float delta_coef;   // diff_alpha * h * c_ref * rho_ref (DELTA diffusive acceleration)
+  float delta_rho_coef;  // c_ref * diff_delta * h (DELTA density diffusion)
   int g_kind;
   float g[3], g_lo, g_hi;
   int bc_kind;
@@ -469,6 +470,7 @@ struct LaunchCtx {
   cudaStream_t stream;
   int dim, kernel, solver;
   int rho_evol, bc_trick, free_slip, mask_self, kahan;
+  int rho_renorm;         // renormalise the evolved density
   long long N;
   int n_cases;
   const CaseDev* cases;   // device
@@ -484,6 +486,8 @@ struct LaunchCtx {
   unsigned* vflag;        // a rebuild is due
   int canonical;          // candidate lists in ascending original index
   int* inv;               // sorted position of every original index (last binning)
+  float4* R4e;            // evolved density before renormalisation (rho_renorm)
+  float4* dscr;           // delta-SPH density scratch: 5 planes of N float4
   int block;              // threads per block of the forward passes (<= 256)
   int* launches;          // optional host counter of kernel launches
   cudaEvent_t* ev;        // optional phase events: bin start, bin end, density end,
@@ -537,6 +541,14 @@ cudaError_t prepare_kernels(int kv);
 void launch_forward(const LaunchCtx& L, Buffers b, const float4* R4, float4* R4w, float4* UT4,
                     const int* cellid, const int* start, unsigned long long* edgecnt,
                     const float* g_arr, bool apply_bc, bool has_walls);
+
+// sph_delta.cu (after the density pass has written the step's neighbour list)
+// delta-SPH density evolution into Rout (rho, p, drho/dt, eta).
+void launch_delta_density(const LaunchCtx& L, Buffers b, float4* Rout, const int* cellid,
+                          const int* start, int sph_gwbc);
+// Density renormalisation of the evolved densities in Rin into Rout.
+void launch_renorm(const LaunchCtx& L, Buffers b, const float4* Rin, float4* Rout,
+                   const int* cellid, const int* start, int sph_gwbc);
 
 size_t scan_tmp_ints(long long n);
 

@@ -37,7 +37,7 @@ class SphConfig(ctypes.Structure):
                 ("is_free_slip", ctypes.c_int32), ("mask_self", ctypes.c_int32),
                 ("kahan", ctypes.c_int32), ("fp64_positions", ctypes.c_int32),
                 ("capacity_multiplier", ctypes.c_double), ("verlet_skin", ctypes.c_double),
-                ("canonical_order", ctypes.c_int32), ("pad1", ctypes.c_int32)]
+                ("canonical_order", ctypes.c_int32), ("is_rho_renorm", ctypes.c_int32)]
 
 
 class SphCase(ctypes.Structure):

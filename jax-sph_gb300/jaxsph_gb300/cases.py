@@ -146,7 +146,7 @@ def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref
             dt=None, t_end=1.0, solver_name="SPH", kernel="QSK", h_fac=1.0, tvf=0.0,
             is_bc_trick=False, density_evolution=False, artificial_alpha=0.0,
             free_slip=False, eta_limiter=3, g_ext=None, bc=None, nw=None, dtype=np.float32,
-            diff_alpha=0.01, diff_delta=0.1):
+            diff_alpha=0.01, diff_delta=0.1, rho_renorm=False):
     """The common part of ``initialize`` (case_setup.py:71-231)."""
     c_ref = c_ref_factor * u_ref
     p_ref = rho_ref * c_ref ** 2 / gamma
@@ -184,7 +184,8 @@ def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref
     bc = bc or BC(_lib.BC_NONE)
     state = bc(state)  # case_setup.py:203
     solver = dict(solver=solver_name, kernel=kernel, h_fac=h_fac, is_bc_trick=is_bc_trick,
-                  is_rho_evol=density_evolution, artificial_alpha=artificial_alpha,
+                  is_rho_evol=density_evolution, is_rho_renorm=rho_renorm,
+                  artificial_alpha=artificial_alpha,
                   is_free_slip=free_slip, eta_limiter=eta_limiter,
                   diff_alpha=diff_alpha, diff_delta=diff_delta)  # defaults.py:96-99
     return CaseSetup(name, dim, dx, np.asarray(box, dtype=np.float64), state, dt,
@@ -221,9 +222,10 @@ def tgv(dim=2, dx=None, viscosity=None, solver_name="SPH", tvf=None, kernel=None
         kernel = kernel or "WC2K"
         tvf = 1.0 if tvf is None else tvf
     tag = np.full(r.shape[0], FLUID)
+    kw.setdefault("density_evolution", solver_name == "RIE")
     return _finish(f"tgv{dim}d", dim, dx, box, r, tag, v, viscosity=viscosity,
                    solver_name=solver_name, kernel=kernel, tvf=tvf, t_end=t_end, dtype=dtype,
-                   density_evolution=(solver_name == "RIE"), **kw)
+                   **kw)
 
 
 def _nws_scipy(r, tag, dx, n_walls, offset_vec, wall_part_fn, dtype):
@@ -261,11 +263,15 @@ def dam_break(dx=0.005, n_walls=3, dtype=np.float32, t_end=12.0, dt=None, **kw):
     offset_vec = np.ones(2) * n_walls * dx
     nw = _nws_scipy(r, tag, dx, n_walls, offset_vec, walls, dtype)
     v = np.zeros_like(r, dtype=np.float64)
-    return _finish("db", 2, dx, box, r, tag, v, viscosity=0.00005, u_ref=u_ref,
-                   g_ext_magnitude=g, solver_name="RIE", kernel="QSK", is_bc_trick=True,
-                   density_evolution=True, artificial_alpha=0.1, t_end=t_end, dt=dt,
+    # db.yaml's settings; keywords override them (e.g. the delta-SPH validation
+    # run of validation/db2d.sh: solver_name="DELTA", gamma=7, u_ref=1.95,
+    # viscosity=0, free_slip=True, artificial_alpha=0)
+    opts = dict(viscosity=0.00005, u_ref=u_ref, solver_name="RIE", kernel="QSK",
+                is_bc_trick=True, density_evolution=True, artificial_alpha=0.1)
+    opts.update(kw)
+    return _finish("db", 2, dx, box, r, tag, v, g_ext_magnitude=g, t_end=t_end, dt=dt,
                    g_ext=GExt(_lib.GEXT_CONST, (0.0, -g, 0.0)), bc=BC(_lib.BC_SOLID_ZERO_P),
-                   nw=nw, dtype=dtype, **kw)
+                   nw=nw, dtype=dtype, **opts)
 
 
 def lid_driven_cavity(dx=0.02, n_walls=3, viscosity=0.01, u_lid=1.0, dtype=np.float32,

@@ -79,9 +79,15 @@ class _SlabEngines:
         self.device = torch.device(device)
         self.cutoff = float(self.solver._kernel_fn.cutoff)
         # cutoff levels a particle's step reaches: force <- neighbour density
-        # <- its neighbours; the wall BC of SPH and DELTA adds wall pressure
-        # <- fluid pressure (solver.py:431-530)
-        self.levels = 3 if (self.solver.solver != "RIE" and self.solver.is_bc_trick) else 2
+        # <- its neighbours (delta-SPH evolution: density <- H of the
+        # neighbours <- L of theirs <- their neighbours, three levels; a
+        # renormalisation adds one); the wall BC of SPH and DELTA adds wall
+        # pressure <- fluid pressure (solver.py:431-530)
+        v = self.solver
+        density = 3 if (v.solver == "DELTA" and v.is_rho_evol) else 1
+        renorm = 1 if (v.is_rho_evol and v.is_rho_renorm) else 0
+        gwbc = 1 if (v.solver != "RIE" and v.is_bc_trick) else 0
+        self.levels = density + renorm + 1 + gwbc
         self.cv = float(setup.tvf) * 0.5 * float(setup.dt)
         self._engines = {}
         if self.solver.g_spec()["kind"] == _lib.GEXT_ARRAY:

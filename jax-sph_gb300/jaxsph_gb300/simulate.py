@@ -32,7 +32,8 @@ def make_solver(setup, kahan=False):
                  diff_alpha=s.get("diff_alpha", 0.01), solver=s["solver"], kernel=s["kernel"],
                  h_fac=s.get("h_fac", 1.0), is_bc_trick=s["is_bc_trick"],
                  is_rho_evol=s["is_rho_evol"], artificial_alpha=s["artificial_alpha"],
-                 is_free_slip=s["is_free_slip"], kahan=kahan)
+                 is_free_slip=s["is_free_slip"], is_rho_renorm=s.get("is_rho_renorm", False),
+                 kahan=kahan)
 
 
 def make_neighbor_fns(setup, solver, mask_self=False, capacity_multiplier=1.25):

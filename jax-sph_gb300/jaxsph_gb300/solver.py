@@ -80,11 +80,8 @@ class WCSPH:
         if solver not in _lib.SOLVERS:
             raise NotImplementedError(
                 f"solver {solver!r}: the GPU hot path implements SPH, RIE and DELTA")
-        if solver == "DELTA" and is_rho_evol:
-            raise NotImplementedError(
-                "DELTA with density evolution (rho_evol_fn_delta) is not on the GPU path")
-        if is_rho_renorm or is_heat_conduction:
-            raise NotImplementedError("density renormalisation and heat conduction are not on the path")
+        if is_heat_conduction:
+            raise NotImplementedError("heat conduction is not on the GPU path")
         self.displacement_fn = displacement_fn
         self.eos = eos
         self.g_ext_fn = g_ext_fn
@@ -96,6 +93,7 @@ class WCSPH:
         self._kernel_fn = make_kernel(kernel, h_fac * dx, dim)
         self.is_bc_trick = bool(is_bc_trick)
         self.is_rho_evol = bool(is_rho_evol)
+        self.is_rho_renorm = bool(is_rho_renorm)
         self.artificial_alpha = float(artificial_alpha)
         self.is_free_slip = bool(is_free_slip)
         self.kahan = bool(kahan)
@@ -106,7 +104,8 @@ class WCSPH:
     # ---------------------------------------------------------------- engine
     def solver_flags(self):
         return dict(kernel=_lib.KERNELS[self.kernel], solver=_lib.SOLVERS[self.solver],
-                    is_rho_evol=self.is_rho_evol, is_bc_trick=self.is_bc_trick,
+                    is_rho_evol=self.is_rho_evol, is_rho_renorm=self.is_rho_renorm,
+                    is_bc_trick=self.is_bc_trick,
                     is_free_slip=self.is_free_slip, kahan=self.kahan)
 
     def g_spec(self):

@@ -121,10 +121,18 @@ def dot(a, b):
     return (a * b).sum(-1)
 
 
+def rho_renorm(rho, mass, i_s, j_s, w_dist, N):
+    """``rho_renorm_fn`` (solver.py:167-173)."""
+    nominator = seg(mass[j_s] * w_dist, i_s, N)
+    denominator = seg((mass / rho)[j_s] * w_dist, i_s, N)
+    denominator = torch.where(denominator > 1, torch.ones_like(denominator), denominator)
+    return nominator / denominator
+
+
 # ---------------------------------------------------------------- solver
 class WCSPH:
-    """``WCSPH`` (solver.py:613-951) for the SPH, RIE and DELTA solvers
-    (DELTA with density summation).
+    """``WCSPH`` (solver.py:613-951) for the SPH, RIE and DELTA solvers, with
+    density summation, evolution and renormalisation.
 
     ``g_ext_fn(r)`` returns the external acceleration per particle (torch).
     """
@@ -132,11 +140,9 @@ class WCSPH:
     def __init__(self, box, eos, g_ext_fn, dx, dim, dt, c_ref, eta_limiter=3,
                  solver="SPH", kernel="QSK", h_fac=1.0, is_bc_trick=False,
                  is_rho_evol=False, artificial_alpha=0.0, is_free_slip=False,
-                 diff_alpha=0.1):
+                 diff_alpha=0.1, diff_delta=0.02, is_rho_renorm=False):
         if solver not in ("SPH", "RIE", "DELTA"):
             raise NotImplementedError(f"solver {solver} is outside the hot-path scope")
-        if solver == "DELTA" and is_rho_evol:
-            raise NotImplementedError("rho_evol_fn_delta is outside the hot-path scope")
         self.box = box
         self.eos = eos
         self.g_ext_fn = g_ext_fn
@@ -151,6 +157,9 @@ class WCSPH:
         # acceleration_delta_fn_wrapper(kernel, alpha, support=h_fac*dx, c_ref,
         # rho_ref) (solver.py:684-690)
         self.delta_coef = diff_alpha * h_fac * dx * c_ref * eos.rho_ref
+        # rho_evol_fn_delta_wrapper(delta, support=h_fac*dx, c_ref) (:691-694)
+        self.delta_rho_coef = c_ref * diff_delta * h_fac * dx
+        self.is_rho_renorm = is_rho_renorm
 
     # limiter_fn_wrapper (solver.py:574-588)
     def beta_fn(self, u_L, u_R):
@@ -201,13 +210,18 @@ class WCSPH:
             temp = v_j_s * ((u[i_s] - u[j_s]) * grad_w_dist).sum(axis=1)
             drhodt = rho * seg(temp, i_s, N)
             rho = rho + self.dt * drhodt
+        elif self.is_rho_evol and self.solver == "DELTA":
+            rho, drhodt = self._rho_evol_delta(rho, mass, dr_i_j, dist, u, i_s, j_s,
+                                               fluid_mask[j_s], gw, N)
         elif self.is_rho_evol and self.solver == "RIE":
             temp = self._rho_evol_riemann(e_s, rho[i_s], rho[j_s], mass[j_s], u[i_s],
                                           u[j_s], p[i_s], p[j_s], dr_i_j, dist,
                                           tag[j_s], nw[j_s], g_ext[i_s], gw)
             drhodt = seg(temp, i_s, N) * fluid_mask
             rho = rho + self.dt * drhodt
-        else:
+        if self.is_rho_evol and self.is_rho_renorm:                       # :755, :770, :792
+            rho = rho_renorm(rho, mass, i_s, j_s, w_dist, N)
+        if not self.is_rho_evol:
             # rho_summation_fn (:176-178)
             rho_ = mass * seg(w_dist, i_s, N)
             rho = torch.where(fluid_mask > 0, rho_, rho)
@@ -283,6 +297,33 @@ class WCSPH:
                      + (rho_j[:, None] * u_j) * dot(v_j - u_j, r_ij)[:, None])
         u_ij = u_i - u_j
         return c[:, None] * (-p_ij[:, None] * r_ij + A_r + eta_ij[:, None] * u_ij)
+
+    # rho_evol_fn_delta (:33-105): continuity plus Marrone's density diffusion
+    # with the renormalised density gradients L_i and L_j
+    def _rho_evol_delta(self, rho, mass, r_ij, d_ij, u, i_s, j_s, fluid_j, gw, N):
+        e_ij = r_ij / (d_ij[:, None] + EPS)
+        kg = gw[:, None] * e_ij
+        V = mass / rho
+        V_i, V_j = V[i_s], V[j_s]
+
+        def outer(a, b):            # L_fn: tensordot(-r_ab, kg V_b, axes=0)
+            return a[:, :, None] * b[:, None, :]
+
+        # jnp.linalg.inv does not raise on a singular matrix: neither does inv_ex
+        L_i = torch.linalg.inv_ex(seg(outer(-r_ij, kg * V_j[:, None]), i_s, N))[0]
+        L_j = torch.linalg.inv_ex(seg(outer(r_ij, kg * V_i[:, None]), j_s, N))[0]
+
+        def rho_grad(rho_a, rho_b, L_a, kgv):    # rho_grad_fn
+            return (rho_b - rho_a)[:, None] * torch.einsum("eab,eb->ea", L_a, kgv)
+
+        g_i = seg(rho_grad(rho[i_s], rho[j_s], L_i[i_s], kg * V_j[:, None]), i_s, N)
+        g_j = seg(rho_grad(rho[j_s], rho[i_s], L_j[j_s], -kg * V_i[:, None]), i_s, N)
+        rho_term = 2 * (rho[j_s] - rho[i_s])[:, None] * (-r_ij) / (d_ij[:, None] + EPS) ** 2
+        psi = rho_term - g_i[i_s] - g_j[j_s]
+        diff = seg(dot(psi, kg) * V_j * fluid_j, i_s, N)
+        cont = seg(dot(u[i_s] - u[j_s], kg) * V_j, i_s, N)
+        drhodt = rho * cont + self.delta_rho_coef * diff
+        return rho + self.dt * drhodt, drhodt
 
     # the diffusive term of acceleration_delta_fn (:293-309)
     def _acc_delta_diff(self, r_ij, d_ij, rho_i, rho_j, u_i, u_j, m_j, gw, fluid_j):

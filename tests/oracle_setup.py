@@ -61,7 +61,9 @@ def oracle_case(setup, dtype=torch.float64, mask_self=False, state=None):
                               is_bc_trick=s["is_bc_trick"], is_rho_evol=s["is_rho_evol"],
                               artificial_alpha=s["artificial_alpha"],
                               is_free_slip=s["is_free_slip"],
-                              diff_alpha=s.get("diff_alpha", 0.01))
+                              diff_alpha=s.get("diff_alpha", 0.01),
+                              diff_delta=s.get("diff_delta", 0.1),
+                              is_rho_renorm=s.get("is_rho_renorm", False))
     fns = oracle.partition.NeighborListFns(setup.box, solver.kernel.cutoff, dtype,
                                            mask_self=mask_self)
     src = setup.state if state is None else state

@@ -43,6 +43,20 @@ def small_cases():
         "pf_delta": lambda: cases.poiseuille(dx=0.05, solver_name="DELTA"),
         "ldc_delta_tvf": lambda: cases.lid_driven_cavity(dx=0.04, tvf=1.0,
                                                          solver_name="DELTA"),
+        # delta-SPH density evolution (validation/db2d.sh's delta-SPH dam break)
+        "pf_delta_evol": lambda: cases.poiseuille(dx=0.05, solver_name="DELTA",
+                                                  density_evolution=True),
+        "db_delta_evol": lambda: cases.dam_break(dx=0.04, solver_name="DELTA", gamma=7.0,
+                                                 u_ref=1.95, viscosity=0.0, free_slip=True,
+                                                 artificial_alpha=0.0),
+        "tgv3d_delta_evol": lambda: cases.tgv(dim=3, dx=2 * np.pi / 16, solver_name="DELTA",
+                                              density_evolution=True, diff_delta=0.5),
+        # density renormalisation after each kind of density evolution
+        "tgv2d_delta_evol_renorm": lambda: cases.tgv(dim=2, dx=0.02, solver_name="DELTA",
+                                                     density_evolution=True, rho_renorm=True),
+        "ldc_sph_evol_renorm": lambda: cases.lid_driven_cavity(dx=0.04, density_evolution=True,
+                                                               rho_renorm=True),
+        "db_rie_renorm": lambda: cases.dam_break(dx=0.04, rho_renorm=True),
     }
 
 
@@ -93,7 +107,8 @@ def test_forward_matches_oracle(name):
         assert e_gpu <= max(tol, 10 * e_f32 + 1e-7 * tol * 1e5), (key, e_gpu, e_f32, tol)
 
 
-@pytest.mark.parametrize("name", ["tgv2d_sph", "tgv3d_sph_tvf", "db_rie", "ldc_sph", "pf_sph"])
+@pytest.mark.parametrize("name", ["tgv2d_sph", "tgv3d_sph_tvf", "db_rie", "ldc_sph", "pf_sph",
+                                  "db_delta_evol", "tgv2d_delta_evol_renorm"])
 def test_rollout_matches_oracle(name):
     setup = small_cases()[name]()
     steps = 20

@@ -139,6 +139,34 @@ def test_oracle_delta_diffusion_term():
     assert (st["mass"][:, None] * st["u"] * diff).sum().item() < 0.0
 
 
+def _delta_evol_rates(perturb, u_zero):
+    from jaxsph_gb300 import cases
+    from oracle_setup import oracle_case
+
+    out = {}
+    for name in ("SPH", "DELTA"):
+        setup = cases.tgv(dim=2, dx=0.05, solver_name=name, density_evolution=True)
+        solver, fns, bc, st = oracle_case(setup, torch.float64)
+        st["rho"] = st["rho"] * (1 + perturb * torch.sin(2 * math.pi * st["r"][:, 0]))
+        if u_zero:
+            st["u"] = torch.zeros_like(st["u"])
+        out[name] = solver.forward(st, fns.allocate(st["r"]).idx)["drhodt"], st
+    return out
+
+
+def test_oracle_delta_density_evolution():
+    """rho_evol_fn_delta: with a uniform density only the continuity term
+    remains (that of rho_evol_fn); with the fluid at rest the diffusion of a
+    density wave reduces it."""
+    r = _delta_evol_rates(0.0, False)
+    assert torch.allclose(r["DELTA"][0], r["SPH"][0], rtol=0, atol=1e-12)
+    r = _delta_evol_rates(1e-3, True)
+    drhodt, st = r["DELTA"]
+    assert r["SPH"][0].abs().max().item() == 0.0
+    dev = st["rho"] - st["rho"].mean()
+    assert (drhodt * dev).sum().item() < 0.0
+
+
 def test_oracle_gradient_through_steps():
     """torch autograd through the float64 oracle (the gradient oracle of the adjoint)."""
     from jaxsph_gb300 import cases
