@@ -9,7 +9,9 @@ Drop-in modules with the reference's call signatures:
 * ``eos.TaitEoS`` / ``eos.RIEMANNEoS`` and the QSK / WC2K ``kernel`` classes
 
 plus ``cases`` (initial states of TGV, dam break, lid-driven cavity,
-Poiseuille flow) and ``simulate`` (resident and batched GPU rollouts).
+Poiseuille and Couette flow), ``simulate`` (resident and batched GPU
+rollouts), ``decompose`` (slab domain decomposition over GPUs) and
+``io_state`` (the reference's .h5 state files and restarts).
 All arithmetic runs in ``libsph_gb300.so`` (hand-written CUDA, C ABI in
 ``include/sph_gb300.h``); there is no CPU path.
 """
@@ -23,6 +25,7 @@ def __getattr__(name):
     # modules that need torch.cuda are imported lazily
     import importlib
 
-    if name in ("partition", "solver", "integrator", "cases", "simulate"):
+    if name in ("partition", "solver", "integrator", "cases", "simulate", "decompose",
+                "io_state", "adjoint"):
         return importlib.import_module(f".{name}", __name__)
     raise AttributeError(name)

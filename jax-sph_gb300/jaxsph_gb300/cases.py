@@ -140,6 +140,15 @@ class CaseSetup:
         st = {k: v.to(device) for k, v in self.state.items()}
         return st
 
+    def load_state0(self, path, keys=("r",)):
+        """Take ``keys`` of the fluid particles from a saved .h5 state
+        (``case.state0_path`` / ``case.state0_keys``, case_setup.py:184-194);
+        every key restarts a run."""
+        from .io_state import apply_state0
+
+        apply_state0(self.state, path, keys, fluid_tag=FLUID)
+        return self
+
 
 def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref=1.0,
             c_ref_factor=10.0, gamma=1.0, p_bg_factor=0.0, g_ext_magnitude=0.0, cfl=0.25,

@@ -153,10 +153,31 @@ class Simulation:
         return self.engine.diagnostics(self.device)
 
 
-def simulate(setup, steps=None, check_every=100, kahan=False):
-    """The reference driver loop on the GPU (simulate.py:110-134); returns the final state."""
+def simulate(setup, steps=None, check_every=100, kahan=False, data_path=None, write_every=1):
+    """The reference driver loop on the GPU (simulate.py:110-134); returns the final state.
+
+    With ``data_path``, writes ``traj_<k>.h5`` every ``write_every`` files like
+    the reference: file k holds the state after k + 1 steps (the loop writes
+    before each step, skipping the initial state, simulate.py:114-115).
+    """
     sim = Simulation(setup, kahan=kahan)
     steps = setup.sequence_length + 2 if steps is None else steps
     # warm-up advance(0.0, ...) of the reference: its result is discarded
-    sim.run(steps, check_every=check_every)
+    if data_path is None:
+        sim.run(steps, check_every=check_every)
+        return sim.state()[0]
+    import os
+
+    from .io_state import write_state
+
+    os.makedirs(data_path, exist_ok=True)
+    seq = setup.sequence_length
+    done = 0
+    for k in range(0, steps - 1, int(write_every)):
+        # file k: the state after k + 1 steps
+        sim.run(k + 1 - done, check_every=check_every)
+        done = k + 1
+        write_state(k, sim.state()[0], data_path, seq, write_every)
+    if steps > done:
+        sim.run(steps - done, check_every=check_every)
     return sim.state()[0]
