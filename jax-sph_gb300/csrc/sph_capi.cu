@@ -78,6 +78,8 @@ struct SphHandle {
   cudaStream_t hs = nullptr, hs2 = nullptr;  // capture streams (step, rebuild body)
   cudaGraphExec_t gexec = nullptr;           // one steady step
   const float* graph_g_arr = nullptr;
+  cudaGraphExec_t gadv = nullptr;            // sph_advance: kick, decide, rebuild
+  const float* gadv_g_arr = nullptr;
   int launch_count = 0;       // kernel launches of the last step
   cudaEvent_t* ev = nullptr;  // phase events while profiling
   // adjoint tape: per recorded step the sorted order, P4, U4, R4 and the
@@ -316,17 +318,23 @@ int upload_cases(SphHandle* h, cudaStream_t st) {
 
 void drop_graph(SphHandle* h) {
   if (h->gexec) cudaGraphExecDestroy(h->gexec);
-  h->gexec = nullptr;
+  if (h->gadv) cudaGraphExecDestroy(h->gadv);
+  h->gexec = h->gadv = nullptr;
 }
 
 int launch_status(const char* what) { return cuda_check(cudaGetLastError(), what); }
 
 // Sets the conditional of the rebuild node of a captured step from the flag
-// the kick raised, and clears the flag.
-__global__ void k_decide(unsigned* vflag, unsigned long long* rebuilds,
+// the kick raised (and, for a drop-in step, the load's "positions differ from
+// the binning" flag), and clears the flags.
+__global__ void k_decide(unsigned* vflag, int nflags, unsigned long long* rebuilds,
                          cudaGraphConditionalHandle cond) {
-  const unsigned v = *vflag;
-  *vflag = 0u;
+  unsigned v = vflag[0];
+  vflag[0] = 0u;
+  if (nflags > 1) {
+    v |= vflag[1];
+    vflag[1] = 0u;
+  }
   if (v) *rebuilds += 1ull;
   cudaGraphSetConditional(cond, v ? 1u : 0u);
 }
@@ -418,11 +426,13 @@ bool steady(const SphHandle* h) { return h->lists && h->from_forward && h->pendi
 
 // Capture one steady step: kick, decide, a conditional node whose body is the
 // rebuild, forward pass. The rebuild runs on the device's own decision, so a
-// replay never waits for the host.
-int capture_step(SphHandle* h, cudaStream_t st) {
+// replay never waits for the host. `advance`: the core of a drop-in step on a
+// freshly loaded state instead -- kick (nothing pending to fold in), decide on
+// both flags, rebuild; the caller launches the rest.
+int capture_step(SphHandle* h, cudaStream_t st, bool advance = false) {
   h->launch_count = 0;
   LaunchCtx L = h->ctx(st);
-  launch_kick(L, h->buf[0], h->R4, h->ref_cells, true, true);
+  launch_kick(L, h->buf[0], h->R4, h->ref_cells, !advance, !advance);
   cudaStreamCaptureStatus cs;
   cudaGraph_t g = nullptr;
   const cudaGraphNode_t* deps = nullptr;
@@ -432,7 +442,7 @@ int capture_step(SphHandle* h, cudaStream_t st) {
   cudaGraphConditionalHandle cond;
   e = cudaGraphConditionalHandleCreate(&cond, g, 0u, 0u);
   if (e != cudaSuccess) return cuda_check(e, "conditional handle");
-  k_decide<<<1, 1, 0, st>>>(h->vflag, h->rebuilds_d, cond);
+  k_decide<<<1, 1, 0, st>>>(h->vflag, advance ? 2 : 1, h->rebuilds_d, cond);
   count_launch(L);
   e = cudaStreamGetCaptureInfo(st, &cs, nullptr, &g, &deps, nullptr, &nd);
   if (e != cudaSuccess) return cuda_check(e, "capture info");
@@ -457,13 +467,16 @@ int capture_step(SphHandle* h, cudaStream_t st) {
   e = cudaStreamEndCapture(h->hs2, &body);
   if (rc) return rc;
   if (e != cudaSuccess) return cuda_check(e, "end rebuild capture");
-  launch_forward(L, h->buf[0], h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr,
-                 true, true);
+  if (!advance)
+    launch_forward(L, h->buf[0], h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt,
+                   h->g_arr, true, true);
   return launch_status("step capture");
 }
 
-int capture_graph(SphHandle* h) {
-  drop_graph(h);
+int capture_graph(SphHandle* h, bool advance = false) {
+  cudaGraphExec_t& slot = advance ? h->gadv : h->gexec;
+  if (slot) cudaGraphExecDestroy(slot);
+  slot = nullptr;
   for (cudaStream_t* s : {&h->hs, &h->hs2}) {
     if (!*s) {
       cudaError_t e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
@@ -473,17 +486,17 @@ int capture_graph(SphHandle* h) {
   cudaGraph_t graph = nullptr;
   cudaError_t e = cudaStreamBeginCapture(h->hs, cudaStreamCaptureModeThreadLocal);
   if (e != cudaSuccess) return cuda_check(e, "begin capture");
-  int rc = capture_step(h, h->hs);
+  int rc = capture_step(h, h->hs, advance);
   e = cudaStreamEndCapture(h->hs, &graph);
   if (rc) {
     if (graph) cudaGraphDestroy(graph);
     return rc;
   }
   if (e != cudaSuccess) return cuda_check(e, "end capture");
-  e = cudaGraphInstantiate(&h->gexec, graph, 0);
+  e = cudaGraphInstantiate(&slot, graph, 0);
   cudaGraphDestroy(graph);
   if (e != cudaSuccess) return cuda_check(e, "graph instantiate");
-  h->graph_g_arr = h->g_arr;
+  (advance ? h->gadv_g_arr : h->graph_g_arr) = h->g_arr;
   return 0;
 }
 
@@ -862,6 +875,16 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
       {"g_ext", (void**)&vin.g_ext, nullptr, vec},
   };
   constexpr int kFields = sizeof(fields) / sizeof(fields[0]);
+  // inputs the step never reads: v (the kick sets v = u + tvf dt/2 dvdt
+  // before anything reads it, integrator.py:26-27), the old pressure (read by
+  // the Riemann continuity only) and drho/dt (carried over by a summation,
+  // when asked for); they are neither copied nor loaded
+  const bool rie_evol = h->cfg.solver == SPH_SOLVER_RIE && h->cfg.is_rho_evol;
+  if (!in_->v || !in_->p) return fail((int)SPH_ERR_INVALID_ARG, "missing state field");
+  vin.v = nullptr;
+  if (!rie_evol) vin.p = nullptr;
+  const bool drhodt_unread = h->cfg.is_rho_evol || !vout.drhodt;
+  if (drhodt_unread) vin.drhodt = nullptr;
   bool hin[kFields], hout[kFields], href = false, hst = false;
   bool any = false;
   for (int k = 0; k < kFields; ++k) {
@@ -937,7 +960,9 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   if (e != cudaSuccess) return cuda_check(e, "advance input copy");
   if (in->n != h->N || out->n != h->N)
     return fail((int)SPH_ERR_INVALID_ARG, "state has the wrong particle count");
-  if (!in->r || !in->tag || !in->u || !in->v || !in->dudt || !in->dvdt || !in->rho || !in->p ||
+  if (!h->cfg.is_rho_evol && out_->drhodt && !in_->drhodt)
+    return fail((int)SPH_ERR_INVALID_ARG, "missing state field");
+  if (!in->r || !in->tag || !in->u || !in->dudt || !in->dvdt || !in->rho ||
       !in->mass || !in->eta || !out->r || !out->u || !out->v || !out->dudt || !out->dvdt ||
       !out->rho || !out->p)
     return fail((int)SPH_ERR_INVALID_ARG, "missing state field");
@@ -960,18 +985,24 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     // only the skin test decides on a rebuild -- the host reads both flags
     if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, 2 * sizeof(unsigned), st);
     launch_pack(L, *in, A, h->case_off_d, h->inv, h->vflag + 1);
-    launch_kick(L, A, h->R4, h->ref_cells, false, false);
-    unsigned f[2] = {0u, 0u};
-    if (e == cudaSuccess)
-      e = cudaMemcpyAsync(f, h->vflag, sizeof(f), cudaMemcpyDeviceToHost, st);
-    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
-    if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, 2 * sizeof(unsigned), st);
-    if (e != cudaSuccess) return cuda_check(e, "advance flags");
-    if (f[0] || f[1] || !h->lists) {
+    if (h->lists) {
+      // kick, then a rebuild if the kick or the load asked for one: decided
+      // on the device inside a captured graph, no host round trip
+      if (h->gadv && h->gadv_g_arr != h->g_arr) {
+        cudaGraphExecDestroy(h->gadv);
+        h->gadv = nullptr;
+      }
+      int rc = 0;
+      if (!h->gadv && (rc = capture_graph(h, true))) return rc;
+      if (e == cudaSuccess) e = cudaGraphLaunch(h->gadv, st);
+    } else {
+      launch_kick(L, A, h->R4, h->ref_cells, false, false);
       int rc = rebuild(h, st, false, false);
       if (rc) return rc;
       ++h->rebuilds_h;
+      if (e == cudaSuccess) e = cudaMemsetAsync(h->vflag, 0, 2 * sizeof(unsigned), st);
     }
+    if (e != cudaSuccess) return cuda_check(e, "advance core");
   } else {
     // cold: load into the scratch set, kick there, sort into the resident
     // set (the rebuild needs no copy)
@@ -985,15 +1016,18 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   }
   bool any_out = false;
   for (int k = 0; k < kFields; ++k) any_out = any_out || host_dst[k];
-  // copy the result fields in [k0, k1) of `fields` back to host memory
+  // copy the result fields in `mask` (bit k: fields[k]) back to host memory
   ncopy = 0;
-  auto copy_back = [&](int k0, int k1) {
+  auto copy_back = [&](unsigned mask) {
+    if (!any_out) return;  // device outputs: the unpack wrote them in place
     if (e == cudaSuccess) e = fork();
-    for (int k = k0; k < k1; ++k)
-      if (host_dst[k] && e == cudaSuccess)
+    for (int k = 0; k < kFields; ++k)
+      if ((mask >> k & 1u) && host_dst[k] && e == cudaSuccess)
         e = cudaMemcpyAsync(host_dst[k], h->stage + h->stage_slot * k, fields[k].bytes,
                             cudaMemcpyDeviceToHost, h->cs[ncopy++ % SphHandle::kCopyStreams]);
   };
+  constexpr unsigned kRUV = 1u << 0 | 1u << 2 | 1u << 3, kRhoP = 1u << 7 | 1u << 8,
+                     kRates = 1u << 4 | 1u << 5 | 1u << 6;
   // r, u and v are final after the kick unless the wall BC pass of the SPH
   // and DELTA solvers rewrites wall velocities: then they go back to host
   // memory while the forward pass runs (fields 0..3 of the list: r, tag, u, v)
@@ -1005,15 +1039,32 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     first.u = out->u;
     first.v = out->v;
     launch_unpack(L, A, h->R4, first, false, true, ref_r, threshold_sq, h->inv);
-    copy_back(0, 4);
+    copy_back(kRUV);
     out->r = out->u = out->v = nullptr;
     ref_r = nullptr;
   }
+  // density passes and wall BC: rho and p (and r, u, v, when the wall BC
+  // rewrote wall velocities) are final and go back while the force pass runs
   launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
-                 true);
-  launch_unpack(L, A, h->R4, *out, true, true, ref_r, threshold_sq, h->inv);
+                 true, 1);
+  {
+    SphStateView mid{};
+    mid.n = out->n;
+    mid.rho = out->rho;
+    mid.p = out->p;
+    mid.r = out->r;
+    mid.u = out->u;
+    mid.v = out->v;
+    launch_unpack(L, A, h->R4, mid, true, true, ref_r, threshold_sq, h->inv);
+    copy_back(kRhoP | (early ? 0u : kRUV));
+    out->rho = out->p = out->r = out->u = out->v = nullptr;
+    ref_r = nullptr;
+  }
+  launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
+                 true, 2);
+  launch_unpack(L, A, h->R4, *out, true, true, nullptr, threshold_sq, h->inv);
   if (any_out) {
-    copy_back(early ? 4 : 0, kFields);
+    copy_back(kRates);
     if (e == cudaSuccess) e = join();
   }
   if (e == cudaSuccess)

@@ -316,6 +316,8 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
     if constexpr (MODE != 3) {
       float rho_new = rho_i, drhodt = 0.f;
       if (MODE == 0) {
+        // a summation leaves drho/dt as the state had it (solver.py:794-796)
+        drhodt = b.A4[i].w;
         if (fluid) rho_new = ri.w * s0.s;
       } else if (MODE == 1) {
         drhodt = rho_i * s0.s;
@@ -556,7 +558,7 @@ k_force(long long N, Buffers b, const CaseDev* cases, const int* cellid, const i
 template <int DIM, int KER, bool KAHAN>
 void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int* cellid,
                const int* start, unsigned long long* edgecnt, const float* g_arr, bool apply_bc,
-               bool has_walls) {
+               bool has_walls, int phases) {
   const int bt = L.block > 0 ? L.block : kBlock;
   const int g = nblocks(L.N, bt);
   const size_t smem = sizeof(int) * kListSlots * bt;
@@ -568,34 +570,37 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
   NList nl{L.nbr, L.nbr_cnt, L.kmax, L.vl, L.vcnt, L.kv, L.rref};
   // with renormalisation the evolved density goes to R4e first; the wall
   // BC's rho = EOS^-1(p) then follows the renormalisation
-  const bool renorm = L.rho_evol && L.rho_renorm;
-  float4* Rd = renorm ? L.R4e : R4;
-  const int gw_d = renorm ? 0 : sph_gwbc;
-#define SPH_DENSITY(MODE)                                                                 \
-  k_density<DIM, KER, MODE, KAHAN><<<g, bt, smem, st>>>(L.N, b, L.cases, cellid, start,  \
-                                                         L.mask_self, rie_shepard,        \
-                                                         gw_d, g_arr, Rd, ut, nl,         \
-                                                         edgecnt, L.status)
-  if (!L.rho_evol)
-    SPH_DENSITY(0);
-  else if (rie)
-    SPH_DENSITY(2);
-  else if (L.solver == SPH_SOLVER_DELTA)
-    SPH_DENSITY(3);
-  else
-    SPH_DENSITY(1);
-#undef SPH_DENSITY
-  count_launch(L);
-  if (L.rho_evol && L.solver == SPH_SOLVER_DELTA)
-    launch_delta_density(L, b, Rd, cellid, start, gw_d);
-  if (renorm) launch_renorm(L, b, Rd, R4, cellid, start, sph_gwbc);
-  mark(L, 2);
-  if (sph_gwbc && has_walls) {
-    k_wall<DIM, KER, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start, L.free_slip,
-                                                  g_arr, R4, nl);
+  if (phases & 1) {
+    const bool renorm = L.rho_evol && L.rho_renorm;
+    float4* Rd = renorm ? L.R4e : R4;
+    const int gw_d = renorm ? 0 : sph_gwbc;
+  #define SPH_DENSITY(MODE)                                                                 \
+    k_density<DIM, KER, MODE, KAHAN><<<g, bt, smem, st>>>(L.N, b, L.cases, cellid, start,  \
+                                                           L.mask_self, rie_shepard,        \
+                                                           gw_d, g_arr, Rd, ut, nl,         \
+                                                           edgecnt, L.status)
+    if (!L.rho_evol)
+      SPH_DENSITY(0);
+    else if (rie)
+      SPH_DENSITY(2);
+    else if (L.solver == SPH_SOLVER_DELTA)
+      SPH_DENSITY(3);
+    else
+      SPH_DENSITY(1);
+  #undef SPH_DENSITY
     count_launch(L);
+    if (L.rho_evol && L.solver == SPH_SOLVER_DELTA)
+      launch_delta_density(L, b, Rd, cellid, start, gw_d);
+    if (renorm) launch_renorm(L, b, Rd, R4, cellid, start, sph_gwbc);
+    mark(L, 2);
+    if (sph_gwbc && has_walls) {
+      k_wall<DIM, KER, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start, L.free_slip,
+                                                    g_arr, R4, nl);
+      count_launch(L);
+    }
+    mark(L, 3);
   }
-  mark(L, 3);
+  if (!(phases & 2)) return;
   if (rie)
     k_force<DIM, KER, 1, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
                                                         L.bc_trick, L.free_slip, g_arr, R4, UT4,
@@ -615,11 +620,13 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
 template <int DIM, int KER>
 void forward_k(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int* cellid,
                const int* start, unsigned long long* edgecnt, const float* g_arr, bool apply_bc,
-               bool has_walls) {
+               bool has_walls, int phases) {
   if (L.kahan)
-    forward_t<DIM, KER, true>(L, b, R4, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+    forward_t<DIM, KER, true>(L, b, R4, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls,
+                              phases);
   else
-    forward_t<DIM, KER, false>(L, b, R4, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+    forward_t<DIM, KER, false>(L, b, R4, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls,
+                               phases);
 }
 
 }  // namespace
@@ -666,18 +673,19 @@ void launch_verlet(const LaunchCtx& L, Buffers b, const int* cellid, const int* 
 
 void launch_forward(const LaunchCtx& L, Buffers b, const float4* /*R4*/, float4* R4w, float4* UT4,
                     const int* cellid, const int* start, unsigned long long* edgecnt,
-                    const float* g_arr, bool apply_bc, bool has_walls) {
-  cudaMemsetAsync(edgecnt, 0, sizeof(unsigned long long) * L.n_cases, L.stream);
+                    const float* g_arr, bool apply_bc, bool has_walls, int phases) {
+  if (phases & 1)
+    cudaMemsetAsync(edgecnt, 0, sizeof(unsigned long long) * L.n_cases, L.stream);
   if (L.dim == 3) {
     if (L.kernel == SPH_KERNEL_QSK)
-      forward_k<3, 0>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+      forward_k<3, 0>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls, phases);
     else
-      forward_k<3, 1>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+      forward_k<3, 1>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls, phases);
   } else {
     if (L.kernel == SPH_KERNEL_QSK)
-      forward_k<2, 0>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+      forward_k<2, 0>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls, phases);
     else
-      forward_k<2, 1>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls);
+      forward_k<2, 1>(L, b, R4w, UT4, cellid, start, edgecnt, g_arr, apply_bc, has_walls, phases);
   }
 }
 

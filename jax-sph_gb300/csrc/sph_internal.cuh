@@ -538,9 +538,10 @@ void launch_diagnostics(const LaunchCtx& L, Buffers b, const float4* R4, bool fr
 void launch_verlet(const LaunchCtx& L, Buffers b, const int* cellid, const int* start);
 // One-time kernel attributes (shared-memory opt-in); returns a CUDA error.
 cudaError_t prepare_kernels(int kv);
+// phases: 1 the density passes and the wall BC, 2 the force pass, 3 both.
 void launch_forward(const LaunchCtx& L, Buffers b, const float4* R4, float4* R4w, float4* UT4,
                     const int* cellid, const int* start, unsigned long long* edgecnt,
-                    const float* g_arr, bool apply_bc, bool has_walls);
+                    const float* g_arr, bool apply_bc, bool has_walls, int phases = 3);
 
 // sph_delta.cu (after the density pass has written the step's neighbour list)
 // delta-SPH density evolution into Rout (rho, p, drho/dt, eta).

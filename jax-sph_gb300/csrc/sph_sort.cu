@@ -52,8 +52,9 @@ __global__ void k_pack(SphStateView s, int dim, Buffers o, const long long* case
     r.w = s.mass[i];
     float4 u = ld4(s.u, dim, i);
     u.w = s.rho[i];
-    float4 v = ld4(s.v, dim, i);
-    v.w = s.p[i];
+    // a drop-in step need not pass v: the kick recomputes it from u
+    float4 v = s.v ? ld4(s.v, dim, i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    v.w = s.p ? s.p[i] : 0.0f;
     float4 a = ld4(s.dudt, dim, i);
     a.w = s.drhodt ? s.drhodt[i] : 0.0f;
     float4 b = ld4(s.dvdt, dim, i);

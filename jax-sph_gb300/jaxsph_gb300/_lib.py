@@ -283,7 +283,8 @@ class Engine:
         vin, vout = self._views
         v = SphStateView.from_buffer_copy(vin)
         for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p"):
-            setattr(v, k, getattr(vout, k))
+            if getattr(vout, k):  # a field not written is the input's own
+                setattr(v, k, getattr(vout, k))
         return v
 
     def rebuild_stats(self):

@@ -42,6 +42,7 @@ def prepare_state(state, dim, device="cuda"):
 
 
 OUT_KEYS = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
+OUT_KEYS_SUMMATION = ("r", "u", "v", "dudt", "dvdt", "rho", "p")
 
 
 def empty_outputs(st):
@@ -244,8 +245,11 @@ class WCSPH:
             e = self.engine(nl_fns, case)
             cap = neighbors.cell_list_capacity
             e.nl_set_capacity(cap if cap is not None else 2 ** 31 - 1, neighbors.max_occupancy)
+            # a summation carries drho/dt over unchanged (solver.py:794-796):
+            # the result keeps the input's tensor, nothing is copied
+            keys = OUT_KEYS if self.is_rho_evol else OUT_KEYS_SUMMATION
             out = {k: torch.empty(st[k].shape, dtype=st[k].dtype, pin_memory=True)
-                   for k in OUT_KEYS}
+                   for k in keys}
             if thr > 0.0 and not (ref.device.type == "cpu" and ref.is_pinned()):
                 ref = ref.to(torch.float32).contiguous().pin_memory()
             try:

@@ -263,6 +263,34 @@ def test_drop_in_advance_on_pinned_host_state():
     assert not hn.did_buffer_overflow
 
 
+def test_summation_carries_drhodt_over():
+    # density summation leaves drho/dt as the state had it (solver.py:794-796):
+    # the forward pass, the drop-in step on device tensors and on pinned host
+    # tensors all return the input's values
+    setup = cases.tgv(dim=2, dx=0.05)
+    g = torch.Generator().manual_seed(5)
+    drhodt = torch.randn(setup.n, generator=g)
+    keys = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
+    base = {k: setup.state[k].to(torch.int32 if k == "tag" else torch.float32).contiguous()
+            for k in keys}
+    base["drhodt"] = drhodt
+    wc = gpu_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    dev = {k: v.cuda() for k, v in base.items()}
+    out = wc.forward_wrapper()(dev, fns.allocate(dev["r"]))
+    assert torch.equal(out["drhodt"].cpu(), drhodt)
+    _, shift = setup.space()
+    for place in ("cuda", "pinned"):
+        st = ({k: v.cuda() for k, v in base.items()} if place == "cuda"
+              else {k: v.pin_memory() for k, v in base.items()})
+        wc = gpu_solver(setup)
+        adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
+        nb = fns.allocate(st["r"])
+        for _ in range(3):
+            st, nb = adv(setup.dt, st, nb)
+        assert torch.equal(st["drhodt"].cpu(), drhodt), place
+
+
 def test_drop_in_advance_rejects_pageable_host_arrays():
     setup = cases.tgv(dim=2, dx=0.05)
     wc = gpu_solver(setup)
