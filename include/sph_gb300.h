@@ -212,14 +212,20 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream);
  * jitted advance(dt, state, neighbors) runs (jax_sph/integrator.py:22-56,
  * jax_sph/simulate.py:115-123): load `in`, kick, drift, neighbour update,
  * forward pass, bc_fn, and write the new state to `out` (which may alias
- * `in`). Arrays may be device memory or pinned host memory (copied by DMA
- * through device staging the handle allocates on the first such call);
- * pageable host memory is rejected. Then, stream-ordered and without a host synchronization, the device
- * status word is copied to `status_dev` (a device uint32) and cleared; it
- * carries SPH_INFO_MOVED when some new position lies farther than
- * sqrt(threshold_sq) from `ref_r` (the list's reference positions, device
- * (n, dim) float32; NULL skips the test) under the periodic metric -- the
- * reference's test for rebuilding the list (jax_md/partition.py:1010-1018). */
+ * `in`). Arrays may be device memory or pinned host memory (read over the
+ * host link by the load kernel, results copied back by DMA through device
+ * staging the handle allocates on the first such call); pageable host
+ * memory is rejected. `in->v` and, outside Riemann density evolution,
+ * `in->p` are required but not read (the kick recomputes v); with a
+ * summation `out->drhodt` may be NULL (the input's drho/dt is unchanged).
+ * Then the status word is copied to `status_dev` (a device or pinned host
+ * uint32) and cleared; it carries SPH_INFO_MOVED when some new position lies
+ * farther than sqrt(threshold_sq) from `ref_r` (the list's reference
+ * positions, (n, dim) float32; NULL skips the test) under the periodic
+ * metric -- the reference's test for rebuilding the list
+ * (jax_md/partition.py:1010-1018). With device arrays only, everything is
+ * stream-ordered and the call does not wait; when a result or the status
+ * word is in host memory, the call returns once it is there. */
 int sph_advance(SphHandle* h, const SphStateView* in, SphStateView* out, const float* ref_r,
                 float threshold_sq, uint32_t* status_dev, void* stream);
 

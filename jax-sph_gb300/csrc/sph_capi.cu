@@ -1074,6 +1074,8 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   h->has_state = h->binned = h->lists = true;
   h->fresh = false;  // the binning may predate the kick
   h->from_forward = h->pending_bc = true;
+  // results in host memory: return once they are there
+  if (e == cudaSuccess && (any_out || hst)) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_check(e, "advance");
   return launch_status("advance");
 }

@@ -145,6 +145,45 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
+_VEC_OUT = ("r", "u", "v", "dudt", "dvdt")
+
+
+def host_outputs(n, dim, keys):
+    """Result arrays of a drop-in step in ONE pinned host block (one
+    allocation per step): a dict of float32 tensors (``(n, dim)`` for vector
+    fields, ``(n,)`` for scalars), a one-element int32 status word in the
+    same block and the ``SphStateView`` over the arrays. The vector fields
+    come first, then the scalars (each group one ``unbind``)."""
+    vec = [k for k in keys if k in _VEC_OUT]
+    sca = [k for k in keys if k not in _VEC_OUT]
+    nv, ns = len(vec) * n * dim, len(sca) * n
+    flat = torch.empty(nv + ns + 4, dtype=torch.float32, pin_memory=True)
+    out = dict(zip(vec, flat[:nv].view(len(vec), n, dim).unbind(0)))
+    out.update(zip(sca, flat[nv:nv + ns].view(len(sca), n).unbind(0)))
+    status = flat[nv + ns:nv + ns + 1].view(torch.int32)
+    base = flat.data_ptr()
+    v = SphStateView()
+    v.n = n
+    for i, k in enumerate(vec):
+        setattr(v, k, base + 4 * i * n * dim)
+    for i, k in enumerate(sca):
+        setattr(v, k, base + 4 * (nv + i * n))
+    return out, status, v
+
+
+try:
+    _raw_stream_of = torch._C._cuda_getCurrentRawStream
+except AttributeError:  # pragma: no cover - older builds
+    _raw_stream_of = None
+
+
+def raw_stream():
+    """The current CUDA stream as a raw handle (the cheap way where torch has it)."""
+    if _raw_stream_of is not None:
+        return _raw_stream_of(torch.cuda.current_device())
+    return torch.cuda.current_stream().cuda_stream
+
+
 def require_cuda():
     if not torch.cuda.is_available():
         raise RuntimeError("jaxsph_gb300 needs a CUDA device (GB300, sm_103a); none is available")
@@ -263,18 +302,25 @@ class Engine:
         _check(self.lib.sph_read_status(self.h, ctypes.byref(s), int(bool(clear)), _stream()))
         return int(s.value)
 
-    def advance(self, state, out, ref=None, threshold_sq=0.0, vin=None):
+    def advance(self, state, out, ref=None, threshold_sq=0.0, vin=None, vout=None,
+                status=None, stream=None):
         """One fused drop-in step (load, step, read back); returns the status
-        word as a 0-d int32 device tensor (no host synchronisation). ``vin``:
-        a view of ``state`` already built (see ``next_view``)."""
+        word, by default a 0-d int32 device tensor (no host synchronisation).
+        ``vin`` / ``vout``: views of ``state`` / ``out`` already built (see
+        ``next_view`` and ``host_outputs``); ``status``: where the word goes
+        (a device or pinned host int32 tensor); ``stream``: a raw stream
+        handle (default: the current stream). With any result in host memory
+        the call returns once it is there."""
         vin = vin if vin is not None else self.view(state, self.n, pinned_ok=True)
-        vout = self.view(out, self.n, pinned_ok=True)
+        vout = vout if vout is not None else self.view(out, self.n, pinned_ok=True)
         self._views = (vin, vout)
-        status = torch.empty((), dtype=torch.int32, device="cuda")
+        if status is None:
+            status = torch.empty((), dtype=torch.int32, device="cuda")
         self._keep = state
         _check(self.lib.sph_advance(self.h, ctypes.byref(vin), ctypes.byref(vout),
                                     _ptr(ref) if ref is not None else None,
-                                    float(threshold_sq), _ptr(status), _stream()))
+                                    float(threshold_sq), status.data_ptr(),
+                                    stream if stream is not None else raw_stream()))
         return status
 
     def next_view(self):

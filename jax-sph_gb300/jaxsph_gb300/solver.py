@@ -248,12 +248,15 @@ class WCSPH:
             # a summation carries drho/dt over unchanged (solver.py:794-796):
             # the result keeps the input's tensor, nothing is copied
             keys = OUT_KEYS if self.is_rho_evol else OUT_KEYS_SUMMATION
-            out = {k: torch.empty(st[k].shape, dtype=st[k].dtype, pin_memory=True)
-                   for k in keys}
+            # results and the status word in one pinned block: the status is
+            # host memory, read without a device synchronisation
+            out, status_h, vout = _lib.host_outputs(key[1], self.dim, keys)
             if thr > 0.0 and not (ref.device.type == "cpu" and ref.is_pinned()):
                 ref = ref.to(torch.float32).contiguous().pin_memory()
             try:
-                status = e.advance(st, out, ref if thr > 0.0 else None, thr, vin=vin)
+                # returns once the results are in host memory
+                status = e.advance(st, out, ref if thr > 0.0 else None, thr, vin=vin,
+                                   vout=vout, status=status_h)
             except _lib.SphError as err:
                 if "pinned" not in str(err):
                     raise
@@ -267,8 +270,6 @@ class WCSPH:
             # value inside the returned list's error code until the caller
             # tests it (host-side failures raise from the call)
             status = e.advance(st, out, ref if thr > 0.0 else None, thr)
-        if host:
-            torch.cuda.current_stream().synchronize()
         res = self._result(state, out)
         if host:
             fields = {k: res[k] for k in STATE_KEYS if res.get(k) is not None}
