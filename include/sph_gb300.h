@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPH_ABI_VERSION 3
+#define SPH_ABI_VERSION 4
 
 /* Reference PartitionErrorCode bits (jax_sph/jax_md/partition.py:453-457). */
 #define SPH_NEIGHBOR_LIST_OVERFLOW 0x1u
@@ -74,7 +74,11 @@ enum {
   SPH_BC_NONE = 0,          /* TGV (cases/tgv.py:56-57) */
   SPH_BC_SOLID_ZERO = 1,    /* u,v,dudt,dvdt = 0 on SOLID_WALL (PF, cases/pf.py:133-146) */
   SPH_BC_SOLID_ZERO_P = 2,  /* as above and p = 0 (DB, cases/db.py:128-142) */
-  SPH_BC_LID = 3            /* SOLID_WALL at rest, MOVING_WALL at u_lid (LDC, cases/ldc.py:127-144) */
+  SPH_BC_LID = 3,           /* SOLID_WALL at rest, MOVING_WALL at u_lid (LDC, cases/ldc.py:127-144) */
+  SPH_BC_HT = 4             /* heat transfer over a plate (cases/ht.py:176-211): SOLID_WALL and
+                               DIRICHLET_WALL at rest; T = bc_T[0] (dTdt = 0) on SOLID_WALL and
+                               on fluid with x < bc_x[0], T = bc_T[1] on DIRICHLET_WALL,
+                               dTdt = 0 on fluid with x > bc_x[1] */
 };
 
 /* Configuration shared by every case of a handle. */
@@ -100,6 +104,9 @@ typedef struct SphConfig {
                               0 sums in cell order, deterministic for a given run */
   int32_t is_rho_renorm;  /* density renormalisation after density evolution
                              (rho_renorm_fn, solver.py:167-173, :755-793) */
+  int32_t is_heat_conduction; /* temperature equation (solver.py:591-610, :832-850) and
+                                 the wall temperature BC (:518-526, :556-565) */
+  int32_t pad2;
 } SphConfig;
 
 /* Per-case parameters (all in the reference's units). */
@@ -125,6 +132,8 @@ typedef struct SphCase {
   double u_lid[3];
   double diff_alpha;      /* delta-SPH acceleration diffusion (DELTA solver) */
   double diff_delta;      /* delta-SPH density diffusion (DELTA, density evolution) */
+  double bc_T[2];         /* SPH_BC_HT: reference and hot-wall temperature */
+  double bc_x[2];         /* SPH_BC_HT: inflow below x = bc_x[0], outflow above bc_x[1] */
 } SphCase;
 
 /* Caller-owned device arrays in the reference state-dict layout
@@ -146,6 +155,10 @@ typedef struct SphStateView {
   const float* eta;
   const float* nw;
   const float* g_ext;
+  float* T;               /* temperature, its rate, conductivity, heat capacity (n,): */
+  float* dTdt;            /*   required with is_heat_conduction, else ignored */
+  const float* kappa;
+  const float* Cp;
 } SphStateView;
 
 /* Capacities of the reference's two-phase neighbour list

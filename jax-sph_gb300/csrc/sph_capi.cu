@@ -128,6 +128,7 @@ struct SphHandle {
     L.canonical = cfg.canonical_order;
     L.inv = inv;
     L.rho_renorm = cfg.is_rho_renorm;
+    L.heat = cfg.is_heat_conduction;
     L.R4e = R4e;
     L.dscr = dscr;
     L.block = block;
@@ -303,7 +304,15 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
   }
   c.g_lo = (float)in.g_band_lo;
   c.g_hi = (float)in.g_band_hi;
+  if (in.bc_kind < SPH_BC_NONE || in.bc_kind > SPH_BC_HT) {
+    err = "unknown bc_kind";
+    return -1;
+  }
   c.bc_kind = in.bc_kind;
+  for (int k = 0; k < 2; ++k) {
+    c.bc_T[k] = (float)in.bc_T[k];
+    c.bc_x[k] = (float)in.bc_x[k];
+  }
   return 0;
 }
 
@@ -363,6 +372,7 @@ int rebuild(SphHandle* h, cudaStream_t st, bool from_forward, bool apply_bc,
   cp(B.ORIG, A.ORIG, sizeof(int) * N);
   if (A.NW4) cp(B.NW4, A.NW4, sizeof(float4) * N);
   if (A.RD) cp(B.RD, A.RD, sizeof(double4_32a) * N);
+  if (A.TH4) cp(B.TH4, A.TH4, sizeof(float4) * N);
   if (e != cudaSuccess) return cuda_check(e, "rebuild copy");
   launch_bin(L, B, A, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc, h->tkey,
              h->tcell, h->scan_tmp, h->C, false, from_forward, apply_bc, h->rref);
@@ -577,6 +587,11 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
           h->alloc(&b.ORIG, N);
     if (need_nw) rc |= h->alloc(&b.NW4, N);
     if (cfg->fp64_positions) rc |= h->alloc(&b.RD, N);
+    if (cfg->is_heat_conduction) rc |= h->alloc(&b.TH4, N);
+  }
+  if (!rc && cfg->is_heat_conduction) {
+    rc |= h->alloc(&h->buf[0].TO, N);
+    h->buf[1].TO = h->buf[0].TO;
   }
   if (!rc) {
     rc |= h->alloc(&h->R4, N) | h->alloc(&h->cellid, N);
@@ -663,6 +678,8 @@ int sph_set_state(SphHandle* h, const SphStateView* s, void* stream) {
     return fail((int)SPH_ERR_INVALID_ARG, "missing state field");
   if (h->buf[0].NW4 && !s->nw)
     return fail((int)SPH_ERR_INVALID_ARG, "wall normals nw are required by this solver");
+  if (h->buf[0].TH4 && (!s->T || !s->dTdt || !s->kappa || !s->Cp))
+    return fail((int)SPH_ERR_INVALID_ARG, "heat conduction needs T, dTdt, kappa and Cp");
   bool garr = false;
   for (const auto& c : h->hc) garr |= c.g_kind == SPH_GEXT_ARRAY;
   if (garr && !s->g_ext)
@@ -873,6 +890,10 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
       {"eta", (void**)&vin.eta, nullptr, sc},
       {"nw", (void**)&vin.nw, nullptr, vec},
       {"g_ext", (void**)&vin.g_ext, nullptr, vec},
+      {"T", (void**)&vin.T, (void**)&vout.T, sc},
+      {"dTdt", (void**)&vin.dTdt, (void**)&vout.dTdt, sc},
+      {"kappa", (void**)&vin.kappa, nullptr, sc},
+      {"Cp", (void**)&vin.Cp, nullptr, sc},
   };
   constexpr int kFields = sizeof(fields) / sizeof(fields[0]);
   // inputs the step never reads: v (the kick sets v = u + tvf dt/2 dvdt
@@ -968,6 +989,9 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     return fail((int)SPH_ERR_INVALID_ARG, "missing state field");
   if (h->buf[0].NW4 && !in->nw)
     return fail((int)SPH_ERR_INVALID_ARG, "wall normals nw are required by this solver");
+  if (h->buf[0].TH4 &&
+      (!in->T || !in->dTdt || !in->kappa || !in->Cp || !out->T || !out->dTdt))
+    return fail((int)SPH_ERR_INVALID_ARG, "heat conduction needs T, dTdt, kappa and Cp");
   bool garr = false;
   for (const auto& c : h->hc) garr |= c.g_kind == SPH_GEXT_ARRAY;
   if (garr && !in->g_ext)
@@ -1026,7 +1050,8 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
         e = cudaMemcpyAsync(host_dst[k], h->stage + h->stage_slot * k, fields[k].bytes,
                             cudaMemcpyDeviceToHost, h->cs[ncopy++ % SphHandle::kCopyStreams]);
   };
-  constexpr unsigned kRUV = 1u << 0 | 1u << 2 | 1u << 3, kRhoP = 1u << 7 | 1u << 8,
+  constexpr unsigned kRUV = 1u << 0 | 1u << 2 | 1u << 3,
+                     kRhoP = 1u << 7 | 1u << 8 | 1u << 13 | 1u << 14,  // with T, dTdt
                      kRates = 1u << 4 | 1u << 5 | 1u << 6;
   // r, u and v are final after the kick unless the wall BC pass of the SPH
   // and DELTA solvers rewrites wall velocities: then they go back to host
@@ -1055,9 +1080,11 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     mid.r = out->r;
     mid.u = out->u;
     mid.v = out->v;
+    mid.T = out->T;
+    mid.dTdt = out->dTdt;
     launch_unpack(L, A, h->R4, mid, true, true, ref_r, threshold_sq, h->inv);
     copy_back(kRhoP | (early ? 0u : kRUV));
-    out->rho = out->p = out->r = out->u = out->v = nullptr;
+    out->rho = out->p = out->r = out->u = out->v = out->T = out->dTdt = nullptr;
     ref_r = nullptr;
   }
   launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
@@ -1128,7 +1155,8 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) {
 int sph_adjoint_init(SphHandle* h, int32_t slots) {
   if (!h || slots <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
   const SphConfig& c = h->cfg;
-  if (c.solver != SPH_SOLVER_SPH || c.is_rho_evol || c.is_bc_trick || h->n_cases != 1)
+  if (c.solver != SPH_SOLVER_SPH || c.is_rho_evol || c.is_bc_trick || c.is_heat_conduction ||
+      h->n_cases != 1)
     return fail((int)SPH_ERR_INVALID_ARG,
                 "the adjoint covers one case of the SPH solver with density summation and "
                 "no wall boundary condition");

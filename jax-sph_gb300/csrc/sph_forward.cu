@@ -346,7 +346,10 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
 // ------------------------------------------------------------------ wall pass
 // gwbc_fn (solver.py:431-530) for wall receivers: Shepard sums over fluid
 // senders of u, v, p and rho*dr; writes u, v (U4/V4 xyz) and R4 (rho, p).
-template <int DIM, int KER, bool KAHAN>
+// HEAT: also the wall temperature, the Shepard average of the fluid
+// temperatures on SOLID_WALL and MOVING_WALL (:518-526; the Riemann solver's
+// heat_bc, :556-565, is the same sum: FULL = false runs it alone).
+template <int DIM, int KER, bool KAHAN, bool FULL, bool HEAT>
 __global__ void __launch_bounds__(kBlock, 4)
 k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
        int free_slip, const float* g_arr, float4* R4, NList nl) {
@@ -356,14 +359,16 @@ k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const in
   if (!is_wall(tag_of(meta))) return;
   const CaseDev& c = cases[case_of(meta)];
   const float4 ri = b.P4[i];
-  Acc<KAHAN> sw, su[3], sv[3], sp, sr[3];
+  Acc<KAHAN> sw, su[3], sv[3], sp, sr[3], sT;
   for_each_neighbour<DIM>(N, i, ri, c, cases + case_of(meta), b.P4, cellid, start, nl,
                           [&](int j, const float4& rj, const float3& dr, float d2) {
     if (tag_of(b.META[j]) != FLUID) return;
     const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
     const float w = kw<KER>(dist, c);
-    const float4 Uj = b.U4[j], Vj = b.V4[j], Rj = R4[j];
     sw.add(w);
+    if (HEAT) sT.add(w * b.TH4[j].x);
+    if (!FULL) return;
+    const float4 Uj = b.U4[j], Vj = b.V4[j], Rj = R4[j];
     su[0].add(w * Uj.x); su[1].add(w * Uj.y); su[2].add(w * Uj.z);
     sv[0].add(w * Vj.x); sv[1].add(w * Vj.y); sv[2].add(w * Vj.z);
     sp.add(w * Rj.y);
@@ -371,6 +376,8 @@ k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const in
     sr[0].add(rw * dr.x); sr[1].add(rw * dr.y); sr[2].add(rw * dr.z);
   });
   const float den = sw.s + kEps;
+  if (HEAT && tag_of(meta) != DIRICHLET_WALL) b.TH4[i].x = sT.s / den;
+  if (!FULL) return;
   float3 uw = make_float3(su[0].s / den, su[1].s / den, su[2].s / den);
   float3 vw = make_float3(sv[0].s / den, sv[1].s / den, sv[2].s / den);
   if (free_slip) {
@@ -387,6 +394,41 @@ k_wall(long long N, Buffers b, const CaseDev* cases, const int* cellid, const in
   const float pw = (sp.s + (gi.x * sr[0].s + gi.y * sr[1].s + gi.z * sr[2].s)) / den;
   const float4 Ri = R4[i];
   R4[i] = make_float4(eos_rho(pw, c), pw, Ri.z, Ri.w);
+}
+
+// ------------------------------------------------------------------ heat pass
+// Heat conduction (solver.py:832-850): the temperature first takes the rate
+// it came with, T' = T + dt dT/dt (walls after the wall temperature BC),
+// then the new rate (temperature_derivative_wrapper, :591-610)
+//   dT/dt_i = sum_j 4 m_j kappa_ij (T'_i - T'_j) F_ij / (Cp_i rho_i rho_j),
+//   kappa_ij = kappa_i kappa_j / (kappa_i + kappa_j),
+//   F_ij = r_ij . grad W_ij / (d^2 + eps),
+// on the densities after the density passes and the wall BC. Writes
+// (T', dT/dt) to TO; the state takes them when it folds the forward result.
+template <int DIM, int KER, bool KAHAN>
+__global__ void __launch_bounds__(kBlock)
+k_heat(long long N, Buffers b, const CaseDev* cases, const int* cellid, const int* start,
+       const float4* R4, NList nl) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int ci = case_of(b.META[i]);
+  const CaseDev& c = cases[ci];
+  const float4 ri = b.P4[i];
+  const float4 ti = b.TH4[i];
+  const float Ti = ti.x + c.dt_rho * ti.y;
+  const float rho_i = R4[i].x;
+  Acc<KAHAN> s;
+  for_each_neighbour<DIM>(N, i, ri, c, cases + ci, b.P4, cellid, start, nl,
+                          [&](int j, const float4& rj, const float3& dr, float d2) {
+    const float dist = d2 > 0.f ? sqrtf(d2) : 0.f;
+    const float4 tj = b.TH4[j];
+    const float Tj = tj.x + c.dt_rho * tj.y;
+    const float g = kdw<KER>(dist, c) / (dist + kEps);
+    const float F = g * (dr.x * dr.x + dr.y * dr.y + dr.z * dr.z) / (dist * dist + kEps);
+    const float keff = ti.z * tj.z / (ti.z + tj.z);
+    s.add(4.0f * rj.w * keff * (Ti - Tj) * F / (ti.w * rho_i * R4[j].x));
+  });
+  b.TO[i] = make_float2(Ti, s.s);
 }
 
 // ------------------------------------------------------------------ force pass
@@ -594,8 +636,20 @@ void forward_t(const LaunchCtx& L, Buffers b, float4* R4, float4* UT4, const int
     if (renorm) launch_renorm(L, b, Rd, R4, cellid, start, sph_gwbc);
     mark(L, 2);
     if (sph_gwbc && has_walls) {
-      k_wall<DIM, KER, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start, L.free_slip,
-                                                    g_arr, R4, nl);
+      if (L.heat)
+        k_wall<DIM, KER, KAHAN, true, true><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
+                                                              L.free_slip, g_arr, R4, nl);
+      else
+        k_wall<DIM, KER, KAHAN, true, false><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
+                                                               L.free_slip, g_arr, R4, nl);
+      count_launch(L);
+    } else if (L.heat && rie && L.bc_trick && has_walls) {
+      k_wall<DIM, KER, KAHAN, false, true><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start,
+                                                             L.free_slip, g_arr, R4, nl);
+      count_launch(L);
+    }
+    if (L.heat) {
+      k_heat<DIM, KER, KAHAN><<<g, bt, 0, st>>>(L.N, b, L.cases, cellid, start, R4, nl);
       count_launch(L);
     }
     mark(L, 3);

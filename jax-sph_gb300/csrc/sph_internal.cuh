@@ -78,6 +78,7 @@ struct CaseDev {
   float g[3], g_lo, g_hi;
   int bc_kind;
   float u_lid[3];
+  float bc_T[2], bc_x[2];  // SPH_BC_HT temperatures and inflow / outflow bounds
   // Fast membership test (every axis has >= 5 cells, so adjacent-cell images
   // are minimum images): squared distances below cut_lo are edges, above
   // cut_hi are not, and only the band between takes the reference metric.
@@ -106,6 +107,9 @@ struct Buffers {
   float* ETA;
   int *META, *ORIG;
   double4_32a* RD;  // float64 positions of the precision form (else null)
+  float4* TH4;      // heat conduction: (T, dTdt, kappa, Cp) (else null)
+  float2* TO;       // heat conduction: the forward pass's new (T, dTdt), in the
+                    // order of the buffers it ran on (shared by both sets, like R4)
 };
 
 // ------------------------------------------------------------------ helpers
@@ -229,6 +233,8 @@ __device__ __forceinline__ float3 bc_vel(float3 u, int tag, const CaseDev& c) {
   } else if (c.bc_kind == SPH_BC_LID) {
     if (tag == SOLID_WALL) u = make_float3(0.f, 0.f, 0.f);
     if (tag == MOVING_WALL) u = make_float3(c.u_lid[0], c.u_lid[1], c.u_lid[2]);
+  } else if (c.bc_kind == SPH_BC_HT) {
+    if (tag == SOLID_WALL || tag == DIRICHLET_WALL) u = make_float3(0.f, 0.f, 0.f);
   }
   return u;
 }
@@ -238,8 +244,24 @@ __device__ __forceinline__ float3 bc_acc(float3 a, int tag, const CaseDev& c) {
     if (tag == SOLID_WALL) a = make_float3(0.f, 0.f, 0.f);
   } else if (c.bc_kind == SPH_BC_LID) {
     if (tag == SOLID_WALL || tag == MOVING_WALL) a = make_float3(0.f, 0.f, 0.f);
+  } else if (c.bc_kind == SPH_BC_HT) {
+    if (tag == SOLID_WALL || tag == DIRICHLET_WALL) a = make_float3(0.f, 0.f, 0.f);
   }
   return a;
+}
+// bc_fn on the temperature and its rate (cases/ht.py:176-211), `x` the
+// particle's (new) first coordinate.
+__device__ __forceinline__ void bc_temp(float& T, float& dTdt, int tag, float x,
+                                        const CaseDev& c) {
+  if (c.bc_kind != SPH_BC_HT) return;
+  if ((tag == FLUID && x < c.bc_x[0]) || tag == SOLID_WALL) {
+    T = c.bc_T[0];
+    dTdt = 0.f;
+  } else if (tag == DIRICHLET_WALL) {
+    T = c.bc_T[1];
+    dTdt = 0.f;
+  }
+  if (tag == FLUID && x > c.bc_x[1]) dTdt = 0.f;
 }
 __device__ __forceinline__ float bc_p(float p, int tag, const CaseDev& c) {
   return (c.bc_kind == SPH_BC_SOLID_ZERO_P && tag == SOLID_WALL) ? 0.0f : p;
@@ -471,6 +493,7 @@ struct LaunchCtx {
   int dim, kernel, solver;
   int rho_evol, bc_trick, free_slip, mask_self, kahan;
   int rho_renorm;         // renormalise the evolved density
+  int heat;               // heat conduction
   long long N;
   int n_cases;
   const CaseDev* cases;   // device

@@ -73,6 +73,9 @@ __global__ void k_pack(SphStateView s, int dim, Buffers o, const long long* case
     o.META[q] = (c << kTagBits) | (tag & kTagMask);
     o.ORIG[q] = (int)i;
     if (o.NW4) o.NW4[q] = s.nw ? ld4(s.nw, dim, i) : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (o.TH4)
+      o.TH4[q] = make_float4(s.T ? s.T[i] : 0.f, s.dTdt ? s.dTdt[i] : 0.f,
+                             s.kappa ? s.kappa[i] : 0.f, s.Cp ? s.Cp[i] : 0.f);
     if (o.RD && (!inv || moved)) o.RD[q] = make_double4_32a(r.x, r.y, r.z, 0.0);
   }
   if (changed && __any_sync(0xffffffffu, moved) && (threadIdx.x & 31) == 0)
@@ -84,6 +87,7 @@ __global__ void k_pack(SphStateView s, int dim, Buffers o, const long long* case
 struct Final {
   float3 u, v;
   float rho, p;
+  float T, dTdt;  // heat conduction only
 };
 __device__ __forceinline__ Final finalize(const Buffers& b, const float4* R4, long long q,
                                           const CaseDev& c, int tag, bool from_forward,
@@ -100,10 +104,23 @@ __device__ __forceinline__ Final finalize(const Buffers& b, const float4* R4, lo
     f.rho = U.w;
     f.p = V.w;
   }
+  f.T = f.dTdt = 0.f;
+  if (b.TH4) {
+    if (from_forward) {
+      const float2 t = b.TO[q];
+      f.T = t.x;
+      f.dTdt = t.y;
+    } else {
+      const float4 t = b.TH4[q];
+      f.T = t.x;
+      f.dTdt = t.y;
+    }
+  }
   if (apply_bc) {
     f.u = bc_vel(f.u, tag, c);
     f.v = bc_vel(f.v, tag, c);
     f.p = bc_p(f.p, tag, c);
+    if (b.TH4) bc_temp(f.T, f.dTdt, tag, b.P4[q].x, c);
   }
   return f;
 }
@@ -136,6 +153,10 @@ __global__ void k_unpack(SphStateView s, int dim, Buffers b, const float4* R4,
     if (s.drhodt) s.drhodt[o] = a.w;
     if (s.rho) s.rho[o] = f.rho;
     if (s.p) s.p[o] = f.p;
+    if (b.TH4) {
+      if (s.T) s.T[o] = f.T;
+      if (s.dTdt) s.dTdt[o] = f.dTdt;
+    }
     if (ref) {
       const float4 r0 = make_float4(ref[o * dim], ref[o * dim + 1],
                                     dim == 3 ? ref[o * dim + 2] : 0.f, 0.f);
@@ -284,6 +305,10 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
     out.META[dest] = meta;
     out.ORIG[dest] = key;
     if (out.NW4) out.NW4[dest] = in.NW4[src];
+    if (out.TH4) {
+      const float4 t = in.TH4[src];
+      out.TH4[dest] = make_float4(f.T, f.dTdt, t.z, t.w);
+    }
     cellid[dest] = cell;
     if (rref) rref[dest] = r;
     if (inv) inv[key] = dest;
@@ -327,6 +352,10 @@ __global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* 
     b.P4[i] = r;
     b.U4[i] = make_float4(u.x, u.y, u.z, f.rho);
     b.V4[i] = make_float4(v.x, v.y, v.z, f.p);
+    if (b.TH4) {
+      const float4 t = b.TH4[i];
+      b.TH4[i] = make_float4(f.T, f.dTdt, t.z, t.w);
+    }
     const float4 q = rref[i];
     float dx = r.x - q.x, dy = r.y - q.y, dz = (DIM == 3) ? r.z - q.z : 0.f;
     dx = fmaf(-c.box[0], rintf(dx * c.inv_box[0]), dx);

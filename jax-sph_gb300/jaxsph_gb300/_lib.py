@@ -28,7 +28,7 @@ KERNELS = {"QSK": 0, "WC2K": 1}
 SOLVERS = {"SPH": 0, "RIE": 1, "DELTA": 2}
 EOS_TAIT, EOS_RIEMANN = 0, 1
 GEXT_ZERO, GEXT_CONST, GEXT_BAND_X, GEXT_ARRAY = 0, 1, 2, 3
-BC_NONE, BC_SOLID_ZERO, BC_SOLID_ZERO_P, BC_LID = 0, 1, 2, 3
+BC_NONE, BC_SOLID_ZERO, BC_SOLID_ZERO_P, BC_LID, BC_HT = 0, 1, 2, 3, 4
 
 
 class SphConfig(ctypes.Structure):
@@ -37,7 +37,8 @@ class SphConfig(ctypes.Structure):
                 ("is_free_slip", ctypes.c_int32), ("mask_self", ctypes.c_int32),
                 ("kahan", ctypes.c_int32), ("fp64_positions", ctypes.c_int32),
                 ("capacity_multiplier", ctypes.c_double), ("verlet_skin", ctypes.c_double),
-                ("canonical_order", ctypes.c_int32), ("is_rho_renorm", ctypes.c_int32)]
+                ("canonical_order", ctypes.c_int32), ("is_rho_renorm", ctypes.c_int32),
+                ("is_heat_conduction", ctypes.c_int32), ("pad2", ctypes.c_int32)]
 
 
 class SphCase(ctypes.Structure):
@@ -52,13 +53,15 @@ class SphCase(ctypes.Structure):
                 ("artificial_alpha", ctypes.c_double), ("g", ctypes.c_double * 3),
                 ("g_band_lo", ctypes.c_double), ("g_band_hi", ctypes.c_double),
                 ("u_lid", ctypes.c_double * 3), ("diff_alpha", ctypes.c_double),
-                ("diff_delta", ctypes.c_double)]
+                ("diff_delta", ctypes.c_double), ("bc_T", ctypes.c_double * 2),
+                ("bc_x", ctypes.c_double * 2)]
 
 
 class SphStateView(ctypes.Structure):
     _fields_ = [("n", ctypes.c_int64)] + [
         (k, ctypes.c_void_p) for k in ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho",
-                                       "p", "mass", "eta", "nw", "g_ext")]
+                                       "p", "mass", "eta", "nw", "g_ext", "T", "dTdt",
+                                       "kappa", "Cp")]
 
 
 class SphNLCapacity(ctypes.Structure):
@@ -118,7 +121,7 @@ def load(build_if_missing=True):
     for name in EXPORTS:
         if name not in ("sph_abi_version", "sph_last_error"):
             getattr(lib, name).restype = I
-    if lib.sph_abi_version() != 3:
+    if lib.sph_abi_version() != 4:
         raise RuntimeError("libsph_gb300 ABI version mismatch")
     _LIB = lib
     return lib
@@ -223,7 +226,7 @@ class Engine:
         v = SphStateView()
         v.n = n
         for k in ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta",
-                  "nw", "g_ext"):
+                  "nw", "g_ext", "T", "dTdt", "kappa", "Cp"):
             t = state.get(k)
             if t is not None:
                 # host tensors: the library itself refuses pageable memory
@@ -328,7 +331,7 @@ class Engine:
         inputs' other fields (tag, mass, eta, nw, g_ext)."""
         vin, vout = self._views
         v = SphStateView.from_buffer_copy(vin)
-        for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p"):
+        for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "T", "dTdt"):
             if getattr(vout, k):  # a field not written is the input's own
                 setattr(v, k, getattr(vout, k))
         return v

@@ -79,15 +79,20 @@ class GExt:
 
 
 class BC:
-    """Boundary condition ``bc_fn(state)`` with a GPU spec (kind, lid velocity)."""
+    """Boundary condition ``bc_fn(state)`` with a GPU spec (kind, lid velocity;
+    heat transfer: reference / hot-wall temperature ``T`` and the inflow /
+    outflow bounds ``x``)."""
 
-    def __init__(self, kind, u_lid=(0.0, 0.0, 0.0)):
-        self.spec = dict(kind=kind, u_lid=tuple(float(x) for x in u_lid))
+    def __init__(self, kind, u_lid=(0.0, 0.0, 0.0), T=(0.0, 0.0), x=(0.0, 0.0)):
+        self.spec = dict(kind=kind, u_lid=tuple(float(v) for v in u_lid),
+                         T=tuple(float(v) for v in T), x=tuple(float(v) for v in x))
 
     def __call__(self, state):
         k = self.spec["kind"]
         if k == _lib.BC_NONE:
             return state
+        if k == _lib.BC_HT:
+            return self._heat_transfer(dict(state))
         st = dict(state)
         tag = st["tag"]
         solid = (tag == SOLID_WALL)[:, None]
@@ -103,6 +108,25 @@ class BC:
             st[key] = torch.where(m, torch.zeros_like(st[key]), st[key])
         if k == _lib.BC_SOLID_ZERO_P:
             st["p"] = torch.where(solid[:, 0], torch.zeros_like(st["p"]), st["p"])
+        return st
+
+    def _heat_transfer(self, st):
+        # HT._boundary_conditions_fn (cases/ht.py:176-211)
+        tag, x = st["tag"], st["r"][:, 0]
+        (t_ref, t_hot), (x_in, x_out) = self.spec["T"], self.spec["x"]
+        fluid = tag == FLUID
+        hot, solid = tag == DIRICHLET_WALL, tag == SOLID_WALL
+        if "T" in st:
+            T, dT = st["T"], st["dTdt"]
+            inflow = fluid & (x < x_in)
+            for m, val in ((inflow, t_ref), (hot, t_hot), (solid, t_ref)):
+                T = torch.where(m, torch.full_like(T, val), T)
+                dT = torch.where(m, torch.zeros_like(dT), dT)
+            dT = torch.where(fluid & (x > x_out), torch.zeros_like(dT), dT)
+            st["T"], st["dTdt"] = T, dT
+        static = (hot | solid)[:, None]
+        for key in ("u", "v", "dudt", "dvdt"):
+            st[key] = torch.where(static, torch.zeros_like(st[key]), st[key])
         return st
 
 
@@ -155,7 +179,8 @@ def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref
             dt=None, t_end=1.0, solver_name="SPH", kernel="QSK", h_fac=1.0, tvf=0.0,
             is_bc_trick=False, density_evolution=False, artificial_alpha=0.0,
             free_slip=False, eta_limiter=3, g_ext=None, bc=None, nw=None, dtype=np.float32,
-            diff_alpha=0.01, diff_delta=0.1, rho_renorm=False):
+            diff_alpha=0.01, diff_delta=0.1, rho_renorm=False, heat_conduction=False,
+            T_ref=1.0, kappa_ref=0.0, Cp_ref=0.0):
     """The common part of ``initialize`` (case_setup.py:71-231)."""
     c_ref = c_ref_factor * u_ref
     p_ref = rho_ref * c_ref ** 2 / gamma
@@ -189,11 +214,16 @@ def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref
         "eta": torch.full((n,), viscosity, dtype=t),
         "nw": torch.as_tensor(nw if nw is not None else np.zeros((n, dim)), dtype=t),
     }
+    if heat_conduction:  # case_setup.py:298-306
+        state.update(T=torch.full((n,), T_ref, dtype=t), dTdt=torch.zeros((n,), dtype=t),
+                     kappa=torch.full((n,), kappa_ref, dtype=t),
+                     Cp=torch.full((n,), Cp_ref, dtype=t))
     g_ext = g_ext or GExt(_lib.GEXT_ZERO)
     bc = bc or BC(_lib.BC_NONE)
     state = bc(state)  # case_setup.py:203
     solver = dict(solver=solver_name, kernel=kernel, h_fac=h_fac, is_bc_trick=is_bc_trick,
                   is_rho_evol=density_evolution, is_rho_renorm=rho_renorm,
+                  is_heat_conduction=heat_conduction,
                   artificial_alpha=artificial_alpha,
                   is_free_slip=free_slip, eta_limiter=eta_limiter,
                   diff_alpha=diff_alpha, diff_delta=diff_delta)  # defaults.py:96-99
@@ -321,6 +351,51 @@ def poiseuille(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, g_ext_magni
     return _finish("pf", 2, dx, box, r, tag, v, viscosity=viscosity, u_ref=u_ref,
                    g_ext_magnitude=g_ext_magnitude, is_bc_trick=True, t_end=t_end, dt=dt,
                    g_ext=g, bc=BC(_lib.BC_SOLID_ZERO), nw=nw, dtype=dtype, **kw)
+
+
+def heat_transfer(dx=0.02, n_walls=3, dtype=np.float32, t_end=1.5, dt=None,
+                  r0_noise_factor=0.05, seed=0, hot_wall_temperature=1.23,
+                  hot_wall_half_width=0.25, **kw):
+    """2D heat transfer over a flat plate (cases/ht.py, cases/ht.yaml).
+
+    A fluid layer L=1 x H=0.2 between two 3-layer walls, periodic along x,
+    driven by a body force on the fluid band; the bottom wall within
+    hot_wall_half_width of the middle is a hot Dirichlet wall. Fluid
+    positions get Gaussian noise of r0_noise_factor*dx (seeded here; the
+    reference draws it from its JAX key), wrapped into the box.
+    """
+    L, H = 1.0, 0.2
+    dxn = n_walls * dx
+    box = np.array([L, H + 2 * dxn])
+    r_f = _add(pos_init_cartesian_2d(np.array([L, H]), dx, dtype), [0.0, dxn], dtype)
+
+    def walls(ddx, nw_):  # HT._init_walls_2d (cases/ht.py:40-54)
+        hz = pos_init_cartesian_2d(np.array([L, ddx * nw_]), ddx, dtype)
+        return np.concatenate([hz, _add(hz, [0.0, H + ddx * nw_], dtype)])
+
+    r_w = walls(dx, n_walls)
+    r = np.concatenate([r_w, r_f])
+    tag = np.concatenate([np.full(len(r_w), SOLID_WALL), np.full(len(r_f), FLUID)])
+    x, y = r[:, 0].astype(np.float64), r[:, 1].astype(np.float64)
+    hot = (y < dxn) & (x < L / 2 + hot_wall_half_width) & (x > L / 2 - hot_wall_half_width)
+    tag = np.where(hot, DIRICHLET_WALL, tag)
+    if r0_noise_factor:
+        # case_setup.py:138-144: noise on the fluid, then the periodic shift
+        rng = np.random.default_rng(seed)
+        noise = rng.normal(0.0, r0_noise_factor * dx, r.shape) * (tag == FLUID)[:, None]
+        r = np.mod(r.astype(np.float64) + noise, box).astype(dtype)
+    v = np.zeros_like(r, dtype=np.float64)
+    nw = None
+    if kw.get("solver_name") == "RIE" or kw.get("free_slip"):
+        nw = _nws_scipy(r, tag, dx, n_walls, np.array([0.0, dxn]), walls, dtype)
+    g_mag = 2.3
+    g = GExt(_lib.GEXT_BAND_X, (g_mag, 0.0, 0.0), (dxn, box[1] - dxn))
+    bc = BC(_lib.BC_HT, T=(1.0, hot_wall_temperature), x=(dxn, L - dxn))
+    opts = dict(g_ext_magnitude=g_mag, is_bc_trick=True, p_bg_factor=0.05,
+                heat_conduction=True, T_ref=1.0, kappa_ref=7.313, Cp_ref=305.27)
+    opts.update(kw)
+    return _finish("ht", 2, dx, box, r, tag, v, t_end=t_end, dt=dt, g_ext=g, bc=bc, nw=nw,
+                   dtype=dtype, **opts)
 
 
 def couette(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, u_x_wall=1.25,

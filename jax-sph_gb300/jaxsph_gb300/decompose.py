@@ -92,6 +92,8 @@ class _SlabEngines:
         self._engines = {}
         if self.solver.g_spec()["kind"] == _lib.GEXT_ARRAY:
             raise NotImplementedError("slabs need a g_ext_fn with a GPU spec")
+        if self.solver.is_heat_conduction:
+            raise NotImplementedError("slabs do not carry the temperature fields")
 
     def engine(self, n):
         e = self._engines.get(n)

@@ -197,6 +197,7 @@ class NeighborListFns:
         c.verlet_skin = float(solver.get("verlet_skin", 0.0))
         c.canonical_order = int(solver.get("canonical_order", 0))
         c.is_rho_renorm = int(solver.get("is_rho_renorm", 0))
+        c.is_heat_conduction = int(solver.get("is_heat_conduction", 0))
         return c
 
     def case(self, n):

@@ -33,7 +33,7 @@ def make_solver(setup, kahan=False):
                  h_fac=s.get("h_fac", 1.0), is_bc_trick=s["is_bc_trick"],
                  is_rho_evol=s["is_rho_evol"], artificial_alpha=s["artificial_alpha"],
                  is_free_slip=s["is_free_slip"], is_rho_renorm=s.get("is_rho_renorm", False),
-                 kahan=kahan)
+                 is_heat_conduction=s.get("is_heat_conduction", False), kahan=kahan)
 
 
 def make_neighbor_fns(setup, solver, mask_self=False, capacity_multiplier=1.25):
@@ -94,7 +94,8 @@ class Simulation:
             self.load([s.state for s in self.setups])  # tuning ran steps: start over
 
     def load(self, states):
-        parts = [prepare_state(st, self.dim, self.device) for st in states]
+        heat = self.solvers[0].is_heat_conduction
+        parts = [prepare_state(st, self.dim, self.device, heat=heat) for st in states]
         full = {k: torch.cat([p[k] for p in parts]).contiguous() for k in parts[0]}
         if "nw" not in full:
             full["nw"] = torch.zeros_like(full["r"])
@@ -136,10 +137,14 @@ class Simulation:
     def state(self, split=True):
         """Current state(s) in the original particle order (device tensors)."""
         full = self._full
-        out = {k: torch.empty_like(full[k]) for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")}
+        keys = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
+        if "T" in full:
+            keys = keys + ("T", "dTdt")
+        out = {k: torch.empty_like(full[k]) for k in keys}
         self.engine.get_state(out)
-        for k in ("tag", "mass", "eta", "nw"):
-            out[k] = full[k]
+        for k in ("tag", "mass", "eta", "nw", "kappa", "Cp"):
+            if k in full:
+                out[k] = full[k]
         if not split:
             return out
         res, o = [], 0

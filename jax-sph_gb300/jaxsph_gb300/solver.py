@@ -16,19 +16,20 @@ from . import _lib
 from .kernel import make_kernel
 
 STATE_KEYS = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
+HEAT_KEYS = ("T", "dTdt", "kappa", "Cp")  # with heat conduction (case_setup.py:164-181)
 _VEC = ("r", "u", "v", "dudt", "dvdt", "nw")
 
 
-def prepare_state(state, dim, device="cuda"):
+def prepare_state(state, dim, device="cuda", heat=False):
     """Contiguous float32 / int32 CUDA copies of the fields the kernels read."""
     n = int(state["r"].shape[0])
     out = {}
-    for k in STATE_KEYS:
+    for k in STATE_KEYS + (HEAT_KEYS if heat else ()):
         x = state.get(k)
         if x is None:
             if k == "nw":
                 continue
-            if k == "drhodt":
+            if k in ("drhodt", "dTdt"):
                 x = torch.zeros(n)
             else:
                 raise KeyError(f"state is missing '{k}'")
@@ -43,18 +44,19 @@ def prepare_state(state, dim, device="cuda"):
 
 OUT_KEYS = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
 OUT_KEYS_SUMMATION = ("r", "u", "v", "dudt", "dvdt", "rho", "p")
+HEAT_OUT_KEYS = ("T", "dTdt")
 
 
-def empty_outputs(st):
-    return {k: torch.empty_like(st[k]) for k in OUT_KEYS}
+def empty_outputs(st, heat=False):
+    return {k: torch.empty_like(st[k]) for k in OUT_KEYS + (HEAT_OUT_KEYS if heat else ())}
 
 
-def host_state(state, dim, need_nw):
+def host_state(state, dim, need_nw, heat=False):
     """The state's own tensors when every field is a contiguous host tensor of
     the kernels' dtype (float32, int32 tags) and shape; else None. (Whether
     they are pinned the library checks itself, before any work.)"""
     out = {}
-    for k in STATE_KEYS:
+    for k in STATE_KEYS + (HEAT_KEYS if heat else ()):
         t = state.get(k)
         if t is None:
             if k == "nw" and not need_nw:
@@ -81,8 +83,6 @@ class WCSPH:
         if solver not in _lib.SOLVERS:
             raise NotImplementedError(
                 f"solver {solver!r}: the GPU hot path implements SPH, RIE and DELTA")
-        if is_heat_conduction:
-            raise NotImplementedError("heat conduction is not on the GPU path")
         self.displacement_fn = displacement_fn
         self.eos = eos
         self.g_ext_fn = g_ext_fn
@@ -95,6 +95,7 @@ class WCSPH:
         self.is_bc_trick = bool(is_bc_trick)
         self.is_rho_evol = bool(is_rho_evol)
         self.is_rho_renorm = bool(is_rho_renorm)
+        self.is_heat_conduction = bool(is_heat_conduction)
         self.artificial_alpha = float(artificial_alpha)
         self.is_free_slip = bool(is_free_slip)
         self.kahan = bool(kahan)
@@ -106,7 +107,7 @@ class WCSPH:
     def solver_flags(self):
         return dict(kernel=_lib.KERNELS[self.kernel], solver=_lib.SOLVERS[self.solver],
                     is_rho_evol=self.is_rho_evol, is_rho_renorm=self.is_rho_renorm,
-                    is_bc_trick=self.is_bc_trick,
+                    is_heat_conduction=self.is_heat_conduction, is_bc_trick=self.is_bc_trick,
                     is_free_slip=self.is_free_slip, kahan=self.kahan)
 
     def g_spec(self):
@@ -142,6 +143,9 @@ class WCSPH:
         s.bc_kind = bc["kind"]
         for d in range(3):
             s.u_lid[d] = bc["u_lid"][d]
+        for k in range(2):
+            s.bc_T[k] = bc.get("T", (0.0, 0.0))[k]
+            s.bc_x[k] = bc.get("x", (0.0, 0.0))[k]
         return s
 
     def engine(self, nl_fns, case):
@@ -160,7 +164,7 @@ class WCSPH:
 
     def _load(self, state, neighbors, case, load=True):
         nl_fns = neighbors._fns
-        st = prepare_state(state, self.dim)
+        st = prepare_state(state, self.dim, heat=self.is_heat_conduction)
         if self.g_spec()["kind"] == _lib.GEXT_ARRAY:
             st["g_ext"] = torch.as_tensor(self.g_ext_fn(st["r"])).to(
                 device=st["r"].device, dtype=torch.float32).contiguous()
@@ -196,7 +200,7 @@ class WCSPH:
             case = self.sph_case(nl_fns, r.shape[0])
             e, st = self._load(state, neighbors, case)
             e.forward()
-            out = empty_outputs(st)
+            out = empty_outputs(st, self.is_heat_conduction)
             e.get_state(out)
             return self._result(state, out)
 
@@ -235,7 +239,8 @@ class WCSPH:
                 and all(state.get(k) is t for k, t in last[1].items())):
             st, vin = last[1], last[2]
         else:
-            st = host_state(state, self.dim, self.solver == "RIE" or self.is_free_slip)
+            st = host_state(state, self.dim, self.solver == "RIE" or self.is_free_slip,
+                            self.is_heat_conduction)
         self._last_host = None
         thr = nl_fns.threshold_sq
         ref = torch.as_tensor(neighbors.reference_position)
@@ -248,6 +253,8 @@ class WCSPH:
             # a summation carries drho/dt over unchanged (solver.py:794-796):
             # the result keeps the input's tensor, nothing is copied
             keys = OUT_KEYS if self.is_rho_evol else OUT_KEYS_SUMMATION
+            if self.is_heat_conduction:
+                keys = keys + HEAT_OUT_KEYS
             # results and the status word in one pinned block: the status is
             # host memory, read without a device synchronisation
             out, status_h, vout = _lib.host_outputs(key[1], self.dim, keys)
@@ -263,7 +270,7 @@ class WCSPH:
                 host = False  # pageable host arrays: go through device copies instead
         if not host:
             e, st = self._load(state, neighbors, case, load=False)
-            out = empty_outputs(st)
+            out = empty_outputs(st, self.is_heat_conduction)
             if thr > 0.0:
                 ref = ref.to(device=st["r"].device, dtype=torch.float32).contiguous()
             # one fused call: load, step, read back; the status stays a device
@@ -272,7 +279,7 @@ class WCSPH:
             status = e.advance(st, out, ref if thr > 0.0 else None, thr)
         res = self._result(state, out)
         if host:
-            fields = {k: res[k] for k in STATE_KEYS if res.get(k) is not None}
+            fields = {k: res[k] for k in STATE_KEYS + HEAT_KEYS if res.get(k) is not None}
             self._last_host = (res, fields, e.next_view(), e)
         if bc_fn is not None and bc_spec is None:
             res = bc_fn(res)

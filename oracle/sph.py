@@ -140,7 +140,8 @@ class WCSPH:
     def __init__(self, box, eos, g_ext_fn, dx, dim, dt, c_ref, eta_limiter=3,
                  solver="SPH", kernel="QSK", h_fac=1.0, is_bc_trick=False,
                  is_rho_evol=False, artificial_alpha=0.0, is_free_slip=False,
-                 diff_alpha=0.1, diff_delta=0.02, is_rho_renorm=False):
+                 diff_alpha=0.1, diff_delta=0.02, is_rho_renorm=False,
+                 is_heat_conduction=False):
         if solver not in ("SPH", "RIE", "DELTA"):
             raise NotImplementedError(f"solver {solver} is outside the hot-path scope")
         self.box = box
@@ -160,6 +161,7 @@ class WCSPH:
         # rho_evol_fn_delta_wrapper(delta, support=h_fac*dx, c_ref) (:691-694)
         self.delta_rho_coef = c_ref * diff_delta * h_fac * dx
         self.is_rho_renorm = is_rho_renorm
+        self.is_heat_conduction = is_heat_conduction
 
     # limiter_fn_wrapper (solver.py:574-588)
     def beta_fn(self, u_L, u_R):
@@ -229,14 +231,28 @@ class WCSPH:
         p = self.eos.p_fn(rho)                                            # :801
         p_bg_tvf = self.eos.p_fn(torch.zeros_like(p))                     # :802
 
+        heat = self.is_heat_conduction
+        temperature = state["T"] if heat else None
         if self.is_bc_trick and self.solver in ("SPH", "DELTA"):          # :796
             p, rho, u, v = self._gwbc(rho, tag, u, v, p, g_ext, i_s, j_s, w_dist,
                                       dr_i_j, nw, N)
+            if heat:                                                      # :518-526
+                temperature = self._wall_temperature(temperature, tag, w_dist, i_s, j_s, N)
             mask = None
         elif self.is_bc_trick and self.solver == "RIE":
             mask = fluid_mask[i_s] if self.is_free_slip else torch.ones_like(i_s, dtype=dtype)
+            if heat:                                                      # heat_bc :556-565
+                temperature = self._wall_temperature(temperature, tag, w_dist, i_s, j_s, N)
         elif self.solver == "RIE":
             mask = torch.ones_like(i_s, dtype=dtype)
+
+        dTdt = state["dTdt"] if heat else None
+        if heat:                                                          # :832-850
+            temperature = temperature + self.dt * dTdt
+            dTdt = seg(self._temperature_derivative(
+                e_s, dr_i_j, dist, rho[i_s], rho[j_s], mass[j_s], state["kappa"][i_s],
+                state["kappa"][j_s], state["Cp"][i_s], temperature[i_s], temperature[j_s],
+                gw), i_s, N)
 
         if self.solver in ("SPH", "DELTA"):
             out = self._acc_standard(dr_i_j, dist, rho[i_s], rho[j_s], u[i_s], u[j_s],
@@ -266,7 +282,25 @@ class WCSPH:
         out_state = dict(state)
         out_state.update(u=u, v=v, drhodt=drhodt, dudt=dudt + g_ext, dvdt=dvdt,
                          rho=rho, p=p)
+        if heat:
+            out_state.update(T=temperature, dTdt=dTdt)
         return out_state
+
+    # gwbc_fn's temperature part / heat_bc: Shepard average of the fluid
+    # temperatures on SOLID_WALL and MOVING_WALL particles
+    def _wall_temperature(self, temperature, tag, w_dist, i_s, j_s, N):
+        w_f = w_dist * (tag[j_s] == FLUID).to(w_dist.dtype)
+        t_wall = seg(w_f * temperature[j_s], i_s, N) / (seg(w_f, i_s, N) + EPS)
+        mask = (tag == SOLID_WALL) | (tag == MOVING_WALL)
+        return torch.where(mask, t_wall, temperature)
+
+    # temperature_derivative_wrapper (:591-610), Cleary 1998
+    def _temperature_derivative(self, e_ij, r_ij, d_ij, rho_i, rho_j, m_j, kappa_i, kappa_j,
+                                Cp_i, T_i, T_j, gw):
+        kernel_grad = gw[:, None] * e_ij
+        kappa_eff = (kappa_i * kappa_j) / (kappa_i + kappa_j)
+        F_ab = dot(r_ij, kernel_grad) / ((d_ij * d_ij) + EPS)
+        return (4 * m_j * kappa_eff * (T_i - T_j) * F_ab) / (Cp_i * rho_i * rho_j)
 
     # rho_evol_riemann_fn (:108-164)
     def _rho_evol_riemann(self, e_ij, rho_i, rho_j, m_j, u_i, u_j, p_i, p_j, r_ij, d_ij,
@@ -451,6 +485,30 @@ def bc_solid_zero(state, zero_p=False):
     if zero_p:
         st["p"] = torch.where(m[:, 0], torch.zeros_like(st["p"]), st["p"])
     return st
+
+
+def make_bc_ht(T_ref, T_hot, x_in, x_out):
+    """HT: inflow / wall temperatures, static walls (cases/ht.py:176-211)."""
+    def f(state):
+        st = dict(state)
+        tag, x = st["tag"], st["r"][:, 0]
+        fluid = tag == FLUID
+        hot, solid = tag == DIRICHLET_WALL, tag == SOLID_WALL
+        T, dT = st["T"], st["dTdt"]
+        inflow = fluid & (x < x_in)
+        T = torch.where(inflow, torch.full_like(T, T_ref), T)
+        dT = torch.where(inflow, torch.zeros_like(dT), dT)
+        T = torch.where(hot, torch.full_like(T, T_hot), T)
+        dT = torch.where(hot, torch.zeros_like(dT), dT)
+        T = torch.where(solid, torch.full_like(T, T_ref), T)
+        dT = torch.where(solid, torch.zeros_like(dT), dT)
+        static = (hot | solid)[:, None]
+        for k in ("u", "v", "dudt", "dvdt"):
+            st[k] = torch.where(static, torch.zeros_like(st[k]), st[k])
+        dT = torch.where(fluid & (x > x_out), torch.zeros_like(dT), dT)
+        st["T"], st["dTdt"] = T, dT
+        return st
+    return f
 
 
 def make_bc_ldc(u_lid):

@@ -50,6 +50,8 @@ def oracle_bc(setup):
         return lambda s: oracle.sph.bc_solid_zero(s, zero_p=True)
     if k == _lib.BC_LID:
         return oracle.sph.make_bc_ldc(spec["u_lid"][:setup.dim])
+    if k == _lib.BC_HT:
+        return oracle.sph.make_bc_ht(*spec["T"], *spec["x"])
     return oracle.sph.bc_identity
 
 
@@ -63,7 +65,8 @@ def oracle_case(setup, dtype=torch.float64, mask_self=False, state=None):
                               is_free_slip=s["is_free_slip"],
                               diff_alpha=s.get("diff_alpha", 0.01),
                               diff_delta=s.get("diff_delta", 0.1),
-                              is_rho_renorm=s.get("is_rho_renorm", False))
+                              is_rho_renorm=s.get("is_rho_renorm", False),
+                              is_heat_conduction=s.get("is_heat_conduction", False))
     fns = oracle.partition.NeighborListFns(setup.box, solver.kernel.cutoff, dtype,
                                            mask_self=mask_self)
     src = setup.state if state is None else state

@@ -57,6 +57,11 @@ def small_cases():
         "ldc_sph_evol_renorm": lambda: cases.lid_driven_cavity(dx=0.04, density_evolution=True,
                                                                rho_renorm=True),
         "db_rie_renorm": lambda: cases.dam_break(dx=0.04, rho_renorm=True),
+        # heat conduction with the wall temperature BC (cases/ht.py)
+        "ht_sph": lambda: cases.heat_transfer(dx=0.04),
+        "ht_rie": lambda: cases.heat_transfer(dx=0.04, solver_name="RIE"),
+        "ht_delta_evol": lambda: cases.heat_transfer(dx=0.04, solver_name="DELTA",
+                                                     density_evolution=True),
     }
 
 
@@ -67,8 +72,8 @@ def scales(setup):
 
 
 def err(a, b):
-    a = a.double().cpu()
-    b = b.double().cpu()
+    a = a.detach().double().cpu()
+    b = b.detach().double().cpu()
     return (a - b).abs().max().item()
 
 
@@ -101,6 +106,9 @@ def test_forward_matches_oracle(name):
     prs = setup.c_ref ** 2
     checks = [("rho", 2e-6), ("p", 2e-6 * prs), ("dudt", 1e-5 * F), ("dvdt", 1e-5 * F),
               ("u", 1e-5), ("v", 1e-5), ("drhodt", 1e-5 * F)]
+    if "T" in r64:
+        dT = float(r64["dTdt"].detach().abs().max()) + 1.0
+        checks += [("T", 1e-6), ("dTdt", 1e-5 * dT)]
     for key, tol in checks:
         e_gpu = err(out[key], r64[key])
         e_f32 = err(r32[key], r64[key])
@@ -108,7 +116,7 @@ def test_forward_matches_oracle(name):
 
 
 @pytest.mark.parametrize("name", ["tgv2d_sph", "tgv3d_sph_tvf", "db_rie", "ldc_sph", "pf_sph",
-                                  "db_delta_evol", "tgv2d_delta_evol_renorm"])
+                                  "db_delta_evol", "tgv2d_delta_evol_renorm", "ht_sph"])
 def test_rollout_matches_oracle(name):
     setup = small_cases()[name]()
     steps = 20
@@ -117,13 +125,22 @@ def test_rollout_matches_oracle(name):
     assert code & 0xF == 0
     got = sim.state()[0]
     ref = oracle_rollout(setup, steps, torch.float64)
+    # the float32 oracle's own drift from float64 over the rollout bounds
+    # what float32 rounding alone explains (a noisy initial state amplifies it)
+    ref32 = oracle_rollout(setup, steps, torch.float32)
     box = float(np.max(setup.box))
     F = scales(setup)
     side = torch.as_tensor(setup.box, dtype=torch.float64)
-    dr = oracle.space.periodic_displacement(side, got["r"].double().cpu() - ref["r"])
-    assert dr.abs().max().item() <= 1e-6 * box
-    assert err(got["rho"], ref["rho"]) <= 2e-5
-    assert err(got["u"], ref["u"]) <= 1e-4 * (setup.u_ref + F * setup.dt)
+
+    def drift(a):
+        return oracle.space.periodic_displacement(side, a["r"].double().cpu() - ref["r"])
+
+    assert drift(got).abs().max().item() <= max(1e-6 * box, 10 * drift(ref32).abs().max().item())
+    assert err(got["rho"], ref["rho"]) <= max(2e-5, 10 * err(ref32["rho"], ref["rho"]))
+    assert err(got["u"], ref["u"]) <= max(1e-4 * (setup.u_ref + F * setup.dt),
+                                          10 * err(ref32["u"], ref["u"]))
+    if "T" in ref:
+        assert err(got["T"], ref["T"]) <= max(1e-5, 10 * err(ref32["T"], ref["T"]))
 
 
 def test_drop_in_advance_equals_resident_rollout():
@@ -289,6 +306,28 @@ def test_summation_carries_drhodt_over():
         for _ in range(3):
             st, nb = adv(setup.dt, st, nb)
         assert torch.equal(st["drhodt"].cpu(), drhodt), place
+
+
+def test_drop_in_heat_transfer_matches_the_resident_rollout():
+    # the temperature fields go in and out of the drop-in step (pinned host
+    # memory) like the others; T and dT/dt match the resident run
+    setup = cases.heat_transfer(dx=0.04)
+    wc = gpu_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    _, shift = setup.space()
+    adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
+    st = {k: v.to(torch.int32 if k == "tag" else torch.float32).contiguous().pin_memory()
+          for k, v in setup.state.items()}
+    nb = fns.allocate(st["r"])
+    for _ in range(5):
+        st, nb = adv(setup.dt, st, nb)
+    assert st["T"].is_pinned() and st["dTdt"].is_pinned()
+    sim = simulate.Simulation(setup)
+    sim.run(5)
+    got = sim.state()[0]
+    for k in ("r", "u", "rho", "T", "dTdt"):
+        a, b = st[k].double(), got[k].double().cpu()
+        assert float((a - b).abs().max()) <= 1e-5 * (float(b.abs().max()) + 1e-30), k
 
 
 def test_drop_in_advance_rejects_pageable_host_arrays():

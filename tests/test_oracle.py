@@ -167,6 +167,39 @@ def test_oracle_delta_density_evolution():
     assert (drhodt * dev).sum().item() < 0.0
 
 
+def test_oracle_heat_conduction_conserves_energy():
+    """Cleary's pair term is antisymmetric: on a periodic box without walls
+    sum_i m_i Cp_i dT/dt_i vanishes, and heat flows from hot to cold."""
+    from jaxsph_gb300 import cases
+    from oracle_setup import oracle_case
+
+    setup = cases.tgv(dim=2, dx=0.05, heat_conduction=True, kappa_ref=1.0, Cp_ref=2.0)
+    solver, fns, _, st = oracle_case(setup, torch.float64)
+    st["T"] = 1 + 0.1 * torch.sin(2 * math.pi * st["r"][:, 0])
+    out = solver.forward(st, fns.allocate(st["r"]).idx)
+    rate = out["dTdt"]
+    assert abs(float((st["mass"] * st["Cp"] * rate).sum())) < 1e-12 * float(rate.abs().max())
+    assert float((rate * (st["T"] - st["T"].mean())).sum()) < 0.0
+
+
+def test_heat_transfer_bc_matches_the_oracle():
+    from jaxsph_gb300 import cases
+    from oracle_setup import oracle_bc
+
+    setup = cases.heat_transfer(dx=0.04)
+    g = torch.Generator().manual_seed(0)
+    st = {k: v.clone() for k, v in setup.state.items()}
+    for k in ("u", "v", "dudt", "dvdt", "T", "dTdt"):
+        st[k] = torch.randn(st[k].shape, generator=g)
+    st["r"][:, 0] = torch.rand(setup.n, generator=g)
+    want = oracle_bc(setup)({k: v.double() if v.is_floating_point() else v
+                             for k, v in st.items()})
+    got = setup.bc_fn(st)
+    for k in ("u", "v", "dudt", "dvdt", "T", "dTdt"):
+        assert torch.equal(got[k], want[k].float()), k  # the values set are float32 here
+    assert (got["T"][st["tag"] == 3] == 1.23).all()
+
+
 def test_oracle_gradient_through_steps():
     """torch autograd through the float64 oracle (the gradient oracle of the adjoint)."""
     from jaxsph_gb300 import cases
