@@ -153,7 +153,8 @@ typedef struct SphStateView {
   float* p;
   const float* mass;
   const float* eta;
-  const float* nw;
+  float* nw;              /* wall normals (n, dim); written by sph_advance and
+                             sph_get_state when given (recomputed with a wall layer) */
   const float* g_ext;
   float* T;               /* temperature, its rate, conductivity, heat capacity (n,): */
   float* dTdt;            /*   required with is_heat_conduction, else ignored */
@@ -241,6 +242,18 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream);
  * word is in host memory, the call returns once it is there. */
 int sph_advance(SphHandle* h, const SphStateView* in, SphStateView* out, const float* ref_r,
                 float threshold_sq, uint32_t* status_dev, void* stream);
+
+/* Moving walls (the integrator's nw_fn, jax_sph/integrator.py:33-34;
+ * compute_nws_jax_wrapper, jax_sph/utils.py:197-275): from now on every step
+ * sets, after the drift, the normal of each wall particle to the normalised
+ * displacement from r - offset to its nearest point of `layer` (host (m, dim)
+ * float32, the walls discretised 5x finer, in the same frame) within `cutoff`
+ * (zero if none; layer point 0 is never a candidate, as in the reference;
+ * ties go to the lowest index), and fluid normals to zero. m = 0 switches it
+ * off. Single-case handles of a solver that keeps normals (Riemann or free
+ * slip). Synchronous (host-side binning and upload). */
+int sph_set_wall_layer(SphHandle* h, const float* layer, int64_t m, const double* offset,
+                       double cutoff);
 
 /* Threads per block of the density, wall and force passes (a multiple of 32
  * in [32, 256]; default 256). A tuning knob: results do not depend on it. */

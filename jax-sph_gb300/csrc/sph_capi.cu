@@ -42,6 +42,9 @@ struct SphHandle {
   float4* R4 = nullptr;
   float4* UT4 = nullptr;
   float4* R4e = nullptr;   // evolved density before renormalisation
+  WallLayer layer{};         // wall normals recomputed each step (layer.n > 0)
+  float4* layer_pts = nullptr;
+  int* layer_start = nullptr;
   float4* dscr = nullptr;  // delta-SPH density scratch (5 planes of N)
   int* cellid = nullptr;
   int *count = nullptr, *start = nullptr, *keyc = nullptr, *keys = nullptr;
@@ -129,6 +132,7 @@ struct SphHandle {
     L.inv = inv;
     L.rho_renorm = cfg.is_rho_renorm;
     L.heat = cfg.is_heat_conduction;
+    L.layer = layer;
     L.R4e = R4e;
     L.dscr = dscr;
     L.block = block;
@@ -643,6 +647,8 @@ int sph_destroy(SphHandle* h) {
   if (h->hs) cudaStreamDestroy(h->hs);
   if (h->hs2) cudaStreamDestroy(h->hs2);
   for (void* p : h->allocs) cudaFree(p);
+  cudaFree(h->layer_pts);
+  cudaFree(h->layer_start);
   delete h;
   return 0;
 }
@@ -888,7 +894,7 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
       {"p", (void**)&vin.p, (void**)&vout.p, sc},
       {"mass", (void**)&vin.mass, nullptr, sc},
       {"eta", (void**)&vin.eta, nullptr, sc},
-      {"nw", (void**)&vin.nw, nullptr, vec},
+      {"nw", (void**)&vin.nw, (void**)&vout.nw, vec},  // out: recomputed normals
       {"g_ext", (void**)&vin.g_ext, nullptr, vec},
       {"T", (void**)&vin.T, (void**)&vout.T, sc},
       {"dTdt", (void**)&vin.dTdt, (void**)&vout.dTdt, sc},
@@ -1050,7 +1056,7 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
         e = cudaMemcpyAsync(host_dst[k], h->stage + h->stage_slot * k, fields[k].bytes,
                             cudaMemcpyDeviceToHost, h->cs[ncopy++ % SphHandle::kCopyStreams]);
   };
-  constexpr unsigned kRUV = 1u << 0 | 1u << 2 | 1u << 3,
+  constexpr unsigned kRUV = 1u << 0 | 1u << 2 | 1u << 3 | 1u << 11,  // with nw
                      kRhoP = 1u << 7 | 1u << 8 | 1u << 13 | 1u << 14,  // with T, dTdt
                      kRates = 1u << 4 | 1u << 5 | 1u << 6;
   // r, u and v are final after the kick unless the wall BC pass of the SPH
@@ -1063,9 +1069,10 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     first.r = out->r;
     first.u = out->u;
     first.v = out->v;
+    first.nw = out->nw;
     launch_unpack(L, A, h->R4, first, false, true, ref_r, threshold_sq, h->inv);
     copy_back(kRUV);
-    out->r = out->u = out->v = nullptr;
+    out->r = out->u = out->v = out->nw = nullptr;
     ref_r = nullptr;
   }
   // density passes and wall BC: rho and p (and r, u, v, when the wall BC
@@ -1082,9 +1089,10 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
     mid.v = out->v;
     mid.T = out->T;
     mid.dTdt = out->dTdt;
+    mid.nw = out->nw;
     launch_unpack(L, A, h->R4, mid, true, true, ref_r, threshold_sq, h->inv);
     copy_back(kRhoP | (early ? 0u : kRUV));
-    out->rho = out->p = out->r = out->u = out->v = out->T = out->dTdt = nullptr;
+    out->rho = out->p = out->r = out->u = out->v = out->T = out->dTdt = out->nw = nullptr;
     ref_r = nullptr;
   }
   launch_forward(L, A, h->R4, h->R4, h->UT4, h->cellid, h->start, h->edgecnt, h->g_arr, true,
@@ -1105,6 +1113,76 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   if (e == cudaSuccess && (any_out || hst)) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_check(e, "advance");
   return launch_status("advance");
+}
+
+int sph_set_wall_layer(SphHandle* h, const float* layer, int64_t m, const double* offset,
+                       double cutoff) {
+  if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
+  if (m < 0 || (m > 0 && (!layer || !offset || !(cutoff > 0.0))))
+    return fail((int)SPH_ERR_INVALID_ARG, "bad wall layer");
+  if (m > INT_MAX / 2) return fail((int)SPH_ERR_INVALID_ARG, "wall layer too large");
+  if (m > 0 && h->n_cases != 1)
+    return fail((int)SPH_ERR_INVALID_ARG, "a wall layer needs a single-case handle");
+  if (m > 0 && !h->buf[0].NW4)
+    return fail((int)SPH_ERR_INVALID_ARG,
+                "wall normals are kept only by the Riemann solver or with free slip");
+  cudaFree(h->layer_pts);
+  cudaFree(h->layer_start);
+  h->layer_pts = nullptr;
+  h->layer_start = nullptr;
+  h->layer = WallLayer{};
+  drop_graph(h);  // the kick of a captured step carries the layer
+  if (m == 0) return 0;
+  const int dim = h->cfg.dim;
+  const CaseDev& c = h->hc[0];
+  WallLayer w{};
+  w.n = (int)m;
+  for (int d = 0; d < 3; ++d) {
+    const double box = d < dim ? (double)c.box[d] : 1.0;
+    int n = d < dim ? (int)std::floor(box / cutoff) : 1;
+    n = n < 1 ? 1 : n;
+    w.nc[d] = n;
+    w.cs[d] = (float)(box / n);  // >= cutoff: the 3^d cells around hold the radius
+    w.off[d] = d < dim ? (float)offset[d] : 0.f;
+  }
+  w.cut2 = (float)(cutoff * cutoff);
+  // counting sort of the points by cell (stable: ascending index in a cell)
+  const long long ncell = (long long)w.nc[0] * w.nc[1] * w.nc[2];
+  std::vector<int> cell(m), start(ncell + 1, 0);
+  for (int64_t k = 0; k < m; ++k) {
+    int ci[3] = {0, 0, 0};
+    for (int d = 0; d < dim; ++d) {
+      const double box = c.box[d];
+      double x = layer[k * dim + d];
+      x -= box * std::floor(x / box);
+      int q = (int)(x / w.cs[d]);
+      ci[d] = q < 0 ? 0 : (q >= w.nc[d] ? w.nc[d] - 1 : q);
+    }
+    cell[k] = ci[0] + w.nc[0] * (ci[1] + w.nc[1] * ci[2]);
+    ++start[cell[k] + 1];
+  }
+  for (long long q = 0; q < ncell; ++q) start[q + 1] += start[q];
+  std::vector<int> fill(start.begin(), start.end() - 1);
+  std::vector<float4> pts(m);
+  for (int64_t k = 0; k < m; ++k) {
+    float4 p = make_float4(layer[k * dim], layer[k * dim + 1], dim == 3 ? layer[k * dim + 2] : 0.f,
+                           0.f);
+    int idx = (int)k;
+    std::memcpy(&p.w, &idx, sizeof(int));
+    pts[fill[cell[k]]++] = p;
+  }
+  cudaError_t e = cudaMalloc(&h->layer_pts, sizeof(float4) * m);
+  if (e == cudaSuccess) e = cudaMalloc(&h->layer_start, sizeof(int) * (ncell + 1));
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h->layer_pts, pts.data(), sizeof(float4) * m, cudaMemcpyHostToDevice);
+  if (e == cudaSuccess)
+    e = cudaMemcpy(h->layer_start, start.data(), sizeof(int) * (ncell + 1),
+                   cudaMemcpyHostToDevice);
+  if (e != cudaSuccess) return cuda_check(e, "wall layer upload");
+  w.pts = h->layer_pts;
+  w.start = h->layer_start;
+  h->layer = w;
+  return 0;
 }
 
 int sph_set_block_size(SphHandle* h, int32_t threads) {

@@ -17,6 +17,8 @@
 #include <cuda_runtime.h>
 #include <stdint.h>
 
+#include <climits>
+
 #include <string>
 
 #include "../../include/sph_gb300.h"
@@ -485,6 +487,72 @@ struct Acc {
   }
 };
 
+// ------------------------------------------------------------------ wall normals
+// A static, 5x finer layer of points along the walls (utils.py:197-275): each
+// step the wall particles' normals point to their nearest layer point.
+// Points are binned in a grid of at least the search radius (cs >= cutoff).
+struct WallLayer {
+  const float4* pts;  // (x, y, z, layer index as int bits), sorted by cell
+  const int* start;   // [ncell + 1] cell offsets into pts
+  int n;              // layer points (0: no recomputation)
+  int nc[3];
+  float cs[3];
+  float off[3];       // wall particles are searched at r - off
+  float cut2;         // squared search radius
+};
+
+// The displacement from wall particle position `r` to its nearest layer
+// point within the search radius, normalised: nw = dr / (|dr| + eps); zero
+// when none is within it (compute_nws_jax_wrapper, utils.py:239-270). The
+// reference's candidates are the layer points of a dense neighbour list with
+// index > 0 only (it compares the list index with the number of walls
+// strictly), so layer point 0 never counts; among equally near points the
+// one with the lowest index wins.
+template <int DIM>
+__device__ __forceinline__ float4 wall_normal(const float4& r, const WallLayer& w,
+                                              const CaseDev& c) {
+  const float4 p = make_float4(__fsub_rn(r.x, w.off[0]), __fsub_rn(r.y, w.off[1]),
+                               DIM == 3 ? __fsub_rn(r.z, w.off[2]) : 0.f, 0.f);
+  int cell[3] = {0, 0, 0};
+  const float pc[3] = {p.x, p.y, p.z};
+  for (int d = 0; d < DIM; ++d) {
+    float x = pc[d] - c.box[d] * floorf(pc[d] / c.box[d]);  // wrap for binning only
+    int k = (int)(x / w.cs[d]);
+    cell[d] = k < 0 ? 0 : (k >= w.nc[d] ? w.nc[d] - 1 : k);
+  }
+  float best = INFINITY;
+  int best_idx = INT_MAX;
+  float3 bdr = make_float3(0.f, 0.f, 0.f);
+  const int span[3] = {w.nc[0] < 3 ? w.nc[0] : 3, w.nc[1] < 3 ? w.nc[1] : 3,
+                       DIM == 3 ? (w.nc[2] < 3 ? w.nc[2] : 3) : 1};
+  for (int a = 0; a < span[0]; ++a)
+    for (int b = 0; b < span[1]; ++b)
+      for (int e = 0; e < span[2]; ++e) {
+        const int ox = w.nc[0] < 3 ? a : cell[0] + a - 1;
+        const int oy = w.nc[1] < 3 ? b : cell[1] + b - 1;
+        const int oz = DIM == 3 ? (w.nc[2] < 3 ? e : cell[2] + e - 1) : 0;
+        const int cx = (ox + w.nc[0]) % w.nc[0], cy = (oy + w.nc[1]) % w.nc[1];
+        const int cz = DIM == 3 ? (oz + w.nc[2]) % w.nc[2] : 0;
+        const int q = cx + w.nc[0] * (cy + w.nc[1] * cz);
+        for (int t = w.start[q]; t < w.start[q + 1]; ++t) {
+          const float4 l = w.pts[t];
+          const int li = __float_as_int(l.w);
+          if (li == 0) continue;
+          if (!(sqd<DIM>(pdisp3<DIM>(p, l, c)) < w.cut2)) continue;
+          const float3 dr = pdisp3<DIM>(l, p, c);
+          const float dist = sqrtf(sqd<DIM>(dr));
+          if (dist < best || (dist == best && li < best_idx)) {
+            best = dist;
+            best_idx = li;
+            bdr = dr;
+          }
+        }
+      }
+  if (best_idx == INT_MAX) return make_float4(0.f, 0.f, 0.f, 0.f);
+  const float den = best + kEps;
+  return make_float4(bdr.x / den, bdr.y / den, bdr.z / den, 0.f);
+}
+
 // ------------------------------------------------------------------ launchers
 struct Workspace;  // defined in sph_capi.cu
 
@@ -494,6 +562,7 @@ struct LaunchCtx {
   int rho_evol, bc_trick, free_slip, mask_self, kahan;
   int rho_renorm;         // renormalise the evolved density
   int heat;               // heat conduction
+  WallLayer layer;        // wall normals recomputed in the kick (layer.n > 0)
   long long N;
   int n_cases;
   const CaseDev* cases;   // device

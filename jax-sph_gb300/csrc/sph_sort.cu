@@ -157,6 +157,10 @@ __global__ void k_unpack(SphStateView s, int dim, Buffers b, const float4* R4,
       if (s.T) s.T[o] = f.T;
       if (s.dTdt) s.dTdt[o] = f.dTdt;
     }
+    if (s.nw && b.NW4) {  // the (possibly recomputed) wall normals
+      const float4 n = b.NW4[q];
+      st3(s.nw, dim, o, n.x, n.y, n.z);
+    }
     if (ref) {
       const float4 r0 = make_float4(ref[o * dim], ref[o * dim + 1],
                                     dim == 3 ? ref[o * dim + 2] : 0.f, 0.f);
@@ -330,7 +334,7 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
 template <int DIM>
 __global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* cases,
                        const float4* rref, int* cref_count, unsigned* vflag, unsigned* status,
-                       bool from_forward, bool apply_bc) {
+                       bool from_forward, bool apply_bc, WallLayer layer) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   bool rebuild = false, over = false;
@@ -352,6 +356,10 @@ __global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* 
     b.P4[i] = r;
     b.U4[i] = make_float4(u.x, u.y, u.z, f.rho);
     b.V4[i] = make_float4(v.x, v.y, v.z, f.p);
+    // moving walls: the normals follow the new positions (integrator.py:33-34)
+    if (layer.n > 0 && b.NW4)
+      b.NW4[i] = is_wall(tag_of(meta)) ? wall_normal<DIM>(r, layer, c)
+                                       : make_float4(0.f, 0.f, 0.f, 0.f);
     if (b.TH4) {
       const float4 t = b.TH4[i];
       b.TH4[i] = make_float4(f.T, f.dTdt, t.z, t.w);
@@ -651,10 +659,10 @@ void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_
   int g = nblocks(L.N);
   if (L.dim == 3)
     k_kick<3><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, L.rref, L.cref_count, L.vflag,
-                                          L.status, from_forward, apply_bc);
+                                          L.status, from_forward, apply_bc, L.layer);
   else
     k_kick<2><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, L.rref, L.cref_count, L.vflag,
-                                          L.status, from_forward, apply_bc);
+                                          L.status, from_forward, apply_bc, L.layer);
   count_launch(L);
 }
 

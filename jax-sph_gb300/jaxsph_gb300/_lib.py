@@ -8,6 +8,7 @@ present, every call raises.
 import ctypes
 import os
 
+import numpy as np
 import torch
 
 from . import _build
@@ -74,7 +75,7 @@ EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sp
            "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_set_block_size",
            "sph_step_launch_count", "sph_profile_step", "sph_adjoint_init", "sph_tape_record",
            "sph_adjoint_step", "sph_read_status", "sph_read_status_async", "sph_diagnostics",
-           "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance"]
+           "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance", "sph_set_wall_layer"]
 
 _LIB = None
 
@@ -115,6 +116,7 @@ def load(build_if_missing=True):
     lib.sph_rebuild_stats.argtypes = [V, P(ctypes.c_int64), P(ctypes.c_int32), V]
     lib.sph_advance.argtypes = [V, P(SphStateView), P(SphStateView), V, ctypes.c_float, V, V]
     lib.sph_diagnostics.argtypes = [V, V, V]
+    lib.sph_set_wall_layer.argtypes = [V, V, ctypes.c_int64, P(ctypes.c_double), ctypes.c_double]
     lib.sph_nl_edges_noalloc.argtypes = [ctypes.c_int32, P(ctypes.c_double), ctypes.c_double,
                                          ctypes.c_int32, V, ctypes.c_int64, V, ctypes.c_int64,
                                          V, V, V]
@@ -148,7 +150,7 @@ def _ptr(t):
     return ctypes.c_void_p(t.data_ptr()) if t is not None else None
 
 
-_VEC_OUT = ("r", "u", "v", "dudt", "dvdt")
+_VEC_OUT = ("r", "u", "v", "dudt", "dvdt", "nw")
 
 
 def host_outputs(n, dim, keys):
@@ -300,6 +302,17 @@ class Engine:
         _check(self.lib.sph_adjoint_step(self.h, int(slot), _ptr(lam_r), _ptr(lam_u),
                                          _ptr(lam_a_in), _ptr(lam_a_out), _stream()))
 
+    def set_wall_layer(self, layer, offset, cutoff):
+        """Recompute the wall normals every step from a static fine wall layer
+        (host ``(m, dim)`` float32 array; ``None`` switches it off)."""
+        if layer is None:
+            _check(self.lib.sph_set_wall_layer(self.h, None, 0, None, 0.0))
+            return
+        arr = np.ascontiguousarray(np.asarray(layer, dtype=np.float32))
+        off = (ctypes.c_double * 3)(*[float(x) for x in list(offset) + [0.0] * (3 - len(offset))])
+        _check(self.lib.sph_set_wall_layer(self.h, arr.ctypes.data, int(arr.shape[0]), off,
+                                           float(cutoff)))
+
     def read_status(self, clear=False):
         s = ctypes.c_uint32(0)
         _check(self.lib.sph_read_status(self.h, ctypes.byref(s), int(bool(clear)), _stream()))
@@ -331,7 +344,7 @@ class Engine:
         inputs' other fields (tag, mass, eta, nw, g_ext)."""
         vin, vout = self._views
         v = SphStateView.from_buffer_copy(vin)
-        for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "T", "dTdt"):
+        for k in ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "T", "dTdt", "nw"):
             if getattr(vout, k):  # a field not written is the input's own
                 setattr(v, k, getattr(vout, k))
         return v

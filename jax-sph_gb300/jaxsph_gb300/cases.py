@@ -152,6 +152,7 @@ class CaseSetup:
     bc_fn: BC
     solver: dict = field(default_factory=dict)  # WCSPH keyword arguments
     tvf: float = 0.0
+    nw_fn: object = None  # WallNormals when moving walls need recomputed normals
 
     @property
     def n(self):
@@ -180,7 +181,7 @@ def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref
             is_bc_trick=False, density_evolution=False, artificial_alpha=0.0,
             free_slip=False, eta_limiter=3, g_ext=None, bc=None, nw=None, dtype=np.float32,
             diff_alpha=0.01, diff_delta=0.1, rho_renorm=False, heat_conduction=False,
-            T_ref=1.0, kappa_ref=0.0, Cp_ref=0.0):
+            T_ref=1.0, kappa_ref=0.0, Cp_ref=0.0, wall_layer=None):
     """The common part of ``initialize`` (case_setup.py:71-231)."""
     c_ref = c_ref_factor * u_ref
     p_ref = rho_ref * c_ref ** 2 / gamma
@@ -227,9 +228,15 @@ def _finish(name, dim, dx, box, r, tag, v, *, rho_ref=1.0, viscosity=0.01, u_ref
                   artificial_alpha=artificial_alpha,
                   is_free_slip=free_slip, eta_limiter=eta_limiter,
                   diff_alpha=diff_alpha, diff_delta=diff_delta)  # defaults.py:96-99
-    return CaseSetup(name, dim, dx, np.asarray(box, dtype=np.float64), state, dt,
-                     sequence_length, c_ref, p_ref, p_bg, u_ref, viscosity, eos, g_ext, bc,
-                     solver, tvf)
+    setup = CaseSetup(name, dim, dx, np.asarray(box, dtype=np.float64), state, dt,
+                      sequence_length, c_ref, p_ref, p_bg, u_ref, viscosity, eos, g_ext, bc,
+                      solver, tvf)
+    if wall_layer is not None and (tag == MOVING_WALL).any() and (
+            (solver_name == "RIE" or free_slip) and is_bc_trick):
+        # case_setup.py:209-218: moving walls recompute their normals each step
+        setup.nw_fn = WallNormals(*wall_layer, box=box, wall=np.isin(
+            tag, [SOLID_WALL, MOVING_WALL, DIRICHLET_WALL]))
+    return setup
 
 
 # ------------------------------------------------------------ cases
@@ -265,6 +272,53 @@ def tgv(dim=2, dx=None, viscosity=None, solver_name="SPH", tvf=None, kernel=None
     return _finish(f"tgv{dim}d", dim, dx, box, r, tag, v, viscosity=viscosity,
                    solver_name=solver_name, kernel=kernel, tvf=tvf, t_end=t_end, dtype=dtype,
                    **kw)
+
+
+class WallNormals:
+    """The integrator's ``nw_fn`` for moving walls (compute_nws_jax_wrapper,
+    utils.py:197-275) with a GPU spec: every wall particle's normal is the
+    normalised displacement from ``r - offset`` to its nearest point of a
+    static wall layer discretised 5x finer, searched within ``cutoff``
+    (layer point 0 never counts, as in the reference; ties go to the lowest
+    index); fluid normals are zero."""
+
+    def __init__(self, layer, offset, cutoff, box, wall):
+        self.spec = dict(layer=np.ascontiguousarray(layer, dtype=np.float32),
+                         offset=tuple(float(x) for x in offset), cutoff=float(cutoff))
+        self.box = np.asarray(box, dtype=np.float64)
+        self.wall = np.asarray(wall, dtype=bool)
+
+    def __call__(self, r):
+        from .space import periodic
+
+        disp, _ = periodic(self.box)
+        wall = torch.as_tensor(self.wall, device=r.device)
+        off = torch.as_tensor(self.spec["offset"][:r.shape[1]], dtype=torch.float32,
+                              device=r.device)
+        layer = torch.as_tensor(self.spec["layer"], device=r.device)
+        p = r[wall].float() - off
+        d_in = disp(p[:, None, :], layer[None, :, :])  # membership: metric(wall, layer)
+        ok = (d_in * d_in).sum(-1) < np.float32(self.spec["cutoff"] ** 2)
+        ok[:, 0] = False
+        dr = disp(layer[None, :, :], p[:, None, :])
+        dist = torch.sqrt((dr * dr).sum(-1))
+        dist = torch.where(ok, dist, torch.full_like(dist, float("inf")))
+        k = torch.argmin(dist, dim=1)  # the first of equally near points
+        rows = torch.arange(p.shape[0], device=r.device)
+        best = dist[rows, k]
+        nw_w = dr[rows, k] / (best[:, None] + EPS)
+        nw_w = torch.where(torch.isfinite(best)[:, None], nw_w, torch.zeros_like(nw_w))
+        nw = torch.zeros_like(r, dtype=torch.float32)
+        nw[wall] = nw_w
+        return nw
+
+
+def _wall_layer(dx, n_walls, offset_vec, wall_part_fn, dtype):
+    """The fine layer of compute_nws (utils.py:214-217), in float32 like the
+    reference, with the offset and the search radius."""
+    off = np.asarray(offset_vec, dtype=np.float64)
+    layer = (wall_part_fn(dx / 5, 1).astype(dtype) - (off / n_walls / 5).astype(dtype))
+    return layer.astype(dtype), off.astype(dtype), dx * n_walls * 2.0 ** 0.5 * 1.01
 
 
 def _nws_scipy(r, tag, dx, n_walls, offset_vec, wall_part_fn, dtype):
@@ -323,9 +377,18 @@ def lid_driven_cavity(dx=0.02, n_walls=3, viscosity=0.01, u_lid=1.0, dtype=np.fl
     tag = np.concatenate([np.full(len(r_w), SOLID_WALL), np.full(len(r_f), FLUID)])
     tag = np.where(r[:, 1].astype(np.float64) > box[1] - n_walls * dx, MOVING_WALL, tag)
     v = np.zeros_like(r, dtype=np.float64)
+
+    def walls(ddx, nw_):  # LDC._init_walls_2d (cases/ldc.py:49-51)
+        return pos_box_2d(np.ones(2), ddx, nw_, dtype)
+
+    offset_vec = np.ones(2) * n_walls * dx  # LDC._offset_vec (cases/ldc.py:103-108)
+    nw = None
+    if kw.get("solver_name") == "RIE" or kw.get("free_slip"):
+        nw = _nws_scipy(r, tag, dx, n_walls, offset_vec, walls, dtype)
     return _finish("ldc", 2, dx, box, r, tag, v, viscosity=viscosity, p_bg_factor=0.01,
                    is_bc_trick=True, t_end=t_end, dt=dt,
-                   bc=BC(_lib.BC_LID, (u_lid, 0.0, 0.0)), dtype=dtype, **kw)
+                   bc=BC(_lib.BC_LID, (u_lid, 0.0, 0.0)), nw=nw, dtype=dtype,
+                   wall_layer=_wall_layer(dx, n_walls, offset_vec, walls, dtype), **kw)
 
 
 def poiseuille(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, g_ext_magnitude=1000.0,
@@ -424,7 +487,9 @@ def couette(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, u_x_wall=1.25,
     # (cases/cf.py:156-171): the lid boundary condition
     return _finish("cf", 2, dx, box, r, tag, v, viscosity=viscosity, u_ref=u_ref,
                    is_bc_trick=True, t_end=t_end, dt=dt,
-                   bc=BC(_lib.BC_LID, (u_x_wall, 0.0, 0.0)), nw=nw, dtype=dtype, **kw)
+                   bc=BC(_lib.BC_LID, (u_x_wall, 0.0, 0.0)), nw=nw, dtype=dtype,
+                   wall_layer=_wall_layer(dx, n_walls, np.array([0.0, dxn]), walls, dtype),
+                   **kw)
 
 
 def fourier_perturbation(r, sigma=0.1, kmax=8, seed=1):

@@ -12,12 +12,13 @@ def si_euler(tvf, model, shift_fn, bc_fn, nw_fn):
     solver = getattr(model, "__wcsph__", None)
     if solver is None:
         raise NotImplementedError("model must be WCSPH(...).forward_wrapper() of jaxsph_gb300")
-    if nw_fn is not None:
-        raise NotImplementedError("moving-wall normal recomputation is not on the path")
+    if nw_fn is not None and getattr(nw_fn, "spec", None) is None:
+        raise NotImplementedError(
+            "nw_fn must be the GPU descriptor jaxsph_gb300.cases.WallNormals")
     tvf = float(tvf)
 
     def advance(dt, state, neighbors):
-        return solver.advance(float(dt), tvf, state, neighbors, bc_fn)
+        return solver.advance(float(dt), tvf, state, neighbors, bc_fn, nw_fn)
 
     advance.__si_euler__ = (solver, tvf, bc_fn)
     return advance

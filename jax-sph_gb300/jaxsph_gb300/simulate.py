@@ -79,6 +79,12 @@ class Simulation:
             if v.g_spec()["kind"] == _lib.GEXT_ARRAY:
                 raise NotImplementedError("resident rollouts need g_ext_fn with a GPU spec")
         self.engine = _lib.Engine(cfg, self.cases)
+        self.wall_normals = any(s.nw_fn is not None for s in self.setups)
+        if self.wall_normals:
+            if len(self.setups) > 1:
+                raise NotImplementedError("moving-wall normals need a single case")
+            spec = self.setups[0].nw_fn.spec
+            self.engine.set_wall_layer(spec["layer"], spec["offset"], spec["cutoff"])
         self.sizes = [s.n for s in self.setups]
         self.dim = self.setups[0].dim
         self.steps_done = 0
@@ -140,10 +146,12 @@ class Simulation:
         keys = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
         if "T" in full:
             keys = keys + ("T", "dTdt")
+        if self.wall_normals:
+            keys = keys + ("nw",)  # recomputed every step
         out = {k: torch.empty_like(full[k]) for k in keys}
         self.engine.get_state(out)
         for k in ("tag", "mass", "eta", "nw", "kappa", "Cp"):
-            if k in full:
+            if k in full and k not in out:
                 out[k] = full[k]
         if not split:
             return out

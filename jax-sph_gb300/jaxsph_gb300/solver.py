@@ -162,6 +162,14 @@ class WCSPH:
             e.update_cases([case])
         return e
 
+    @staticmethod
+    def _wall_layer(e, nw_fn):
+        """Give the engine the moving walls' layer once (it keeps it)."""
+        if getattr(e, "_nw_fn", None) is not nw_fn:
+            spec = nw_fn.spec
+            e.set_wall_layer(spec["layer"], spec["offset"], spec["cutoff"])
+            e._nw_fn = nw_fn
+
     def _load(self, state, neighbors, case, load=True):
         nl_fns = neighbors._fns
         st = prepare_state(state, self.dim, heat=self.is_heat_conduction)
@@ -207,7 +215,7 @@ class WCSPH:
         forward.__wcsph__ = self
         return forward
 
-    def advance(self, dt, tvf, state, neighbors, bc_fn):
+    def advance(self, dt, tvf, state, neighbors, bc_fn, nw_fn=None):
         """One fused si_euler step on the GPU (integrator.py:22-56).
 
         A state of pinned (page-locked) host tensors is copied to the GPU and
@@ -246,6 +254,8 @@ class WCSPH:
         ref = torch.as_tensor(neighbors.reference_position)
         status = None
         host = st is not None
+        if nw_fn is not None:
+            self._wall_layer(self.engine(nl_fns, case), nw_fn)
         if host:
             e = self.engine(nl_fns, case)
             cap = neighbors.cell_list_capacity
@@ -255,6 +265,8 @@ class WCSPH:
             keys = OUT_KEYS if self.is_rho_evol else OUT_KEYS_SUMMATION
             if self.is_heat_conduction:
                 keys = keys + HEAT_OUT_KEYS
+            if nw_fn is not None:
+                keys = keys + ("nw",)  # recomputed after the drift (integrator.py:33-34)
             # results and the status word in one pinned block: the status is
             # host memory, read without a device synchronisation
             out, status_h, vout = _lib.host_outputs(key[1], self.dim, keys)
@@ -271,6 +283,8 @@ class WCSPH:
         if not host:
             e, st = self._load(state, neighbors, case, load=False)
             out = empty_outputs(st, self.is_heat_conduction)
+            if nw_fn is not None:
+                out["nw"] = torch.empty_like(st["nw"])
             if thr > 0.0:
                 ref = ref.to(device=st["r"].device, dtype=torch.float32).contiguous()
             # one fused call: load, step, read back; the status stays a device

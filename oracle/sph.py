@@ -433,17 +433,52 @@ class WCSPH:
 
 
 # ---------------------------------------------------------------- integrator
-def si_euler_advance(dt, tvf, state, nbrs, nl_fns, solver, bc_fn):
-    """``si_euler.advance`` (integrator.py:22-56); moving-wall normals are out of scope."""
+def si_euler_advance(dt, tvf, state, nbrs, nl_fns, solver, bc_fn, nw_fn=None):
+    """``si_euler.advance`` (integrator.py:22-56)."""
     side = torch.as_tensor(solver.box, dtype=state["r"].dtype)
     st = dict(state)
     st["u"] = st["u"] + 1.0 * dt * st["dudt"]
     st["v"] = st["u"] + tvf * 0.5 * dt * st["dvdt"]
     st["r"] = space.periodic_shift(side, st["r"], 1.0 * dt * st["v"])
+    if nw_fn is not None:                                                 # :33-34
+        st["nw"] = nw_fn(st["r"])
     nbrs = nl_fns.update(st["r"], nbrs)
     st = solver.forward(st, nbrs.idx)
     st = bc_fn(st)
     return st, nbrs
+
+
+def make_wall_normals(layer, offset, cutoff, box, wall):
+    """``compute_nws_jax_wrapper`` body (utils.py:197-275): for each wall
+    particle, the displacement to its nearest layer point among the
+    neighbour-list candidates within ``cutoff``, normalised; zero without one.
+    The reference's candidates are the dense-list entries with index >
+    len(r_walls), so layer point 0 never counts. Its argmin takes the first
+    minimum in dense-list order; here ties go to the lowest layer index (the
+    same point whenever the nearest one is unique)."""
+    layer = torch.as_tensor(layer)
+    wall = torch.as_tensor(wall)
+
+    def nw_fn(r):
+        side = torch.as_tensor(box, dtype=r.dtype)
+        L = layer.to(r.dtype)
+        p = r[wall] - torch.as_tensor(offset, dtype=r.dtype)
+        metric = space.periodic_displacement(side, p[:, None, :] - L[None, :, :])
+        ok = (metric * metric).sum(-1) < cutoff ** 2
+        ok[:, 0] = False
+        dr = space.periodic_displacement(side, L[None, :, :] - p[:, None, :])
+        dist = space.distance(dr)
+        dist = torch.where(ok, dist, torch.full_like(dist, math.inf))
+        k = torch.argmin(dist, dim=1)
+        rows = torch.arange(p.shape[0])
+        best = dist[rows, k]
+        nw_w = dr[rows, k] / (best[:, None] + EPS)
+        nw_w = torch.where(torch.isfinite(best)[:, None], nw_w, torch.zeros_like(nw_w))
+        nw = torch.zeros_like(r)
+        nw[wall] = nw_w
+        return nw
+
+    return nw_fn
 
 
 # ---------------------------------------------------------------- case callbacks

@@ -75,14 +75,26 @@ def oracle_case(setup, dtype=torch.float64, mask_self=False, state=None):
     return solver, fns, oracle_bc(setup), st
 
 
+def oracle_nw_fn(setup):
+    """The oracle's moving-wall normals for a case with a WallNormals nw_fn."""
+    if setup.nw_fn is None:
+        return None
+    spec = setup.nw_fn.spec
+    return oracle.sph.make_wall_normals(spec["layer"], spec["offset"][:setup.dim],
+                                        spec["cutoff"], setup.box, setup.nw_fn.wall)
+
+
 def oracle_rollout(setup, steps, dtype=torch.float64, state=None):
     solver, fns, bc, st = oracle_case(setup, dtype, state=state)
+    nw_fn = oracle_nw_fn(setup)
     nb = fns.allocate(st["r"])
     for _ in range(steps):
-        st_, nb_ = oracle.sph.si_euler_advance(setup.dt, setup.tvf, st, nb, fns, solver, bc)
+        st_, nb_ = oracle.sph.si_euler_advance(setup.dt, setup.tvf, st, nb, fns, solver, bc,
+                                               nw_fn)
         if nb_.did_buffer_overflow:  # simulate.py:120-128: re-allocate and redo the step
             nb = fns.allocate(st["r"])
-            st, nb = oracle.sph.si_euler_advance(setup.dt, setup.tvf, st, nb, fns, solver, bc)
+            st, nb = oracle.sph.si_euler_advance(setup.dt, setup.tvf, st, nb, fns, solver, bc,
+                                                 nw_fn)
         else:
             st, nb = st_, nb_
     return st

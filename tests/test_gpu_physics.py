@@ -62,6 +62,8 @@ def small_cases():
         "ht_rie": lambda: cases.heat_transfer(dx=0.04, solver_name="RIE"),
         "ht_delta_evol": lambda: cases.heat_transfer(dx=0.04, solver_name="DELTA",
                                                      density_evolution=True),
+        # moving lid with Riemann walls: normals recomputed every step
+        "ldc_rie": lambda: cases.lid_driven_cavity(dx=0.04, solver_name="RIE"),
     }
 
 
@@ -116,7 +118,8 @@ def test_forward_matches_oracle(name):
 
 
 @pytest.mark.parametrize("name", ["tgv2d_sph", "tgv3d_sph_tvf", "db_rie", "ldc_sph", "pf_sph",
-                                  "db_delta_evol", "tgv2d_delta_evol_renorm", "ht_sph"])
+                                  "db_delta_evol", "tgv2d_delta_evol_renorm", "ht_sph",
+                                  "ldc_rie", "ldc_sph_freeslip_av"])
 def test_rollout_matches_oracle(name):
     setup = small_cases()[name]()
     steps = 20
@@ -141,6 +144,8 @@ def test_rollout_matches_oracle(name):
                                           10 * err(ref32["u"], ref["u"]))
     if "T" in ref:
         assert err(got["T"], ref["T"]) <= max(1e-5, 10 * err(ref32["T"], ref["T"]))
+    if setup.nw_fn is not None:  # the recomputed normals of the moved walls
+        assert err(got["nw"], ref["nw"]) <= max(1e-5, 10 * err(ref32["nw"], ref["nw"]))
 
 
 def test_drop_in_advance_equals_resident_rollout():
@@ -328,6 +333,30 @@ def test_drop_in_heat_transfer_matches_the_resident_rollout():
     for k in ("r", "u", "rho", "T", "dTdt"):
         a, b = st[k].double(), got[k].double().cpu()
         assert float((a - b).abs().max()) <= 1e-5 * (float(b.abs().max()) + 1e-30), k
+
+
+def test_drop_in_moving_wall_normals():
+    # si_euler with the case's nw_fn: the drop-in step returns the recomputed
+    # normals, and they follow the resident rollout
+    setup = cases.lid_driven_cavity(dx=0.04, solver_name="RIE")
+    wc = gpu_solver(setup)
+    fns = simulate.make_neighbor_fns(setup, wc)
+    _, shift = setup.space()
+    adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, setup.nw_fn)
+    st = setup.to("cuda")
+    nb = fns.allocate(st["r"])
+    for _ in range(5):
+        st, nb = adv(setup.dt, st, nb)
+    want = setup.nw_fn(st["r"])
+    assert float((st["nw"] - want).abs().max()) < 1e-5
+    sim = simulate.Simulation(setup)
+    sim.run(5)
+    got = sim.state()[0]
+    for k in ("r", "u", "nw"):
+        a, b = st[k].double(), got[k].double()
+        assert float((a - b).abs().max()) <= 1e-5 * (float(b.abs().max()) + 1e-30), k
+    with pytest.raises(NotImplementedError):
+        integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, lambda r: r)
 
 
 def test_drop_in_advance_rejects_pageable_host_arrays():

@@ -200,6 +200,37 @@ def test_heat_transfer_bc_matches_the_oracle():
     assert (got["T"][st["tag"] == 3] == 1.23).all()
 
 
+def test_moving_wall_normals_match_the_oracle():
+    """The nw_fn of a moving-lid case (compute_nws_jax_wrapper): the case's
+    torch restatement equals the oracle's, and both equal the scipy normals
+    of the initial state except where the nearest layer point is point 0
+    (which the reference's recomputation never takes: its corner block)."""
+    from jaxsph_gb300 import cases
+    from oracle_setup import oracle_nw_fn
+
+    setup = cases.lid_driven_cavity(dx=0.04, solver_name="RIE")
+    assert setup.nw_fn is not None
+    r = setup.state["r"]
+    got = setup.nw_fn(r)
+    want = oracle_nw_fn(setup)(r.double())
+    # float32 normals carry eps |r| / |dr| of rounding (|r| ~ 1, |dr| >= dx / 10)
+    assert (got.double() - want).abs().max().item() < 1e-4
+    moved = torch.remainder(r + torch.tensor([0.013, 0.0]), torch.as_tensor(setup.box).float())
+    assert (setup.nw_fn(moved).double() - oracle_nw_fn(setup)(moved.double())).abs().max() < 1e-4
+    # against scipy on the initial positions
+    layer = setup.nw_fn.spec["layer"].astype(np.float64)
+    wall = setup.nw_fn.wall
+    p = r.double().numpy()[wall] - np.asarray(setup.nw_fn.spec["offset"][:2])
+    d = np.linalg.norm(layer[None, :, :] - p[:, None, :], axis=-1)
+    nearest0 = np.argmin(d, axis=1) == 0
+    diff = (got - setup.state["nw"]).abs().max(1).values.numpy()[wall]
+    assert (diff[~nearest0] < 1e-5).all() and nearest0.any()
+    assert setup.state["nw"][~torch.as_tensor(wall)].abs().max() == 0
+    # no moving walls or no normals needed: no recomputation
+    assert cases.lid_driven_cavity(dx=0.04).nw_fn is None
+    assert cases.poiseuille(dx=0.05, solver_name="RIE").nw_fn is None
+
+
 def test_oracle_gradient_through_steps():
     """torch autograd through the float64 oracle (the gradient oracle of the adjoint)."""
     from jaxsph_gb300 import cases
