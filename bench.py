@@ -202,17 +202,21 @@ def e2e_rate(setup, steps, device):
     _, shift = setup.space()
     adv = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, None)
     keys_in = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
-    keys_out = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
     host = {k: setup.state[k].to(torch.int32 if k == "tag" else torch.float32)
             .contiguous().pin_memory() for k in keys_in}
-    h2d = sum(host[k].numel() * host[k].element_size() for k in keys_in)
-    d2h = sum(host[k].numel() * host[k].element_size() for k in keys_out)
+    # the bytes that cross the host link each step: the step reads neither v
+    # (the kick recomputes it), the old p, drho/dt (a summation carries it
+    # over) nor nw (no walls); the results are r, u, v, dudt, dvdt, rho, p
+    moved_in = ("r", "tag", "u", "dudt", "dvdt", "rho", "mass", "eta")
+    moved_out = ("r", "u", "v", "dudt", "dvdt", "rho", "p")
+    h2d = sum(host[k].numel() * host[k].element_size() for k in moved_in)
+    d2h = sum(host[k].numel() * host[k].element_size() for k in moved_out)
     nb = fns.allocate(host["r"])
     st = host
     for _ in range(3):  # warm-up (engine creation, pinned output blocks)
         st, nb = adv(setup.dt, st, nb)
     torch.cuda.synchronize()
-    assert all(st[k].device.type == "cpu" and st[k].is_pinned() for k in keys_out)
+    assert all(st[k].device.type == "cpu" and st[k].is_pinned() for k in moved_out)
     times, redone = [], 0
     for _ in range(steps):
         t0 = time.perf_counter()
@@ -295,14 +299,23 @@ def adjoint_form(device, steps=100, checkpoint_every=10):
     target = adjoint.AdjointRollout(b, steps, checkpoint_every).forward(b.state["u"].to(device))
     roll = adjoint.AdjointRollout(a, steps, checkpoint_every, device=device)
     u0 = a.state["u"].to(device)
-    roll.forward(u0)  # warm-up (graphs, allocation)
+
+    def gradient():
+        u = u0.clone().requires_grad_(True)
+        loss = adjoint.position_mse(adjoint.rollout(u, roll), target, a.box)
+        (g,) = torch.autograd.grad(loss, u)
+        return loss, g
+
+    # warm-up: one whole gradient (graphs, allocations, the autograd engine's
+    # and torch's own first-use costs stay out of the timed region)
+    gradient()
     torch.cuda.synchronize()
+    reps = 3
     t0 = time.perf_counter()
-    u = u0.clone().requires_grad_(True)
-    loss = adjoint.position_mse(adjoint.rollout(u, roll), target, a.box)
-    (g,) = torch.autograd.grad(loss, u)
+    for _ in range(reps):
+        loss, g = gradient()
     torch.cuda.synchronize()
-    t_grad = time.perf_counter() - t0
+    t_grad = (time.perf_counter() - t0) / reps
     plain = simulate.Simulation(a, device=device)
     plain.run(3)
     torch.cuda.synchronize()
@@ -315,8 +328,9 @@ def adjoint_form(device, steps=100, checkpoint_every=10):
                         f"gradient of the final-position MSE w.r.t. the initial velocity",
             "value": a.n * steps / t_grad, "unit": UNIT,
             "note": "forward (with checkpoints) + reverse sweep, wall clock",
-            "checkpoint_every": checkpoint_every, "loss": float(loss),
-            "grad_norm": float(g.norm()), "plain_forward_value": a.n * steps / t_plain,
+            "checkpoint_every": checkpoint_every, "loss": float(loss.detach()),
+            "grad_norm": float(g.norm()), "timed_gradients": reps,
+            "plain_forward_value": a.n * steps / t_plain,
             "ratio_vs_plain_forward": t_plain / t_grad}
 
 

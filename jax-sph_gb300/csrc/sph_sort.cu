@@ -334,7 +334,7 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
 template <int DIM>
 __global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* cases,
                        const float4* rref, int* cref_count, unsigned* vflag, unsigned* status,
-                       bool from_forward, bool apply_bc, WallLayer layer) {
+                       bool from_forward, bool apply_bc) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   bool rebuild = false, over = false;
@@ -356,10 +356,6 @@ __global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* 
     b.P4[i] = r;
     b.U4[i] = make_float4(u.x, u.y, u.z, f.rho);
     b.V4[i] = make_float4(v.x, v.y, v.z, f.p);
-    // moving walls: the normals follow the new positions (integrator.py:33-34)
-    if (layer.n > 0 && b.NW4)
-      b.NW4[i] = is_wall(tag_of(meta)) ? wall_normal<DIM>(r, layer, c)
-                                       : make_float4(0.f, 0.f, 0.f, 0.f);
     if (b.TH4) {
       const float4 t = b.TH4[i];
       b.TH4[i] = make_float4(f.T, f.dTdt, t.z, t.w);
@@ -388,6 +384,17 @@ __global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* 
     }
   }
   if (__any_sync(0xffffffffu, over) && lane == 0) atomicOr(status, SPH_CELL_LIST_OVERFLOW);
+}
+
+// Wall normals of the moved walls (a pass of its own so that the kick keeps
+// its registers): walls point to their nearest layer point, fluid normals are 0.
+template <int DIM>
+__global__ void k_wall_normals(long long N, Buffers b, const CaseDev* cases, WallLayer layer) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int meta = b.META[i];
+  b.NW4[i] = is_wall(tag_of(meta)) ? wall_normal<DIM>(b.P4[i], layer, cases[case_of(meta)])
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
 }
 
 // ------------------------------------------------------------------ scan
@@ -659,11 +666,19 @@ void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_
   int g = nblocks(L.N);
   if (L.dim == 3)
     k_kick<3><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, L.rref, L.cref_count, L.vflag,
-                                          L.status, from_forward, apply_bc, L.layer);
+                                          L.status, from_forward, apply_bc);
   else
     k_kick<2><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, L.rref, L.cref_count, L.vflag,
-                                          L.status, from_forward, apply_bc, L.layer);
+                                          L.status, from_forward, apply_bc);
   count_launch(L);
+  // moving walls: the normals follow the new positions (integrator.py:33-34)
+  if (L.layer.n > 0 && b.NW4) {
+    if (L.dim == 3)
+      k_wall_normals<3><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, L.layer);
+    else
+      k_wall_normals<2><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, L.layer);
+    count_launch(L);
+  }
 }
 
 // Capacities of an allocate (jax_md/partition.py:195-199, :956-971), per
