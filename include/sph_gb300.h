@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPH_ABI_VERSION 4
+#define SPH_ABI_VERSION 5
 
 /* Reference PartitionErrorCode bits (jax_sph/jax_md/partition.py:453-457). */
 #define SPH_NEIGHBOR_LIST_OVERFLOW 0x1u
@@ -106,8 +106,16 @@ typedef struct SphConfig {
                              (rho_renorm_fn, solver.py:167-173, :755-793) */
   int32_t is_heat_conduction; /* temperature equation (solver.py:591-610, :832-850) and
                                  the wall temperature BC (:518-526, :556-565) */
-  int32_t pad2;
+  int32_t nl_backend;     /* SPH_NL_JAXMD: the reference metric in float32 (jax_md);
+                             SPH_NL_MATSCIPY: float64 minimum-image distance < cutoff
+                             (partition.py:356-482, matscipy.neighbours) */
 } SphConfig;
+
+/* Neighbour-list backends. Particles tagged SPH_TAG_PAD (-1, Tag.PAD_VALUE,
+ * utils.py:25) pad a state to a fixed size: they are in no neighbour list
+ * with either backend, and are kicked like any particle. */
+enum { SPH_NL_JAXMD = 0, SPH_NL_MATSCIPY = 1 };
+#define SPH_TAG_PAD (-1)
 
 /* Per-case parameters (all in the reference's units). */
 typedef struct SphCase {

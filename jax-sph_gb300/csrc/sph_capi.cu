@@ -252,6 +252,11 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
   c.cell_cap = INT_MAX;
   c.edge_cap = LLONG_MAX;
   c.cutoff_sq = cut * cut;
+  // matscipy backend: the cutoff and box as the reference passes them to
+  // matscipy (float64), distances in float64 (partition.py:393-395)
+  c.f64_metric = cfg.nl_backend == SPH_NL_MATSCIPY;
+  c.cut64_sq = in.r_cutoff * in.r_cutoff;
+  for (int d = 0; d < 3; ++d) c.mat_box[d] = d < dim ? in.box[d] : 1.0;
   // kernels (kernel.py:51-103): sigma from the Python-float expressions
   const double ih = 1.0 / in.h;
   double sigma;
@@ -530,6 +535,8 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
     return fail((int)SPH_ERR_INVALID_ARG, "Cell list spatial dimension must be 2 or 3");
   if (cfg->kernel != SPH_KERNEL_QSK && cfg->kernel != SPH_KERNEL_WC2K)
     return fail((int)SPH_ERR_INVALID_ARG, "kernel must be QSK or WC2K");
+  if (cfg->nl_backend != SPH_NL_JAXMD && cfg->nl_backend != SPH_NL_MATSCIPY)
+    return fail((int)SPH_ERR_INVALID_ARG, "nl_backend must be SPH_NL_JAXMD or SPH_NL_MATSCIPY");
   if (cfg->solver != SPH_SOLVER_SPH && cfg->solver != SPH_SOLVER_RIE &&
       cfg->solver != SPH_SOLVER_DELTA)
     return fail((int)SPH_ERR_INVALID_ARG, "solver must be SPH, RIE or DELTA");
@@ -554,7 +561,7 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
       return fail((int)SPH_ERR_INVALID_ARG, "case " + std::to_string(i) + ": " + err);
     }
     h->hc[i].cref_off = (int)ref_cells;
-    cells += h->hc[i].ncell;
+    cells += h->hc[i].ncell + 1;  // + the parking cell of padding particles
     ref_cells += h->hc[i].ncref;
     off[i + 1] = off[i] + cases[i].n;
   }

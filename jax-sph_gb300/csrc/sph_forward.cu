@@ -73,6 +73,10 @@ k_verlet(long long N, Buffers b, const CaseDev* cases, const int* cellid, const 
   int* keys = s_v + kv * bs;
   const long long i = blockIdx.x * (long long)bs + tid;
   if (i >= N) return;
+  if (tag_of(b.META[i]) == PAD) {  // padding has no candidates
+    vcnt[i] = 0;
+    return;
+  }
   const CaseDev& c = cases[case_of(b.META[i])];
   const float4 ri = b.P4[i];
   int m = 0;
@@ -224,7 +228,7 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
                                 ++m;
                               });
     }
-    cnt = m + (self_term ? 1 : 0);
+    cnt = tag == PAD ? 0 : m + (self_term ? 1 : 0);
     nl.cnt[i] = m;
 
     // phase 2: pair physics over the senders

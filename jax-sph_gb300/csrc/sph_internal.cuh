@@ -30,6 +30,9 @@ constexpr int kTagBits = 4;
 constexpr int kTagMask = 0xF;
 
 enum Tag { FLUID = 0, SOLID_WALL = 1, MOVING_WALL = 2, DIRICHLET_WALL = 3 };
+// Padding particles (Tag.PAD_VALUE = -1 in the state): binned into a cell of
+// their own past the case's grid that no walk visits, with no lists.
+constexpr int PAD = 15;
 
 // Neighbour-list slots per particle. The density pass stages them in shared
 // memory (kListSlots * 256 threads * 4 B = 40 KB per block); a particle with
@@ -66,6 +69,8 @@ struct CaseDev {
   int cell_cap;       // cell capacity for the CELL_LIST_OVERFLOW test
   long long edge_cap; // neighbour-list capacity for NEIGHBOR_LIST_OVERFLOW
   float cutoff_sq;
+  int f64_metric;     // matscipy backend: float64 minimum-image distance < cutoff
+  double cut64_sq, mat_box[3];
   float inv_h, sigma, dsigma;  // W(r) = sigma*f(q); dW/dr = dsigma*g(q)
   float dt, cv;       // f32(dt), f32(tvf*0.5*dt) of si_euler
   float dt_rho;       // WCSPH dt of density evolution
@@ -159,8 +164,24 @@ __device__ __forceinline__ float sqd(const float3& d) {
 
 // Neighbour-list membership of edge (receiver a, sender b): the reference
 // prunes with metric(r[sender], r[receiver]) < cutoff_sq (partition.py:897).
+// The matscipy backend's membership: the pair's distance in float64 from
+// the float32 positions, nearest periodic image, strictly below the cutoff.
+template <int DIM>
+__device__ __noinline__ bool is_edge_f64(const float4& recv, const float4& send,
+                                         const CaseDev& c) {
+  const double p[3] = {(double)send.x - (double)recv.x, (double)send.y - (double)recv.y,
+                       DIM == 3 ? (double)send.z - (double)recv.z : 0.0};
+  double s = 0.0;
+  for (int d = 0; d < DIM; ++d) {
+    const double x = p[d] - c.mat_box[d] * rint(p[d] / c.mat_box[d]);
+    s += x * x;
+  }
+  return s < c.cut64_sq;
+}
+
 template <int DIM>
 __device__ __forceinline__ bool is_edge(const float4& recv, const float4& send, const CaseDev& c) {
+  if (c.f64_metric) return is_edge_f64<DIM>(recv, send, c);
   return sqd<DIM>(pdisp3<DIM>(send, recv, c)) < c.cutoff_sq;
 }
 

@@ -47,7 +47,10 @@ __global__ void k_pack(SphStateView s, int dim, Buffers o, const long long* case
     int c = 0;
     while (c + 1 < n_cases && i >= case_off[c + 1]) ++c;
     int tag = s.tag[i];
-    if (tag < 0 || tag > 3) atomicOr(status, SPH_ERR_INVALID_ARG);
+    if (tag == SPH_TAG_PAD)
+      tag = PAD;
+    else if (tag < 0 || tag > 3)
+      atomicOr(status, SPH_ERR_INVALID_ARG);
     float4 r = ld4(s.r, dim, i);
     r.w = s.mass[i];
     float4 u = ld4(s.u, dim, i);
@@ -243,7 +246,8 @@ __global__ void k_hash_count(long long N, Buffers in, const float4* R4, const Ca
         kick_drift<DIM>(r, u, v, in.A4[k], in.A2[k], c);
       }
     }
-    cell = c.cell_off + cell_hash<DIM>(r, c, status);
+    // padding goes to the parking cell past the grid: no walk visits it
+    cell = c.cell_off + (tag_of(meta) == PAD ? c.ncell : cell_hash<DIM>(r, c, status));
   }
   unsigned mask = __ballot_sync(kFull, valid);
   if (!valid) return;
@@ -316,8 +320,8 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
     cellid[dest] = cell;
     if (rref) rref[dest] = r;
     if (inv) inv[key] = dest;
-    // one test per occupied cell, against the reference's cell
-    if (c.use_cells && q == a)
+    // one test per occupied cell (of the grid), against the reference's cell
+    if (c.use_cells && q == a && cell - c.cell_off < c.ncell)
       over = ref_cell_occupancy<DIM>(c, cell - c.cell_off, start) > c.cell_cap;
   }
   if (__any_sync(kFull, over) && (threadIdx.x & 31) == 0) atomicOr(status, SPH_CELL_LIST_OVERFLOW);
@@ -365,8 +369,9 @@ __global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* 
     dx = fmaf(-c.box[0], rintf(dx * c.inv_box[0]), dx);
     dy = fmaf(-c.box[1], rintf(dy * c.inv_box[1]), dy);
     if (DIM == 3) dz = fmaf(-c.box[2], rintf(dz * c.inv_box[2]), dz);
-    rebuild = !(dx * dx + dy * dy + dz * dz <= c.v_dmax2);  // NaN rebuilds too
-    if (c.use_cells) {
+    const bool pad = tag_of(meta) == PAD;  // no lists, no cell
+    rebuild = !pad && !(dx * dx + dy * dy + dz * dz <= c.v_dmax2);  // NaN rebuilds too
+    if (c.use_cells && !pad) {
       key = ref_cell_hash<DIM>(r, c);
       if (key < 0) atomicOr(status, SPH_ERR_NONFINITE);
       else key += c.cref_off;
@@ -507,6 +512,10 @@ __global__ void k_row_counts(long long N, Buffers b, const CaseDev* cases, const
   const CaseDev& c = cases[case_of(meta)];
   float4 rs = b.P4[s];
   int cnt = 0;
+  if (tag_of(meta) == PAD) {  // padding is in no list
+    rowcnt[b.ORIG[s]] = 0;
+    return;
+  }
   for_each_receiver<DIM>(c, cases + case_of(meta), cellid[s] - c.cell_off, rs, s, mask_self,
                          start, b.P4, [&](int) { ++cnt; });
   rowcnt[b.ORIG[s]] = cnt;
@@ -519,6 +528,7 @@ __global__ void k_emit(long long N, Buffers b, const CaseDev* cases, const int* 
   long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (s >= N) return;
   int meta = b.META[s];
+  if (tag_of(meta) == PAD) return;
   const CaseDev& c = cases[case_of(meta)];
   float4 rs = b.P4[s];
   int sender = b.ORIG[s];
@@ -695,7 +705,9 @@ __global__ void k_alloc_stats(long long N, Buffers b, const CaseDev* cases, cons
     ci = case_of(b.META[s]);
     const CaseDev& c = cases[ci];
     const int cell = cellid[s] - c.cell_off;
-    occ = dim == 3 ? ref_cell_occupancy<3>(c, cell, start) : ref_cell_occupancy<2>(c, cell, start);
+    if (cell < c.ncell)  // padding sits in the parking cell, outside the grid
+      occ = dim == 3 ? ref_cell_occupancy<3>(c, cell, start)
+                     : ref_cell_occupancy<2>(c, cell, start);
     rows = rowcnt[b.ORIG[s]];
   }
   const unsigned mask = __ballot_sync(kFull, valid);

@@ -30,6 +30,8 @@ SOLVERS = {"SPH": 0, "RIE": 1, "DELTA": 2}
 EOS_TAIT, EOS_RIEMANN = 0, 1
 GEXT_ZERO, GEXT_CONST, GEXT_BAND_X, GEXT_ARRAY = 0, 1, 2, 3
 BC_NONE, BC_SOLID_ZERO, BC_SOLID_ZERO_P, BC_LID, BC_HT = 0, 1, 2, 3, 4
+NL_JAXMD, NL_MATSCIPY = 0, 1
+TAG_PAD = -1  # Tag.PAD_VALUE (utils.py:25)
 
 
 class SphConfig(ctypes.Structure):
@@ -39,7 +41,7 @@ class SphConfig(ctypes.Structure):
                 ("kahan", ctypes.c_int32), ("fp64_positions", ctypes.c_int32),
                 ("capacity_multiplier", ctypes.c_double), ("verlet_skin", ctypes.c_double),
                 ("canonical_order", ctypes.c_int32), ("is_rho_renorm", ctypes.c_int32),
-                ("is_heat_conduction", ctypes.c_int32), ("pad2", ctypes.c_int32)]
+                ("is_heat_conduction", ctypes.c_int32), ("nl_backend", ctypes.c_int32)]
 
 
 class SphCase(ctypes.Structure):
@@ -123,7 +125,7 @@ def load(build_if_missing=True):
     for name in EXPORTS:
         if name not in ("sph_abi_version", "sph_last_error"):
             getattr(lib, name).restype = I
-    if lib.sph_abi_version() != 4:
+    if lib.sph_abi_version() != 5:
         raise RuntimeError("libsph_gb300 ABI version mismatch")
     _LIB = lib
     return lib

@@ -120,12 +120,19 @@ class NeighborList:
         self.cell_size = fns.cutoff
         self._idx = idx
         self._occupancy = occupancy
+        # matscipy backend: the particles that count (an int or a 0-d tensor,
+        # read when idx is emitted) and the padding value of idx
+        self._num_particles = None
+        self._pad = None
 
     @property
     def idx(self):
         if self._idx is None:
+            n = self._num_particles
+            n = int(n.item()) if isinstance(n, torch.Tensor) else n
             self._idx, self._occupancy, code = self._fns._emit(
-                self.reference_position, self.cell_list_capacity, self.max_occupancy)
+                self.reference_position, self.cell_list_capacity, self.max_occupancy, n,
+                self._pad)
             self.error = self.error.update(code, code != 0)
         return self._idx
 
@@ -162,7 +169,7 @@ class NeighborListFns:
     """``NeighborListFns(allocate, update)`` (jax_md/partition.py:674-717)."""
 
     def __init__(self, box_size, r_cutoff, dr_threshold=0.0, capacity_multiplier=1.25,
-                 mask_self=True, format=Sparse):
+                 mask_self=True, format=Sparse, backend="jaxmd_vmap", num_particles_max=None):
         self.box = np.asarray(box_size, dtype=np.float64).reshape(-1)
         self.dim = int(self.box.size)
         if self.dim not in (2, 3):
@@ -175,6 +182,11 @@ class NeighborListFns:
         self.capacity_multiplier = float(capacity_multiplier)
         self.mask_self = bool(mask_self)
         self.format = format
+        # the matscipy backend (partition.py:356-482): a variable number of
+        # particles padded to num_particles_max, float64 distances, edges
+        # ordered by their first index with the self edges first
+        self.matscipy = backend == "matscipy"
+        self.num_particles_max = num_particles_max
         self._metric = PeriodicDisplacement(self.box)
         self._engines = OrderedDict()
 
@@ -198,6 +210,7 @@ class NeighborListFns:
         c.canonical_order = int(solver.get("canonical_order", 0))
         c.is_rho_renorm = int(solver.get("is_rho_renorm", 0))
         c.is_heat_conduction = int(solver.get("is_heat_conduction", 0))
+        c.nl_backend = _lib.NL_MATSCIPY if self.matscipy else _lib.NL_JAXMD
         return c
 
     def case(self, n):
@@ -206,7 +219,8 @@ class NeighborListFns:
         s.n = int(n)
         for d in range(3):
             s.box[d] = float(self.box[d]) if d < self.dim else 1.0
-        s.r_cutoff = self.cutoff
+        # matscipy compares float64 distances with the cutoff as given
+        s.r_cutoff = self.r_cutoff if self.matscipy else self.cutoff
         s.dx = s.h = self.r_cutoff
         s.eos = _lib.EOS_TAIT
         s.p_ref = s.rho_ref = s.gamma = s.u_ref = 1.0
@@ -222,7 +236,7 @@ class NeighborListFns:
                 self._engines.popitem(last=False)
         return e
 
-    def _load(self, position):
+    def _load(self, position, num_particles=None):
         r = _as_device_f32(position)
         n = r.shape[0]
         if r.ndim != 2 or r.shape[1] != self.dim:
@@ -230,20 +244,44 @@ class NeighborListFns:
         e = self._engine(n)
         z1 = torch.zeros(n, dtype=torch.float32, device=r.device)
         zd = torch.zeros_like(r)
-        state = dict(r=r, tag=torch.zeros(n, dtype=torch.int32, device=r.device), u=zd, v=zd,
-                     dudt=zd, dvdt=zd, rho=z1 + 1.0, p=z1, mass=z1 + 1.0, eta=z1)
+        tag = torch.zeros(n, dtype=torch.int32, device=r.device)
+        if num_particles is not None:  # positions[num_particles:] pad the state
+            tag[int(num_particles):] = _lib.TAG_PAD
+        state = dict(r=r, tag=tag, u=zd, v=zd, dudt=zd, dvdt=zd, rho=z1 + 1.0, p=z1,
+                     mass=z1 + 1.0, eta=z1)
         e.set_state(state)
         return e, r
 
-    def _emit(self, position, cell_capacity, max_occupancy):
-        e, r = self._load(position)
+    def _emit(self, position, cell_capacity, max_occupancy, num_particles=None, pad=None):
+        e, r = self._load(position, num_particles)
         e.nl_set_capacity(cell_capacity if cell_capacity is not None else 2 ** 31 - 1,
                           max_occupancy)
         e.read_status(clear=True)
         e.nl_update()
         idx, count = e.nl_edges(max_occupancy, r.device)
         code = e.read_status(clear=True)
-        return idx, int(count.item()), code & 0xFF
+        n_edges = int(count.item())
+        if self.matscipy:
+            if n_edges > max_occupancy:  # all of them, to order before truncating
+                idx, _ = e.nl_edges(n_edges, r.device)
+            idx = self._matscipy_order(idx[:, :n_edges], max_occupancy,
+                                       r.shape[0] if pad is None else pad)
+        return idx, n_edges, code & 0xFF
+
+    def _matscipy_order(self, edges, capacity, pad):
+        """matscipy's "ij" list as the reference returns it: the self edges
+        (when not masked) first, then every pair by first index (partition.py:
+        387-404; within an index the second ascending here), truncated to
+        ``capacity`` or padded with ``pad``."""
+        i, j = edges[0].long(), edges[1].long()
+        self_e = i == j
+        n = int(max(int(torch.maximum(i, j).max()) + 1 if i.numel() else 0, 1))
+        key = torch.where(self_e, i, n + i * n + j)  # self edges sort before all pairs
+        order = torch.argsort(key)
+        out = torch.full((2, int(capacity)), int(pad), dtype=torch.int32, device=edges.device)
+        k = min(int(capacity), int(order.numel()))
+        out[:, :k] = edges[:, order[:k]]
+        return out
 
     # -- reference API
     def allocate(self, position, extra_capacity=0, **kwargs):
@@ -251,10 +289,23 @@ class NeighborListFns:
 
         The edge array ``idx`` is emitted when first read (the same array the
         reference's allocate returns); a fused si_euler step never reads it.
+        With the matscipy backend ``num_particles`` (default all) particles
+        count, the rest pad the state.
         """
-        e, _ = self._load(position)  # loading clears the status word
+        num = kwargs.get("num_particles") if self.matscipy else None
+        e, r = self._load(position, num)  # loading clears the status word
         cap = e.nl_allocate(extra_capacity)
         code = e.read_status(clear=True) & 0xFF
+        if self.matscipy:
+            # (2, round(E * multiplier * num_particles_max / num_particles + extra)),
+            # padded with num_particles (partition.py:458-466)
+            n = int(r.shape[0] if num is None else num)
+            n_max = int(self.num_particles_max or r.shape[0])
+            edges = int(cap.occupancy)
+            size = round(edges * (self.capacity_multiplier * n_max / n) + extra_capacity)
+            nbrs = NeighborList(self, position, 0, None, size, occupancy=edges)
+            nbrs._num_particles, nbrs._pad = n, n
+            return nbrs
         cell_cap = int(cap.cell_capacity) if self._uses_cells() else None
         return NeighborList(self, position, code, cell_cap, cap.max_occupancy,
                             occupancy=int(cap.occupancy))
@@ -279,6 +330,18 @@ class NeighborListFns:
 
     def update(self, position, neighbors, **kwargs):
         """Rebuild with fixed capacities if any particle moved beyond the threshold."""
+        if self.matscipy:
+            # always rebuilt; more edges than the capacity truncate and raise
+            # NEIGHBOR_LIST_OVERFLOW; padded with num_particles_max (:414-443)
+            n = kwargs.get("num_particles")
+            r = _as_device_f32(position)
+            n_max = int(self.num_particles_max or r.shape[0])
+            idx, count, code = self._emit(position, None, neighbors.max_occupancy, n, n_max)
+            over = PEC.NEIGHBOR_LIST_OVERFLOW if count > neighbors.max_occupancy else 0
+            nbrs = NeighborList(self, position, neighbors.error.code | over, None,
+                                neighbors.max_occupancy, idx=idx, occupancy=count)
+            nbrs._num_particles, nbrs._pad = n, n_max
+            return nbrs
         if not self.moved(position, neighbors):
             return neighbors
         idx, count, code = self._emit(position, neighbors.cell_list_capacity,
@@ -288,7 +351,7 @@ class NeighborListFns:
                             occupancy=count)
 
 
-BACKENDS = ("jaxmd_vmap", "jaxmd_scan")
+BACKENDS = ("jaxmd_vmap", "jaxmd_scan", "matscipy")
 
 
 def neighbor_list(displacement_or_metric, box_size, r_cutoff, backend="jaxmd_vmap",
@@ -304,9 +367,9 @@ def neighbor_list(displacement_or_metric, box_size, r_cutoff, backend="jaxmd_vma
     and is likewise served by the cell list.
     """
     if backend not in BACKENDS:
-        raise NotImplementedError(
-            f"backend {backend!r}: only {BACKENDS} are on the GPU path "
-            "(the matscipy backend is a CPU library callback)")
+        raise NotImplementedError(f"backend {backend!r}: the GPU path serves {BACKENDS}")
+    if backend == "matscipy" and pbc is not None and not np.all(np.asarray(pbc)):
+        raise NotImplementedError("the matscipy backend is served for periodic boxes only")
     if format is not Sparse:
         raise NotImplementedError("only the Sparse format is on the hot path")
     if custom_mask_function is not None:
@@ -314,4 +377,4 @@ def neighbor_list(displacement_or_metric, box_size, r_cutoff, backend="jaxmd_vma
     if fractional_coordinates:
         raise NotImplementedError("fractional coordinates are not supported")
     return NeighborListFns(box_size, r_cutoff, dr_threshold, capacity_multiplier, mask_self,
-                           format)
+                           format, backend, num_particles_max)

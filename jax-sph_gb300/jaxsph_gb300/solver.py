@@ -317,4 +317,8 @@ class WCSPH:
             # whose reference position and overflow bits equal the new ones
             nbrs = NeighborList(nl_fns, res["r"], neighbors.error.merged(status),
                                 neighbors.cell_list_capacity, neighbors.max_occupancy)
+        if nl_fns.matscipy:
+            # the particles that count are the unpadded ones (integrator.py:47)
+            nbrs._num_particles = (res["tag"] != _lib.TAG_PAD).sum()
+            nbrs._pad = int(nl_fns.num_particles_max or key[1])
         return res, nbrs

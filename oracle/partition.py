@@ -251,3 +251,43 @@ def canonical_edges(idx, N):
     real = real[:, o]
     o = torch.argsort(real[1], stable=True)
     return real[:, o]
+
+
+# ---------------------------------------------------------------- matscipy backend
+def matscipy_edges(position, num_particles, box, r_cutoff, mask_self):
+    """The edge list of the reference's matscipy backend (jax_sph/partition.py:
+    356-482) for ``position[:num_particles]``: matscipy's ``neighbour_list("ij",
+    cutoff, positions, cell=diag(box), pbc=True)`` -- every ordered pair i != j
+    whose distance between nearest periodic images, in float64 from the float32
+    positions, is below the cutoff -- with the self edges ``(arange(n),
+    arange(n))`` in front when ``mask_self`` is off. matscipy (not installed
+    here) orders the pairs by i; within an i they are taken in ascending j.
+    Returns an int64 (2, E) tensor."""
+    n = int(num_particles)
+    r = torch.as_tensor(position)[:n].to(torch.float64)
+    side = torch.as_tensor(np.asarray(box, dtype=np.float64))
+    d = r[:, None, :] - r[None, :, :]
+    d = d - side * torch.round(d / side)
+    within = (d * d).sum(-1) < float(r_cutoff) ** 2
+    within.fill_diagonal_(False)
+    i, j = torch.nonzero(within, as_tuple=True)  # row-major: by i, then j
+    pairs = torch.stack([i, j])
+    if mask_self:
+        return pairs
+    ar = torch.arange(n)
+    return torch.cat([torch.stack([ar, ar]), pairs], dim=1)
+
+
+def matscipy_capacity(n_edges, num_particles, num_particles_max, capacity_multiplier=1.25,
+                      extra_capacity=0):
+    """``allocate``'s list size: round(E * multiplier * N_max / n + extra) (:458-463)."""
+    factor = capacity_multiplier * num_particles_max / num_particles
+    return round(n_edges * factor + extra_capacity)
+
+
+def matscipy_idx(edges, capacity, pad):
+    """The (2, capacity) list: truncated, or padded with ``pad`` (:399-404, :464-466)."""
+    out = torch.full((2, int(capacity)), int(pad), dtype=torch.int64)
+    k = min(int(capacity), edges.shape[1])
+    out[:, :k] = edges[:, :k]
+    return out, edges.shape[1] > capacity
