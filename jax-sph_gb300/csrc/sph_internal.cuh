@@ -69,8 +69,6 @@ struct CaseDev {
   int cell_cap;       // cell capacity for the CELL_LIST_OVERFLOW test
   long long edge_cap; // neighbour-list capacity for NEIGHBOR_LIST_OVERFLOW
   float cutoff_sq;
-  int f64_metric;     // matscipy backend: float64 minimum-image distance < cutoff
-  double cut64_sq, mat_box[3];
   float inv_h, sigma, dsigma;  // W(r) = sigma*f(q); dW/dr = dsigma*g(q)
   float dt, cv;       // f32(dt), f32(tvf*0.5*dt) of si_euler
   float dt_rho;       // WCSPH dt of density evolution
@@ -107,6 +105,10 @@ struct CaseDev {
   float v_r2, v_dmax2;
   int cref_off, ncref;  // this case's reference cells in the per-step occupancy count
   double dt64, box64[3];  // float64 drift of the precision form
+  // matscipy backend: float64 minimum-image distance < cutoff (kept last: the
+  // hot loops read the fields above)
+  double cut64_sq, mat_box[3];
+  int f64_metric;
 };
 
 struct Buffers {
@@ -167,8 +169,8 @@ __device__ __forceinline__ float sqd(const float3& d) {
 // The matscipy backend's membership: the pair's distance in float64 from
 // the float32 positions, nearest periodic image, strictly below the cutoff.
 template <int DIM>
-__device__ __noinline__ bool is_edge_f64(const float4& recv, const float4& send,
-                                         const CaseDev& c) {
+__device__ __forceinline__ bool is_edge_f64(const float4& recv, const float4& send,
+                                            const CaseDev& c) {
   const double p[3] = {(double)send.x - (double)recv.x, (double)send.y - (double)recv.y,
                        DIM == 3 ? (double)send.z - (double)recv.z : 0.0};
   double s = 0.0;
@@ -179,9 +181,9 @@ __device__ __noinline__ bool is_edge_f64(const float4& recv, const float4& send,
   return s < c.cut64_sq;
 }
 
+// The jax_md membership (float32 reference metric).
 template <int DIM>
 __device__ __forceinline__ bool is_edge(const float4& recv, const float4& send, const CaseDev& c) {
-  if (c.f64_metric) return is_edge_f64<DIM>(recv, send, c);
   return sqd<DIM>(pdisp3<DIM>(send, recv, c)) < c.cutoff_sq;
 }
 
@@ -440,6 +442,18 @@ __device__ __forceinline__ int ref_cell_hash(const float4& r, const CaseDev& c) 
 // reach it, so the hot loop stays small.
 template <int DIM>
 __device__ __noinline__ bool exact_edge(float4 ri, float4 rj, const CaseDev* c) {
+  return is_edge<DIM>(ri, rj, *c);
+}
+
+// Membership as the list's backend defines it, for the emitted edge lists and
+// their counts: the matscipy backend's float64 rule or the reference metric.
+// The passes' per-step sums keep the float32 test (exact_edge): the two rules
+// differ only for a pair at the cutoff distance, where W and W' vanish, so no
+// sum changes. (A float64 branch inside exact_edge makes every caller of it
+// save more registers: the hot loops would spill.)
+template <int DIM>
+__device__ __noinline__ bool list_edge(float4 ri, float4 rj, const CaseDev* c) {
+  if (c->f64_metric) return is_edge_f64<DIM>(ri, rj, *c);
   return is_edge<DIM>(ri, rj, *c);
 }
 

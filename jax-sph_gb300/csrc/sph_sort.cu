@@ -475,7 +475,8 @@ __global__ void k_tile_scan(const int* in, long long n, int* out, const int* til
 // metric(r[s], r[c]) < cutoff_sq (jax_md/partition.py:885-909): the walk of
 // the sender's cells (rows trimmed in fast cases) with the band test of the
 // passes -- the shifted squared distance decides outside the band, the
-// reference metric inside it (every candidate without the fast test).
+// list's own rule inside it (every candidate without the fast test): the
+// reference metric, or the matscipy backend's float64 distance.
 template <int DIM, typename F>
 __device__ __forceinline__ void for_each_receiver(const CaseDev& c, const CaseDev* cp, int cell,
                                                   const float4& rs, long long s, int mask_self,
@@ -489,9 +490,11 @@ __device__ __forceinline__ void for_each_receiver(const CaseDev& c, const CaseDe
       if (c.fast) {
         const float dx = qx - rc.x, dy = qy - rc.y, dz = (DIM == 3) ? qz - rc.z : 0.f;
         const float d2 = dx * dx + dy * dy + dz * dz;
-        e = d2 < c.cut_lo || (d2 < c.cut_hi && exact_edge<DIM>(rc, rs, cp));
+        // below the band an edge for either rule (the float64 cutoff^2 is
+        // within 2^-24 of the float32 one, far inside the band)
+        e = d2 < c.cut_lo || (d2 < c.cut_hi && list_edge<DIM>(rc, rs, cp));
       } else {
-        e = is_edge<DIM>(rc, rs, c);
+        e = list_edge<DIM>(rc, rs, cp);
       }
       if (e) f(j);
     }
