@@ -54,8 +54,8 @@ PHASE_BYTES = (BIN_BYTES, DENSITY_BYTES, 0, FORCE_BYTES)
 # (profiles/k_kick_tgv3d_128.md, k_density_tgv3d_128.md, k_force_tgv3d_128.md); traffic
 # grows in proportion to the particle count, so it scales to 64^3 per particle. The
 # kick phase's figure is the kick alone (the rebuild kernels run every few steps).
-PHASE_TRAFFIC = (131.5, 289.8, None, 220.6)
-PHASE_FP32_PIPE = (0.157, 0.193, None, 0.409)
+PHASE_TRAFFIC = (131.5, 308.3, None, 220.5)
+PHASE_FP32_PIPE = (0.157, 0.226, None, 0.409)
 
 
 def dist_env():
