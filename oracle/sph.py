@@ -74,12 +74,15 @@ def make_kernel(name, h, dim):
 
 
 def grad_w(kernel, r):
-    """dW/dr by autograd of ``w`` (kernel.py:20-23); keeps the graph for adjoints."""
+    """dW/dr by autograd of ``w`` (kernel.py:20-23). The graph is kept only
+    when ``r`` is part of one (gradients through steps); otherwise the result
+    is a plain tensor, so that a rollout does not chain its steps' graphs."""
+    need = torch.is_grad_enabled() and r.requires_grad
     with torch.enable_grad():
-        rr = r if r.requires_grad else r.detach().requires_grad_(True)
+        rr = r if need else r.detach().requires_grad_(True)
         w = kernel.w(rr)
-        (g,) = torch.autograd.grad(w.sum(), rr, create_graph=True)
-    return g
+        (g,) = torch.autograd.grad(w.sum(), rr, create_graph=need)
+    return g if need else g.detach()
 
 
 # ---------------------------------------------------------------- EOS
