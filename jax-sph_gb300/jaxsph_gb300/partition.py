@@ -364,7 +364,10 @@ def neighbor_list(displacement_or_metric, box_size, r_cutoff, backend="jaxmd_vma
     served by the same GPU cell list; ``num_partitions`` is accepted for
     signature compatibility (the GPU search never materialises candidates, so
     it needs no memory chunking). ``disable_cell_list`` selects the same sets
-    and is likewise served by the cell list.
+    and is likewise served by the cell list. ``matscipy`` (periodic boxes) takes
+    ``num_particles`` on allocate/update, the rest of the positions padding, and
+    follows that backend's float64 membership, edge order, capacity rule and
+    padding values; ``num_particles_max`` sizes its capacity.
     """
     if backend not in BACKENDS:
         raise NotImplementedError(f"backend {backend!r}: the GPU path serves {BACKENDS}")

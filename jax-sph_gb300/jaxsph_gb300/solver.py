@@ -2,11 +2,13 @@
 
 ``WCSPH(...).forward_wrapper()`` returns ``forward(state, neighbors) -> state``
 with the reference's state-dict contract. The computation runs in
-``libsph_gb300`` (density pass, generalized wall BC pass, force pass; see
-``csrc/sph_forward.cu``) in float32 on the GPU. The branches on the hot path
-are the SPH and Riemann solvers with density summation or evolution, the
-generalized wall boundary condition (no-slip and free-slip), transport
-velocity and artificial viscosity, over the quintic and Wendland C2 kernels.
+``libsph_gb300`` (density passes, generalized wall BC pass, heat pass, force
+pass; see ``csrc/sph_forward.cu`` and ``csrc/sph_delta.cu``) in float32 on the
+GPU. The branches on the hot path are the SPH, Riemann and delta-SPH solvers
+with density summation or evolution (continuity, Riemann, Marrone's delta-SPH)
+and renormalisation, the generalized wall boundary condition (no-slip and
+free-slip) with the wall temperature, heat conduction, transport velocity and
+artificial viscosity, over the quintic and Wendland C2 kernels.
 """
 
 import numpy as np
