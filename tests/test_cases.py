@@ -87,7 +87,8 @@ def test_cavity_channel_batch_shapes():
 @pytest.mark.parametrize("make", [lambda: cases.dam_break(dx=0.05),
                                   lambda: cases.lid_driven_cavity(dx=0.05),
                                   lambda: cases.poiseuille(dx=0.05),
-                                  lambda: cases.couette(dx=0.05)])
+                                  lambda: cases.couette(dx=0.05),
+                                  lambda: cases.heat_transfer(dx=0.05)])
 def test_descriptors_match_oracle_callbacks(make):
     s = make()
     g = torch.Generator().manual_seed(0)
@@ -99,3 +100,52 @@ def test_descriptors_match_oracle_callbacks(make):
     for k in ("u", "v", "dudt", "dvdt", "p"):
         assert torch.equal(ours[k], ref[k]), k
     assert torch.equal(s.g_ext_fn(st64["r"]), oracle_g(s)(st64["r"]))
+
+
+def test_heat_transfer_layout():
+    """cases/ht.py: a 1 x 0.2 fluid layer between two 3-layer walls, the hot
+    Dirichlet part of the bottom wall within 0.25 of the middle, the
+    temperature fields of case_setup.py:298-306, noise on the fluid only."""
+    dx = 0.02
+    s = cases.heat_transfer(dx=dx, r0_noise_factor=0.0)
+    tag = s.state["tag"].numpy()
+    assert (tag == 0).sum() == 50 * 10 and (tag > 0).sum() == 2 * 50 * 3
+    hot = s.state["r"][torch.as_tensor(tag == 3)].double()
+    assert len(hot) == 24 * 3 and (hot[:, 1] < 3 * dx).all()
+    assert ((hot[:, 0] - 0.5).abs() < 0.25).all()
+    for k, v in (("T", 1.0), ("kappa", 7.313), ("Cp", 305.27)):
+        assert torch.allclose(s.state[k][torch.as_tensor(tag != 3)], torch.tensor(v))
+    assert (s.state["T"][torch.as_tensor(tag == 3)] == np.float32(1.23)).all()
+    assert s.solver["is_heat_conduction"] and s.solver["is_bc_trick"]
+    noisy = cases.heat_transfer(dx=dx, seed=3)
+    moved = (noisy.state["r"] - s.state["r"]).abs().sum(1) > 0
+    assert moved[torch.as_tensor(tag == 0)].all() and not moved[torch.as_tensor(tag > 0)].any()
+
+
+def test_moving_wall_normals_only_where_the_reference_recomputes():
+    # case_setup.py:209-218: moving walls with the Riemann solver or free slip
+    assert cases.lid_driven_cavity(dx=0.05, solver_name="RIE").nw_fn is not None
+    assert cases.lid_driven_cavity(dx=0.05, free_slip=True).nw_fn is not None
+    assert cases.couette(dx=0.05, solver_name="RIE").nw_fn is not None
+    assert cases.lid_driven_cavity(dx=0.05).nw_fn is None
+    assert cases.dam_break(dx=0.05).nw_fn is None  # walls at rest
+    s = cases.lid_driven_cavity(dx=0.05, solver_name="RIE")
+    wall = torch.as_tensor(s.nw_fn.wall)
+    assert s.state["nw"][wall].norm(dim=1).min() > 0.99
+    assert s.state["nw"][~wall].abs().max() == 0
+
+
+def test_matscipy_backend_arguments():
+    from jaxsph_gb300 import partition, space
+
+    disp, _ = space.periodic(np.ones(2))
+    fns = partition.neighbor_list(disp, np.ones(2), 0.1, backend="matscipy",
+                                  num_particles_max=100, pbc=np.array([True, True]))
+    assert fns.matscipy and fns.num_particles_max == 100
+    assert fns.config().nl_backend == _lib.NL_MATSCIPY
+    assert fns.case(10).r_cutoff == 0.1  # the cutoff as matscipy gets it
+    with pytest.raises(NotImplementedError):
+        partition.neighbor_list(disp, np.ones(2), 0.1, backend="matscipy",
+                                pbc=np.array([True, False]))
+    with pytest.raises(NotImplementedError):
+        partition.neighbor_list(disp, np.ones(2), 0.1, backend="unknown")
