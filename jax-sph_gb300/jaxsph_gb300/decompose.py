@@ -30,6 +30,26 @@ from .solver import prepare_state
 
 STATE_FIELDS = ("r", "tag", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p", "mass", "eta", "nw")
 OUT_FIELDS = ("r", "u", "v", "dudt", "dvdt", "drhodt", "rho", "p")
+HEAT_FIELDS = ("T", "dTdt", "kappa", "Cp")
+_VECTOR = ("r", "u", "v", "dudt", "dvdt", "nw")
+
+
+def state_fields(setup):
+    """The fields a slab exchanges and keeps: with heat conduction the
+    temperature fields too."""
+    heat = setup.solver.get("is_heat_conduction", False)
+    return STATE_FIELDS + (HEAT_FIELDS if heat else ())
+
+
+def out_fields(setup):
+    """The fields a step changes: with heat conduction T and dT/dt, with
+    moving walls the recomputed normals."""
+    out = OUT_FIELDS
+    if setup.solver.get("is_heat_conduction", False):
+        out = out + ("T", "dTdt")
+    if setup.nw_fn is not None:
+        out = out + ("nw",)
+    return out
 
 
 def longest_axis(box):
@@ -92,8 +112,8 @@ class _SlabEngines:
         self._engines = {}
         if self.solver.g_spec()["kind"] == _lib.GEXT_ARRAY:
             raise NotImplementedError("slabs need a g_ext_fn with a GPU spec")
-        if self.solver.is_heat_conduction:
-            raise NotImplementedError("slabs do not carry the temperature fields")
+        self.fields = state_fields(setup)
+        self.out = out_fields(setup)
 
     def engine(self, n):
         e = self._engines.get(n)
@@ -103,6 +123,9 @@ class _SlabEngines:
             if len(self._engines) > 8:
                 self._engines.clear()
             e = _lib.Engine(self.cfg, [case])
+            if s.nw_fn is not None:  # moving walls: each slab recomputes its walls' normals
+                spec = s.nw_fn.spec
+                e.set_wall_layer(spec["layer"], spec["offset"], spec["cutoff"])
             self._engines[n] = e
         return e
 
@@ -113,7 +136,7 @@ class _SlabEngines:
         e = self.engine(n)
         e.set_state(local)
         e.step(1)
-        out = {k: torch.empty_like(local[k]) for k in OUT_FIELDS}
+        out = {k: torch.empty_like(local[k]) for k in self.out}
         e.get_state(out)
         return out
 
@@ -132,7 +155,8 @@ class VirtualSlabs:
         self.length = float(setup.box[self.axis])
         self.dim = setup.dim
         self.slabs = _SlabEngines(setup, device)
-        st = prepare_state(setup.state, setup.dim, device)
+        st = prepare_state(setup.state, setup.dim, device,
+                           heat=setup.solver.get("is_heat_conduction", False))
         if "nw" not in st:
             st["nw"] = torch.zeros_like(st["r"])
         self.state = st
@@ -146,7 +170,7 @@ class VirtualSlabs:
             w = halo_width(self.slabs.cutoff, step_drift(st, s.dt, self.slabs.cv),
                            self.slabs.levels)
             owner = slab_of(x, self.length, self.n_parts)
-            new = {k: st[k].clone() for k in OUT_FIELDS}
+            new = {k: st[k].clone() for k in self.slabs.out}
             self.last_sizes = []
             for k in range(self.n_parts):
                 local = (owner == k) | near_slab(x, k, self.n_parts, self.length, w)
@@ -154,20 +178,20 @@ class VirtualSlabs:
                 if idx.numel() == 0:
                     continue
                 owned = owner[idx] == k
-                out = self.slabs.advance({f: st[f][idx].contiguous() for f in STATE_FIELDS})
+                out = self.slabs.advance({f: st[f][idx].contiguous() for f in self.slabs.fields})
                 keep = idx[owned]
-                for f in OUT_FIELDS:
+                for f in self.slabs.out:
                     new[f][keep] = out[f][owned]
                 self.last_sizes.append((int(owned.sum()), int(idx.numel())))
             st.update(new)
 
 
 # ------------------------------------------------------------------ distributed
-def _pack(rows):
+def _pack(rows, fields=STATE_FIELDS):
     """Fields of a set of particles as one float64 matrix (global index,
     tag and every float field; float32 and int32 values are exact in it)."""
     cols = [rows["gid"].double()[:, None], rows["tag"].double()[:, None]]
-    for f in STATE_FIELDS:
+    for f in fields:
         if f in ("tag",):
             continue
         t = rows[f].double()
@@ -175,25 +199,24 @@ def _pack(rows):
     return torch.cat(cols, dim=1).contiguous()
 
 
-def _unpack(mat, dim):
+def _unpack(mat, dim, fields=STATE_FIELDS):
     out = {"gid": mat[:, 0].long(), "tag": mat[:, 1].to(torch.int32)}
     c = 2
-    for f in STATE_FIELDS:
+    for f in fields:
         if f == "tag":
             continue
-        width = dim if f in ("r", "u", "v", "dudt", "dvdt", "nw") else 1
+        width = dim if f in _VECTOR else 1
         t = mat[:, c:c + width].to(torch.float32)
         out[f] = t.contiguous() if width > 1 else t[:, 0].contiguous()
         c += width
     return out
 
 
-def _columns(dim):
-    return 2 + sum(dim if f in ("r", "u", "v", "dudt", "dvdt", "nw") else 1
-                   for f in STATE_FIELDS if f != "tag")
+def _columns(dim, fields=STATE_FIELDS):
+    return 2 + sum(dim if f in _VECTOR else 1 for f in fields if f != "tag")
 
 
-def exchange(rows, dest, dim, group=None):
+def exchange(rows, dest, dim, group=None, fields=STATE_FIELDS):
     """Point-to-point exchange: rank r receives the rows with ``dest[r]``
     true from every rank. ``rows``: fields of this rank's particles plus
     ``gid``; ``dest``: a bool mask per rank. Returns the received rows of all
@@ -201,7 +224,7 @@ def exchange(rows, dest, dim, group=None):
     import torch.distributed as dist
 
     ws, me = dist.get_world_size(group), dist.get_rank(group)
-    mat = _pack(rows)
+    mat = _pack(rows, fields)
     # on the rows' device: NCCL exchanges device tensors, gloo host tensors
     counts = torch.tensor([int(dest[r].sum()) if r != me else 0 for r in range(ws)],
                           dtype=torch.int64, device=mat.device)
@@ -221,9 +244,9 @@ def exchange(rows, dest, dim, group=None):
     for q in reqs:
         q.wait()
     if not recv:
-        return _unpack(torch.empty((0, _columns(dim)), dtype=torch.float64,
-                                   device=mat.device), dim)
-    return _unpack(torch.cat(recv), dim)
+        return _unpack(torch.empty((0, _columns(dim, fields)), dtype=torch.float64,
+                                   device=mat.device), dim, fields)
+    return _unpack(torch.cat(recv), dim, fields)
 
 
 def merge(a, b):
@@ -253,19 +276,20 @@ class DistributedSlabs:
         self.dim = setup.dim
         self.device = torch.device(device)
         self.slabs = _SlabEngines(setup, device)
-        st = prepare_state(setup.state, setup.dim, self.device)
+        st = prepare_state(setup.state, setup.dim, self.device,
+                           heat=setup.solver.get("is_heat_conduction", False))
         if "nw" not in st:
             st["nw"] = torch.zeros_like(st["r"])
         gid = torch.arange(setup.n, device=self.device)
         mine = slab_of(st["r"][:, self.axis], self.length, self.ws) == self.rank
-        self.owned = {f: st[f][mine].contiguous() for f in STATE_FIELDS}
+        self.owned = {f: st[f][mine].contiguous() for f in self.slabs.fields}
         self.owned["gid"] = gid[mine]
 
     def local_state(self, width):
         """Owned particles plus the halo received from the other ranks."""
         x = self.owned["r"][:, self.axis]
         dest = [near_slab(x, r, self.ws, self.length, width) for r in range(self.ws)]
-        halo = exchange(self.owned, dest, self.dim, self.group)
+        halo = exchange(self.owned, dest, self.dim, self.group, self.slabs.fields)
         halo = {f: halo[f].to(self.device) for f in halo}
         return merge(self.owned, halo)
 
@@ -280,8 +304,8 @@ class DistributedSlabs:
             local = self.local_state(halo_width(self.slabs.cutoff, float(drift),
                                                 self.slabs.levels))
             owned = torch.isin(local["gid"], self.owned["gid"])
-            out = self.slabs.advance({f: local[f] for f in STATE_FIELDS})
-            for f in OUT_FIELDS:
+            out = self.slabs.advance({f: local[f] for f in self.slabs.fields})
+            for f in self.slabs.out:
                 self.owned[f] = out[f][owned].contiguous()
             self.migrate()
 
@@ -290,7 +314,7 @@ class DistributedSlabs:
         x = self.owned["r"][:, self.axis]
         owner = slab_of(x, self.length, self.ws)
         dest = [owner == r for r in range(self.ws)]
-        arrived = exchange(self.owned, dest, self.dim, self.group)
+        arrived = exchange(self.owned, dest, self.dim, self.group, self.slabs.fields)
         arrived = {f: arrived[f].to(self.device) for f in arrived}
         stay = owner == self.rank
         kept = {f: self.owned[f][stay] for f in self.owned}
