@@ -9,7 +9,6 @@ and float32 rounding. Each ``g_ext_fn``/``bc_fn`` is a callable that also
 carries a ``spec`` the GPU engine evaluates inside its kernels.
 """
 
-import math
 from dataclasses import dataclass, field
 
 import numpy as np

@@ -15,7 +15,6 @@ capacities (nothing is truncated on the GPU), so an overflow only triggers a
 re-allocation of the capacities, without re-running steps.
 """
 
-import numpy as np
 import torch
 
 from . import _lib

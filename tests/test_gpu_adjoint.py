@@ -11,7 +11,6 @@ notebooks/iclr24_inverse.ipynb); gradient w.r.t. the initial velocity.
   truncation and the float32 forward set this floor).
 """
 
-import numpy as np
 import pytest
 import torch
 

@@ -6,7 +6,6 @@ launch shape picked by the autotuner must not change any result, and a batched
 instance must match the float64 oracle like a plain run does.
 """
 
-import numpy as np
 import pytest
 import torch
 
