@@ -105,3 +105,27 @@ def test_halo_width_covers_two_cutoffs_and_the_drift():
     assert abs(d - 0.1 * float(np.linalg.norm([1.0, 0.2, 0.2]))) < 1e-12
     assert dc.halo_width(0.5, d) > 1.0 + 2 * d
     assert dc.halo_width(0.5, d, levels=3) > 1.5 + 2 * d
+
+
+def test_slab_fields_follow_the_case():
+    """Heat conduction adds the temperature fields to what slabs exchange and
+    keep; moving walls add the recomputed normals to what a step changes; the
+    exchange matrix round-trips every field exactly."""
+    sys.path.insert(0, os.path.join(ROOT, "jax-sph_gb300"))
+    from jaxsph_gb300 import cases
+    from jaxsph_gb300 import decompose as dc
+
+    ht = cases.heat_transfer(dx=0.05)
+    assert dc.state_fields(ht)[-4:] == ("T", "dTdt", "kappa", "Cp")
+    assert dc.out_fields(ht)[-2:] == ("T", "dTdt")
+    ldc = cases.lid_driven_cavity(dx=0.05, solver_name="RIE")
+    assert dc.out_fields(ldc)[-1] == "nw" and "T" not in dc.state_fields(ldc)
+    assert dc.state_fields(cases.tgv(dim=2, dx=0.1)) == dc.STATE_FIELDS
+    fields = dc.state_fields(ht)
+    g = torch.Generator().manual_seed(0)
+    rows = {k: (torch.randn(v.shape, generator=g) if v.is_floating_point() else v)
+            for k, v in ht.state.items() if k in fields}
+    rows["gid"] = torch.arange(ht.n)
+    back = dc._unpack(dc._pack(rows, fields), ht.dim, fields)
+    for k in fields + ("gid",):
+        assert torch.equal(back[k], rows[k]), k

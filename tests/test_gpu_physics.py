@@ -29,6 +29,9 @@ def small_cases():
     return {
         "tgv2d_sph": lambda: cases.tgv(dim=2, dx=0.02),
         "tgv3d_sph_tvf": lambda: cases.tgv(dim=3, dx=2 * np.pi / 20),
+        # the other kernel in each dimension: quintic in 3D, Wendland C2 in 2D
+        "tgv3d_qsk": lambda: cases.tgv(dim=3, dx=2 * np.pi / 16, kernel="QSK"),
+        "tgv2d_wc2k_tvf": lambda: cases.tgv(dim=2, dx=0.02, kernel="WC2K", tvf=1.0),
         "tgv2d_rie": lambda: cases.tgv(dim=2, dx=0.04, solver_name="RIE"),
         "db_rie": lambda: cases.dam_break(dx=0.04),
         "db_rie_freeslip": lambda: cases.dam_break(dx=0.04, free_slip=True),
