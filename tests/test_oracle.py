@@ -182,6 +182,37 @@ def test_oracle_heat_conduction_conserves_energy():
     assert float((rate * (st["T"] - st["T"].mean())).sum()) < 0.0
 
 
+def test_heat_conduction_decays_a_temperature_wave_at_the_analytic_rate():
+    """Physics pin of Cleary's temperature equation (solver.py:591-610,
+    :832-850): on a periodic lattice at rest a wave T = 1 + a sin(2 pi x)
+    decays as exp(-kappa k^2 t / (rho Cp)), k = 2 pi (the reference's Poiseuille
+    and Couette tests pin the momentum terms the same way). 400 steps, within
+    1 % of the analytic decay."""
+    from jaxsph_gb300 import cases
+    from oracle_setup import oracle_case
+
+    kappa, cp = 0.07, 1.0
+    setup = cases.tgv(dim=2, dx=0.02, heat_conduction=True, kappa_ref=kappa, Cp_ref=cp)
+    setup.state["u"] = torch.zeros_like(setup.state["u"])
+    setup.state["v"] = torch.zeros_like(setup.state["v"])
+    solver, fns, bc, st = oracle_case(setup, torch.float64)
+    x = st["r"][:, 0]
+    wave = torch.sin(2 * math.pi * x)
+    st["T"] = 1.0 + 0.1 * wave
+
+    def amplitude(T):
+        return 2 * ((T - 1.0) * wave).mean().item()
+
+    a0, steps = amplitude(st["T"]), 400
+    nb = fns.allocate(st["r"])
+    with torch.no_grad():
+        for _ in range(steps):
+            st, nb = oracle.sph.si_euler_advance(setup.dt, setup.tvf, st, nb, fns, solver, bc)
+    alpha = kappa / (st["rho"].mean().item() * cp)
+    want = math.exp(-alpha * (2 * math.pi) ** 2 * steps * setup.dt)
+    assert abs(amplitude(st["T"]) / a0 - want) < 0.01 * want
+
+
 def test_heat_transfer_bc_matches_the_oracle():
     from jaxsph_gb300 import cases
     from oracle_setup import oracle_bc
