@@ -53,6 +53,9 @@ extern "C" {
 #define SPH_WARN_BOX_EDGE 0x1000u
 /* sph_advance: a particle moved beyond the neighbour list's threshold. */
 #define SPH_INFO_MOVED 0x2000u
+/* A host-side failure inside the library (host memory exhausted or another
+ * C++ exception), returned instead of letting it cross the ABI. */
+#define SPH_ERR_HOST 0x4000u
 
 enum { SPH_KERNEL_QSK = 0, SPH_KERNEL_WC2K = 1 };   /* jax_sph/kernel.py:51-103 */
 /* jax_sph/solver.py:676-694; DELTA: the standard SPH acceleration plus the

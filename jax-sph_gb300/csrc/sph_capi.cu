@@ -144,6 +144,23 @@ struct SphHandle {
 
 void sph::set_last_error(const std::string& msg) { g_last_error = msg; }
 
+int sph::host_error() noexcept {
+  try {
+    try {
+      throw;
+    } catch (const std::bad_alloc&) {
+      g_last_error = "host memory exhausted";
+    } catch (const std::exception& e) {
+      g_last_error = std::string("host error: ") + e.what();
+    } catch (...) {
+      g_last_error = "host error";
+    }
+  } catch (...) {
+    // recording the message itself failed; the status bit still reports it
+  }
+  return (int)SPH_ERR_HOST;
+}
+
 // Per-case float32 constants, rounded the way the reference's float32
 // program rounds its Python-float parameters (weak types become float32).
 int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long long cell_off,
@@ -527,7 +544,8 @@ int sph_abi_version(void) { return SPH_ABI_VERSION; }
 
 const char* sph_last_error(void) { return g_last_error.c_str(); }
 
-int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphHandle** out) {
+int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases,
+               SphHandle** out) try {
   if (!cfg || !cases || !out || n_cases <= 0)
     return fail((int)SPH_ERR_INVALID_ARG, "null argument or no cases");
   *out = nullptr;
@@ -544,6 +562,16 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
   if (!(cfg->verlet_skin >= 0.0 && cfg->verlet_skin <= 0.5))
     return fail((int)SPH_ERR_INVALID_ARG, "verlet_skin must lie in [0, 0.5]");
   SphHandle* h = new SphHandle();
+  // frees the handle and its device buffers on every early return and on an
+  // exception; released once the handle is complete
+  struct Reclaim {
+    SphHandle* h;
+    ~Reclaim() {
+      if (!h) return;
+      for (void* p : h->allocs) cudaFree(p);
+      delete h;
+    }
+  } reclaim{h};
   h->cfg = *cfg;
   h->n_cases = n_cases;
   h->cases.assign(cases, cases + n_cases);
@@ -551,15 +579,11 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
   std::vector<long long> off(n_cases + 1, 0);
   long long cells = 0, ref_cells = 0;
   for (int i = 0; i < n_cases; ++i) {
-    if (cases[i].n <= 0) {
-      delete h;
+    if (cases[i].n <= 0)
       return fail((int)SPH_ERR_INVALID_ARG, "every case needs at least one particle");
-    }
     std::string err;
-    if (make_case(*cfg, cases[i], off[i], cells, h->hc[i], err)) {
-      delete h;
+    if (make_case(*cfg, cases[i], off[i], cells, h->hc[i], err))
       return fail((int)SPH_ERR_INVALID_ARG, "case " + std::to_string(i) + ": " + err);
-    }
     h->hc[i].cref_off = (int)ref_cells;
     cells += h->hc[i].ncell + 1;  // + the parking cell of padding particles
     ref_cells += h->hc[i].ncref;
@@ -584,10 +608,8 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
     kv = kv < kVerletMinSlots ? kVerletMinSlots : (kv > kVerletMaxSlots ? kVerletMaxSlots : kv);
     h->kv = (int)kv;
   }
-  if (h->N >= INT_MAX / 2 || h->C >= INT_MAX / 2) {
-    delete h;
+  if (h->N >= INT_MAX / 2 || h->C >= INT_MAX / 2)
     return fail((int)SPH_ERR_INVALID_ARG, "problem too large for 32-bit indices");
-  }
   const long long N = h->N;
   const bool need_nw = cfg->solver == SPH_SOLVER_RIE || cfg->is_free_slip;
   int rc = 0;
@@ -634,16 +656,15 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases, SphH
                                cudaMemcpyHostToDevice),
                     "upload offsets");
   if (!rc) rc = upload_cases(h, 0);
-  if (rc) {
-    for (void* p : h->allocs) cudaFree(p);
-    delete h;
-    return rc;
-  }
+  if (rc) return rc;
+  reclaim.h = nullptr;
   *out = h;
   return 0;
+} catch (...) {
+  return host_error();
 }
 
-int sph_destroy(SphHandle* h) {
+int sph_destroy(SphHandle* h) try {
   if (!h) return 0;
   drop_graph(h);
   for (int k = 0; k < SphHandle::kCopyStreams; ++k) {
@@ -658,9 +679,11 @@ int sph_destroy(SphHandle* h) {
   cudaFree(h->layer_start);
   delete h;
   return 0;
+} catch (...) {
+  return host_error();
 }
 
-int sph_update_cases(SphHandle* h, const SphCase* cases, int32_t n_cases) {
+int sph_update_cases(SphHandle* h, const SphCase* cases, int32_t n_cases) try {
   if (!h || !cases) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (n_cases != h->n_cases) return fail((int)SPH_ERR_INVALID_ARG, "case count changed");
   std::vector<CaseDev> next(n_cases);
@@ -681,9 +704,11 @@ int sph_update_cases(SphHandle* h, const SphCase* cases, int32_t n_cases) {
   h->hc = next;
   drop_graph(h);
   return upload_cases(h, 0);
+} catch (...) {
+  return host_error();
 }
 
-int sph_set_state(SphHandle* h, const SphStateView* s, void* stream) {
+int sph_set_state(SphHandle* h, const SphStateView* s, void* stream) try {
   if (!h || !s) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (s->n != h->N) return fail((int)SPH_ERR_INVALID_ARG, "state has the wrong particle count");
   if (!s->r || !s->tag || !s->u || !s->v || !s->dudt || !s->dvdt || !s->rho || !s->p ||
@@ -704,9 +729,11 @@ int sph_set_state(SphHandle* h, const SphStateView* s, void* stream) {
   h->has_state = true;
   h->binned = h->lists = h->fresh = h->from_forward = h->pending_bc = false;
   return launch_status("set_state");
+} catch (...) {
+  return host_error();
 }
 
-int sph_get_state(SphHandle* h, SphStateView* s, void* stream) {
+int sph_get_state(SphHandle* h, SphStateView* s, void* stream) try {
   if (!h || !s) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   if (s->n != h->N) return fail((int)SPH_ERR_INVALID_ARG, "state has the wrong particle count");
@@ -716,15 +743,20 @@ int sph_get_state(SphHandle* h, SphStateView* s, void* stream) {
   launch_unpack(h->ctx((cudaStream_t)stream), h->buf[0], h->R4, *s, h->from_forward,
                 h->pending_bc, nullptr, 0.f, h->binned ? h->inv : nullptr);
   return launch_status("get_state");
+} catch (...) {
+  return host_error();
 }
 
-int sph_nl_update(SphHandle* h, void* stream) {
+int sph_nl_update(SphHandle* h, void* stream) try {
   if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   return bin_static(h, (cudaStream_t)stream);
+} catch (...) {
+  return host_error();
 }
 
-int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out, void* stream) {
+int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out,
+                    void* stream) try {
   if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   cudaStream_t st = (cudaStream_t)stream;
@@ -773,9 +805,11 @@ int sph_nl_allocate(SphHandle* h, int64_t extra_capacity, SphNLCapacity* cap_out
   }
   // the captured step reads the capacities from device memory: no re-capture
   return upload_cases(h, st);
+} catch (...) {
+  return host_error();
 }
 
-int sph_nl_set_capacity(SphHandle* h, const SphNLCapacity* cap) {
+int sph_nl_set_capacity(SphHandle* h, const SphNLCapacity* cap) try {
   if (!h || !cap) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (cap->cell_capacity < 0 || cap->cell_capacity > INT_MAX || cap->max_occupancy < 0)
     return fail((int)SPH_ERR_INVALID_ARG, "capacity out of range");
@@ -788,10 +822,12 @@ int sph_nl_set_capacity(SphHandle* h, const SphNLCapacity* cap) {
     c.edge_cap = cap->max_occupancy;
   }
   return upload_cases(h, 0);
+} catch (...) {
+  return host_error();
 }
 
 int sph_nl_edges(SphHandle* h, int32_t* idx, int64_t capacity, int64_t* count_dev,
-                 void* stream) {
+                 void* stream) try {
   if (!h || !idx || !count_dev || capacity < 0)
     return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (!h->binned) return fail((int)SPH_ERR_INVALID_ARG, "neighbour list not built");
@@ -804,9 +840,11 @@ int sph_nl_edges(SphHandle* h, int32_t* idx, int64_t capacity, int64_t* count_de
   launch_edges(L, h->buf[0], h->cellid, h->start, h->rowcnt, h->rowoff, h->scan_tmp, idx,
                capacity, (long long*)count_dev);
   return launch_status("edges");
+} catch (...) {
+  return host_error();
 }
 
-int sph_forward(SphHandle* h, void* stream) {
+int sph_forward(SphHandle* h, void* stream) try {
   if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   cudaStream_t st = (cudaStream_t)stream;
@@ -818,9 +856,11 @@ int sph_forward(SphHandle* h, void* stream) {
   h->from_forward = true;
   h->pending_bc = false;
   return launch_status("forward");
+} catch (...) {
+  return host_error();
 }
 
-int sph_step(SphHandle* h, int32_t nsteps, void* stream) {
+int sph_step(SphHandle* h, int32_t nsteps, void* stream) try {
   if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   if (nsteps < 0) return fail((int)SPH_ERR_INVALID_ARG, "negative step count");
@@ -841,6 +881,8 @@ int sph_step(SphHandle* h, int32_t nsteps, void* stream) {
     --nsteps;
   }
   return 0;
+} catch (...) {
+  return host_error();
 }
 
 }  // extern "C"
@@ -873,7 +915,7 @@ int pinned_host(const void* p, const char* name, bool* host, void** mapped = nul
 extern "C" {
 
 int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const float* ref_r_,
-                float threshold_sq, uint32_t* status_dev, void* stream) {
+                float threshold_sq, uint32_t* status_dev, void* stream) try {
   if (!h || !in_ || !out_ || !status_dev) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   SphStateView vin = *in_, vout = *out_;
   const SphStateView* in = &vin;
@@ -1120,10 +1162,12 @@ int sph_advance(SphHandle* h, const SphStateView* in_, SphStateView* out_, const
   if (e == cudaSuccess && (any_out || hst)) e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) return cuda_check(e, "advance");
   return launch_status("advance");
+} catch (...) {
+  return host_error();
 }
 
 int sph_set_wall_layer(SphHandle* h, const float* layer, int64_t m, const double* offset,
-                       double cutoff) {
+                       double cutoff) try {
   if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
   if (m < 0 || (m > 0 && (!layer || !offset || !(cutoff > 0.0))))
     return fail((int)SPH_ERR_INVALID_ARG, "bad wall layer");
@@ -1144,12 +1188,23 @@ int sph_set_wall_layer(SphHandle* h, const float* layer, int64_t m, const double
   const CaseDev& c = h->hc[0];
   WallLayer w{};
   w.n = (int)m;
+  // cells at least one search radius wide, so the 3^d cells around a point
+  // hold its radius; the grid is coarsened (widest side halved) until it has
+  // no more cells than about four per layer point -- any such grid finds the
+  // same nearest point
+  long long n[3];
+  for (int d = 0; d < 3; ++d) {
+    const double q = d < dim ? std::floor((double)c.box[d] / cutoff) : 1.0;
+    n[d] = q < 1.0 ? 1 : (q > 1048576.0 ? 1048576 : (long long)q);
+  }
+  while (n[0] * n[1] * n[2] > 4 * m + 64) {
+    const int d = n[0] >= n[1] && n[0] >= n[2] ? 0 : (n[1] >= n[2] ? 1 : 2);
+    n[d] = (n[d] + 1) / 2;
+  }
   for (int d = 0; d < 3; ++d) {
     const double box = d < dim ? (double)c.box[d] : 1.0;
-    int n = d < dim ? (int)std::floor(box / cutoff) : 1;
-    n = n < 1 ? 1 : n;
-    w.nc[d] = n;
-    w.cs[d] = (float)(box / n);  // >= cutoff: the 3^d cells around hold the radius
+    w.nc[d] = (int)n[d];
+    w.cs[d] = (float)(box / n[d]);
     w.off[d] = d < dim ? (float)offset[d] : 0.f;
   }
   w.cut2 = (float)(cutoff * cutoff);
@@ -1190,33 +1245,39 @@ int sph_set_wall_layer(SphHandle* h, const float* layer, int64_t m, const double
   w.start = h->layer_start;
   h->layer = w;
   return 0;
+} catch (...) {
+  return host_error();
 }
 
-int sph_set_block_size(SphHandle* h, int32_t threads) {
+int sph_set_block_size(SphHandle* h, int32_t threads) try {
   if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
   if (threads < 32 || threads > 256 || threads % 32)
     return fail((int)SPH_ERR_INVALID_ARG, "block size must be a multiple of 32 in [32, 256]");
   h->block = threads;
   drop_graph(h);
   return 0;
+} catch (...) {
+  return host_error();
 }
 
-int sph_step_launch_count(SphHandle* h, int32_t* count) {
+int sph_step_launch_count(SphHandle* h, int32_t* count) try {
   if (!h || !count) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   *count = h->launch_count;
   return 0;
+} catch (...) {
+  return host_error();
 }
 
-int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) {
+int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) try {
   if (!h || !ms || nsteps <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   cudaStream_t st = (cudaStream_t)stream;
   // events: 0 step start, 5 kick end, 6 rebuild start (after the host read
   // the flag), 1 rebuild end, 2 density end, 3 wall end, 4 force end
-  cudaEvent_t ev[7];
-  for (int k = 0; k < 7; ++k) cudaEventCreate(&ev[k]);
-  for (int k = 0; k < 4; ++k) ms[k] = 0.f;
+  cudaEvent_t ev[7] = {};
   int rc = 0;
+  for (int k = 0; k < 7 && !rc; ++k) rc = cuda_check(cudaEventCreate(&ev[k]), "profile events");
+  for (int k = 0; k < 4; ++k) ms[k] = 0.f;
   for (int i = 0; i < nsteps && !rc; ++i) {
     h->ev = ev;
     rc = step_once(h, st);
@@ -1233,11 +1294,14 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) {
       ms[k] += t / nsteps;
     }
   }
-  for (int k = 0; k < 7; ++k) cudaEventDestroy(ev[k]);
+  for (int k = 0; k < 7; ++k)
+    if (ev[k]) cudaEventDestroy(ev[k]);
   return rc;
+} catch (...) {
+  return host_error();
 }
 
-int sph_adjoint_init(SphHandle* h, int32_t slots) {
+int sph_adjoint_init(SphHandle* h, int32_t slots) try {
   if (!h || slots <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
   const SphConfig& c = h->cfg;
   if (c.solver != SPH_SOLVER_SPH || c.is_rho_evol || c.is_bc_trick || c.is_heat_conduction ||
@@ -1257,9 +1321,11 @@ int sph_adjoint_init(SphHandle* h, int32_t slots) {
   if (rc) return rc;
   h->tape_slots = slots;
   return 0;
+} catch (...) {
+  return host_error();
 }
 
-int sph_tape_record(SphHandle* h, int32_t slot, void* stream) {
+int sph_tape_record(SphHandle* h, int32_t slot, void* stream) try {
   if (!h || slot < 0 || slot >= h->tape_slots)
     return fail((int)SPH_ERR_INVALID_ARG, "tape slot out of range");
   if (!(h->from_forward && h->pending_bc))
@@ -1278,10 +1344,12 @@ int sph_tape_record(SphHandle* h, int32_t slot, void* stream) {
   cp(h->t_nbr + (size_t)slot * h->kmax * N, h->nbr, sizeof(int) * h->kmax * N);
   cp(h->t_cnt + slot * N, h->nbr_cnt, sizeof(int) * N);
   return cuda_check(e, "tape record");
+} catch (...) {
+  return host_error();
 }
 
 int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u,
-                     const float* lam_a_in, float* lam_a_out, void* stream) {
+                     const float* lam_a_in, float* lam_a_out, void* stream) try {
   if (!h || slot < 0 || slot >= h->tape_slots)
     return fail((int)SPH_ERR_INVALID_ARG, "tape slot out of range");
   if (!lam_r || !lam_u || !lam_a_in || !lam_a_out || lam_a_in == lam_a_out)
@@ -1292,9 +1360,11 @@ int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u,
                  h->t_R4 + slot * N, h->t_nbr + (size_t)slot * h->kmax * N,
                  h->t_cnt + slot * N, h->t_mu, lam_a_in, lam_a_out, lam_r, lam_u);
   return launch_status("adjoint step");
+} catch (...) {
+  return host_error();
 }
 
-int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream) {
+int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream) try {
   if (!h || !status) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   unsigned v = 0;
@@ -1304,11 +1374,14 @@ int sph_read_status(SphHandle* h, uint32_t* status, int32_t clear, void* stream)
   int rc = cuda_check(e, "read status");
   *status = v;
   return rc;
+} catch (...) {
+  return host_error();
 }
 
 int sph_rebuild_stats(SphHandle* h, int64_t* rebuilds, int32_t* kernels_per_rebuild,
-                      void* stream) {
-  if (!h || !rebuilds || !kernels_per_rebuild) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+                      void* stream) try {
+  if (!h || !rebuilds || !kernels_per_rebuild)
+    return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   unsigned long long v = 0;
   cudaError_t e = cudaMemcpyAsync(&v, h->rebuilds_d, sizeof(v), cudaMemcpyDeviceToHost, st);
@@ -1316,23 +1389,29 @@ int sph_rebuild_stats(SphHandle* h, int64_t* rebuilds, int32_t* kernels_per_rebu
   *rebuilds = (int64_t)v + h->rebuilds_h;
   *kernels_per_rebuild = h->rebuild_launches;
   return cuda_check(e, "rebuild stats");
+} catch (...) {
+  return host_error();
 }
 
-int sph_read_status_async(SphHandle* h, uint32_t* status_dev, int32_t clear, void* stream) {
+int sph_read_status_async(SphHandle* h, uint32_t* status_dev, int32_t clear, void* stream) try {
   if (!h || !status_dev) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   cudaStream_t st = (cudaStream_t)stream;
   cudaError_t e = cudaMemcpyAsync(status_dev, h->status, sizeof(unsigned),
                                   cudaMemcpyDeviceToDevice, st);
   if (e == cudaSuccess && clear) e = cudaMemsetAsync(h->status, 0, sizeof(unsigned), st);
   return cuda_check(e, "read status async");
+} catch (...) {
+  return host_error();
 }
 
-int sph_diagnostics(SphHandle* h, double* out, void* stream) {
+int sph_diagnostics(SphHandle* h, double* out, void* stream) try {
   if (!h || !out) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");
   launch_diagnostics(h->ctx((cudaStream_t)stream), h->buf[0], h->R4, h->from_forward,
                      h->pending_bc, out);
   return launch_status("diagnostics");
+} catch (...) {
+  return host_error();
 }
 
 }  // extern "C"

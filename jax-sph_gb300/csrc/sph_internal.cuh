@@ -691,5 +691,9 @@ int make_case(const SphConfig& cfg, const SphCase& in, long long p_off, long lon
               CaseDev& c, std::string& err, bool fine_cells = true);
 // sph_capi.cu: the message sph_last_error returns on this host thread.
 void set_last_error(const std::string& msg);
+// sph_capi.cu: called from the catch clause of an entry point; records the
+// in-flight C++ exception as the last error and returns SPH_ERR_HOST, so no
+// exception crosses the C ABI.
+int host_error() noexcept;
 
 }  // namespace sph

@@ -143,7 +143,7 @@ extern "C" {
 
 int sph_nl_edges_noalloc(int32_t dim, const double* box, double r_cutoff, int32_t mask_self,
                          const float* r, int64_t n, int32_t* idx, int64_t capacity,
-                         int64_t* count_dev, uint32_t* status_dev, void* stream) {
+                         int64_t* count_dev, uint32_t* status_dev, void* stream) try {
   if (dim != 2 && dim != 3) return fail((int)SPH_ERR_INVALID_ARG, "dimension must be 2 or 3");
   if (!box || !r || !idx || !count_dev) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
   if (n < 1 || n > kMaxN)
@@ -217,6 +217,8 @@ int sph_nl_edges_noalloc(int32_t dim, const double* box, double r_cutoff, int32_
   cudaError_t e = cudaGetLastError();
   if (e != cudaSuccess) return cuda_fail(e, "sph_nl_edges_noalloc launch");
   return 0;
+} catch (...) {
+  return host_error();
 }
 
 }  // extern "C"

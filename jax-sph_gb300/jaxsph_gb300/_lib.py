@@ -24,6 +24,7 @@ ERR_TIMEOUT = 0x400
 ERR_NONFINITE = 0x800
 INFO_MOVED = 0x2000
 WARN_BOX_EDGE = 0x1000
+ERR_HOST = 0x4000
 
 KERNELS = {"QSK": 0, "WC2K": 1}
 SOLVERS = {"SPH": 0, "RIE": 1, "DELTA": 2}

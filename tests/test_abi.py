@@ -41,6 +41,15 @@ def test_abi_version_and_error_string(lib):
     assert isinstance(lib.sph_last_error(), bytes)
 
 
+def test_status_bits_match_the_header():
+    src = open(HEADER).read()
+    bits = dict(re.findall(r"^#define SPH_(\w+) (0x[0-9a-f]+)u", src, re.M))
+    assert len(bits) >= 11 and "ERR_HOST" in bits
+    for name, value in bits.items():
+        assert getattr(_lib, name) == int(value, 16), name
+    assert len(set(bits.values())) == len(bits)  # every bit distinct
+
+
 def test_create_rejects_bad_arguments_without_touching_the_gpu(lib):
     lib.sph_create.restype = ctypes.c_int
     cfg = _lib.SphConfig(dim=4)
