@@ -8,7 +8,8 @@ state field in the root group (``write_h5``), and reads them back with
 reads the subset of the HDF5 format such files use, as the HDF5 file format
 specification defines it --
 
-* superblock version 0 or 1, 8- or 4-byte offsets and lengths;
+* superblock version 0 or 1, 8- or 4-byte offsets and lengths, at offset 0
+  or after a user block (offset 512, 1024, 2048, ...);
 * the root group as a symbol table (version-1 B-tree of symbol nodes, names
   in a local heap);
 * version-1 object headers (with continuation blocks) holding a dataspace
@@ -195,15 +196,21 @@ def write_h5(data_dict, path):
 class _File:
     def __init__(self, buf):
         self.b = buf
-        if buf[:8] != _SIG:
-            raise ValueError("not an HDF5 file (no signature at offset 0)")
-        ver = buf[8]
+        # the superblock starts at 0 or, after a user block, at 512 * 2^k;
+        # its base address is absolute and every other address is relative
+        # to it
+        sb = 0
+        while buf[sb:sb + 8] != _SIG:
+            sb = 512 if sb == 0 else 2 * sb
+            if sb + 8 > len(buf):
+                raise ValueError("not an HDF5 file (no signature at offset 0, 512, 1024, ...)")
+        ver = buf[sb + 8]
         if ver not in (0, 1):
             raise ValueError(f"HDF5 superblock version {ver} (libver='latest') is not supported")
-        self.so, self.sl = buf[13], buf[14]
+        self.so, self.sl = buf[sb + 13], buf[sb + 14]
         if self.so not in (4, 8) or self.sl not in (4, 8):
             raise ValueError("unsupported HDF5 offset/length sizes")
-        p = 24 + (4 if ver == 1 else 0)
+        p = sb + 24 + (4 if ver == 1 else 0)
         self.base = self.off(p)
         p += 4 * self.so
         self.root = p   # root group symbol table entry

@@ -1,8 +1,8 @@
 """The .h5 state files (io_state.py:30-85 of the reference) and restarts
 (case_setup.py:184-194): the writer's structure against the HDF5 file format
 specification (several symbol nodes under the root B-tree), round trips of
-every field type a state holds, the reader on big-endian data and on files it
-cannot read, the trajectory naming and the fluid-only state0 overwrite.
+every field type a state holds, the reader on a file libhdf5 wrote, on
+big-endian data, after a user block and on files it cannot read, the trajectory naming and the fluid-only state0 overwrite.
 """
 
 import os
@@ -138,6 +138,34 @@ def test_reader_takes_big_endian_data(tmp_path):
     p.write_bytes(bytes(b))
     back = io.read_h5(str(p), "numpy")["x"]
     assert back.dtype == np.float32 and np.array_equal(back, a)
+
+
+def test_reader_takes_a_file_written_by_libhdf5():
+    """An HDF5 file that libhdf5 itself wrote (MATLAB 7.3 format: a 512-byte
+    user block, then a version-0 superblock; one float64 dataset with
+    attribute messages the reader passes over), from scipy's test data."""
+    scipy_io = pytest.importorskip("scipy.io")
+    path = os.path.join(os.path.dirname(scipy_io.__file__), "matlab", "tests", "data",
+                        "testhdf5_7.4_GLNX86.mat")
+    if not os.path.exists(path):
+        pytest.skip("scipy's test data is not installed")
+    back = io.read_h5(path, "numpy")
+    assert list(back) == ["testdouble"]
+    x = back["testdouble"]
+    assert x.dtype == np.float64 and x.shape == (9, 1)
+    assert np.allclose(x[:, 0], np.arange(9) * np.pi / 4, rtol=0, atol=1e-15)
+
+
+def test_reader_finds_the_superblock_after_a_user_block(tmp_path):
+    a = np.arange(12, dtype=np.int32).reshape(3, 4)
+    p = tmp_path / "s.h5"
+    io.write_h5({"a": a}, str(p))
+    b = bytearray(p.read_bytes())
+    for ub in (512, 2048):
+        q = bytearray(b"u" * ub) + b
+        struct.pack_into("<Q", q, ub + 24, ub)          # base address: the superblock
+        p.write_bytes(bytes(q))
+        assert np.array_equal(io.read_h5(str(p), "numpy")["a"], a)
 
 
 def test_reader_rejects_what_it_does_not_read(tmp_path):
