@@ -140,7 +140,7 @@ def test_reader_takes_big_endian_data(tmp_path):
     assert back.dtype == np.float32 and np.array_equal(back, a)
 
 
-def test_reader_takes_a_file_written_by_libhdf5():
+def test_reader_takes_a_file_written_by_libhdf5(tmp_path):
     """An HDF5 file that libhdf5 itself wrote (MATLAB 7.3 format: a 512-byte
     user block, then a version-0 superblock; one float64 dataset with
     attribute messages the reader passes over), from scipy's test data."""
@@ -154,6 +154,38 @@ def test_reader_takes_a_file_written_by_libhdf5():
     x = back["testdouble"]
     assert x.dtype == np.float64 and x.shape == (9, 1)
     assert np.allclose(x[:, 0], np.arange(9) * np.pi / 4, rtol=0, atol=1e-15)
+    # the writer encodes the same array's dataspace and datatype messages
+    # byte for byte as libhdf5 did
+    mine = tmp_path / "mine.h5"
+    io.write_h5({"testdouble": x}, str(mine))
+
+    def messages(file_name):
+        f = io._File(open(file_name, "rb").read())
+        e = f.root
+        (entry,) = f.group_entries(f.off(e + f.sl + f.so + 8), f.off(e + f.sl + f.so + 16))
+        return {t: bytes(d) for t, d in f.messages(entry[1])}
+
+    theirs, ours = messages(path), messages(str(mine))
+    for mtype in (0x0001, 0x0003):                 # dataspace, datatype
+        assert ours[mtype] == theirs[mtype], hex(mtype)
+
+    def group(file_name):
+        """Root group fields that do not depend on sizes or addresses."""
+        b = open(file_name, "rb").read()
+        f = io._File(b)
+        e = f.root
+        cache = f.uint(e + 16, 4)
+        bt, hp = f.addr(f.off(e + 24)), f.addr(f.off(e + 32))
+        dsize, free, data = struct.unpack_from("<QQQ", b, hp + 8)
+        nxt, fsize = struct.unpack_from("<QQ", b, f.addr(data) + free)
+        node = struct.unpack_from("<4sBBHQQQ", b, bt)   # sig, type, level, used, left, right, key0
+        child, key1 = struct.unpack_from("<QQ", b, bt + 32)
+        snod = struct.unpack_from("<4sBBH", b, f.addr(child))
+        entry = struct.unpack_from("<QQI", b, f.addr(child) + 8)
+        return (cache, b[hp:hp + 8], free, nxt, free + fsize == dsize, node, key1, snod,
+                entry[0], entry[2])
+
+    assert group(str(mine)) == group(path)
 
 
 def test_reader_finds_the_superblock_after_a_user_block(tmp_path):
