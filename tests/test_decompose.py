@@ -25,10 +25,17 @@ def _free_port():
     return port
 
 
-def _setup():
+def _setup(case="tgv"):
     sys.path.insert(0, os.path.join(ROOT, "jax-sph_gb300"))
     from jaxsph_gb300 import cases
 
+    if case == "ht":
+        # heat transfer: walls, and the temperature fields ride along
+        s = cases.heat_transfer(dx=0.05)
+        g = torch.Generator().manual_seed(4)
+        s.state["T"] = 1.0 + torch.rand(s.n, generator=g)
+        s.state["dTdt"] = torch.randn(s.n, generator=g)
+        return s
     s = cases.tgv(dim=3, dx=2 * np.pi / 12)
     g = torch.Generator().manual_seed(3)
     L = 2 * np.pi
@@ -37,27 +44,31 @@ def _setup():
     return s
 
 
-def _worker(rank, ws, port, out):
+def _worker(rank, ws, port, out, case="tgv"):
     os.environ.update(MASTER_ADDR="127.0.0.1", MASTER_PORT=str(port), RANK=str(rank),
                       WORLD_SIZE=str(ws))
     import torch.distributed as dist
 
     dist.init_process_group("gloo", rank=rank, world_size=ws)
     from jaxsph_gb300 import decompose as dc
+    from jaxsph_gb300.solver import prepare_state
 
-    s = _setup()
+    s = _setup(case)
     slabs = dc.DistributedSlabs(s, device="cpu")
+    whole = prepare_state(s.state, s.dim, "cpu", heat=case == "ht")
+    whole.setdefault("nw", torch.zeros_like(whole["r"]))
     L = slabs.length
     x = s.state["r"][:, slabs.axis]
     owner = dc.slab_of(x, L, ws)
     ok = torch.equal(slabs.owned["gid"], torch.nonzero(owner == rank).squeeze(1))
-    # halo: everything within w of this slab, from the other ranks
-    w = 1.7
+    # halo: everything within w of this slab, from the other ranks, every
+    # field the slabs exchange
+    w = 0.27 * L
     local = slabs.local_state(w)
     want = torch.nonzero((owner == rank) | dc.near_slab(x, rank, ws, L, w)).squeeze(1)
     ok = ok and torch.equal(local["gid"], want)
-    ok = ok and torch.equal(local["r"], s.state["r"][want])
-    ok = ok and torch.equal(local["tag"], s.state["tag"][want])
+    for f in slabs.slabs.fields:
+        ok = ok and torch.equal(local[f], whole[f][want])
     # migration after a move along the slab axis
     shift = torch.zeros(s.dim)
     shift[slabs.axis] = 0.4 * L / ws
@@ -67,6 +78,9 @@ def _worker(rank, ws, port, out):
     new_owner = dc.slab_of(moved[:, slabs.axis], L, ws)
     ok = ok and torch.equal(slabs.owned["gid"], torch.nonzero(new_owner == rank).squeeze(1))
     ok = ok and torch.equal(slabs.owned["r"], moved[new_owner == rank])
+    for f in slabs.slabs.fields:
+        if f != "r":
+            ok = ok and torch.equal(slabs.owned[f], whole[f][new_owner == rank])
     counts = [torch.zeros(1, dtype=torch.int64) for _ in range(ws)]
     dist.all_gather(counts, torch.tensor([slabs.owned["gid"].numel()]))
     ok = ok and int(sum(c.item() for c in counts)) == s.n
@@ -74,11 +88,11 @@ def _worker(rank, ws, port, out):
     dist.destroy_process_group()
 
 
-def _run(ws):
+def _run(ws, case="tgv"):
     port = _free_port()
     ctx = mp.get_context("spawn")
     out = ctx.Manager().dict()
-    procs = [ctx.Process(target=_worker, args=(r, ws, port, out)) for r in range(ws)]
+    procs = [ctx.Process(target=_worker, args=(r, ws, port, out, case)) for r in range(ws)]
     for p in procs:
         p.start()
     for p in procs:
@@ -93,6 +107,10 @@ def test_exchange_and_migration_two_ranks():
 
 def test_exchange_and_migration_three_ranks():
     _run(3)
+
+
+def test_exchange_and_migration_of_heat_fields_two_ranks():
+    _run(2, "ht")
 
 
 def test_halo_width_covers_two_cutoffs_and_the_drift():
