@@ -64,7 +64,7 @@ def tune(engine, steps=6, candidates=CANDIDATES, use_cache=True):
     k = key(engine)
     if use_cache and k in db:
         engine.set_block_size(db[k]["block"])
-        return db[k]["block"], db[k]["ms"]
+        return db[k]["block"], {int(b): t for b, t in db[k]["ms"].items()}
     times = {}
     engine.profile(1)  # warm-up: first step of a freshly loaded state
     for b in candidates:
