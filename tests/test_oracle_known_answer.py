@@ -16,7 +16,10 @@ derivatives in closed form instead of autograd --
   (jax_md/space.py:170-181), EPS = 2.22e-16 (solver.py:21);
 * the Riemann solver's acceleration with the wall mirror states, the
   Shepard wall velocity and the limiter (solver.py:316-401, :533-588), on
-  fluid particles above a row of wall particles under gravity.
+  fluid particles above a row of wall particles under gravity;
+* the generalized wall BC, no-slip and free-slip (solver.py:431-530: Shepard
+  wall velocity and pressure with the gravity term, inverse EOS for every
+  particle) and Monaghan's artificial viscosity (:404-428).
 
 One pair sits across a periodic face, so a wrong image or sign shows. The
 vectorised oracle (gather / index_add over the edge list, gradients by
@@ -266,3 +269,134 @@ def test_oracle_riemann_forward_with_walls_matches_hand_computed_sums():
     scale = max(abs(x) for row in dudt for x in row)
     torch.testing.assert_close(out["dudt"], torch.tensor(dudt, dtype=torch.float64),
                                rtol=0, atol=1e-12 * scale)
+
+
+def _scalar_sph_walls(name, st, box, h, dx, cutoff, p_ref, rho0, p_bg, gamma, g, alpha,
+                      free_slip):
+    """Standard SPH with the generalized wall BC (solver.py:431-530, order of
+    :796-821) and Monaghan's artificial viscosity (:404-428, c_ab = 10)."""
+    r, m, eta, tag, nw = st["r"], st["mass"], st["eta"], st["tag"], st["nw"]
+    u, v = [list(x) for x in st["u"]], [list(x) for x in st["v"]]
+    n, dim = len(r), len(r[0])
+
+    def dot(a, b):
+        return sum(a[k] * b[k] for k in range(dim))
+
+    pairs = []
+    for i in range(n):
+        for j in range(n):
+            rij = _min_image(r[i], r[j], box)
+            d = math.sqrt(sum(x * x for x in rij))
+            if d < cutoff:
+                pairs.append((i, j, rij, d))
+    summ = [0.0] * n
+    for i, j, rij, d in pairs:
+        summ[i] += _w_dw(name, dim, h, d)[0]
+    rho = [m[i] * summ[i] if tag[i] == 0 else st["rho"][i] for i in range(n)]
+    p = [p_ref * ((x / rho0) ** gamma - 1) + p_bg for x in rho]
+    p_bg_tvf = p_ref * (0.0 - 1) + p_bg
+    gvec = [0.0, -g] + [0.0] * (dim - 2)
+    # wall particles: Shepard sums over their fluid neighbours
+    wsum = [0.0] * n
+    uw = [[0.0] * dim for _ in range(n)]
+    vw = [[0.0] * dim for _ in range(n)]
+    pw = [0.0] * n
+    rwf = [[0.0] * dim for _ in range(n)]
+    for i, j, rij, d in pairs:
+        if tag[j] != 0:
+            continue
+        w = _w_dw(name, dim, h, d)[0]
+        wsum[i] += w
+        pw[i] += w * p[j]
+        for k in range(dim):
+            uw[i][k] += w * u[j][k]
+            vw[i][k] += w * v[j][k]
+            rwf[i][k] += rho[j] * w * rij[k]
+    for i in range(n):
+        if tag[i] == 0:
+            continue
+        xu = [x / (wsum[i] + EPS) for x in uw[i]]
+        xv = [x / (wsum[i] + EPS) for x in vw[i]]
+        if free_slip:
+            nn = [-x for x in nw[i]]
+            xu = [nn[k] * dot(xu, nn) for k in range(dim)]
+            xv = [nn[k] * dot(xv, nn) for k in range(dim)]
+        u[i] = [2 * u[i][k] - xu[k] for k in range(dim)]
+        v[i] = [2 * v[i][k] - xv[k] for k in range(dim)]
+        p[i] = (pw[i] + dot(gvec, rwf[i])) / (wsum[i] + EPS)
+    rho = [rho0 * ((x + p_ref - p_bg) / p_ref) ** (1 / gamma) for x in p]
+    dudt = [list(gvec) for _ in range(n)]
+    dvdt = [[0.0] * dim for _ in range(n)]
+    for i, j, rij, d in pairs:
+        dw = _w_dw(name, dim, h, d)[1]
+        e = [x / (d + EPS) for x in rij]
+        c = ((m[i] / rho[i]) ** 2 + (m[j] / rho[j]) ** 2) / m[i] * dw / (d + EPS)
+        eta_ij = 2 * eta[i] * eta[j] / (eta[i] + eta[j] + EPS)
+        p_ij = (rho[j] * p[i] + rho[i] * p[j]) / (rho[i] + rho[j])
+        si = dot([v[i][k] - u[i][k] for k in range(dim)], rij)
+        sj = dot([v[j][k] - u[j][k] for k in range(dim)], rij)
+        both_fluid = tag[i] == 0 and tag[j] == 0
+        av = 0.0
+        if both_fluid:
+            av = m[j] * alpha * dx * 10.0 * dot([u[i][k] - u[j][k] for k in range(dim)], rij) \
+                / ((rho[i] + rho[j]) / 2 * (d * d + 0.01 * dx * dx))
+        for k in range(dim):
+            a_r = 0.5 * (rho[i] * u[i][k] * si + rho[j] * u[j][k] * sj)
+            dudt[i][k] += c * (-p_ij * rij[k] + a_r + eta_ij * (u[i][k] - u[j][k]))
+            dudt[i][k] += av * dw * e[k]
+            dvdt[i][k] += c * p_bg_tvf * rij[k]
+    return rho, p, u, v, dudt, dvdt
+
+
+@pytest.mark.parametrize("free_slip", [False, True])
+def test_oracle_wall_bc_forward_matches_hand_computed_sums(free_slip):
+    name, dim = "QSK", 2
+    g = torch.Generator().manual_seed(13)
+    dx = h = 0.05
+    box = [1.0, 1.0]
+    cutoff = 3 * h
+    fluid = [[0.50, 0.50], [0.56, 0.52], [0.45, 0.55], [0.52, 0.44], [0.47, 0.47]]
+    walls = [[0.42 + 0.05 * k, 0.40] for k in range(5)] + [[0.44 + 0.05 * k, 0.36]
+                                                          for k in range(4)]
+    r = torch.tensor(fluid + walls, dtype=torch.float64)
+    n, nf = r.shape[0], len(fluid)
+    tag = torch.tensor([0] * nf + [1] * (n - nf), dtype=torch.int32)
+    tag[-1] = 2  # one MOVING_WALL
+    nw = torch.zeros(n, dim, dtype=torch.float64)
+    nw[nf:, 1] = 1.0
+    p_ref, rho0, p_bg, gamma, grav, alpha = 100.0, 1.0, 2.0, 1.0, 1.0, 0.1
+    u = 0.3 * torch.randn(n, dim, generator=g, dtype=torch.float64)
+    u[nf:] = 0.0
+    u[-1, 0] = 1.0
+    st = {
+        "r": r, "tag": tag, "nw": nw, "u": u,
+        "v": u + 0.05 * torch.randn(n, dim, generator=g, dtype=torch.float64),
+        "mass": dx * dx * (1.0 + 0.1 * torch.rand(n, generator=g, dtype=torch.float64)),
+        "eta": 0.01 * (1.0 + torch.rand(n, generator=g, dtype=torch.float64)),
+        "dudt": torch.zeros(n, dim, dtype=torch.float64),
+        "dvdt": torch.zeros(n, dim, dtype=torch.float64),
+        "rho": 1.0 + 0.01 * torch.rand(n, generator=g, dtype=torch.float64),
+        "drhodt": torch.zeros(n, dtype=torch.float64),
+        "p": torch.zeros(n, dtype=torch.float64),
+    }
+    fns = oracle.partition.NeighborListFns(box, cutoff, torch.float64, mask_self=False)
+    nb = fns.allocate(r)
+    solver = oracle.sph.WCSPH(box, oracle.sph.TaitEoS(p_ref, rho0, p_bg, gamma),
+                              oracle.sph.make_g_ext_db(grav), dx, dim, 1e-4, 10.0,
+                              kernel=name, is_bc_trick=True, artificial_alpha=alpha,
+                              is_free_slip=free_slip)
+    out = solver.forward(st, nb.idx)
+    plain = {k: v.tolist() for k, v in st.items()}
+    rho, p, uu, vv, dudt, dvdt = _scalar_sph_walls(name, plain, box, h, dx, cutoff, p_ref, rho0,
+                                                   p_bg, gamma, grav, alpha, free_slip)
+    f64 = torch.float64
+    torch.testing.assert_close(out["p"], torch.tensor(p, dtype=f64), rtol=0, atol=1e-10)
+    torch.testing.assert_close(out["rho"], torch.tensor(rho, dtype=f64), rtol=1e-12, atol=0)
+    torch.testing.assert_close(out["u"], torch.tensor(uu, dtype=f64), rtol=0, atol=1e-13)
+    torch.testing.assert_close(out["v"], torch.tensor(vv, dtype=f64), rtol=0, atol=1e-13)
+    for key, want in (("dudt", dudt), ("dvdt", dvdt)):
+        scale = max(abs(x) for row in want for x in row)
+        torch.testing.assert_close(out[key], torch.tensor(want, dtype=f64), rtol=0,
+                                   atol=1e-12 * scale)
+    # the walls really took the BC: a wall velocity differs from its input
+    assert (out["u"][nf:] - st["u"][nf:]).abs().max() > 1e-3
