@@ -19,7 +19,10 @@ derivatives in closed form instead of autograd --
   fluid particles above a row of wall particles under gravity;
 * the generalized wall BC, no-slip and free-slip (solver.py:431-530: Shepard
   wall velocity and pressure with the gravity term, inverse EOS for every
-  particle) and Monaghan's artificial viscosity (:404-428).
+  particle) and Monaghan's artificial viscosity (:404-428);
+* one si_euler step (integrator.py:22-56) with SPH continuity (solver.py:24-30)
+  and a particle drifting through a periodic face, and the Riemann continuity
+  with wall mirror states (solver.py:108-164).
 
 One pair sits across a periodic face, so a wrong image or sign shows. The
 vectorised oracle (gather / index_add over the edge list, gradients by
@@ -400,3 +403,170 @@ def test_oracle_wall_bc_forward_matches_hand_computed_sums(free_slip):
                                    atol=1e-12 * scale)
     # the walls really took the BC: a wall velocity differs from its input
     assert (out["u"][nf:] - st["u"][nf:]).abs().max() > 1e-3
+
+
+def _pairs(r, box, cutoff):
+    out = []
+    for i in range(len(r)):
+        for j in range(len(r)):
+            rij = _min_image(r[i], r[j], box)
+            d = math.sqrt(sum(x * x for x in rij))
+            if d < cutoff:
+                out.append((i, j, rij, d))
+    return out
+
+
+def test_oracle_si_euler_step_with_continuity_matches_hand_computed_values():
+    """si_euler (integrator.py:22-56): u += dt dudt, v = u + tvf dt/2 dvdt,
+    r = (r + dt v) mod L, then SPH continuity (solver.py:24-30) from the
+    state's density and the standard + TVF accelerations on the new density."""
+    name, dim = "WC2K", 3
+    g = torch.Generator().manual_seed(17)
+    dx = h = 0.05
+    box = [1.0, 1.0, 1.0]
+    cutoff = 2 * h
+    r = torch.tensor(POSITIONS[3], dtype=torch.float64)
+    r[4, 0] = 0.001  # drifts across the lower face
+    n = r.shape[0]
+    p_ref, rho0, p_bg, gamma, tvf, dt = 100.0, 1.0, 0.0, 1.0, 1.0, 2e-3
+    st = {
+        "r": r, "tag": torch.zeros(n, dtype=torch.int32),
+        "mass": 1e-4 * (1.0 + 0.3 * torch.rand(n, generator=g, dtype=torch.float64)),
+        "eta": 0.01 * (1.0 + torch.rand(n, generator=g, dtype=torch.float64)),
+        "u": torch.randn(n, dim, generator=g, dtype=torch.float64),
+        "v": torch.zeros(n, dim, dtype=torch.float64),
+        "dudt": torch.randn(n, dim, generator=g, dtype=torch.float64),
+        "dvdt": torch.randn(n, dim, generator=g, dtype=torch.float64),
+        "rho": 1.0 + 0.02 * torch.rand(n, generator=g, dtype=torch.float64),
+        "drhodt": torch.zeros(n, dtype=torch.float64),
+        "p": torch.zeros(n, dtype=torch.float64),
+        "nw": torch.zeros(n, dim, dtype=torch.float64),
+    }
+    st["u"][4, 0] = -2.0  # 4 moves by about -4e-3: through x = 0
+    st["dudt"][4, 0] = 0.0
+    # room for particle 4 in its new cell: the update keeps the allocated capacities
+    fns = oracle.partition.NeighborListFns(box, cutoff, torch.float64, mask_self=False,
+                                           capacity_multiplier=4.0)
+    nb = fns.allocate(r)
+    solver = oracle.sph.WCSPH(box, oracle.sph.TaitEoS(p_ref, rho0, p_bg, gamma),
+                              oracle.sph.g_ext_zero, dx, dim, dt, 10.0, kernel=name,
+                              is_rho_evol=True)
+    out, nb = oracle.sph.si_euler_advance(dt, tvf, st, nb, fns, solver, oracle.sph.bc_identity)
+    assert not nb.did_buffer_overflow
+
+    s = {k: v.tolist() for k, v in st.items()}
+    u = [[s["u"][i][k] + dt * s["dudt"][i][k] for k in range(dim)] for i in range(n)]
+    v = [[u[i][k] + tvf * 0.5 * dt * s["dvdt"][i][k] for k in range(dim)] for i in range(n)]
+    rr = [[(s["r"][i][k] + dt * v[i][k]) % box[k] for k in range(dim)] for i in range(n)]
+    assert rr[4][0] > 0.99  # wrapped
+    m, eta, rho_in = s["mass"], s["eta"], s["rho"]
+    pairs = _pairs(rr, box, cutoff)
+    drho = [0.0] * n
+    for i, j, rij, d in pairs:
+        dw = _w_dw(name, dim, h, d)[1]
+        gradw = [dw * x / (d + EPS) for x in rij]
+        drho[i] += m[j] / rho_in[j] * sum((u[i][k] - u[j][k]) * gradw[k] for k in range(dim))
+    drho = [rho_in[i] * drho[i] for i in range(n)]
+    rho = [rho_in[i] + dt * drho[i] for i in range(n)]
+    p = [p_ref * ((x / rho0) ** gamma - 1) + p_bg for x in rho]
+    p_bg_tvf = p_ref * (0.0 - 1) + p_bg
+    dudt = [[0.0] * dim for _ in range(n)]
+    dvdt = [[0.0] * dim for _ in range(n)]
+    for i, j, rij, d in pairs:
+        dw = _w_dw(name, dim, h, d)[1]
+        c = ((m[i] / rho[i]) ** 2 + (m[j] / rho[j]) ** 2) / m[i] * dw / (d + EPS)
+        eta_ij = 2 * eta[i] * eta[j] / (eta[i] + eta[j] + EPS)
+        p_ij = (rho[j] * p[i] + rho[i] * p[j]) / (rho[i] + rho[j])
+        si = sum((v[i][k] - u[i][k]) * rij[k] for k in range(dim))
+        sj = sum((v[j][k] - u[j][k]) * rij[k] for k in range(dim))
+        for k in range(dim):
+            a_r = 0.5 * (rho[i] * u[i][k] * si + rho[j] * u[j][k] * sj)
+            dudt[i][k] += c * (-p_ij * rij[k] + a_r + eta_ij * (u[i][k] - u[j][k]))
+            dvdt[i][k] += c * p_bg_tvf * rij[k]
+
+    f64 = torch.float64
+    assert any(i == 4 and j == 5 for i, j, _, _ in pairs)
+    torch.testing.assert_close(out["r"], torch.tensor(rr, dtype=f64), rtol=0, atol=1e-15)
+    torch.testing.assert_close(out["u"], torch.tensor(u, dtype=f64), rtol=0, atol=1e-15)
+    torch.testing.assert_close(out["v"], torch.tensor(v, dtype=f64), rtol=0, atol=1e-15)
+    torch.testing.assert_close(out["drhodt"], torch.tensor(drho, dtype=f64), rtol=0,
+                               atol=1e-12 * max(map(abs, drho)))
+    torch.testing.assert_close(out["rho"], torch.tensor(rho, dtype=f64), rtol=1e-13, atol=0)
+    for key, want in (("dudt", dudt), ("dvdt", dvdt)):
+        scale = max(abs(x) for row in want for x in row)
+        torch.testing.assert_close(out[key], torch.tensor(want, dtype=f64), rtol=0,
+                                   atol=1e-12 * scale)
+
+
+def test_oracle_riemann_continuity_matches_hand_computed_values():
+    """Riemann continuity (solver.py:108-164, applied :772-790): the linear
+    Riemann mass flux, wall senders mirrored through their normals, fluid
+    receivers only."""
+    name, dim = "QSK", 2
+    g = torch.Generator().manual_seed(19)
+    dx = h = 0.05
+    box = [1.0, 1.0]
+    cutoff = 3 * h
+    fluid = [[0.50, 0.50], [0.56, 0.52], [0.45, 0.55], [0.52, 0.44], [0.47, 0.47]]
+    walls = [[0.42 + 0.05 * k, 0.40] for k in range(5)]
+    r = torch.tensor(fluid + walls, dtype=torch.float64)
+    n, nf = r.shape[0], len(fluid)
+    tag = torch.tensor([0] * nf + [1] * (n - nf), dtype=torch.int32)
+    nw = torch.zeros(n, dim, dtype=torch.float64)
+    nw[nf:, 1] = 1.0
+    u_ref, rho0, p_bg, c_ref, grav, dt = 1.0, 1.0, 0.0, 10.0, 1.0, 1e-4
+    u = 0.3 * torch.randn(n, dim, generator=g, dtype=torch.float64)
+    u[nf:] = 0.0
+    rho_in = 1.0 + 0.01 * torch.rand(n, generator=g, dtype=torch.float64)
+    st = {
+        "r": r, "tag": tag, "nw": nw, "u": u, "v": u.clone(),
+        "mass": dx * dx * (1.0 + 0.1 * torch.rand(n, generator=g, dtype=torch.float64)),
+        "eta": 0.01 * (1.0 + torch.rand(n, generator=g, dtype=torch.float64)),
+        "dudt": torch.zeros(n, dim, dtype=torch.float64),
+        "dvdt": torch.zeros(n, dim, dtype=torch.float64),
+        "rho": rho_in,
+        "drhodt": torch.zeros(n, dtype=torch.float64),
+        "p": 100 * u_ref**2 * (rho_in - rho0) + p_bg,
+    }
+    fns = oracle.partition.NeighborListFns(box, cutoff, torch.float64, mask_self=False)
+    nb = fns.allocate(r)
+    solver = oracle.sph.WCSPH(box, oracle.sph.RIEMANNEoS(rho0, p_bg, u_ref),
+                              oracle.sph.make_g_ext_db(grav), dx, dim, dt, c_ref,
+                              solver="RIE", kernel=name, is_bc_trick=True, is_rho_evol=True)
+    out = solver.forward(st, nb.idx)
+
+    s = {k: v.tolist() for k, v in st.items()}
+    m, rho, p, uu, nws = s["mass"], s["rho"], s["p"], s["u"], s["nw"]
+    gvec = [0.0, -grav]
+
+    def dot(a, b):
+        return a[0] * b[0] + a[1] * b[1]
+
+    drho = [0.0] * n
+    for i, j, rij, d in _pairs(s["r"], box, cutoff):
+        dw = _w_dw(name, dim, h, d)[1]
+        e = [x / (d + EPS) for x in rij]
+        gradw = [dw * x for x in e]
+        if s["tag"][j] != 0:
+            u_l = -dot(uu[i], nws[j])
+            u_r = -u_l + 2 * dot(uu[j], nws[j])
+            p_r = p[i] + rho[i] * (-dot(gvec, rij))
+            rho_r = (p_r - p_bg) / (100 * u_ref**2) + rho0
+        else:
+            u_l, u_r = -dot(uu[i], e), -dot(uu[j], e)
+            p_r, rho_r = p[j], rho[j]
+        u_avg = (u_l + u_r) / 2
+        rho_avg = (rho[i] + rho_r) / 2
+        u_star = u_avg + 0.5 * (p[i] - p_r) / (rho_avg * c_ref)
+        v_star = [u_star * (-e[k]) + ((uu[i][k] + uu[j][k]) / 2 - u_avg * (-e[k]))
+                  for k in range(dim)]
+        drho[i] += 2 * rho[i] * m[j] / rho[j] * dot([uu[i][k] - v_star[k] for k in range(dim)],
+                                                  gradw)
+    drho = [drho[i] if s["tag"][i] == 0 else 0.0 for i in range(n)]
+    want_rho = [rho[i] + dt * drho[i] for i in range(n)]
+    f64 = torch.float64
+    torch.testing.assert_close(out["drhodt"], torch.tensor(drho, dtype=f64), rtol=0,
+                               atol=1e-12 * max(map(abs, drho)))
+    torch.testing.assert_close(out["rho"], torch.tensor(want_rho, dtype=f64), rtol=1e-14,
+                               atol=0)
+    assert max(map(abs, drho[:nf])) > 0
