@@ -22,7 +22,11 @@ derivatives in closed form instead of autograd --
   particle) and Monaghan's artificial viscosity (:404-428);
 * one si_euler step (integrator.py:22-56) with SPH continuity (solver.py:24-30)
   and a particle drifting through a periodic face, and the Riemann continuity
-  with wall mirror states (solver.py:108-164).
+  with wall mirror states (solver.py:108-164);
+* delta-SPH: Marrone's density evolution with both renormalised gradient
+  terms and the diffusive acceleration (solver.py:33-105, :259-313), the
+  density renormalisation (:167-173) and Cleary's temperature equation
+  (:591-610, :832-850).
 
 One pair sits across a periodic face, so a wrong image or sign shows. The
 vectorised oracle (gather / index_add over the edge list, gradients by
@@ -570,3 +574,143 @@ def test_oracle_riemann_continuity_matches_hand_computed_values():
     torch.testing.assert_close(out["rho"], torch.tensor(want_rho, dtype=f64), rtol=1e-14,
                                atol=0)
     assert max(map(abs, drho[:nf])) > 0
+
+
+def _inv2(a):
+    det = a[0][0] * a[1][1] - a[0][1] * a[1][0]
+    return [[a[1][1] / det, -a[0][1] / det], [-a[1][0] / det, a[0][0] / det]]
+
+
+@pytest.mark.parametrize("renorm", [False, True])
+def test_oracle_delta_sph_and_heat_match_hand_computed_values(renorm):
+    """delta-SPH density evolution with both renormalised gradient terms
+    (solver.py:33-105, the sender-side term summed over receivers as the
+    reference does), the optional renormalisation (:167-173), the delta-SPH
+    acceleration (:259-313) and Cleary's temperature equation (:591-610,
+    :832-850), on a jittered periodic 8 x 8 lattice."""
+    name, dim = "QSK", 2
+    g = torch.Generator().manual_seed(23)
+    dx = h = 0.05
+    side = 8
+    box = [side * dx, side * dx]
+    cutoff = 3 * h
+    ij = torch.stack(torch.meshgrid(torch.arange(side), torch.arange(side), indexing="xy"),
+                     -1).reshape(-1, 2).to(torch.float64)
+    r = (ij + 0.5) * dx + 0.1 * dx * torch.randn(side * side, 2, generator=g,
+                                                 dtype=torch.float64)
+    r = torch.remainder(r, box[0])
+    n = r.shape[0]
+    p_ref, rho0, p_bg, gamma, c_ref, dt = 100.0, 1.0, 0.0, 1.0, 10.0, 1e-4
+    alpha, delta = 0.1, 0.02
+    st = {
+        "r": r, "tag": torch.zeros(n, dtype=torch.int32),
+        "mass": dx * dx * (1.0 + 0.1 * torch.rand(n, generator=g, dtype=torch.float64)),
+        "eta": 0.01 * (1.0 + torch.rand(n, generator=g, dtype=torch.float64)),
+        "u": 0.5 * torch.randn(n, dim, generator=g, dtype=torch.float64),
+        "dudt": torch.zeros(n, dim, dtype=torch.float64),
+        "dvdt": torch.zeros(n, dim, dtype=torch.float64),
+        "rho": 1.0 + 0.02 * torch.rand(n, generator=g, dtype=torch.float64),
+        "drhodt": torch.zeros(n, dtype=torch.float64),
+        "p": torch.zeros(n, dtype=torch.float64),
+        "nw": torch.zeros(n, dim, dtype=torch.float64),
+        "T": 1.0 + torch.rand(n, generator=g, dtype=torch.float64),
+        "dTdt": torch.randn(n, generator=g, dtype=torch.float64),
+        "kappa": 0.5 + torch.rand(n, generator=g, dtype=torch.float64),
+        "Cp": 1.0 + torch.rand(n, generator=g, dtype=torch.float64),
+    }
+    st["v"] = st["u"] + 0.05 * torch.randn(n, dim, generator=g, dtype=torch.float64)
+    fns = oracle.partition.NeighborListFns(box, cutoff, torch.float64, mask_self=False)
+    nb = fns.allocate(r)
+    solver = oracle.sph.WCSPH(box, oracle.sph.TaitEoS(p_ref, rho0, p_bg, gamma),
+                              oracle.sph.g_ext_zero, dx, dim, dt, c_ref, kernel=name,
+                              solver="DELTA", is_rho_evol=True, diff_alpha=alpha,
+                              diff_delta=delta, is_rho_renorm=renorm,
+                              is_heat_conduction=True)
+    out = solver.forward(st, nb.idx)
+
+    s = {k: v.tolist() for k, v in st.items()}
+    m, rho, u, v, eta = s["mass"], s["rho"], s["u"], s["v"], s["eta"]
+    pairs = _pairs(s["r"], box, cutoff)
+    assert int((nb.idx[0] < n).sum()) == len(pairs)
+
+    def dot(a, b):
+        return a[0] * b[0] + a[1] * b[1]
+
+    def grad(rij, d):
+        dw = _w_dw(name, dim, h, d)[1]
+        return [dw * x / (d + EPS) for x in rij]
+
+    vol = [m[i] / rho[i] for i in range(n)]
+    # M_i = sum over receiver i of outer(-r_ij, gradW_ij V_j); the sender-side
+    # matrix sums outer(r_ij, gradW_ij V_i) over the sender j
+    mi = [[[0.0, 0.0], [0.0, 0.0]] for _ in range(n)]
+    mj = [[[0.0, 0.0], [0.0, 0.0]] for _ in range(n)]
+    for i, j, rij, d in pairs:
+        gw = grad(rij, d)
+        for a in range(2):
+            for b in range(2):
+                mi[i][a][b] += -rij[a] * gw[b] * vol[j]
+                mj[j][a][b] += rij[a] * gw[b] * vol[i]
+    li = [_inv2(x) for x in mi]
+    lj = [_inv2(x) for x in mj]
+    gi = [[0.0, 0.0] for _ in range(n)]
+    gj = [[0.0, 0.0] for _ in range(n)]
+    for i, j, rij, d in pairs:
+        gw = grad(rij, d)
+        for a in range(2):
+            gi[i][a] += (rho[j] - rho[i]) * sum(li[i][a][b] * gw[b] * vol[j] for b in range(2))
+            gj[i][a] += (rho[i] - rho[j]) * sum(lj[j][a][b] * (-gw[b]) * vol[i]
+                                                for b in range(2))
+    cont = [0.0] * n
+    diff = [0.0] * n
+    for i, j, rij, d in pairs:
+        gw = grad(rij, d)
+        cont[i] += dot([u[i][k] - u[j][k] for k in range(2)], gw) * vol[j]
+        psi = [2 * (rho[j] - rho[i]) * (-rij[k]) / (d + EPS) ** 2 - gi[i][k] - gj[j][k]
+               for k in range(2)]
+        diff[i] += dot(psi, gw) * vol[j]
+    drho = [rho[i] * cont[i] + c_ref * delta * h * diff[i] for i in range(n)]
+    rho_new = [rho[i] + dt * drho[i] for i in range(n)]
+    if renorm:
+        num = [0.0] * n
+        den = [0.0] * n
+        for i, j, rij, d in pairs:
+            w = _w_dw(name, dim, h, d)[0]
+            num[i] += m[j] * w
+            den[i] += m[j] / rho_new[j] * w
+        rho_new = [num[i] / min(den[i], 1.0) for i in range(n)]
+    rho = rho_new
+    p = [p_ref * ((x / rho0) ** gamma - 1) + p_bg for x in rho]
+    temp = [s["T"][i] + dt * s["dTdt"][i] for i in range(n)]
+    kap, cp = s["kappa"], s["Cp"]
+    dTdt = [0.0] * n
+    dudt = [[0.0, 0.0] for _ in range(n)]
+    for i, j, rij, d in pairs:
+        gw = grad(rij, d)
+        dw = _w_dw(name, dim, h, d)[1]
+        f_ab = dot(rij, gw) / (d * d + EPS)
+        keff = kap[i] * kap[j] / (kap[i] + kap[j])
+        dTdt[i] += 4 * m[j] * keff * (temp[i] - temp[j]) * f_ab / (cp[i] * rho[i] * rho[j])
+        c = ((m[i] / rho[i]) ** 2 + (m[j] / rho[j]) ** 2) / m[i] * dw / (d + EPS)
+        eta_ij = 2 * eta[i] * eta[j] / (eta[i] + eta[j] + EPS)
+        p_ij = (rho[j] * p[i] + rho[i] * p[j]) / (rho[i] + rho[j])
+        si = dot([v[i][k] - u[i][k] for k in range(2)], rij)
+        sj = dot([v[j][k] - u[j][k] for k in range(2)], rij)
+        pi_ij = dot([u[j][k] - u[i][k] for k in range(2)], [-x for x in rij]) / (d + EPS) ** 2
+        for k in range(2):
+            a_r = 0.5 * (rho[i] * u[i][k] * si + rho[j] * u[j][k] * sj)
+            dudt[i][k] += c * (-p_ij * rij[k] + a_r + eta_ij * (u[i][k] - u[j][k]))
+            dudt[i][k] += (m[j] / rho[j]) * pi_ij * gw[k] * alpha * h * c_ref * rho0 / rho[i]
+
+    f64 = torch.float64
+    torch.testing.assert_close(out["drhodt"], torch.tensor(drho, dtype=f64), rtol=0,
+                               atol=1e-11 * max(map(abs, drho)))
+    torch.testing.assert_close(out["rho"], torch.tensor(rho, dtype=f64), rtol=1e-13, atol=0)
+    torch.testing.assert_close(out["T"], torch.tensor(temp, dtype=f64), rtol=1e-15, atol=0)
+    torch.testing.assert_close(out["dTdt"], torch.tensor(dTdt, dtype=f64), rtol=0,
+                               atol=1e-12 * max(map(abs, dTdt)))
+    scale = max(abs(x) for row in dudt for x in row)
+    torch.testing.assert_close(out["dudt"], torch.tensor(dudt, dtype=f64), rtol=0,
+                               atol=1e-11 * scale)
+    # the diffusion term is really exercised
+    assert max(map(abs, diff)) * c_ref * delta * h > 1e-3 * max(map(abs, drho))
