@@ -427,10 +427,13 @@ def gpu_arm(args, ws, rank, local):
         line["forms"] = {"batched": batched_form(device, 100), "adjoint": adjoint_form(device)}
     if rank == 0 and ws == 1 and not args.no_cpu:
         threads = os.cpu_count() or 1
-        rate, steps, secs, n_cpu, _ = cpu_oracle_rate(64, 2, 30.0, threads)
+        # a bounded sample: steps of the full case until ~10 s of CPU work
+        rate, steps, secs, n_cpu, warm = cpu_oracle_rate(64, 40, 10.0, threads, warmup=3,
+                                                         warmup_budget_s=10.0)
         line["cpu_baseline"] = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                                 "sample": f"{steps} float32 oracle si_euler step(s) of the full "
-                                          f"64^3 case after 1 warm-up step ({secs:.1f} s)"}
+                                          f"64^3 case after {warm} warm-up step(s) "
+                                          f"({secs:.1f} s)"}
     if rank == 0:
         print(json.dumps(line))
 
