@@ -125,9 +125,8 @@ class Simulation:
             self.engine.step(k)
             left -= k
             self.steps_done += k
-            if left > 0 or check_every < nsteps:
-                seen |= self._poll()
-        return seen | self._poll()
+            seen |= self._poll()  # once after every batch of steps
+        return seen if nsteps > 0 else self._poll()
 
     def _poll(self):
         code = self.engine.read_status(clear=True)
