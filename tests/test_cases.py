@@ -149,3 +149,25 @@ def test_matscipy_backend_arguments():
                                 pbc=np.array([True, False]))
     with pytest.raises(NotImplementedError):
         partition.neighbor_list(disp, np.ones(2), 0.1, backend="unknown")
+
+
+def test_fourier_perturbation_is_divergence_free_periodic_and_scaled():
+    """The adjoint workload's initial perturbation: u = (dpsi/dy, -dpsi/dx)
+    has zero divergence, the unit period of the box and RMS speed sigma."""
+    rng = np.random.default_rng(5)
+    pts = rng.uniform(0.0, 1.0, (64, 2))
+    eps = 1e-5
+    # one call for every probe: the field is scaled by its RMS over the points
+    # it is given, so all probes must share that scale
+    probes = [pts + [eps, 0.0], pts - [eps, 0.0], pts + [0.0, eps], pts - [0.0, eps], pts,
+              pts + [1.0, -1.0]]
+    u_all = cases.fourier_perturbation(np.concatenate(probes), 0.1, 8, 1).reshape(6, -1, 2)
+    div = (u_all[0, :, 0] - u_all[1, :, 0] + u_all[2, :, 1] - u_all[3, :, 1]) / (2 * eps)
+    # velocity gradients are ~ 2 pi kmax |u|; central differences leave ~eps^2 of them
+    grad_scale = 2 * np.pi * 8 * np.abs(u_all[4]).max()
+    assert np.abs(div).max() < 1e-6 * grad_scale
+    np.testing.assert_allclose(u_all[5], u_all[4], atol=1e-9)
+    grid = (np.stack(np.meshgrid(np.arange(32), np.arange(32)), -1).reshape(-1, 2) + 0.5) / 32
+    whole = cases.fourier_perturbation(grid, 0.1, 8, 1)
+    assert abs(np.sqrt((whole ** 2).sum(1).mean()) - 0.1) < 1e-12
+    assert not np.allclose(whole, cases.fourier_perturbation(grid, 0.1, 8, 2))
