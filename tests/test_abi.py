@@ -87,3 +87,29 @@ def test_struct_layout_matches_c(tmp_path):
         assert int(c[s]) == ctypes.sizeof(cls), s
         for f in fs:
             assert int(c[f"{s}.{f}"]) == getattr(cls, f).offset, f"{s}.{f}"
+
+
+@pytest.mark.skipif(__import__("torch").cuda.is_available(),
+                    reason="argument checks only: run where no kernel can launch")
+@pytest.mark.parametrize("dim,n,box,cutoff,capacity,word", [
+    (4, 100, 1.0, 0.1, 1000, b"dimension"),
+    (2, 0, 1.0, 0.1, 1000, b"particle count"),
+    (2, 65537, 1.0, 0.1, 1000, b"particle count"),
+    (2, 100, 1.0, 0.1, -1, b"capacity"),
+    (3, 100, 1.0, 0.005, 1000, b"cell"),
+])
+def test_noalloc_rejects_bad_arguments_before_any_gpu_work(lib, dim, n, box, cutoff, capacity,
+                                                            word):
+    fn = lib.sph_nl_edges_noalloc
+    fn.restype = ctypes.c_int
+    fn.argtypes = [ctypes.c_int32, ctypes.POINTER(ctypes.c_double), ctypes.c_double,
+                   ctypes.c_int32, ctypes.c_void_p, ctypes.c_int64, ctypes.c_void_p,
+                   ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    boxes = (ctypes.c_double * 3)(box, box, box)
+    # host placeholders: the checks reject the call before anything is read
+    dummy = ctypes.create_string_buffer(64)
+    addr = ctypes.addressof(dummy)
+    rc = fn(dim, boxes, cutoff, 0, addr, n, addr, capacity, addr, None, None)
+    assert rc == _lib.ERR_INVALID_ARG
+    lib.sph_last_error.restype = ctypes.c_char_p
+    assert word in lib.sph_last_error()
