@@ -113,3 +113,53 @@ def test_noalloc_rejects_bad_arguments_before_any_gpu_work(lib, dim, n, box, cut
     assert rc == _lib.ERR_INVALID_ARG
     lib.sph_last_error.restype = ctypes.c_char_p
     assert word in lib.sph_last_error()
+
+
+def _valid_case():
+    c = _lib.SphCase(n=100, r_cutoff=0.15, dx=0.05, h=0.05, dt=1e-4, dt_solver=1e-4,
+                     c_ref=10.0, eos=_lib.EOS_TAIT, p_ref=100.0, rho_ref=1.0, gamma=1.0,
+                     u_ref=1.0, eta_limiter=3.0)
+    c.box[0] = c.box[1] = c.box[2] = 1.0
+    return c
+
+
+@pytest.mark.parametrize("field,value,word", [
+    ("kernel", 5, b"kernel"),
+    ("solver", 7, b"solver"),
+    ("nl_backend", 3, b"nl_backend"),
+    ("verlet_skin", 0.7, b"verlet_skin"),
+    ("case.n", 0, b"at least one particle"),
+    ("case.r_cutoff", 0.0, b"r_cutoff"),
+    ("case.box", -1.0, b"box"),
+    ("case.bc_kind", 9, b"bc_kind"),
+])
+def test_create_validates_config_and_cases_before_allocating(lib, field, value, word):
+    """Every rejected configuration returns SPH_ERR_INVALID_ARG with a message
+    and no handle, before the first device allocation."""
+    lib.sph_create.restype = ctypes.c_int
+    lib.sph_last_error.restype = ctypes.c_char_p
+    cfg = _lib.SphConfig(dim=2, kernel=0, solver=0, capacity_multiplier=1.25, verlet_skin=0.1)
+    case = _valid_case()
+    if field.startswith("case."):
+        name = field[5:]
+        if name == "box":
+            case.box[0] = value
+        else:
+            setattr(case, name, value)
+    else:
+        setattr(cfg, field, value)
+    h = ctypes.c_void_p()
+    rc = lib.sph_create(ctypes.byref(cfg), ctypes.byref(case), 1, ctypes.byref(h))
+    assert rc == _lib.ERR_INVALID_ARG and not h.value
+    assert word in lib.sph_last_error()
+
+
+def test_handle_entry_points_reject_a_null_handle(lib):
+    lib.sph_last_error.restype = ctypes.c_char_p
+    assert lib.sph_step(None, 1, None) == _lib.ERR_INVALID_ARG
+    assert lib.sph_forward(None, None) == _lib.ERR_INVALID_ARG
+    assert lib.sph_nl_update(None, None) == _lib.ERR_INVALID_ARG
+    assert b"null" in lib.sph_last_error()
+    cfg = _lib.SphConfig(dim=2)
+    h = ctypes.c_void_p()
+    assert lib.sph_create(ctypes.byref(cfg), None, 0, ctypes.byref(h)) == _lib.ERR_INVALID_ARG
