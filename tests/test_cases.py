@@ -5,7 +5,7 @@ import pytest
 import torch
 
 import oracle
-from jaxsph_gb300 import _lib, cases
+from jaxsph_gb300 import _lib, cases, partition
 from oracle_setup import oracle_bc, oracle_g
 
 
@@ -136,7 +136,7 @@ def test_moving_wall_normals_only_where_the_reference_recomputes():
 
 
 def test_matscipy_backend_arguments():
-    from jaxsph_gb300 import partition, space
+    from jaxsph_gb300 import space
 
     disp, _ = space.periodic(np.ones(2))
     fns = partition.neighbor_list(disp, np.ones(2), 0.1, backend="matscipy",
@@ -171,3 +171,22 @@ def test_fourier_perturbation_is_divergence_free_periodic_and_scaled():
     whole = cases.fourier_perturbation(grid, 0.1, 8, 1)
     assert abs(np.sqrt((whole ** 2).sum(1).mean()) - 0.1) < 1e-12
     assert not np.allclose(whole, cases.fourier_perturbation(grid, 0.1, 8, 2))
+
+
+@pytest.mark.parametrize("mask_self", [False, True])
+@pytest.mark.parametrize("cap_factor", [0.6, 1.0, 1.5])
+def test_matscipy_edge_order_truncation_and_padding(mask_self, cap_factor):
+    """The host ordering of the matscipy backend's list (self edges first, then
+    pairs by first index), truncated to the capacity or padded, equals the
+    oracle's restatement for edges arriving in any order."""
+    rng = np.random.default_rng(3)
+    n = 60
+    r = torch.as_tensor(rng.uniform(0.0, 1.0, (n, 2)), dtype=torch.float32)
+    edges = oracle.partition.matscipy_edges(r, n, [1.0, 1.0], 0.2, mask_self)
+    cap = int(edges.shape[1] * cap_factor)
+    want, overflow = oracle.partition.matscipy_idx(edges, cap, n)
+    shuffled = edges[:, torch.as_tensor(rng.permutation(edges.shape[1]))].to(torch.int32)
+    got = partition.NeighborListFns._matscipy_order(None, shuffled, cap, n)
+    assert got.dtype == torch.int32 and got.shape == (2, cap)
+    assert torch.equal(got.long(), want)
+    assert overflow == (cap_factor < 1.0)
