@@ -190,3 +190,17 @@ def test_matscipy_edge_order_truncation_and_padding(mask_self, cap_factor):
     assert got.dtype == torch.int32 and got.shape == (2, cap)
     assert torch.equal(got.long(), want)
     assert overflow == (cap_factor < 1.0)
+
+
+@pytest.mark.parametrize("gamma", [1.0, 7.0])
+def test_product_eos_matches_the_oracle_and_inverts(gamma):
+    from jaxsph_gb300 import eos
+
+    rho = torch.linspace(0.9, 1.1, 41, dtype=torch.float64)
+    pairs = [(eos.TaitEoS(100.0, 1.0, 3.0, gamma), oracle.sph.TaitEoS(100.0, 1.0, 3.0, gamma)),
+             (eos.RIEMANNEoS(1.0, 2.0, 1.4142), oracle.sph.RIEMANNEoS(1.0, 2.0, 1.4142))]
+    for prod, ref in pairs:
+        p = prod.p_fn(rho)
+        torch.testing.assert_close(p, ref.p_fn(rho), rtol=1e-15, atol=1e-12)
+        torch.testing.assert_close(prod.rho_fn(p), ref.rho_fn(p), rtol=1e-15, atol=0)
+        torch.testing.assert_close(prod.rho_fn(p), rho, rtol=1e-13, atol=0)
