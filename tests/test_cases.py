@@ -204,3 +204,27 @@ def test_product_eos_matches_the_oracle_and_inverts(gamma):
         torch.testing.assert_close(p, ref.p_fn(rho), rtol=1e-15, atol=1e-12)
         torch.testing.assert_close(prod.rho_fn(p), ref.rho_fn(p), rtol=1e-15, atol=0)
         torch.testing.assert_close(prod.rho_fn(p), rho, rtol=1e-13, atol=0)
+
+
+@pytest.mark.parametrize("dtype", [torch.float32, torch.float64])
+def test_product_periodic_space_matches_the_oracle_bitwise(dtype):
+    """space.periodic's displacement and shift (jax_md/space.py:170-209) on the
+    host equal the oracle's jnp.mod restatement bit for bit, including values on
+    and just beyond the box faces."""
+    from jaxsph_gb300 import space
+
+    side_np = np.array([1.0, 2.0 * np.pi])
+    side = torch.as_tensor(side_np, dtype=dtype)
+    rng = np.random.default_rng(11)
+    a = torch.as_tensor(rng.uniform(-0.2, 1.2, (500, 2)) * side_np, dtype=dtype)
+    b = torch.as_tensor(rng.uniform(0.0, 1.0, (500, 2)) * side_np, dtype=dtype)
+    edge = torch.tensor([[0.0, 0.0], [1.0, 2 * np.pi], [-0.5, -np.pi], [0.5, np.pi]], dtype=dtype)
+    a = torch.cat([a, edge, torch.nextafter(edge, edge + 1), torch.nextafter(edge, edge - 1)])
+    b = torch.cat([b, torch.zeros_like(edge).repeat(3, 1)])
+    disp, shift = space.periodic(side_np)
+    got = disp(a, b)
+    want = oracle.space.periodic_displacement(side, a - b)
+    assert got.dtype == dtype and torch.equal(got, want)
+    dr = torch.as_tensor(rng.normal(0.0, 0.05, a.shape), dtype=dtype)
+    assert torch.equal(shift(b, dr), oracle.space.periodic_shift(side, b, dr))
+    assert torch.equal(shift(a, dr), oracle.space.periodic_shift(side, a, dr))
