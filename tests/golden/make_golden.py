@@ -6,7 +6,7 @@ four cases in ``tests/test_neighbors.py:87-121`` (positions, box, cutoff,
 mask_self flag and the expected canonical edge list). It writes
 ``neighbors_golden.json`` next to itself.
 
-Usage: python tests/golden/make_golden.py [path/to/jax-sph]
+Usage: python tests/golden/make_golden.py path/to/jax-sph
 """
 
 import ast
@@ -45,7 +45,9 @@ def extract(test_file):
 
 
 def main():
-    root = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+    if len(sys.argv) != 2:
+        sys.exit("usage: make_golden.py path/to/jax-sph (a checkout of the reference)")
+    root = sys.argv[1]
     test_file = os.path.join(root, "tests", "test_neighbors.py")
     cases = extract(test_file)
     out = {
