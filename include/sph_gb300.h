@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPH_ABI_VERSION 5
+#define SPH_ABI_VERSION 6
 
 /* Reference PartitionErrorCode bits (jax_sph/jax_md/partition.py:453-457). */
 #define SPH_NEIGHBOR_LIST_OVERFLOW 0x1u
@@ -279,8 +279,10 @@ int sph_rebuild_stats(SphHandle* h, int64_t* rebuilds, int32_t* kernels_per_rebu
 /* Run `nsteps` steps eagerly, timing their phases with CUDA events on
  * `stream` (where the kernels run): ms[0] kick-drift plus the candidate-list
  * rebuilds that fell in the steps, ms[1] density pass, ms[2] wall pass,
- * ms[3] force pass, averaged per step. Host-synchronous (the host reads the
- * rebuild decision of each step); the steps advance the state like sph_step. */
+ * ms[3] force pass, ms[4] the kick-drift alone, ms[5] the rebuilds alone (the
+ * sort and the candidate lists), each averaged per step; ms holds 6 floats.
+ * Host-synchronous (the host reads the rebuild decision of each step); the
+ * steps advance the state like sph_step. */
 int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream);
 
 /* Differentiable form: hand-written reverse of si_euler steps with the
@@ -333,6 +335,14 @@ int sph_nl_edges_noalloc(int32_t dim, const double* box, double r_cutoff, int32_
  * rho_max} of case c (fluid particles; E_kin follows jax_sph/utils.py:128-133).
  * `out` is a device array of n_cases*8 doubles. */
 int sph_diagnostics(SphHandle* h, double* out, void* stream);
+/* Per-particle size of the neighbour set the last forward pass (sph_forward,
+ * sph_step, sph_advance) summed over: counts[i] (original order, device
+ * int32 array of n) = the number of edges whose receiver is particle i, self
+ * pair included unless mask_self -- i.e. the number of entries of i in row 0
+ * of the reference's NeighborList.idx for the same positions
+ * (jax_md/partition.py:885-909). No counterpart function in the reference; a
+ * diagnostic of the per-step sets. */
+int sph_neighbour_counts(SphHandle* h, int32_t* counts, void* stream);
 
 #ifdef __cplusplus
 }

@@ -216,14 +216,17 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
     c.cut_hi = INFINITY;
   }
   // Fast cases are binned into half-size cells (fewer candidates per
-  // receiver: the walk covers +-2 half cells with trimmed rows instead of
-  // +-1 reference cell).
+  // receiver: the walk covers trimmed rows of half cells instead of +-1
+  // reference cell). It reaches 3 half cells on each side: the reference's
+  // candidates of a receiver in the lower half of its cell extend 3 half
+  // cells up, and where the reference cell is the cutoff to within rounding a
+  // sender at the cutoff distance can lie there.
   long long ncell = 1;
   for (int d = 0; d < 3; ++d) {
     const int sub = (fine_cells && c.fast && nc[d] > 1) ? 2 : 1;
     c.sub[d] = sub;
     c.nc[d] = nc[d] * sub;
-    c.rad[d] = nc[d] > 1 ? sub : 0;
+    c.rad[d] = nc[d] > 1 ? (sub == 2 ? 3 : 1) : 0;
     if (sub == 2) c.cell_size[d] = c.cell_size[d] * 0.5f;
     c.inv_cs[d] = 1.0f / c.cell_size[d];
     c.mult[d] = (int)ncell;
@@ -1277,7 +1280,7 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) try 
   cudaEvent_t ev[7] = {};
   int rc = 0;
   for (int k = 0; k < 7 && !rc; ++k) rc = cuda_check(cudaEventCreate(&ev[k]), "profile events");
-  for (int k = 0; k < 4; ++k) ms[k] = 0.f;
+  for (int k = 0; k < 6; ++k) ms[k] = 0.f;
   for (int i = 0; i < nsteps && !rc; ++i) {
     h->ev = ev;
     rc = step_once(h, st);
@@ -1289,6 +1292,8 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) try 
     cudaEventElapsedTime(&t, ev[0], ev[5]);
     cudaEventElapsedTime(&t2, ev[6], ev[1]);
     ms[0] += (t + t2) / nsteps;  // kick + rebuild, without the host's read
+    ms[4] += t / nsteps;
+    ms[5] += t2 / nsteps;
     for (int k = 1; k < 4; ++k) {
       cudaEventElapsedTime(&t, ev[k], ev[k + 1]);
       ms[k] += t / nsteps;
@@ -1410,6 +1415,16 @@ int sph_diagnostics(SphHandle* h, double* out, void* stream) try {
   launch_diagnostics(h->ctx((cudaStream_t)stream), h->buf[0], h->R4, h->from_forward,
                      h->pending_bc, out);
   return launch_status("diagnostics");
+} catch (...) {
+  return host_error();
+}
+
+int sph_neighbour_counts(SphHandle* h, int32_t* counts, void* stream) try {
+  if (!h || !counts) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+  if (!h->has_state || !h->from_forward || !h->binned)
+    return fail((int)SPH_ERR_INVALID_ARG, "no forward pass since the state was loaded");
+  launch_neighbour_counts(h->ctx((cudaStream_t)stream), h->buf[0], counts);
+  return launch_status("neighbour counts");
 } catch (...) {
   return host_error();
 }

@@ -437,12 +437,37 @@ __device__ __forceinline__ int ref_cell_hash(const float4& r, const CaseDev& c) 
   return h;
 }
 
+// Whether sender b lies in one of the 3^d reference cells around receiver
+// a's (per axis the same cell or a neighbour, periodically): the reference
+// tests only those senders (jax_md/partition.py:832-856). Fast cases walk
+// finer cells a little beyond them, so a pair at the cutoff distance whose
+// reference cells are two apart -- possible where the reference's cell is the
+// cutoff to within rounding -- must not become an edge. Pairs clearly inside
+// the cutoff are always adjacent (the band's margin exceeds the hash's
+// rounding), so only the band's candidates take this test.
+template <int DIM>
+__device__ __forceinline__ bool ref_adjacent(const float4& a, const float4& b, const CaseDev& c) {
+  const float pa[3] = {a.x, a.y, a.z}, pb[3] = {b.x, b.y, b.z};
+#pragma unroll
+  for (int d = 0; d < DIM; ++d) {
+    const int n = c.nc[d] / c.sub[d];
+    if (n < 3) continue;
+    int ia = __float2int_rz(__fdiv_rn(pa[d], c.cell_size[d])) / c.sub[d];
+    int ib = __float2int_rz(__fdiv_rn(pb[d], c.cell_size[d])) / c.sub[d];
+    ia = ia < 0 ? 0 : (ia >= n ? n - 1 : ia);
+    ib = ib < 0 ? 0 : (ib >= n ? n - 1 : ib);
+    const int k = ia > ib ? ia - ib : ib - ia;
+    if (k > 1 && k < n - 1) return false;
+  }
+  return true;
+}
+
 // The reference metric, out of line: only candidates in the narrow band
 // around the cutoff (or every candidate of a case without the fast test)
 // reach it, so the hot loop stays small.
 template <int DIM>
 __device__ __noinline__ bool exact_edge(float4 ri, float4 rj, const CaseDev* c) {
-  return is_edge<DIM>(ri, rj, *c);
+  return is_edge<DIM>(ri, rj, *c) && (!c->fast || ref_adjacent<DIM>(ri, rj, *c));
 }
 
 // Membership as the list's backend defines it, for the emitted edge lists and
@@ -454,7 +479,7 @@ __device__ __noinline__ bool exact_edge(float4 ri, float4 rj, const CaseDev* c) 
 template <int DIM>
 __device__ __noinline__ bool list_edge(float4 ri, float4 rj, const CaseDev* c) {
   if (c->f64_metric) return is_edge_f64<DIM>(ri, rj, *c);
-  return is_edge<DIM>(ri, rj, *c);
+  return is_edge<DIM>(ri, rj, *c) && (!c->fast || ref_adjacent<DIM>(ri, rj, *c));
 }
 
 // Minimum-image r_i - r_j of a pair already known to be an edge.
@@ -659,6 +684,12 @@ void launch_alloc_stats(const LaunchCtx& L, Buffers b, const int* cellid, const 
                         const int* rowcnt, int* case_max, unsigned long long* case_edges);
 void launch_diagnostics(const LaunchCtx& L, Buffers b, const float4* R4, bool from_forward,
                         bool apply_bc, double* out);
+// Per original index, the last forward pass's neighbour count (self pair
+// included unless masked; padding 0).
+void launch_neighbour_counts(const LaunchCtx& L, Buffers b, int32_t* counts);
+// Flag bit on a step-list count: the receiver's senders did not fit the
+// list's format (the lean passes); the count itself is below it.
+constexpr int kCountFlag = 1 << 30;
 
 // sph_forward.cu
 // Verlet candidate lists of the current binning.

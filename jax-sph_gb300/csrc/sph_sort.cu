@@ -615,6 +615,14 @@ __global__ void k_diagnostics(long long N, Buffers b, const float4* R4, const Ca
   atomic_max_pos(o + 7, (double)f.rho);
 }
 
+__global__ void k_neighbour_counts(long long N, const int* inv, const int* meta,
+                                   const int* nbr_cnt, int self_term, int32_t* counts) {
+  const long long t = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (t >= N) return;
+  const int q = inv[t];
+  counts[t] = tag_of(meta[q]) == PAD ? 0 : (nbr_cnt[q] & ~kCountFlag) + self_term;
+}
+
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
@@ -758,6 +766,11 @@ void launch_edges(const LaunchCtx& L, Buffers b, const int* cellid, const int* s
                                            idx, capacity);
   k_pad_edges<<<304, kBlock, 0, L.stream>>>(idx, capacity, rowoff + L.N, (int)L.N, count_dev,
                                             L.status);
+}
+
+void launch_neighbour_counts(const LaunchCtx& L, Buffers b, int32_t* counts) {
+  k_neighbour_counts<<<nblocks(L.N), kBlock, 0, L.stream>>>(L.N, L.inv, b.META, L.nbr_cnt,
+                                                            L.mask_self ? 0 : 1, counts);
 }
 
 void launch_diagnostics(const LaunchCtx& L, Buffers b, const float4* R4, bool from_forward,

@@ -78,7 +78,8 @@ EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sp
            "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_set_block_size",
            "sph_step_launch_count", "sph_profile_step", "sph_adjoint_init", "sph_tape_record",
            "sph_adjoint_step", "sph_read_status", "sph_read_status_async", "sph_diagnostics",
-           "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance", "sph_set_wall_layer"]
+           "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance", "sph_set_wall_layer",
+           "sph_neighbour_counts"]
 
 _LIB = None
 
@@ -118,6 +119,7 @@ def load(build_if_missing=True):
     lib.sph_read_status_async.argtypes = [V, V, ctypes.c_int32, V]
     lib.sph_rebuild_stats.argtypes = [V, P(ctypes.c_int64), P(ctypes.c_int32), V]
     lib.sph_advance.argtypes = [V, P(SphStateView), P(SphStateView), V, ctypes.c_float, V, V]
+    lib.sph_neighbour_counts.argtypes = [V, V, V]
     lib.sph_diagnostics.argtypes = [V, V, V]
     lib.sph_set_wall_layer.argtypes = [V, V, ctypes.c_int64, P(ctypes.c_double), ctypes.c_double]
     lib.sph_nl_edges_noalloc.argtypes = [ctypes.c_int32, P(ctypes.c_double), ctypes.c_double,
@@ -126,7 +128,7 @@ def load(build_if_missing=True):
     for name in EXPORTS:
         if name not in ("sph_abi_version", "sph_last_error"):
             getattr(lib, name).restype = I
-    if lib.sph_abi_version() != 5:
+    if lib.sph_abi_version() != 6:
         raise RuntimeError("libsph_gb300 ABI version mismatch")
     _LIB = lib
     return lib
@@ -286,11 +288,13 @@ class Engine:
         _check(self.lib.sph_step_launch_count(self.h, ctypes.byref(c)))
         return int(c.value)
 
-    def profile(self, nsteps):
-        """Average per-step milliseconds of (binning, density, wall, force)."""
-        ms = (ctypes.c_float * 4)()
+    def profile(self, nsteps, split=False):
+        """Average per-step milliseconds of (kick + rebuilds, density, wall,
+        force); with ``split`` also (kick alone, rebuilds alone)."""
+        ms = (ctypes.c_float * 6)()
         _check(self.lib.sph_profile_step(self.h, int(nsteps), ms, _stream()))
-        return [float(x) for x in ms]
+        out = [float(x) for x in ms]
+        return out if split else out[:4]
 
     def adjoint_init(self, slots):
         _check(self.lib.sph_adjoint_init(self.h, int(slots)))
@@ -362,6 +366,13 @@ class Engine:
         """The status word as a 0-d int32 device tensor (stream-ordered, no sync)."""
         out = torch.empty((), dtype=torch.int32, device="cuda")
         _check(self.lib.sph_read_status_async(self.h, _ptr(out), int(bool(clear)), _stream()))
+        return out
+
+    def neighbour_counts(self, device):
+        """Per particle (original order) the size of its neighbour set in the
+        last forward pass, self pair included unless masked (int32 device tensor)."""
+        out = torch.empty(self.n, dtype=torch.int32, device=device)
+        _check(self.lib.sph_neighbour_counts(self.h, _ptr(out), _stream()))
         return out
 
     def diagnostics(self, device):
