@@ -68,6 +68,7 @@ struct SphHandle {
   cudaStream_t cs[kCopyStreams] = {};
   cudaEvent_t fork = nullptr, join[kCopyStreams] = {};
   int block = 256;        // threads per block of the forward passes
+  int lean = 0;           // served by the lean passes (sph_lean.cu): list format
   unsigned* status = nullptr;
   unsigned long long* edgecnt = nullptr;
   int* case_max = nullptr;  // allocate: largest reference-cell occupancy per case
@@ -136,6 +137,8 @@ struct SphHandle {
     L.R4e = R4e;
     L.dscr = dscr;
     L.block = block;
+    L.lean = lean;
+    L.c1 = hc[0];
     L.launches = const_cast<int*>(&launch_count);
     L.ev = ev;
     return L;
@@ -593,6 +596,7 @@ int sph_create(const SphConfig* cfg, const SphCase* cases, int32_t n_cases,
     off[i + 1] = off[i] + cases[i].n;
   }
   h->N = off[n_cases];
+  h->lean = lean_config(*cfg, n_cases, h->hc[0]);
   h->C = cells;
   h->ref_cells = ref_cells;
   // Verlet slots: the candidates a particle of a case at lattice spacing dx
@@ -705,6 +709,12 @@ int sph_update_cases(SphHandle* h, const SphCase* cases, int32_t n_cases) try {
   }
   h->cases.assign(cases, cases + n_cases);
   h->hc = next;
+  const int lean = lean_config(h->cfg, n_cases, h->hc[0]);
+  if (lean != h->lean) {
+    // the list format changes with the passes: the lists must be rebuilt
+    h->lean = lean;
+    h->lists = false;
+  }
   drop_graph(h);
   return upload_cases(h, 0);
 } catch (...) {

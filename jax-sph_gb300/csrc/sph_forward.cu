@@ -708,6 +708,10 @@ cudaError_t prepare_kernels(int /*kv*/) {
 }
 
 void launch_verlet(const LaunchCtx& L, Buffers b, const int* cellid, const int* start) {
+  if (L.lean) {
+    launch_verlet_lean(L, b, cellid, start);
+    return;
+  }
   const int bt = verlet_block(L.kv);
   const int g = nblocks(L.N, bt);
   const size_t smem = (L.canonical ? 2 : 1) * sizeof(int) * L.kv * bt;
@@ -732,6 +736,10 @@ void launch_verlet(const LaunchCtx& L, Buffers b, const int* cellid, const int* 
 void launch_forward(const LaunchCtx& L, Buffers b, const float4* /*R4*/, float4* R4w, float4* UT4,
                     const int* cellid, const int* start, unsigned long long* edgecnt,
                     const float* g_arr, bool apply_bc, bool has_walls, int phases) {
+  if (L.lean) {
+    launch_forward_lean(L, b, R4w, cellid, start, edgecnt, g_arr, apply_bc, phases);
+    return;
+  }
   if (phases & 1)
     cudaMemsetAsync(edgecnt, 0, sizeof(unsigned long long) * L.n_cases, L.stream);
   if (L.dim == 3) {

@@ -641,6 +641,8 @@ struct LaunchCtx {
   float4* R4e;            // evolved density before renormalisation (rho_renorm)
   float4* dscr;           // delta-SPH density scratch: 5 planes of N float4
   int block;              // threads per block of the forward passes (<= 256)
+  int lean;               // lean passes (sph_lean.cu): 0 no, 1 16-bit lists, 2 32-bit
+  CaseDev c1;             // the single case (the lean passes take it by value)
   int* launches;          // optional host counter of kernel launches
   cudaEvent_t* ev;        // optional phase events: bin start, bin end, density end,
                           // wall end, force end
@@ -700,6 +702,16 @@ cudaError_t prepare_kernels(int kv);
 void launch_forward(const LaunchCtx& L, Buffers b, const float4* R4, float4* R4w, float4* UT4,
                     const int* cellid, const int* start, unsigned long long* edgecnt,
                     const float* g_arr, bool apply_bc, bool has_walls, int phases = 3);
+
+// sph_lean.cu: the lean candidate build and passes (one periodic case with
+// the fast test, standard SPH, density summation, no wall BC, no heat, cell
+// order). Their lists live in the buffers of the 32-bit lists. lean_config:
+// 0 not served, 1 served with 16-bit list offsets, 2 with 32-bit indices.
+int lean_config(const SphConfig& cfg, int n_cases, const CaseDev& c0);
+void launch_verlet_lean(const LaunchCtx& L, Buffers b, const int* cellid, const int* start);
+void launch_forward_lean(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid,
+                         const int* start, unsigned long long* edgecnt, const float* g_arr,
+                         bool apply_bc, int phases);
 
 // sph_delta.cu (after the density pass has written the step's neighbour list)
 // delta-SPH density evolution into Rout (rho, p, drho/dt, eta).

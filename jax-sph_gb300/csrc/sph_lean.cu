@@ -1,0 +1,577 @@
+// Lean candidate-list build, density pass and force pass for the plain
+// drop-in configuration: one periodic case whose every axis has at least five
+// reference cells (the fast membership test), standard SPH with density
+// summation (solver.py:176-178, :794-796), standard + transport-velocity
+// acceleration (:199-256), optional artificial viscosity (:404-428), no
+// generalized wall BC, no heat conduction, pair sums in cell order. The
+// neighbour sets, the membership test and the pair physics are those of the
+// generic passes in sph_forward.cu; what differs is how the passes are fed:
+//
+//  * the case's constants arrive as a kernel parameter (constant bank), so
+//    the hot loops take them as instruction operands instead of loading them
+//    through a pointer into global memory;
+//  * candidate and neighbour lists are k-major groups of four senders, one
+//    load per group: either 16-bit offsets o = j - i of the sender's sorted
+//    index from the receiver's, taken modulo the particle count, in an 8-byte
+//    word (cells are sorted with the last axis slowest, so a neighbour across
+//    that axis' periodic face is N minus a few planes away, i.e. a few planes
+//    modulo N), or -- when a few planes of the case hold more than 16 bits
+//    of particles -- 32-bit indices in a 16-byte word. A receiver with an
+//    offset that does not fit, or with more candidates or neighbours than
+//    slots, re-derives its senders from its cells instead;
+//  * the candidate build walks, for every particle of a cell, the same cells
+//    (those whose box lies within the list radius of the cell's box), so the
+//    lanes of a warp stay converged;
+//  * pair distances come from the reciprocal square root (at most 2 ulp)
+//    rather than the correctly rounded square root, and the pair quotients
+//    from the fast reciprocal; the float32 tolerances against the float64
+//    oracle hold either way, and membership never depends on them (it is
+//    decided on squared distances, exactly as in the generic passes).
+#include "sph_pairs.cuh"
+
+namespace sph {
+
+namespace {
+
+constexpr unsigned kFull = 0xffffffffu;
+
+inline int nblocks(long long n, int b) { return (int)((n + b - 1) / b); }
+
+// ------------------------------------------------------------------ list formats
+// A group of four list slots of one receiver. WIDE = false: four 16-bit
+// offsets modulo n in a uint2; WIDE = true: four 32-bit indices in an int4.
+template <bool WIDE>
+struct Fmt;
+
+template <>
+struct Fmt<false> {
+  using Word = uint2;
+  // the slot's value for sender j (false: no 16-bit representative)
+  static __device__ __forceinline__ bool enc(int i, int j, int n, int& o) {
+    int d = j - i;
+    if (d > 32767) d -= n;
+    else if (d < -32768) d += n;
+    o = d;
+    return d >= -32768 && d <= 32767;
+  }
+  static __device__ __forceinline__ int raw(const Word& w, int q) {
+    const unsigned h = (q & 2) ? w.y : w.x;
+    return (int)(short)(unsigned short)(h >> ((q & 1) * 16));
+  }
+  // the sender of a slot's value
+  static __device__ __forceinline__ int dec(int i, int o, int n) {
+    int j = i + o;
+    j += j < 0 ? n : 0;
+    j -= j >= n ? n : 0;
+    return j;
+  }
+  // the value that stands for the receiver itself (unused slots)
+  static __device__ __forceinline__ int self(int) { return 0; }
+  static __device__ __forceinline__ void put(Word* base, size_t stride, int k, int o) {
+    reinterpret_cast<unsigned short*>(base + (size_t)(k >> 2) * stride)[k & 3] =
+        (unsigned short)o;
+  }
+};
+
+template <>
+struct Fmt<true> {
+  using Word = int4;
+  static __device__ __forceinline__ bool enc(int, int j, int, int& o) {
+    o = j;
+    return true;
+  }
+  static __device__ __forceinline__ int raw(const Word& w, int q) {
+    return q == 0 ? w.x : (q == 1 ? w.y : (q == 2 ? w.z : w.w));
+  }
+  static __device__ __forceinline__ int dec(int, int o, int) { return o; }
+  static __device__ __forceinline__ int self(int i) { return i; }
+  static __device__ __forceinline__ void put(Word* base, size_t stride, int k, int o) {
+    reinterpret_cast<int*>(base + (size_t)(k >> 2) * stride)[k & 3] = o;
+  }
+};
+
+// Minimum-image r_i - r_j and its square (the fast branch of pair_dr).
+template <int DIM>
+__device__ __forceinline__ void mi_dr(const float4& ri, const float4& rj, const CaseDev& c,
+                                      float3& dr, float& d2) {
+  dr.x = ri.x - rj.x;
+  dr.y = ri.y - rj.y;
+  dr.z = (DIM == 3) ? ri.z - rj.z : 0.f;
+  dr.x = fmaf(-c.box[0], rintf(dr.x * c.inv_box[0]), dr.x);
+  dr.y = fmaf(-c.box[1], rintf(dr.y * c.inv_box[1]), dr.y);
+  if (DIM == 3) dr.z = fmaf(-c.box[2], rintf(dr.z * c.inv_box[2]), dr.z);
+  d2 = dr.x * dr.x + dr.y * dr.y + dr.z * dr.z;
+}
+
+// Membership of (receiver ri, sender rj): below the band an edge, above it
+// none, inside it the reference metric (jax_md/partition.py:897).
+template <int DIM>
+__device__ __forceinline__ bool lean_edge(const float4& ri, const float4& rj, const CaseDev& c,
+                                          const CaseDev* cp, float3& dr, float& d2) {
+  mi_dr<DIM>(ri, rj, c, dr, d2);
+  bool in = d2 < c.cut_lo;
+  if (!in && d2 < c.cut_hi) in = exact_edge<DIM>(ri, rj, cp);
+  return in;
+}
+
+// |r| and 1/(|r| + eps) from r^2: 0 and 1/eps for coincident particles,
+// like the reference's safe distance and its 1/(d + EPS).
+__device__ __forceinline__ void dist_inv(float d2, float& dist, float& inv_d) {
+  const float rs = rsqrtf(d2);
+  dist = d2 > 0.f ? d2 * rs : 0.f;
+  inv_d = d2 > 0.f ? rs : 1.0f / kEps;
+}
+
+// An upper bound of sqrt(x) for x > 0 (the reciprocal square root is within
+// 2 ulp; the factor covers it).
+__device__ __forceinline__ float sqrt_up(float x) { return x * rsqrtf(x) * 1.000001f; }
+
+// Visit the cells whose box lies within sqrt(r2) of the box of cell `cell`
+// (gaps between cell boxes, less the rounding margin), clamped to r* cells on
+// each side, as contiguous ranges [j0, j1) of the sorted order with the
+// periodic shift of their image: rows (the last axes) by the gap between the
+// boxes, in each row the cells within the chord of that distance. Every
+// particle of the cell sees the same cells, so the lanes of a warp --
+// receivers in neighbouring cells -- walk rows of the same shape; the price is
+// more candidates than the particle's own sphere holds.
+template <int DIM, typename F>
+__device__ __forceinline__ void box_rows(const CaseDev& c, int cell, const int* __restrict__ start,
+                                         int rx, int ry, int rz, float r2, F&& f) {
+  const int nx = c.nc[0], ny = c.nc[1], nz = (DIM == 3) ? c.nc[2] : 1;
+  const int cx = cell % nx;
+  const int t = cell / nx;
+  const int cy = t % ny;
+  const int cz = (DIM == 3) ? t / ny : 0;
+  const int* cs = start + c.cell_off;
+  const float R = sqrt_up(r2) + 2.f * c.trim_m;
+  const float R2 = R * R;
+  const int zr = (DIM == 3) ? rz : 0;
+  for (int dz = -zr; dz <= zr; ++dz) {
+    const float gz = (float)max(abs(dz) - 1, 0) * c.cell_size[2];
+    const float gz2 = (DIM == 3) ? gz * gz : 0.f;
+    if (gz2 >= R2) continue;
+    int zw = cz + dz;
+    float sz = 0.f;
+    if (zw < 0) { zw += nz; sz = -c.box[2]; }
+    else if (zw >= nz) { zw -= nz; sz = c.box[2]; }
+    for (int dy = -ry; dy <= ry; ++dy) {
+      const float gy = (float)max(abs(dy) - 1, 0) * c.cell_size[1];
+      const float g2 = gz2 + gy * gy;
+      if (g2 >= R2) continue;
+      int yw = cy + dy;
+      float sy = 0.f;
+      if (yw < 0) { yw += ny; sy = -c.box[1]; }
+      else if (yw >= ny) { yw -= ny; sy = c.box[1]; }
+      const int kx = min(rx, 1 + (int)(sqrt_up(R2 - g2) * c.inv_cs[0]));
+      const int xa = cx - kx, xb = cx + kx;
+      const int row = (zw * ny + yw) * nx;
+      if (xa < 0) {
+        f(cs[row], cs[row + xb + 1], make_float3(0.f, sy, sz));
+        f(cs[row + xa + nx], cs[row + nx], make_float3(-c.box[0], sy, sz));
+      } else if (xb >= nx) {
+        f(cs[row + xa], cs[row + nx], make_float3(0.f, sy, sz));
+        f(cs[row], cs[row + xb - nx + 1], make_float3(c.box[0], sy, sz));
+      } else {
+        f(cs[row + xa], cs[row + xb + 1], make_float3(0.f, sy, sz));
+      }
+    }
+  }
+}
+
+// Senders j != i that are edges of receiver i, the slow way: its candidate
+// list when every candidate fitted (but the neighbours did not), else the
+// walk of the cells around its cell at the last binning, where every sender
+// now within the cutoff was within the list radius.
+template <int DIM, bool WIDE, typename F>
+__device__ __forceinline__ void lean_slow(int N, int i, const float4& ri, const CaseDev& c,
+                                          const CaseDev* cp, const float4* __restrict__ P4,
+                                          const typename Fmt<WIDE>::Word* vl, const int* vcnt,
+                                          int kv, const int* cellid, const int* start, F&& f) {
+  using L = Fmt<WIDE>;
+  auto test = [&](int j) {
+    const float4 rj = __ldg(P4 + j);
+    float3 dr;
+    float d2;
+    if (lean_edge<DIM>(ri, rj, c, cp, dr, d2)) f(j, rj, dr, d2);
+  };
+  const int vc = vcnt[i];
+  if (vc <= kv) {
+    for (int k = 0; k < vc; ++k) test(L::dec(i, L::raw(vl[(size_t)(k >> 2) * N + i], k & 3), N));
+    return;
+  }
+  box_rows<DIM>(c, cellid[i] - c.cell_off, start, c.vrad[0], c.vrad[1], c.vrad[2], c.v_r2,
+                [&](int j0, int j1, float3) {
+                  for (int j = j0; j < j1; ++j)
+                    if (j != i) test(j);
+                });
+}
+
+// ------------------------------------------------------------------ candidates
+// The senders within the list radius of every receiver at the current
+// binning (shifted squared distance < v_r2), self excluded, in walk (cell)
+// order, written straight to the k-major list. vcnt = kv + 1 marks a receiver
+// whose candidates do not all fit (too many, or an offset beyond 16 bits):
+// the passes walk its cells instead.
+template <int DIM, bool WIDE>
+__global__ void __launch_bounds__(256)
+k_verlet_lean(int N, Buffers b, const CaseDev c, const int* __restrict__ cellid,
+              const int* __restrict__ start, typename Fmt<WIDE>::Word* vl, int* vcnt, int kv) {
+  using L = Fmt<WIDE>;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  if (tag_of(b.META[i]) == PAD) {
+    vcnt[i] = 0;
+    return;
+  }
+  const float4 ri = b.P4[i];
+  const float r2 = c.v_r2;
+  int m = 0;
+  bool wide = false;
+  typename L::Word* row = vl + i;
+  box_rows<DIM>(c, cellid[i] - c.cell_off, start, c.vrad[0], c.vrad[1], c.vrad[2], r2,
+                [&](int j0, int j1, float3 s) {
+    const float qx = ri.x - s.x, qy = ri.y - s.y, qz = ri.z - s.z;
+#pragma unroll 2
+    for (int j = j0; j < j1; ++j) {
+      const float4 rj = __ldg(b.P4 + j);
+      const float dx = qx - rj.x, dy = qy - rj.y, dz = (DIM == 3) ? qz - rj.z : 0.f;
+      if (j != i && dx * dx + dy * dy + dz * dz < r2) {
+        int o;
+        const bool fits = L::enc(i, j, N, o);
+        wide |= !fits;
+        if (m < kv && fits) L::put(row, (size_t)N, m, o);
+        ++m;
+      }
+    }
+  });
+  vcnt[i] = (wide || m > kv) ? kv + 1 : m;
+}
+
+// Edge count for the NEIGHBOR_LIST_OVERFLOW test (one case). The capacity is
+// read from the device copy of the case: a capacity update does not
+// re-capture the step's graph.
+__device__ __forceinline__ void count_edges1(int cnt, bool valid, unsigned long long* edgecnt,
+                                             const CaseDev* cp, unsigned* status) {
+  const unsigned mask = __ballot_sync(kFull, valid);
+  if (!valid) return;
+  const unsigned tot = __reduce_add_sync(mask, (unsigned)cnt);
+  if ((threadIdx.x & 31) == __ffs(mask) - 1) {
+    const unsigned long long old = atomicAdd(edgecnt, (unsigned long long)tot);
+    if ((long long)(old + tot) > cp->edge_cap) atomicOr(status, SPH_NEIGHBOR_LIST_OVERFLOW);
+  }
+}
+
+// ------------------------------------------------------------------ density
+// Summation density (rho_i = m_i sum_j W_ij over the edges, self pair
+// included unless masked; fluid receivers), Tait / Riemann EOS, and the
+// step's neighbour list (staged in shared memory, written k-major) for the
+// force pass. Candidates are filtered four at a time: one list word, four
+// independent position gathers.
+template <int DIM, int KER, bool KAHAN, bool WIDE>
+__global__ void __launch_bounds__(256, 4)
+k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_term,
+               const int* __restrict__ cellid, const int* __restrict__ start,
+               const typename Fmt<WIDE>::Word* __restrict__ vl, const int* __restrict__ vcnt,
+               int kv, typename Fmt<WIDE>::Word* nb, int* nbcnt, int kmax, float4* R4,
+               unsigned long long* edgecnt, unsigned* status) {
+  using L = Fmt<WIDE>;
+  using Word = typename L::Word;
+  extern __shared__ __align__(16) unsigned char s_raw[];  // [kmax / 4][blockDim.x] words
+  Word* s_nb = reinterpret_cast<Word*>(s_raw);
+  const int tid = threadIdx.x, bs = blockDim.x;
+  const int i = blockIdx.x * bs + tid;
+  const bool valid = i < N;
+  int cnt = 0;
+  if (valid) {
+    const int tag = tag_of(b.META[i]);
+    const bool fluid = tag == FLUID;
+    const float4 ri = b.P4[i];
+    Acc<KAHAN> s0;
+    if (fluid && self_term) s0.add(kw<KER>(0.f, c));
+    Word* srow = s_nb + tid;
+    int m = 0;
+    bool wide = false;
+    const int vc = vcnt[i];
+    if (vc <= kv) {
+      const Word* vli = vl + i;
+      const int ng = (vc + 3) >> 2;
+      Word wn = vli[0];  // (read even without candidates: never used then)
+      for (int g = 0; g < ng; ++g) {
+        const Word w = wn;
+        if (g + 1 < ng) wn = vli[(size_t)(g + 1) * N];
+        const int rem = vc - 4 * g;
+        int o[4];
+        float4 rj[4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          // slots past the count hold stale words: they stand for i itself
+          o[q] = q < rem ? L::raw(w, q) : L::self(i);
+          rj[q] = __ldg(b.P4 + L::dec(i, o[q], N));
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          float3 dr;
+          float d2;
+          const bool e = q < rem && lean_edge<DIM>(ri, rj[q], c, cp, dr, d2);
+          if (e && fluid) {
+            float dist, inv_d;
+            dist_inv(d2, dist, inv_d);
+            s0.add(kw<KER>(dist, c));
+          }
+          if (e && m < kmax) L::put(srow, (size_t)bs, m, o[q]);
+          m += e;
+        }
+      }
+    } else {
+      lean_slow<DIM, WIDE>(N, i, ri, c, cp, b.P4, vl, vcnt, kv, cellid, start,
+                           [&](int j, const float4&, const float3&, float d2) {
+                             if (fluid) {
+                               float dist, inv_d;
+                               dist_inv(d2, dist, inv_d);
+                               s0.add(kw<KER>(dist, c));
+                             }
+                             int o;
+                             wide |= !L::enc(i, j, N, o);
+                             if (m < kmax) L::put(srow, (size_t)bs, m, o);
+                             ++m;
+                           });
+    }
+    cnt = tag == PAD ? 0 : m + (self_term ? 1 : 0);
+    // a receiver whose senders do not fit the format keeps its count, flagged
+    nbcnt[i] = wide ? (m | kCountFlag) : m;
+    if (!wide && m <= kmax) {
+      const int ng = (m + 3) >> 2;
+      for (int g = 0; g < ng; ++g) nb[(size_t)g * N + i] = s_nb[g * bs + tid];
+    }
+    const float rho_i = b.U4[i].w;
+    const float rho_new = fluid ? ri.w * s0.s : rho_i;
+    const float p_new = eos_p(rho_new, c);
+    R4[i] = make_float4(rho_new, p_new, b.A4[i].w, b.ETA[i]);
+    if (!isfinite(rho_new) || !isfinite(p_new)) atomicOr(status, SPH_ERR_NONFINITE);
+  }
+  count_edges1(cnt, valid, edgecnt, cp, status);
+}
+
+// ------------------------------------------------------------------ force
+// Standard acceleration with the transport-velocity stress (solver.py:216-256),
+// the transport-velocity acceleration (:199-213), artificial viscosity
+// (:404-428), g_ext and bc_fn, over the density pass's neighbour list; the
+// next sender's four records are in flight while a pair is evaluated, and the
+// list word after the current one a group ahead.
+template <int DIM, int KER, bool KAHAN, bool WIDE>
+__global__ void __launch_bounds__(256, 3)
+k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* g_arr,
+             const float4* __restrict__ R4, const typename Fmt<WIDE>::Word* __restrict__ nb,
+             const int* __restrict__ nbcnt, int kmax, const typename Fmt<WIDE>::Word* vl,
+             const int* vcnt, int kv, const int* cellid, const int* start, bool apply_bc,
+             unsigned* status) {
+  using L = Fmt<WIDE>;
+  using Word = typename L::Word;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const int tag = tag_of(b.META[i]);
+  const bool fluid_i = tag == FLUID;
+  const float4 ri = b.P4[i];
+  const float m_i = ri.w;
+  const float3 ui = f3(b.U4[i]);
+  const float3 vi = f3(b.V4[i]);
+  const float4 Ri = R4[i];
+  const float rho_i = Ri.x, p_i = Ri.y, eta_i = Ri.w;
+  const float Vi = m_i / rho_i;
+  const float Vi2 = Vi * Vi;
+  const float inv_mi = 1.0f / m_i;
+  const float3 Ai = make_float3(rho_i * ui.x, rho_i * ui.y, rho_i * ui.z);
+  const float3 wi = make_float3(vi.x - ui.x, vi.y - ui.y, vi.z - ui.z);
+  const float3 gi = g_ext<DIM>(c, ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
+  const bool av = c.av_alpha != 0.0f;
+  const float p_bg = c.p_bg_tvf;
+  Acc<KAHAN> ax, ay, az, tx, ty, tz;
+  auto pair = [&](int j, const float4& rj, const float4& Uj4, const float4& Vj4,
+                  const float4& Rj, const float3& dr, float d2) {
+    float dist, inv_d;
+    dist_inv(d2, dist, inv_d);
+    const float gw = kdw<KER>(dist, c);
+    const float rho_j = Rj.x, p_j = Rj.y, eta_j = Rj.w, m_j = rj.w;
+    const float Vj = __fdividef(m_j, rho_j);
+    const float cc = (Vi2 + Vj * Vj) * inv_mi * gw * inv_d;
+    const float3 uj = f3(Uj4);
+    const float3 vj = f3(Vj4);
+    const float eta_ij = __fdividef(2.f * eta_i * eta_j, eta_i + eta_j + kEps);
+    const float p_ij = __fdividef(rho_j * p_i + rho_i * p_j, rho_i + rho_j);
+    const float ki = dot3(wi, dr);
+    const float kj = dot3(make_float3(vj.x - uj.x, vj.y - uj.y, vj.z - uj.z), dr);
+    float3 a = make_float3(cc * (-p_ij * dr.x + 0.5f * (Ai.x * ki + rho_j * uj.x * kj) +
+                                 eta_ij * (ui.x - uj.x)),
+                           cc * (-p_ij * dr.y + 0.5f * (Ai.y * ki + rho_j * uj.y * kj) +
+                                 eta_ij * (ui.y - uj.y)),
+                           cc * (-p_ij * dr.z + 0.5f * (Ai.z * ki + rho_j * uj.z * kj) +
+                                 eta_ij * (ui.z - uj.z)));
+    if (av && fluid_i && tag_of(b.META[j]) == FLUID) {
+      const float rho_ab = 0.5f * (rho_i + rho_j);
+      const float num = m_j * c.av_alpha * c.av_hab * c.av_cab *
+                        ((ui.x - uj.x) * dr.x + (ui.y - uj.y) * dr.y + (ui.z - uj.z) * dr.z);
+      const float k = num * gw * inv_d / (rho_ab * (dist * dist + c.av_eps));
+      a.x += k * dr.x;
+      a.y += k * dr.y;
+      a.z += k * dr.z;
+    }
+    ax.add(a.x);
+    ay.add(a.y);
+    az.add(a.z);
+    const float ct = cc * p_bg;
+    tx.add(ct * dr.x);
+    ty.add(ct * dr.y);
+    tz.add(ct * dr.z);
+  };
+  const int m = nbcnt[i];
+  if (m <= kmax) {
+    const Word* nbi = nb + i;
+    Word w = nbi[0];  // (read even without neighbours: never used then)
+    Word wn = m > 4 ? nbi[N] : w;
+    int j = m > 0 ? L::dec(i, L::raw(w, 0), N) : i;
+    float4 rj = __ldg(b.P4 + j), uj = __ldg(b.U4 + j), vj = __ldg(b.V4 + j), Rj = __ldg(R4 + j);
+    for (int k = 0; k < m; ++k) {
+      const int jc = j;
+      const float4 rc = rj, uc = uj, vc = vj, Rc = Rj;
+      const int kn = k + 1;
+      if (kn < m) {
+        if ((kn & 3) == 0) {
+          w = wn;
+          if (kn + 4 < m) wn = nbi[(size_t)((kn >> 2) + 1) * N];
+        }
+        j = L::dec(i, L::raw(w, kn & 3), N);
+        rj = __ldg(b.P4 + j);
+        uj = __ldg(b.U4 + j);
+        vj = __ldg(b.V4 + j);
+        Rj = __ldg(R4 + j);
+      }
+      float3 dr;
+      float d2;
+      mi_dr<DIM>(ri, rc, c, dr, d2);
+      pair(jc, rc, uc, vc, Rc, dr, d2);
+    }
+  } else {
+    lean_slow<DIM, WIDE>(N, i, ri, c, cp, b.P4, vl, vcnt, kv, cellid, start,
+                         [&](int j, const float4& rj, const float3& dr, float d2) {
+                           pair(j, rj, __ldg(b.U4 + j), __ldg(b.V4 + j), __ldg(R4 + j), dr,
+                                d2);
+                         });
+  }
+  float3 dudt = make_float3(ax.s + gi.x, ay.s + gi.y, az.s + gi.z);
+  float3 dvdt = make_float3(tx.s, ty.s, tz.s);
+  if (DIM == 2) {
+    dudt.z = 0.f;
+    dvdt.z = 0.f;
+  }
+  if (apply_bc) {
+    dudt = bc_acc(dudt, tag, c);
+    dvdt = bc_acc(dvdt, tag, c);
+  }
+  if (!isfinite(dudt.x) || !isfinite(dudt.y) || !isfinite(dudt.z))
+    atomicOr(status, SPH_ERR_NONFINITE);
+  b.A4[i] = make_float4(dudt.x, dudt.y, dudt.z, Ri.z);
+  b.A2[i] = make_float4(dvdt.x, dvdt.y, dvdt.z, 0.f);
+}
+
+template <int DIM, int KER, bool KAHAN, bool WIDE>
+void forward_lean_t(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid,
+                    const int* start, unsigned long long* edgecnt, const float* g_arr,
+                    bool apply_bc, int phases) {
+  using Word = typename Fmt<WIDE>::Word;
+  const int bt = L.block > 0 ? L.block : 256;
+  const int g = nblocks(L.N, bt);
+  const int N = (int)L.N;
+  Word* vl = reinterpret_cast<Word*>(L.vl);
+  Word* nb = reinterpret_cast<Word*>(L.nbr);
+  if (phases & 1) {
+    const size_t smem = sizeof(Word) * (L.kmax / 4) * bt;
+    k_density_lean<DIM, KER, KAHAN, WIDE><<<g, bt, smem, L.stream>>>(
+        N, b, L.c1, L.cases, !L.mask_self, cellid, start, vl, L.vcnt, L.kv, nb, L.nbr_cnt,
+        L.kmax, R4, edgecnt, L.status);
+    count_launch(L);
+    mark(L, 2);
+    mark(L, 3);
+  }
+  if (phases & 2) {
+    k_force_lean<DIM, KER, KAHAN, WIDE><<<g, bt, 0, L.stream>>>(
+        N, b, L.c1, L.cases, g_arr, R4, nb, L.nbr_cnt, L.kmax, vl, L.vcnt, L.kv, cellid, start,
+        apply_bc, L.status);
+    count_launch(L);
+    mark(L, 4);
+  }
+}
+
+template <int DIM, int KER, bool KAHAN>
+void forward_lean_w(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid,
+                    const int* start, unsigned long long* edgecnt, const float* g_arr,
+                    bool apply_bc, int phases) {
+  if (L.lean == 2)
+    forward_lean_t<DIM, KER, KAHAN, true>(L, b, R4, cellid, start, edgecnt, g_arr, apply_bc,
+                                          phases);
+  else
+    forward_lean_t<DIM, KER, KAHAN, false>(L, b, R4, cellid, start, edgecnt, g_arr, apply_bc,
+                                           phases);
+}
+
+template <int DIM, int KER>
+void forward_lean_k(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid,
+                    const int* start, unsigned long long* edgecnt, const float* g_arr,
+                    bool apply_bc, int phases) {
+  if (L.kahan)
+    forward_lean_w<DIM, KER, true>(L, b, R4, cellid, start, edgecnt, g_arr, apply_bc, phases);
+  else
+    forward_lean_w<DIM, KER, false>(L, b, R4, cellid, start, edgecnt, g_arr, apply_bc, phases);
+}
+
+template <int DIM, bool WIDE>
+void verlet_lean_t(const LaunchCtx& L, Buffers b, const int* cellid, const int* start) {
+  using Word = typename Fmt<WIDE>::Word;
+  k_verlet_lean<DIM, WIDE><<<nblocks(L.N, 256), 256, 0, L.stream>>>(
+      (int)L.N, b, L.c1, cellid, start, reinterpret_cast<Word*>(L.vl), L.vcnt, L.kv);
+}
+
+}  // namespace
+
+int lean_config(const SphConfig& cfg, int n_cases, const CaseDev& c0) {
+  if (!(n_cases == 1 && c0.fast && cfg.solver == SPH_SOLVER_SPH && !cfg.is_rho_evol &&
+        !cfg.is_heat_conduction && !cfg.canonical_order && !cfg.is_bc_trick &&
+        cfg.nl_backend == SPH_NL_JAXMD && c0.n < (1 << 30)))
+    return 0;
+  // 16-bit offsets when a sender lies at most vrad + 1 cells away along the
+  // slowest axis (the sorted order's planes) and that many planes hold well
+  // under 2^15 particles at the mean density; else 32-bit indices
+  const int slow = cfg.dim - 1;
+  const double per_plane = (double)c0.n / (double)c0.nc[slow];
+  const double reach = 1.5 * (double)(c0.vrad[slow] + 1) * per_plane;
+  return (c0.n <= 32768 || reach <= 32767.0) ? 1 : 2;
+}
+
+void launch_verlet_lean(const LaunchCtx& L, Buffers b, const int* cellid, const int* start) {
+  if (L.dim == 3) {
+    if (L.lean == 2) verlet_lean_t<3, true>(L, b, cellid, start);
+    else verlet_lean_t<3, false>(L, b, cellid, start);
+  } else {
+    if (L.lean == 2) verlet_lean_t<2, true>(L, b, cellid, start);
+    else verlet_lean_t<2, false>(L, b, cellid, start);
+  }
+  count_launch(L);
+}
+
+void launch_forward_lean(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid,
+                         const int* start, unsigned long long* edgecnt, const float* g_arr,
+                         bool apply_bc, int phases) {
+  if (phases & 1) cudaMemsetAsync(edgecnt, 0, sizeof(unsigned long long), L.stream);
+  if (L.dim == 3) {
+    if (L.kernel == SPH_KERNEL_QSK)
+      forward_lean_k<3, 0>(L, b, R4, cellid, start, edgecnt, g_arr, apply_bc, phases);
+    else
+      forward_lean_k<3, 1>(L, b, R4, cellid, start, edgecnt, g_arr, apply_bc, phases);
+  } else {
+    if (L.kernel == SPH_KERNEL_QSK)
+      forward_lean_k<2, 0>(L, b, R4, cellid, start, edgecnt, g_arr, apply_bc, phases);
+    else
+      forward_lean_k<2, 1>(L, b, R4, cellid, start, edgecnt, g_arr, apply_bc, phases);
+  }
+}
+
+}  // namespace sph
