@@ -44,18 +44,19 @@ WORKLOAD = ("3D Taylor-Green vortex 64^3 = 262,144 particles, periodic (2pi)^3, 
 STEP_BYTES = 128          # fused 3D TVF step: reads r,u,dudt,dvdt,m,eta,tag; writes r,u,v,dudt,dvdt,rho,p
 FORCE_BYTES = 76          # force pass: reads r,m,u,v,rho,p,eta (52 B); writes dudt,dvdt (24 B)
 DENSITY_BYTES = 24        # density pass: reads r,m (16 B); writes rho,p (8 B)
-BIN_BYTES = 104           # kick-drift + neighbour update: reads r,m,u,v,dudt,dvdt,eta,tag
-PHASES = ("kick+rebuild", "density", "wall", "force")
-PHASE_KERNELS = ("k_kick (+ k_hash_count/k_tile_scan/k_scatter/k_permute/k_verlet on rebuild)",
-                 "k_density", "k_wall", "k_force")
-PHASE_BYTES = (BIN_BYTES, DENSITY_BYTES, 0, FORCE_BYTES)
-# DRAM bytes per particle of one launch (dram__bytes_read.sum + dram__bytes_write.sum)
-# and FMA-pipe utilisation measured with ncu on the 128^3 case of the same kernels
-# (profiles/k_kick_tgv3d_128.md, k_density_tgv3d_128.md, k_force_tgv3d_128.md); traffic
-# grows in proportion to the particle count, so it scales to 64^3 per particle. The
-# kick phase's figure is the kick alone (the rebuild kernels run every few steps).
-PHASE_TRAFFIC = (131.5, 308.3, None, 220.5)
-PHASE_FP32_PIPE = (0.157, 0.226, None, 0.409)
+KICK_BYTES = 104          # kick-drift: reads r,m,u,v,dudt,dvdt,eta,tag (56 B); writes r,u,v (48 B)
+# The kernels of one step, with their algorithmic bytes per particle and what
+# one ncu capture of the same kernel on the 64^3 workload measured
+# (profiles/*_tgv3d_64.md): DRAM bytes per particle per launch
+# (dram__bytes_read.sum + dram__bytes_write.sum), FMA-pipe and issue activity.
+KERNELS = {
+    "kick": {"kernel": "k_kick", "alg_bytes": KICK_BYTES, "ncu": None},
+    "rebuild": {"kernel": "k_hash_count + scan + k_scatter + k_permute + k_verlet_lean "
+                          "(every few steps, per-step average)", "alg_bytes": None, "ncu": None},
+    "density": {"kernel": "k_density_lean", "alg_bytes": DENSITY_BYTES, "ncu": None},
+    "force": {"kernel": "k_force_lean", "alg_bytes": FORCE_BYTES, "ncu": None},
+}
+FP64_STEPS = 5  # steps of the float64 comparison run
 
 
 def dist_env():
@@ -180,6 +181,42 @@ def cpu_oracle_rate(n_side, max_steps, budget_s, threads, warmup=1, warmup_budge
     return setup.n * steps / dt, steps, dt, setup.n, warm
 
 
+def workload_config(args, n, ws):
+    """The ``config`` object both arms print (identical dicts)."""
+    return {"workload": (WORKLOAD if args.n_side == 64 else
+                         WORKLOAD.replace("64^3 = 262,144", f"{args.n_side}^3 = {n:,}")),
+            "n_particles": n, "parallelism": f"replicas x{ws}", "verlet_skin": args.skin,
+            "l2": "flushed between timed steps (256 MiB write outside the events)"}
+
+
+def fp64_error(setup, steps, device, threads):
+    """The GPU rollout's error against a float64 run: ``steps`` si_euler steps
+    of the case on the GPU (float32) and in the float64 oracle (the CPU
+    restatement of the reference step) from the same initial state; max over
+    particles of |r - r64| (minimum image) / box, |u - u64| / max|u64| and
+    |rho - rho64| / rho_ref."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from jaxsph_gb300 import simulate
+    from oracle_setup import oracle_rollout
+    import oracle
+
+    sim = simulate.Simulation(setup, device=device)
+    sim.run(steps, check_every=1)
+    got = sim.state()[0]
+    del sim
+    torch.set_num_threads(threads)
+    with torch.no_grad():
+        ref = oracle_rollout(setup, steps, torch.float64)
+    side = torch.as_tensor(setup.box, dtype=torch.float64)
+    dr = oracle.space.periodic_displacement(side, got["r"].double().cpu() - ref["r"])
+    u64 = ref["u"]
+    return {"steps": steps, "against": "float64 oracle (CPU restatement of the reference step)",
+            "r_max_over_box": float(dr.abs().max() / side.max()),
+            "u_max_rel": float((got["u"].double().cpu() - u64).abs().max() / u64.abs().max()),
+            "rho_max_rel": float((got["rho"].double().cpu() - ref["rho"]).abs().max()
+                                 / setup.eos.rho_ref)}
+
+
 def reference_arm(args, ws, rank):
     if rank != 0:
         return
@@ -191,7 +228,7 @@ def reference_arm(args, ws, rank):
         "steps": steps, "warmup": warm, "ms_per_step": 1000.0 * secs / steps,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (reference initial condition of the 3D TGV)",
-        "config": {"workload": WORKLOAD, "n_particles": n},
+        "config": workload_config(args, n, args.gpus),
         "cpu_baseline": {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
                          "sample": f"{steps} float32 oracle si_euler steps of the full 64^3 "
                                    f"case (time-bounded, 150 s budget, after {warm} warm-up "
@@ -261,7 +298,7 @@ def timed_steps(sim, steps):
     return [s.elapsed_time(e) for s, e in zip(starts, ends)]
 
 
-def batched_form(device, steps, n_instances=256):
+def batched_form(device, steps, n_instances=256, fp64=True):
     """The batched form on its own workload: 256 cavity/channel instances with
     log-uniform particle counts as one resident batch (one CUDA graph per step,
     autotuned block size) versus the same instances run one after another on
@@ -292,16 +329,64 @@ def batched_form(device, steps, n_instances=256):
         one.run(5)
         a, b = ref_states[k], one.state()[0]
         diffs.append(max(float((a[x].double() - b[x].double()).abs().max()) for x in ("r", "u", "rho")))
+    errors = None
+    if fp64:
+        # the batched result against float64 runs of the same instances
+        sys.path.insert(0, os.path.join(ROOT, "tests"))
+        from oracle_setup import oracle_rollout
+        import oracle
+
+        errs = {"r_max_over_box": 0.0, "u_max_rel": 0.0, "rho_max_rel": 0.0}
+        with torch.no_grad():
+            for k in (0, n_instances - 1):
+                ref = oracle_rollout(batch[k], 5, torch.float64)
+                got = ref_states[k]
+                side = torch.as_tensor(batch[k].box, dtype=torch.float64)
+                dr = oracle.space.periodic_displacement(side, got["r"].double().cpu() - ref["r"])
+                scale_u = max(float(ref["u"].abs().max()), batch[k].u_ref)
+                e = {"r_max_over_box": float(dr.abs().max() / side.max()),
+                     "u_max_rel": float((got["u"].double().cpu() - ref["u"]).abs().max())
+                                  / scale_u,
+                     "rho_max_rel": float((got["rho"].double().cpu() - ref["rho"]).abs().max()
+                                          / batch[k].eos.rho_ref)}
+                errs = {x: max(errs[x], e[x]) for x in errs}
+        errors = dict(errs, steps=5, instances=[0, n_instances - 1],
+                      against="float64 oracle (CPU restatement of the reference step)")
     per_instance = n_total / (plain_ms * 1e-3)
     return {"workload": f"{n_instances} lid-driven cavities / Poiseuille channels (2D, QSK, SPH, "
                         f"wall BC), fluid particles log-uniform 1e3-4e4, {n_total:,} particles",
             "value": batched, "unit": UNIT, "steps": steps, "block_size": sim.block_size,
             "per_instance_value": per_instance, "speedup_vs_per_instance": batched / per_instance,
             "max_abs_diff_vs_per_instance": max(diffs),
-            "launches_per_step": sim.engine.launch_count()}
+            "launches_per_step": sim.engine.launch_count(), "error_vs_fp64": errors}
 
 
-def adjoint_form(device, steps=100, checkpoint_every=10):
+def oracle_gradient(setup, u0, target, steps):
+    """Loss and gradient w.r.t. u0 through the float64 oracle rollout, the
+    neighbour list frozen per step (jax.grad(..., allow_int=True))."""
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    from jaxsph_gb300 import adjoint
+    from oracle_setup import oracle_case
+    import oracle
+
+    solver, fns, bc, st = oracle_case(setup, torch.float64)
+    u = u0.detach().double().cpu().clone().requires_grad_(True)
+    st = dict(st, u=u, v=u)
+    nb = fns.allocate(st["r"].detach())
+    side = torch.as_tensor(setup.box, dtype=torch.float64)
+    for _ in range(steps):
+        st = dict(st)
+        st["u"] = st["u"] + setup.dt * st["dudt"]
+        st["v"] = st["u"] + setup.tvf * 0.5 * setup.dt * st["dvdt"]
+        st["r"] = oracle.space.periodic_shift(side, st["r"], setup.dt * st["v"])
+        nb = fns.update(st["r"].detach(), nb)
+        st = bc(solver.forward(st, nb.idx))
+    loss = adjoint.position_mse(st["r"], target.double().cpu(), setup.box)
+    (g,) = torch.autograd.grad(loss, u)
+    return float(loss), g
+
+
+def adjoint_form(device, steps=100, checkpoint_every=10, fp64=True):
     """The differentiable form on its own workload: gradient of the final
     positions' mean squared distance to a target rollout (another seed) with
     respect to the initial velocity of a 128^2 perturbed 2D TGV, through the
@@ -330,6 +415,13 @@ def adjoint_form(device, steps=100, checkpoint_every=10):
         loss, g = gradient()
     torch.cuda.synchronize()
     t_grad = (time.perf_counter() - t0) / reps
+    err = None
+    if fp64:
+        loss64, g64 = oracle_gradient(a, u0, target, steps)
+        err = {"grad_rel_l2": float((g.double().cpu() - g64).norm() / g64.norm()),
+               "loss_rel": abs(float(loss) - loss64) / abs(loss64),
+               "against": "torch autograd through the float64 oracle rollout "
+                          "(neighbour lists frozen per step)"}
     plain = simulate.Simulation(a, device=device)
     plain.run(3)
     torch.cuda.synchronize()
@@ -345,7 +437,7 @@ def adjoint_form(device, steps=100, checkpoint_every=10):
             "checkpoint_every": checkpoint_every, "loss": float(loss.detach()),
             "grad_norm": float(g.norm()), "timed_gradients": reps,
             "plain_forward_value": a.n * steps / t_plain,
-            "ratio_vs_plain_forward": t_plain / t_grad}
+            "ratio_vs_plain_forward": t_plain / t_grad, "error_vs_fp64": err}
 
 
 def gpu_arm(args, ws, rank, local):
@@ -380,43 +472,62 @@ def gpu_arm(args, ws, rank, local):
     launches = sim.engine.launch_count() * args.steps + rebuilds * per_rebuild
     n = setup.n
     value = n * args.steps * ws / (total_ms / 1000.0)
-    # phase times, measured with CUDA events on the launching stream
-    phases = sim.engine.profile(20)
+    # per-kernel times, measured with CUDA events on the stream the kernels
+    # are launched on (eager steps; the host reads each rebuild decision)
+    _, dens_ms, _, force_ms, kick_ms, rb_ms = sim.engine.profile(20, split=True)
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
         peaks = json.load(open(peaks_path))
         hbm, peak_src = float(peaks["hbm_gbs"]), "measured"
     else:
         hbm, peak_src = 6800.0, "fallback"
-    dom = int(np.argmax(phases))
-    dom_ms = phases[dom]
-    dom_bytes = PHASE_BYTES[dom] * n
-    achieved = dom_bytes / (dom_ms * 1e-3) / 1e9 if dom_ms > 0 else 0.0
+    times = {"kick": kick_ms, "rebuild": rb_ms, "density": dens_ms, "force": force_ms}
+    table = {}
+    for name, ms in times.items():
+        k = KERNELS[name]
+        row = {"kernel": k["kernel"], "ms": ms, "alg_bytes_per_particle": k["alg_bytes"]}
+        if k["alg_bytes"] and ms > 0:
+            gbs = k["alg_bytes"] * n / (ms * 1e-3) / 1e9
+            row.update(achieved_gbs=gbs, frac=gbs / hbm)
+        if k["ncu"]:
+            row["ncu"] = k["ncu"]
+        table[name] = row
+    # the dominant single kernel (the rebuild is several kernels)
+    dom = max(("kick", "density", "force"), key=lambda x: times[x])
+    d = table[dom]
+    ncu = KERNELS[dom]["ncu"] or {}
     step_ms_mean = total_ms / args.steps
     step_achieved = STEP_BYTES * n / (step_ms_mean * 1e-3) / 1e9
+    cfg = workload_config(args, n, ws)
+    cfg["candidate_rebuilds"] = rebuilds
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": step_ms_mean, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (reference initial condition of the 3D TGV)",
-        "config": {"workload": (WORKLOAD if args.n_side == 64 else
-                                WORKLOAD.replace("64^3 = 262,144", f"{args.n_side}^3 = {n:,}")),
-                   "n_particles": n, "parallelism": f"replicas x{ws}",
-                   "verlet_skin": args.skin, "candidate_rebuilds": rebuilds,
-                   "l2": "flushed between timed steps (256 MiB write outside the events)"},
-        "roofline": {"bound": "hbm", "kernel": PHASE_KERNELS[dom], "achieved": achieved,
-                     "peak": hbm, "unit": "GB/s", "frac": achieved / hbm,
-                     "peak_source": peak_src, "alg_bytes_per_particle": PHASE_BYTES[dom],
-                     "traffic": (PHASE_TRAFFIC[dom] * n if PHASE_TRAFFIC[dom] else None),
-                     "traffic_source": "ncu dram bytes per particle at 128^3, scaled to n",
-                     "fp32_pipe_frac": PHASE_FP32_PIPE[dom],
+        "config": cfg,
+        # the dominant kernel's algorithmic bytes over its CUDA-event time,
+        # against the measured HBM copy bandwidth; what binds it is the
+        # instruction issue (ncu: issue active, FMA pipe), not DRAM
+        "roofline": {"bound": "issue", "kernel": d["kernel"], "achieved": d.get("achieved_gbs"),
+                     "peak": hbm, "unit": "GB/s", "frac": d.get("frac"),
+                     "peak_source": peak_src + " HBM copy bandwidth",
+                     "alg_bytes_per_particle": d["alg_bytes_per_particle"],
+                     "traffic": (ncu["dram_bytes"] * n if ncu.get("dram_bytes") else None),
+                     "traffic_source": "ncu dram bytes per particle of the same kernel at 64^3",
+                     "fp32_pipe_frac": ncu.get("fma_pipe"),
+                     "issue_active": ncu.get("issue_active"),
                      "step": {"alg_bytes_per_particle": STEP_BYTES, "achieved": step_achieved,
                               "frac": step_achieved / hbm}},
-        "phases_ms": dict(zip(PHASES, phases)),
+        "kernels": table,
         "status": status,
         "gpu_launches": launches,
         "clocks": clocks.summary(),
     }
+    del sim
+    threads = os.cpu_count() or 1
+    if rank == 0 and ws == 1 and not args.no_cpu:
+        line["error_vs_fp64"] = fp64_error(setup, FP64_STEPS, device, threads)
     if rank == 0 and ws == 1 and not args.no_e2e:
         rate, h2d, d2h, t, redone = e2e_rate(setup, min(args.steps, 30), device)
         line["e2e"] = {"value": rate, "unit": UNIT, "h2d_bytes_per_step": h2d,
@@ -424,9 +535,10 @@ def gpu_arm(args, ws, rank, local):
                        "path": "si_euler drop-in advance on a pinned host state: each step "
                                "reads its inputs from and writes its result to host memory"}
     if rank == 0 and not args.no_forms:
-        line["forms"] = {"batched": batched_form(device, 100), "adjoint": adjoint_form(device)}
+        line["forms"] = {"batched": batched_form(device, args.batched_steps,
+                                                 fp64=not args.no_cpu),
+                         "adjoint": adjoint_form(device, fp64=not args.no_cpu)}
     if rank == 0 and ws == 1 and not args.no_cpu:
-        threads = os.cpu_count() or 1
         # a bounded sample: steps of the full case until ~10 s of CPU work
         rate, steps, secs, n_cpu, warm = cpu_oracle_rate(64, 40, 10.0, threads, warmup=3,
                                                          warmup_budget_s=10.0)
@@ -450,6 +562,8 @@ def main():
                     help="skip the batched/adjoint form measurements on their own workloads")
     ap.add_argument("--skin", type=float, default=0.1,
                     help="Verlet skin as a fraction of the cutoff (0: rebuild every step)")
+    ap.add_argument("--batched-steps", type=int, default=1000,
+                    help="steps of the batched form (the configuration's 1,000)")
     ap.add_argument("--n-side", type=int, default=64,
                     help="particles per side of the 3D TGV lattice (64 = the benchmark case)")
     args = ap.parse_args()
