@@ -322,8 +322,14 @@ int sph_read_status_async(SphHandle* h, uint32_t* status_dev, int32_t clear, voi
  * on a device: calls that overlap on the GPU race and must be ordered by the
  * caller. The first call on a device looks up the array's address
  * (cudaGetSymbolAddress, with that device current) and should come before any
- * stream capture. *count_dev receives the edge count; *status_dev (optional,
- * device) the call's status bits. */
+ * stream capture. The looked-up address is kept for the life of the process:
+ * do not reset the device (cudaDeviceReset) between calls. Cost: the sort
+ * ranks each particle within its cell and the emission sorts each sender's
+ * receivers by insertion, so both grow with the square of the occupancy of
+ * a cell or of a neighbourhood; inputs that pile many particles into one cell
+ * (thousands, far beyond an SPH particle spacing) make a call slow.
+ * *count_dev receives the edge count; *status_dev (optional, device) the
+ * call's status bits. */
 #define SPH_NOALLOC_MAX_PARTICLES 65536
 #define SPH_NOALLOC_MAX_CELLS 65536
 int sph_nl_edges_noalloc(int32_t dim, const double* box, double r_cutoff, int32_t mask_self,

@@ -49,7 +49,8 @@ struct SphHandle {
   int* cellid = nullptr;
   int *count = nullptr, *start = nullptr, *keyc = nullptr, *keys = nullptr;
   int *tsrc = nullptr, *tkey = nullptr, *tcell = nullptr, *scan_tmp = nullptr;
-  int *rowcnt = nullptr, *rowoff = nullptr;
+  int* rowcnt = nullptr;
+  long long* rowoff = nullptr;  // 64-bit edge offsets per sender
   int *nbr = nullptr, *nbr_cnt = nullptr;
   int kmax = kListSlots;  // neighbour-list slots per particle
   int *vl = nullptr, *vcnt = nullptr;  // Verlet candidates

@@ -676,8 +676,11 @@ void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, i
 void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_cells,
                  bool from_forward, bool apply_bc);
 int launch_scan(cudaStream_t st, const int* in, int* out, long long n, int* tmp);
+// Exclusive scan of n ints into 64-bit offsets (tmp: scan_tmp_ints(n) ints,
+// 8-byte aligned).
+int launch_scan64(cudaStream_t st, const int* in, long long* out, long long n, int* tmp);
 void launch_edges(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
-                  int* rowcnt, int* rowoff, int* scan_tmp, int32_t* idx, long long capacity,
+                  int* rowcnt, long long* rowoff, int* scan_tmp, int32_t* idx, long long capacity,
                   long long* count_dev);
 void launch_row_counts(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
                        int* rowcnt);

@@ -13,7 +13,15 @@
 // on the GPU (different streams, or different host threads) race on the
 // array; the caller must order them. The first call on each device looks the
 // array's device address up (cudaGetSymbolAddress, with that device
-// current); make that first call before any stream capture.
+// current); make that first call before any stream capture. The address is
+// kept for the life of the process, so the device must not be reset
+// (cudaDeviceReset) between calls: the module, and with it the array, would
+// be loaded again elsewhere.
+//
+// Cost on dense inputs: ranking a particle within its cell (k_na_place) and
+// ordering a sender's receivers (the insertion sort of the edge emission) are
+// quadratic in the occupancy of a cell and of a neighbourhood; inputs that
+// put thousands of particles into one cell make a call slow.
 #include <mutex>
 
 #include "sph_internal.cuh"
@@ -42,8 +50,8 @@ constexpr size_t kCellid = align256(kOrig + sizeof(int) * kMaxN);
 constexpr size_t kMeta = align256(kCellid + sizeof(int) * kMaxN);
 constexpr size_t kRowcnt = align256(kMeta + sizeof(int) * kMaxN);
 constexpr size_t kRowoff = align256(kRowcnt + sizeof(int) * (kMaxN + 1));
-constexpr size_t kScan = align256(kRowoff + sizeof(int) * (kMaxN + 1));
-constexpr size_t kScanInts = 4096;  // > scan_tmp_ints(kMaxN + 1)
+constexpr size_t kScan = align256(kRowoff + sizeof(long long) * (kMaxN + 1));
+constexpr size_t kScanInts = 4096;  // > scan_tmp_ints(kMaxN + 1) = 648 (64-bit sums)
 constexpr size_t kP4 = align256(kScan + sizeof(int) * kScanInts);
 constexpr size_t kBytes = align256(kP4 + sizeof(float4) * kMaxN);
 
@@ -186,7 +194,7 @@ int sph_nl_edges_noalloc(int32_t dim, const double* box, double r_cutoff, int32_
   b.META = (int*)(base + kMeta);
   int* cellid = (int*)(base + kCellid);
   int* rowcnt = (int*)(base + kRowcnt);
-  int* rowoff = (int*)(base + kRowoff);
+  long long* rowoff = (long long*)(base + kRowoff);
   int* scan_tmp = (int*)(base + kScan);
 
   const int g = (int)((n + kBlock - 1) / kBlock);

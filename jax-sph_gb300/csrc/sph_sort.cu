@@ -407,63 +407,67 @@ constexpr int kScanThreads = 1024;
 constexpr int kScanItems = 4;
 constexpr int kTile = kScanThreads * kScanItems;
 
-// Block-wide exclusive scan of kTile ints; returns the tile total.
-__device__ int block_scan_tile(int* v /*[kScanItems]*/, int* smem /*[32]*/) {
+// Block-wide exclusive scan of kTile values; returns the tile total.
+template <typename T>
+__device__ T block_scan_tile(T* v /*[kScanItems]*/, T* smem /*[32]*/) {
   int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-  int local = 0;
+  T local = 0;
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) {
-    int t = v[i];
+    T t = v[i];
     v[i] = local;
     local += t;
   }
-  int x = local;
+  T x = local;
 #pragma unroll
   for (int o = 1; o < 32; o <<= 1) {
-    int y = __shfl_up_sync(kFull, x, o);
+    T y = __shfl_up_sync(kFull, x, o);
     if (lane >= o) x += y;
   }
   if (lane == 31) smem[warp] = x;
   __syncthreads();
   if (warp == 0) {
-    int w = smem[lane];
+    T w = smem[lane];
 #pragma unroll
     for (int o = 1; o < 32; o <<= 1) {
-      int y = __shfl_up_sync(kFull, w, o);
+      T y = __shfl_up_sync(kFull, w, o);
       if (lane >= o) w += y;
     }
     smem[lane] = w;
   }
   __syncthreads();
-  int warp_excl = warp > 0 ? smem[warp - 1] : 0;
-  int total = smem[31];
-  int excl = warp_excl + x - local;
+  T warp_excl = warp > 0 ? smem[warp - 1] : 0;
+  T total = smem[31];
+  T excl = warp_excl + x - local;
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i) v[i] += excl;
   __syncthreads();
   return total;
 }
 
-__global__ void k_tile_sums(const int* in, long long n, int* sums) {
-  __shared__ int smem[32];
+// Per-tile totals of `n` values (summed in TO).
+template <typename TI, typename TO>
+__global__ void k_tile_sums(const TI* in, long long n, TO* sums) {
+  __shared__ TO smem[32];
   long long base = blockIdx.x * (long long)kTile + threadIdx.x * kScanItems;
-  int v[kScanItems];
+  TO v[kScanItems];
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? in[base + i] : 0;
-  int total = block_scan_tile(v, smem);
+  for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? (TO)in[base + i] : (TO)0;
+  TO total = block_scan_tile(v, smem);
   if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-// Exclusive scan of `n` ints with an optional per-tile offset array;
+// Exclusive scan of `n` values with an optional per-tile offset array;
 // out[n] receives the grand total when this block owns the last tile.
-__global__ void k_tile_scan(const int* in, long long n, int* out, const int* tile_off) {
-  __shared__ int smem[32];
+template <typename TI, typename TO>
+__global__ void k_tile_scan(const TI* in, long long n, TO* out, const TO* tile_off) {
+  __shared__ TO smem[32];
   long long base = blockIdx.x * (long long)kTile + threadIdx.x * kScanItems;
-  int v[kScanItems];
+  TO v[kScanItems];
 #pragma unroll
-  for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? in[base + i] : 0;
-  int total = block_scan_tile(v, smem);
-  int off = tile_off ? tile_off[blockIdx.x] : 0;
+  for (int i = 0; i < kScanItems; ++i) v[i] = (base + i < n) ? (TO)in[base + i] : (TO)0;
+  TO total = block_scan_tile(v, smem);
+  TO off = tile_off ? tile_off[blockIdx.x] : (TO)0;
 #pragma unroll
   for (int i = 0; i < kScanItems; ++i)
     if (base + i < n) out[base + i] = v[i] + off;
@@ -526,7 +530,7 @@ __global__ void k_row_counts(long long N, Buffers b, const CaseDev* cases, const
 
 template <int DIM>
 __global__ void k_emit(long long N, Buffers b, const CaseDev* cases, const int* cellid,
-                       const int* start, int mask_self, const int* rowoff, int32_t* idx,
+                       const int* start, int mask_self, const long long* rowoff, int32_t* idx,
                        long long capacity) {
   long long s = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (s >= N) return;
@@ -558,7 +562,7 @@ __global__ void k_emit(long long N, Buffers b, const CaseDev* cases, const int* 
   }
 }
 
-__global__ void k_pad_edges(int32_t* idx, long long capacity, const int* total_ptr, int n,
+__global__ void k_pad_edges(int32_t* idx, long long capacity, const long long* total_ptr, int n,
                             long long* count_dev, unsigned* status) {
   long long total = *total_ptr;
   long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -626,20 +630,30 @@ __global__ void k_neighbour_counts(long long N, const int* inv, const int* meta,
 }  // namespace
 
 // ------------------------------------------------------------------ launchers
-size_t scan_tmp_ints(long long n) { return (size_t)((n + kTile - 1) / kTile) * 4 + 256; }
+// Scratch of a scan of n values, in ints: enough for 64-bit partial sums.
+size_t scan_tmp_ints(long long n) { return 2 * ((size_t)((n + kTile - 1) / kTile) * 4 + 256); }
 
-int launch_scan(cudaStream_t st, const int* in, int* out, long long n, int* tmp) {
+template <typename TI, typename TO>
+int scan_t(cudaStream_t st, const TI* in, TO* out, long long n, TO* tmp) {
   long long tiles = (n + kTile - 1) / kTile;
   if (tiles <= 1) {
-    k_tile_scan<<<1, kScanThreads, 0, st>>>(in, n, out, nullptr);
+    k_tile_scan<TI, TO><<<1, kScanThreads, 0, st>>>(in, n, out, nullptr);
     return 1;
   }
-  int* sums = tmp;
-  int* offs = tmp + tiles + 1;
-  k_tile_sums<<<(int)tiles, kScanThreads, 0, st>>>(in, n, sums);
-  int k = launch_scan(st, sums, offs, tiles, tmp + 2 * tiles + 2);
-  k_tile_scan<<<(int)tiles, kScanThreads, 0, st>>>(in, n, out, offs);
+  TO* sums = tmp;
+  TO* offs = tmp + tiles + 1;
+  k_tile_sums<TI, TO><<<(int)tiles, kScanThreads, 0, st>>>(in, n, sums);
+  int k = scan_t<TO, TO>(st, sums, offs, tiles, tmp + 2 * tiles + 2);
+  k_tile_scan<TI, TO><<<(int)tiles, kScanThreads, 0, st>>>(in, n, out, offs);
   return k + 2;
+}
+
+int launch_scan(cudaStream_t st, const int* in, int* out, long long n, int* tmp) {
+  return scan_t<int, int>(st, in, out, n, tmp);
+}
+
+int launch_scan64(cudaStream_t st, const int* in, long long* out, long long n, int* tmp) {
+  return scan_t<int, long long>(st, in, out, n, reinterpret_cast<long long*>(tmp));
 }
 
 void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out,
@@ -753,10 +767,11 @@ void launch_row_counts(const LaunchCtx& L, Buffers b, const int* cellid, const i
 }
 
 void launch_edges(const LaunchCtx& L, Buffers b, const int* cellid, const int* start,
-                  int* rowcnt, int* rowoff, int* scan_tmp, int32_t* idx, long long capacity,
+                  int* rowcnt, long long* rowoff, int* scan_tmp, int32_t* idx, long long capacity,
                   long long* count_dev) {
   launch_row_counts(L, b, cellid, start, rowcnt);
-  launch_scan(L.stream, rowcnt, rowoff, L.N, scan_tmp);
+  // 64-bit edge offsets: the total can exceed 2^31 (dense clusters)
+  launch_scan64(L.stream, rowcnt, rowoff, L.N, scan_tmp);
   int g = nblocks(L.N);
   if (L.dim == 3)
     k_emit<3><<<g, kBlock, 0, L.stream>>>(L.N, b, L.cases, cellid, start, L.mask_self, rowoff,

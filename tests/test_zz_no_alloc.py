@@ -59,6 +59,32 @@ def test_noalloc_equals_handle_path_on_consecutive_calls():
         assert torch.equal(idx, nb.idx)
 
 
+def test_noalloc_equals_handle_path_at_its_limits():
+    """65,536 particles in 65,536 cells (2D, cutoff = spacing, jittered
+    lattice): every region of the fixed array is used to its end."""
+    lib = _lib.load()
+    n_side = 256
+    dx = 1.0 / n_side
+    box = np.array([1.0, 1.0])
+    g = torch.Generator().manual_seed(5)
+    ax = (torch.arange(n_side, dtype=torch.float64) + 0.5) * dx
+    yy, xx = torch.meshgrid(ax, ax, indexing="ij")
+    r = torch.stack([xx.reshape(-1), yy.reshape(-1)], 1)
+    r = torch.remainder(r + 0.2 * dx * torch.randn(r.shape, generator=g, dtype=torch.float64),
+                        1.0).to(torch.float32)
+    r = torch.where(r >= 1.0, torch.zeros_like(r), r).cuda().contiguous()
+    assert r.shape[0] == 65536
+    cutoff = dx
+    disp, _ = space.periodic(box)
+    fns = partition.neighbor_list(disp, box, cutoff, mask_self=False)
+    nb = fns.allocate(r)
+    for _ in range(2):
+        idx, count, status = call_noalloc(lib, r, box, cutoff, False, nb.max_occupancy)
+        assert status & 0xFF == 0
+        assert count == nb.occupancy
+        assert torch.equal(idx, nb.idx)
+
+
 def test_noalloc_rejects_sizes_beyond_its_array():
     lib = _lib.load()
     n = 65537
