@@ -368,10 +368,15 @@ __device__ __forceinline__ void walk_rows(const CaseDev& c, int cell_local, cons
         }
         if (g2 >= trim_r2) continue;
         const float w = sqrtf(trim_r2 - g2) + c.trim_m;
-        const int lo = (int)floorf((ri.x - w) * c.inv_cs[0]);
-        const int hi = (int)floorf((ri.x + w) * c.inv_cs[0]);
-        xa = lo > xa ? lo : xa;
-        xb = hi < xb ? hi : xb;
+        // the chord's cells, clamped in floating point first: a non-finite
+        // position (NaN fails every test, +-inf saturates) keeps the
+        // untrimmed row instead of converting an out-of-range bound
+        const float lo = floorf((ri.x - w) * c.inv_cs[0]);
+        const float hi = floorf((ri.x + w) * c.inv_cs[0]);
+        const int ta = (int)fminf(fmaxf(lo, (float)xa), (float)xb);
+        const int tb = (int)fminf(fmaxf(hi, (float)xa), (float)xb);
+        xa = ta;
+        xb = tb;
       }
       // up to two ranges (the second where the row wraps); the visitor is
       // instantiated once, inside the loop
