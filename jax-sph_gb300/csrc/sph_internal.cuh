@@ -450,6 +450,19 @@ __device__ __forceinline__ int ref_cell_hash(const float4& r, const CaseDev& c) 
 // cutoff to within rounding -- must not become an edge. Pairs clearly inside
 // the cutoff are always adjacent (the band's margin exceeds the hash's
 // rounding), so only the band's candidates take this test.
+//
+// int32(r / cs), the cell hash's index along an axis of cell size cs: r * inv_cs
+// lies within 1.5 * 2^-23 (relative) of the correctly rounded quotient, so its
+// floor is the hash's unless it lies that close to an integer; only then (and
+// for negative or non-finite r) the division decides.
+__device__ __forceinline__ int hash_index(float r, float cs, float inv_cs) {
+  const float q = r * inv_cs;
+  const float f = q - floorf(q);
+  const float tol = fmaxf(q, 1.0f) * 4.8e-7f;
+  if (q >= 0.f && f > tol && f < 1.0f - tol) return (int)q;
+  return __float2int_rz(__fdiv_rn(r, cs));
+}
+
 template <int DIM>
 __device__ __forceinline__ bool ref_adjacent(const float4& a, const float4& b, const CaseDev& c) {
   const float pa[3] = {a.x, a.y, a.z}, pb[3] = {b.x, b.y, b.z};
@@ -457,8 +470,8 @@ __device__ __forceinline__ bool ref_adjacent(const float4& a, const float4& b, c
   for (int d = 0; d < DIM; ++d) {
     const int n = c.nc[d] / c.sub[d];
     if (n < 3) continue;
-    int ia = __float2int_rz(__fdiv_rn(pa[d], c.cell_size[d])) / c.sub[d];
-    int ib = __float2int_rz(__fdiv_rn(pb[d], c.cell_size[d])) / c.sub[d];
+    int ia = hash_index(pa[d], c.cell_size[d], c.inv_cs[d]) / c.sub[d];
+    int ib = hash_index(pb[d], c.cell_size[d], c.inv_cs[d]) / c.sub[d];
     ia = ia < 0 ? 0 : (ia >= n ? n - 1 : ia);
     ib = ib < 0 ? 0 : (ib >= n ? n - 1 : ib);
     const int k = ia > ib ? ia - ib : ib - ia;

@@ -209,15 +209,22 @@ __device__ __forceinline__ void lean_slow(int N, int i, const float4& ri, const 
 // ------------------------------------------------------------------ candidates
 // The senders within the list radius of every receiver at the current
 // binning (shifted squared distance < v_r2), self excluded, in walk (cell)
-// order, written straight to the k-major list. vcnt = kv + 1 marks a receiver
-// whose candidates do not all fit (too many, or an offset beyond 16 bits):
-// the passes walk its cells instead.
+// order. The loop over a range is branch-free: every candidate's slot value
+// is stored at the next free slot of the receiver's column in shared memory
+// and the count advances only for a member; the column is then copied to the
+// k-major list in whole words. vcnt = kv + 1 marks a receiver whose
+// candidates do not all fit (too many, or an offset beyond 16 bits): the
+// passes walk its cells instead.
 template <int DIM, bool WIDE>
 __global__ void __launch_bounds__(256)
 k_verlet_lean(int N, Buffers b, const CaseDev c, const int* __restrict__ cellid,
               const int* __restrict__ start, typename Fmt<WIDE>::Word* vl, int* vcnt, int kv) {
   using L = Fmt<WIDE>;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  using Word = typename L::Word;
+  extern __shared__ __align__(16) unsigned char s_raw[];  // [kv / 4][blockDim.x] words
+  Word* srow = reinterpret_cast<Word*>(s_raw) + threadIdx.x;
+  const int bs = blockDim.x;
+  const int i = blockIdx.x * bs + threadIdx.x;
   if (i >= N) return;
   if (tag_of(b.META[i]) == PAD) {
     vcnt[i] = 0;
@@ -227,24 +234,28 @@ k_verlet_lean(int N, Buffers b, const CaseDev c, const int* __restrict__ cellid,
   const float r2 = c.v_r2;
   int m = 0;
   bool wide = false;
-  typename L::Word* row = vl + i;
   box_rows<DIM>(c, cellid[i] - c.cell_off, start, c.vrad[0], c.vrad[1], c.vrad[2], r2,
                 [&](int j0, int j1, float3 s) {
     const float qx = ri.x - s.x, qy = ri.y - s.y, qz = ri.z - s.z;
-#pragma unroll 2
+#pragma unroll 4
     for (int j = j0; j < j1; ++j) {
       const float4 rj = __ldg(b.P4 + j);
       const float dx = qx - rj.x, dy = qy - rj.y, dz = (DIM == 3) ? qz - rj.z : 0.f;
-      if (j != i && dx * dx + dy * dy + dz * dz < r2) {
-        int o;
-        const bool fits = L::enc(i, j, N, o);
-        wide |= !fits;
-        if (m < kv && fits) L::put(row, (size_t)N, m, o);
-        ++m;
-      }
+      const bool in = j != i && dx * dx + dy * dy + dz * dz < r2;
+      int o;
+      const bool fits = L::enc(i, j, N, o);
+      wide |= in && !fits;
+      L::put(srow, (size_t)bs, m < kv ? m : kv - 1, o);
+      m += in;
     }
   });
-  vcnt[i] = (wide || m > kv) ? kv + 1 : m;
+  const bool listed = !wide && m <= kv;
+  vcnt[i] = listed ? m : kv + 1;
+  if (listed) {
+    Word* out = vl + i;
+    const int ng = (m + 3) >> 2;
+    for (int g = 0; g < ng; ++g) out[(size_t)g * N] = srow[(size_t)g * bs];
+  }
 }
 
 // Edge count for the NEIGHBOR_LIST_OVERFLOW test (one case). The capacity is
@@ -310,15 +321,17 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
+          // branch-free: the kernel value of every candidate (zero beyond
+          // the support) enters the sum only for an edge, and every slot
+          // value is stored at the next free slot, kept only for an edge
           float3 dr;
           float d2;
           const bool e = q < rem && lean_edge<DIM>(ri, rj[q], c, cp, dr, d2);
-          if (e && fluid) {
-            float dist, inv_d;
-            dist_inv(d2, dist, inv_d);
-            s0.add(kw<KER>(dist, c));
-          }
-          if (e && m < kmax) L::put(srow, (size_t)bs, m, o[q]);
+          float dist, inv_d;
+          dist_inv(d2, dist, inv_d);
+          const float w = kw<KER>(dist, c);
+          if (fluid) s0.add(e ? w : 0.f);
+          L::put(srow, (size_t)bs, m < kmax ? m : kmax - 1, o[q]);
           m += e;
         }
       }
@@ -526,7 +539,12 @@ void forward_lean_k(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid
 template <int DIM, bool WIDE>
 void verlet_lean_t(const LaunchCtx& L, Buffers b, const int* cellid, const int* start) {
   using Word = typename Fmt<WIDE>::Word;
-  k_verlet_lean<DIM, WIDE><<<nblocks(L.N, 256), 256, 0, L.stream>>>(
+  // the staging column of kv slots per thread stays within 48 KB per block
+  const int col = (int)sizeof(Word) * (L.kv / 4);
+  int bt = (49152 / col) / 32 * 32;
+  bt = bt > 256 ? 256 : bt;
+  const size_t smem = (size_t)col * bt;
+  k_verlet_lean<DIM, WIDE><<<nblocks(L.N, bt), bt, smem, L.stream>>>(
       (int)L.N, b, L.c1, cellid, start, reinterpret_cast<Word*>(L.vl), L.vcnt, L.kv);
 }
 

@@ -336,45 +336,62 @@ __global__ void k_permute(long long N, Buffers in, Buffers out, const float4* R4
 //  * the rebuild test: a rebuild of the candidate lists is due once the
 //    minimum-image displacement since the last rebuild exceeds sqrt(v_dmax2).
 template <int DIM>
-__global__ void k_kick(long long N, Buffers b, const float4* R4, const CaseDev* cases,
-                       const float4* rref, int* cref_count, unsigned* vflag, unsigned* status,
-                       bool from_forward, bool apply_bc) {
+__device__ __forceinline__ void kick_one(long long i, const Buffers& b, const float4* R4,
+                                         const CaseDev& c, int meta, const float4* rref,
+                                         unsigned* status, bool from_forward, bool apply_bc,
+                                         bool& rebuild, int& key) {
+  const Final f = finalize(b, R4, i, c, tag_of(meta), from_forward, apply_bc);
+  float4 r = b.P4[i];
+  float3 u = f.u, v;
+  const float4 A = b.A4[i], B = b.A2[i];
+  const float4 q = rref[i];
+  if (b.RD) {
+    double4_32a rd = b.RD[i];
+    kick_drift64<DIM>(r, rd, u, v, A, B, c);
+    b.RD[i] = rd;
+  } else {
+    kick_drift<DIM>(r, u, v, A, B, c);
+  }
+  b.P4[i] = r;
+  b.U4[i] = make_float4(u.x, u.y, u.z, f.rho);
+  b.V4[i] = make_float4(v.x, v.y, v.z, f.p);
+  if (b.TH4) {
+    const float4 t = b.TH4[i];
+    b.TH4[i] = make_float4(f.T, f.dTdt, t.z, t.w);
+  }
+  float dx = r.x - q.x, dy = r.y - q.y, dz = (DIM == 3) ? r.z - q.z : 0.f;
+  dx = fmaf(-c.box[0], rintf(dx * c.inv_box[0]), dx);
+  dy = fmaf(-c.box[1], rintf(dy * c.inv_box[1]), dy);
+  if (DIM == 3) dz = fmaf(-c.box[2], rintf(dz * c.inv_box[2]), dz);
+  const bool pad = tag_of(meta) == PAD;  // no lists, no cell
+  rebuild = !pad && !(dx * dx + dy * dy + dz * dz <= c.v_dmax2);  // NaN rebuilds too
+  if (c.use_cells && !pad) {
+    key = ref_cell_hash<DIM>(r, c);
+    if (key < 0) atomicOr(status, SPH_ERR_NONFINITE);
+    else key += c.cref_off;
+  }
+}
+
+// ONE: a single case, its constants a kernel parameter (the capacity, which a
+// capacity update changes without re-capturing the step, is read from the
+// device copy).
+template <int DIM, bool ONE>
+__global__ void __launch_bounds__(kBlock, ONE ? 5 : 1)
+k_kick(long long N, Buffers b, const float4* R4, const CaseDev c1, const CaseDev* cases,
+       const float4* rref, int* cref_count, unsigned* vflag, unsigned* status,
+       bool from_forward, bool apply_bc) {
   const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int lane = threadIdx.x & 31;
   bool rebuild = false, over = false;
   int key = -1, cap = 0;
   if (i < N) {
     const int meta = b.META[i];
-    const CaseDev& c = cases[case_of(meta)];
-    const Final f = finalize(b, R4, i, c, tag_of(meta), from_forward, apply_bc);
-    float4 r = b.P4[i];
-    float3 u = f.u, v;
-    const float4 A = b.A4[i], B = b.A2[i];
-    if (b.RD) {
-      double4_32a rd = b.RD[i];
-      kick_drift64<DIM>(r, rd, u, v, A, B, c);
-      b.RD[i] = rd;
+    if (ONE) {
+      kick_one<DIM>(i, b, R4, c1, meta, rref, status, from_forward, apply_bc, rebuild, key);
+      if (key >= 0) cap = cases[0].cell_cap;
     } else {
-      kick_drift<DIM>(r, u, v, A, B, c);
-    }
-    b.P4[i] = r;
-    b.U4[i] = make_float4(u.x, u.y, u.z, f.rho);
-    b.V4[i] = make_float4(v.x, v.y, v.z, f.p);
-    if (b.TH4) {
-      const float4 t = b.TH4[i];
-      b.TH4[i] = make_float4(f.T, f.dTdt, t.z, t.w);
-    }
-    const float4 q = rref[i];
-    float dx = r.x - q.x, dy = r.y - q.y, dz = (DIM == 3) ? r.z - q.z : 0.f;
-    dx = fmaf(-c.box[0], rintf(dx * c.inv_box[0]), dx);
-    dy = fmaf(-c.box[1], rintf(dy * c.inv_box[1]), dy);
-    if (DIM == 3) dz = fmaf(-c.box[2], rintf(dz * c.inv_box[2]), dz);
-    const bool pad = tag_of(meta) == PAD;  // no lists, no cell
-    rebuild = !pad && !(dx * dx + dy * dy + dz * dz <= c.v_dmax2);  // NaN rebuilds too
-    if (c.use_cells && !pad) {
-      key = ref_cell_hash<DIM>(r, c);
-      if (key < 0) atomicOr(status, SPH_ERR_NONFINITE);
-      else key += c.cref_off;
+      const CaseDev& c = cases[case_of(meta)];
+      kick_one<DIM>(i, b, R4, c, meta, rref, status, from_forward, apply_bc, rebuild, key);
       cap = c.cell_cap;
     }
   }
@@ -699,12 +716,17 @@ void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_
                  bool from_forward, bool apply_bc) {
   if (ref_cells > 0) cudaMemsetAsync(L.cref_count, 0, sizeof(int) * ref_cells, L.stream);
   int g = nblocks(L.N);
-  if (L.dim == 3)
-    k_kick<3><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, L.rref, L.cref_count, L.vflag,
-                                          L.status, from_forward, apply_bc);
-  else
-    k_kick<2><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.cases, L.rref, L.cref_count, L.vflag,
-                                          L.status, from_forward, apply_bc);
+#define SPH_KICK(D, ONE)                                                                      \
+  k_kick<D, ONE><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.c1, L.cases, L.rref, L.cref_count,  \
+                                             L.vflag, L.status, from_forward, apply_bc)
+  if (L.dim == 3) {
+    if (L.n_cases == 1) SPH_KICK(3, true);
+    else SPH_KICK(3, false);
+  } else {
+    if (L.n_cases == 1) SPH_KICK(2, true);
+    else SPH_KICK(2, false);
+  }
+#undef SPH_KICK
   count_launch(L);
   // moving walls: the normals follow the new positions (integrator.py:33-34)
   if (L.layer.n > 0 && b.NW4) {
