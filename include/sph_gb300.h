@@ -300,6 +300,14 @@ int sph_adjoint_init(SphHandle* h, int32_t slots);
 int sph_tape_record(SphHandle* h, int32_t slot, void* stream);
 int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u,
                      const float* lam_a_in, float* lam_a_out, void* stream);
+/* A checkpoint segment in one call each way. sph_tape_segment runs `nsteps`
+ * steps like sph_step from the loaded state, recording step t into slot t
+ * (nsteps <= slots). sph_adjoint_segment then applies sph_adjoint_step to
+ * slots nsteps-1 down to 0, alternating lam_a and lam_a_tmp as the in/out
+ * pair; the result ends in lam_a. */
+int sph_tape_segment(SphHandle* h, int32_t nsteps, void* stream);
+int sph_adjoint_segment(SphHandle* h, int32_t nsteps, float* lam_r, float* lam_u, float* lam_a,
+                        float* lam_a_tmp, void* stream);
 
 /* Read (and optionally clear) the device status word. Synchronizes `stream`.
  * sph_set_state clears the word. */

@@ -1341,6 +1341,43 @@ int sph_adjoint_init(SphHandle* h, int32_t slots) try {
   return host_error();
 }
 
+int sph_tape_segment(SphHandle* h, int32_t nsteps, void* stream) try {
+  if (!h || nsteps < 0 || nsteps > h->tape_slots)
+    return fail((int)SPH_ERR_INVALID_ARG, "segment longer than the tape");
+  for (int t = 0; t < nsteps; ++t) {
+    int rc = sph_step(h, 1, stream);
+    if (!rc) rc = sph_tape_record(h, t, stream);
+    if (rc) return rc;
+  }
+  return 0;
+} catch (...) {
+  return host_error();
+}
+
+int sph_adjoint_segment(SphHandle* h, int32_t nsteps, float* lam_r, float* lam_u, float* lam_a,
+                        float* lam_a_tmp, void* stream) try {
+  if (!h || nsteps < 0 || nsteps > h->tape_slots)
+    return fail((int)SPH_ERR_INVALID_ARG, "segment longer than the tape");
+  if (!lam_a || !lam_a_tmp || lam_a == lam_a_tmp)
+    return fail((int)SPH_ERR_INVALID_ARG, "adjoint arrays missing or aliased");
+  float* in = lam_a;
+  float* out = lam_a_tmp;
+  for (int t = nsteps - 1; t >= 0; --t) {
+    int rc = sph_adjoint_step(h, t, lam_r, lam_u, in, out, stream);
+    if (rc) return rc;
+    float* x = in;
+    in = out;
+    out = x;
+  }
+  if (in != lam_a)
+    return cuda_check(cudaMemcpyAsync(lam_a, in, sizeof(float) * h->N * h->cfg.dim,
+                                      cudaMemcpyDeviceToDevice, (cudaStream_t)stream),
+                      "adjoint copy");
+  return 0;
+} catch (...) {
+  return host_error();
+}
+
 int sph_tape_record(SphHandle* h, int32_t slot, void* stream) try {
   if (!h || slot < 0 || slot >= h->tape_slots)
     return fail((int)SPH_ERR_INVALID_ARG, "tape slot out of range");

@@ -79,7 +79,7 @@ EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sp
            "sph_step_launch_count", "sph_profile_step", "sph_adjoint_init", "sph_tape_record",
            "sph_adjoint_step", "sph_read_status", "sph_read_status_async", "sph_diagnostics",
            "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance", "sph_set_wall_layer",
-           "sph_neighbour_counts"]
+           "sph_neighbour_counts", "sph_tape_segment", "sph_adjoint_segment"]
 
 _LIB = None
 
@@ -120,6 +120,8 @@ def load(build_if_missing=True):
     lib.sph_rebuild_stats.argtypes = [V, P(ctypes.c_int64), P(ctypes.c_int32), V]
     lib.sph_advance.argtypes = [V, P(SphStateView), P(SphStateView), V, ctypes.c_float, V, V]
     lib.sph_neighbour_counts.argtypes = [V, V, V]
+    lib.sph_tape_segment.argtypes = [V, ctypes.c_int32, V]
+    lib.sph_adjoint_segment.argtypes = [V, ctypes.c_int32, V, V, V, V, V]
     lib.sph_diagnostics.argtypes = [V, V, V]
     lib.sph_set_wall_layer.argtypes = [V, V, ctypes.c_int64, P(ctypes.c_double), ctypes.c_double]
     lib.sph_nl_edges_noalloc.argtypes = [ctypes.c_int32, P(ctypes.c_double), ctypes.c_double,
@@ -298,6 +300,15 @@ class Engine:
 
     def adjoint_init(self, slots):
         _check(self.lib.sph_adjoint_init(self.h, int(slots)))
+
+    def tape_segment(self, nsteps):
+        """Run ``nsteps`` steps, recording step t into tape slot t."""
+        _check(self.lib.sph_tape_segment(self.h, int(nsteps), _stream()))
+
+    def adjoint_segment(self, nsteps, lam_r, lam_u, lam_a, lam_a_tmp):
+        """Reverse slots nsteps-1 .. 0; the dudt adjoint ends in ``lam_a``."""
+        _check(self.lib.sph_adjoint_segment(self.h, int(nsteps), _ptr(lam_r), _ptr(lam_u),
+                                            _ptr(lam_a), _ptr(lam_a_tmp), _stream()))
 
     def tape_record(self, slot):
         _check(self.lib.sph_tape_record(self.h, int(slot), _stream()))

@@ -41,12 +41,16 @@ class AdjointRollout:
         self.engine.adjoint_init(self.k)
         self.device = torch.device(device)
         self.checkpoints = []
+        self._base = None
 
     def _initial(self, u0):
-        st = {k: v.clone() for k, v in self.setup.state.items()}
-        u0 = u0.detach().to(device="cpu", dtype=st["u"].dtype)
-        st["u"] = u0.clone()
-        st["v"] = u0.clone()
+        """The case's initial state on the device with u = v = u0, dudt = 0."""
+        if self._base is None:
+            self._base = {k: v.to(self.device) for k, v in self.setup.state.items()}
+        st = dict(self._base)
+        u0 = u0.detach().to(device=self.device, dtype=torch.float32).contiguous()
+        st["u"] = u0
+        st["v"] = u0
         st["dudt"] = torch.zeros_like(st["dudt"])
         st["dvdt"] = torch.zeros_like(st["dvdt"])
         return st
@@ -71,17 +75,14 @@ class AdjointRollout:
         shape = lam_r.shape
         lr = lam_r.detach().to(self.device, torch.float32).contiguous().clone()
         lu = torch.zeros_like(lr)
-        la = [torch.zeros_like(lr), torch.zeros_like(lr)]
-        cur = 0
+        la, tmp = torch.zeros_like(lr), torch.zeros_like(lr)
         for seg in reversed(range(len(self.checkpoints))):
+            # recompute the segment from its checkpoint, recording its steps,
+            # then sweep it backwards (one library call each)
             self.sim.restore(self.checkpoints[seg])
             n = min(self.k, self.steps - seg * self.k)
-            for t in range(n):
-                self.engine.step(1)
-                self.engine.tape_record(t)
-            for t in reversed(range(n)):
-                self.engine.adjoint_step(t, lr, lu, la[cur], la[1 - cur])
-                cur = 1 - cur
+            self.engine.tape_segment(n)
+            self.engine.adjoint_segment(n, lr, lu, la, tmp)
         code = self.engine.read_status(clear=True)
         if code & _lib.ERR_INVALID_ARG:
             raise _lib.SphError(code, "a particle has more neighbours than the adjoint tape holds")
