@@ -483,9 +483,37 @@ __device__ __forceinline__ bool ref_adjacent(const float4& a, const float4& b, c
 // The reference metric, out of line: only candidates in the narrow band
 // around the cutoff (or every candidate of a case without the fast test)
 // reach it, so the hot loop stays small.
+//
+// The band's pairs are at the cutoff, i.e. at most about one reference cell
+// apart: an axis along which the displacement d is clearly shorter than the
+// reference cell (by more than the hash's rounding, 4 n + 8 ulp of the cell
+// index for n cells) cannot separate them by two cells, and only the other
+// axes need the cell indices.
+template <int DIM>
+__device__ __forceinline__ bool ref_adjacent_d(const float4& a, const float4& b, const float3& d,
+                                               const CaseDev& c) {
+  const float pa[3] = {a.x, a.y, a.z}, pb[3] = {b.x, b.y, b.z}, pd[3] = {d.x, d.y, d.z};
+#pragma unroll
+  for (int k = 0; k < DIM; ++k) {
+    const int n = c.nc[k] / c.sub[k];
+    if (n < 3) continue;
+    const float cref = c.cell_size[k] * (float)c.sub[k];
+    if (fabsf(pd[k]) < cref * (1.0f - (float)(4 * n + 8) * 1.2e-7f)) continue;
+    int ia = hash_index(pa[k], c.cell_size[k], c.inv_cs[k]) / c.sub[k];
+    int ib = hash_index(pb[k], c.cell_size[k], c.inv_cs[k]) / c.sub[k];
+    ia = ia < 0 ? 0 : (ia >= n ? n - 1 : ia);
+    ib = ib < 0 ? 0 : (ib >= n ? n - 1 : ib);
+    const int s = ia > ib ? ia - ib : ib - ia;
+    if (s > 1 && s < n - 1) return false;
+  }
+  return true;
+}
+
 template <int DIM>
 __device__ __noinline__ bool exact_edge(float4 ri, float4 rj, const CaseDev* c) {
-  return is_edge<DIM>(ri, rj, *c) && (!c->fast || ref_adjacent<DIM>(ri, rj, *c));
+  const float3 d = pdisp3<DIM>(rj, ri, *c);
+  if (!(sqd<DIM>(d) < c->cutoff_sq)) return false;
+  return !c->fast || ref_adjacent_d<DIM>(ri, rj, d, *c);
 }
 
 // Membership as the list's backend defines it, for the emitted edge lists and

@@ -27,6 +27,8 @@
 //    from the fast reciprocal; the float32 tolerances against the float64
 //    oracle hold either way, and membership never depends on them (it is
 //    decided on squared distances, exactly as in the generic passes).
+#include <type_traits>
+
 #include "sph_pairs.cuh"
 
 namespace sph {
@@ -126,24 +128,30 @@ __device__ __forceinline__ void dist_inv(float d2, float& dist, float& inv_d) {
 // 2 ulp; the factor covers it).
 __device__ __forceinline__ float sqrt_up(float x) { return x * rsqrtf(x) * 1.000001f; }
 
-// Visit the cells whose box lies within sqrt(r2) of the box of cell `cell`
-// (gaps between cell boxes, less the rounding margin), clamped to r* cells on
-// each side, as contiguous ranges [j0, j1) of the sorted order with the
-// periodic shift of their image: rows (the last axes) by the gap between the
-// boxes, in each row the cells within the chord of that distance. Every
-// particle of the cell sees the same cells, so the lanes of a warp --
-// receivers in neighbouring cells -- walk rows of the same shape; the price is
-// more candidates than the particle's own sphere holds.
+// Visit the candidates of a receiver at ri, binned into cell `cell`: the rows
+// of cells whose box lies within sqrt(r2) of the cell's box (gaps between
+// cell boxes, less the rounding margin; r* cells at most on each side) -- the
+// same rows for every particle of a cell, so the lanes of a warp (receivers in
+// neighbouring cells) run the row loop in step -- and in each row the cells
+// within the chord of the particle's own sphere. A row is passed to f as one
+// concatenated run of up to two contiguous ranges of the sorted order, the
+// second where the row wraps around the periodic x face:
+//   f(a0, n0, a1, n1, s1, sy, sz)   -- [a0, a0 + n0) unshifted in x,
+//                                      [a1, a1 + n1) shifted by s1 in x,
+// both shifted by (sy, sz) in y and z, so that one loop of n0 + n1 trips
+// serves both and wrapping lanes do not diverge from the others.
 template <int DIM, typename F>
-__device__ __forceinline__ void box_rows(const CaseDev& c, int cell, const int* __restrict__ start,
-                                         int rx, int ry, int rz, float r2, F&& f) {
+__device__ __forceinline__ void box_rows(const CaseDev& c, int cell, const float4& ri,
+                                         const int* __restrict__ start, int rx, int ry, int rz,
+                                         float r2, F&& f) {
   const int nx = c.nc[0], ny = c.nc[1], nz = (DIM == 3) ? c.nc[2] : 1;
   const int cx = cell % nx;
   const int t = cell / nx;
   const int cy = t % ny;
   const int cz = (DIM == 3) ? t / ny : 0;
   const int* cs = start + c.cell_off;
-  const float R = sqrt_up(r2) + 2.f * c.trim_m;
+  const float m = c.trim_m;
+  const float R = sqrt_up(r2) + 2.f * m;
   const float R2 = R * R;
   const int zr = (DIM == 3) ? rz : 0;
   for (int dz = -zr; dz <= zr; ++dz) {
@@ -154,6 +162,14 @@ __device__ __forceinline__ void box_rows(const CaseDev& c, int cell, const int* 
     float sz = 0.f;
     if (zw < 0) { zw += nz; sz = -c.box[2]; }
     else if (zw >= nz) { zw -= nz; sz = c.box[2]; }
+    // the particle's own gap to the plane (NaN for a non-finite position:
+    // then no chord trimming below)
+    float pz2 = 0.f;
+    if (DIM == 3 && dz != 0) {
+      const float g = (dz > 0 ? (float)(cz + dz) * c.cell_size[2] - ri.z
+                              : ri.z - (float)(cz + dz + 1) * c.cell_size[2]) - m;
+      pz2 = g > 0.f ? g * g : 0.f;
+    }
     for (int dy = -ry; dy <= ry; ++dy) {
       const float gy = (float)max(abs(dy) - 1, 0) * c.cell_size[1];
       const float g2 = gz2 + gy * gy;
@@ -163,17 +179,47 @@ __device__ __forceinline__ void box_rows(const CaseDev& c, int cell, const int* 
       if (yw < 0) { yw += ny; sy = -c.box[1]; }
       else if (yw >= ny) { yw -= ny; sy = c.box[1]; }
       const int kx = min(rx, 1 + (int)(sqrt_up(R2 - g2) * c.inv_cs[0]));
-      const int xa = cx - kx, xb = cx + kx;
-      const int row = (zw * ny + yw) * nx;
-      if (xa < 0) {
-        f(cs[row], cs[row + xb + 1], make_float3(0.f, sy, sz));
-        f(cs[row + xa + nx], cs[row + nx], make_float3(-c.box[0], sy, sz));
-      } else if (xb >= nx) {
-        f(cs[row + xa], cs[row + nx], make_float3(0.f, sy, sz));
-        f(cs[row], cs[row + xb - nx + 1], make_float3(c.box[0], sy, sz));
-      } else {
-        f(cs[row + xa], cs[row + xb + 1], make_float3(0.f, sy, sz));
+      int xa = cx - kx, xb = cx + kx;
+      // the chord of the particle's sphere through this row
+      float p2 = pz2;
+      if (dy != 0) {
+        const float g = (dy > 0 ? (float)(cy + dy) * c.cell_size[1] - ri.y
+                                : ri.y - (float)(cy + dy + 1) * c.cell_size[1]) - m;
+        p2 += g > 0.f ? g * g : 0.f;
       }
+      if (p2 < R2) {
+        const float w = sqrt_up(R2 - p2) + m;
+        const float lo = floorf((ri.x - w) * c.inv_cs[0]);
+        const float hi = floorf((ri.x + w) * c.inv_cs[0]);
+        const int ta = (int)fminf(fmaxf(lo, (float)xa), (float)xb);
+        const int tb = (int)fminf(fmaxf(hi, (float)xa), (float)xb);
+        xa = ta;
+        xb = tb;
+      } else {
+        xb = xa - 1;  // no cell of this row reaches the sphere
+      }
+      const int row = (zw * ny + yw) * nx;
+      int a0, e0, a1 = 0, e1 = 0;
+      float s1 = 0.f;
+      if (xb < xa) {
+        a0 = e0 = 0;
+      } else if (xa < 0) {
+        a0 = cs[row];
+        e0 = cs[row + xb + 1];
+        a1 = cs[row + xa + nx];
+        e1 = cs[row + nx];
+        s1 = -c.box[0];
+      } else if (xb >= nx) {
+        a0 = cs[row + xa];
+        e0 = cs[row + nx];
+        a1 = cs[row];
+        e1 = cs[row + xb - nx + 1];
+        s1 = c.box[0];
+      } else {
+        a0 = cs[row + xa];
+        e0 = cs[row + xb + 1];
+      }
+      f(a0, e0 - a0, a1, e1 - a1, s1, sy, sz);
     }
   }
 }
@@ -186,7 +232,8 @@ template <int DIM, bool WIDE, typename F>
 __device__ __forceinline__ void lean_slow(int N, int i, const float4& ri, const CaseDev& c,
                                           const CaseDev* cp, const float4* __restrict__ P4,
                                           const typename Fmt<WIDE>::Word* vl, const int* vcnt,
-                                          int kv, const int* cellid, const int* start, F&& f) {
+                                          int kv, const int* cellid, const int* start,
+                                          const float4* rref, F&& f) {
   using L = Fmt<WIDE>;
   auto test = [&](int j) {
     const float4 rj = __ldg(P4 + j);
@@ -199,10 +246,12 @@ __device__ __forceinline__ void lean_slow(int N, int i, const float4& ri, const 
     for (int k = 0; k < vc; ++k) test(L::dec(i, L::raw(vl[(size_t)(k >> 2) * N + i], k & 3), N));
     return;
   }
-  box_rows<DIM>(c, cellid[i] - c.cell_off, start, c.vrad[0], c.vrad[1], c.vrad[2], c.v_r2,
-                [&](int j0, int j1, float3) {
-                  for (int j = j0; j < j1; ++j)
+  box_rows<DIM>(c, cellid[i] - c.cell_off, rref[i], start, c.vrad[0], c.vrad[1], c.vrad[2],
+                c.v_r2, [&](int a0, int n0, int a1, int n1, float, float, float) {
+                  for (int t = 0; t < n0 + n1; ++t) {
+                    const int j = t < n0 ? a0 + t : a1 + (t - n0);
                     if (j != i) test(j);
+                  }
                 });
 }
 
@@ -220,10 +269,10 @@ __global__ void __launch_bounds__(256)
 k_verlet_lean(int N, Buffers b, const CaseDev c, const int* __restrict__ cellid,
               const int* __restrict__ start, typename Fmt<WIDE>::Word* vl, int* vcnt, int kv) {
   using L = Fmt<WIDE>;
-  using Word = typename L::Word;
-  extern __shared__ __align__(16) unsigned char s_raw[];  // [kv / 4][blockDim.x] words
-  Word* srow = reinterpret_cast<Word*>(s_raw) + threadIdx.x;
+  using Slot = typename std::conditional<WIDE, int, unsigned short>::type;
+  extern __shared__ __align__(16) unsigned char s_raw[];  // [kv][blockDim.x] slot values
   const int bs = blockDim.x;
+  Slot* col = reinterpret_cast<Slot*>(s_raw) + threadIdx.x;
   const int i = blockIdx.x * bs + threadIdx.x;
   if (i >= N) return;
   if (tag_of(b.META[i]) == PAD) {
@@ -234,27 +283,30 @@ k_verlet_lean(int N, Buffers b, const CaseDev c, const int* __restrict__ cellid,
   const float r2 = c.v_r2;
   int m = 0;
   bool wide = false;
-  box_rows<DIM>(c, cellid[i] - c.cell_off, start, c.vrad[0], c.vrad[1], c.vrad[2], r2,
-                [&](int j0, int j1, float3 s) {
-    const float qx = ri.x - s.x, qy = ri.y - s.y, qz = ri.z - s.z;
-#pragma unroll 4
-    for (int j = j0; j < j1; ++j) {
+  box_rows<DIM>(c, cellid[i] - c.cell_off, ri, start, c.vrad[0], c.vrad[1], c.vrad[2], r2,
+                [&](int a0, int n0, int a1, int n1, float s1, float sy, float sz) {
+    const float qy = ri.y - sy, qz = ri.z - sz;
+    const int n = n0 + n1;
+#pragma unroll 2
+    for (int t = 0; t < n; ++t) {
+      const bool second = t >= n0;
+      const int j = second ? a1 + (t - n0) : a0 + t;
       const float4 rj = __ldg(b.P4 + j);
-      const float dx = qx - rj.x, dy = qy - rj.y, dz = (DIM == 3) ? qz - rj.z : 0.f;
+      const float dx = (ri.x - (second ? s1 : 0.f)) - rj.x, dy = qy - rj.y;
+      const float dz = (DIM == 3) ? qz - rj.z : 0.f;
       const bool in = j != i && dx * dx + dy * dy + dz * dz < r2;
       int o;
       const bool fits = L::enc(i, j, N, o);
       wide |= in && !fits;
-      L::put(srow, (size_t)bs, m < kv ? m : kv - 1, o);
+      col[(m < kv ? m : kv - 1) * bs] = (Slot)o;
       m += in;
     }
   });
   const bool listed = !wide && m <= kv;
   vcnt[i] = listed ? m : kv + 1;
   if (listed) {
-    Word* out = vl + i;
-    const int ng = (m + 3) >> 2;
-    for (int g = 0; g < ng; ++g) out[(size_t)g * N] = srow[(size_t)g * bs];
+    typename L::Word* out = vl + i;
+    for (int k = 0; k < m; ++k) L::put(out, (size_t)N, k, (int)col[k * bs]);
   }
 }
 
@@ -273,6 +325,38 @@ __device__ __forceinline__ void count_edges1(int cnt, bool valid, unsigned long 
 }
 
 // ------------------------------------------------------------------ density
+// The density filter of a receiver whose candidates did not fit its list:
+// out of line, so that the rare walk does not take registers from the hot
+// loop; the case comes from its device copy.
+template <int DIM, int KER, bool KAHAN, bool WIDE>
+struct DensitySlow {
+  Acc<KAHAN> s;
+  int m, wide;
+};
+template <int DIM, int KER, bool KAHAN, bool WIDE>
+__device__ __noinline__ DensitySlow<DIM, KER, KAHAN, WIDE> density_slow(
+    int N, int i, float4 ri, bool fluid, Acc<KAHAN> s0, const CaseDev* cp, const float4* P4,
+    const typename Fmt<WIDE>::Word* vl, const int* vcnt, int kv, const int* cellid,
+    const int* start, const float4* rref, typename Fmt<WIDE>::Word* srow, int bs, int kmax) {
+  using L = Fmt<WIDE>;
+  const CaseDev& c = *cp;
+  int m = 0;
+  bool wide = false;
+  lean_slow<DIM, WIDE>(N, i, ri, c, cp, P4, vl, vcnt, kv, cellid, start, rref,
+                       [&](int j, const float4&, const float3&, float d2) {
+                         if (fluid) {
+                           float dist, inv_d;
+                           dist_inv(d2, dist, inv_d);
+                           s0.add(kw<KER>(dist, c));
+                         }
+                         int o;
+                         wide |= !L::enc(i, j, N, o);
+                         if (m < kmax) L::put(srow, (size_t)bs, m, o);
+                         ++m;
+                       });
+  return {s0, m, wide ? 1 : 0};
+}
+
 // Summation density (rho_i = m_i sum_j W_ij over the edges, self pair
 // included unless masked; fluid receivers), Tait / Riemann EOS, and the
 // step's neighbour list (staged in shared memory, written k-major) for the
@@ -284,7 +368,7 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
                const int* __restrict__ cellid, const int* __restrict__ start,
                const typename Fmt<WIDE>::Word* __restrict__ vl, const int* __restrict__ vcnt,
                int kv, typename Fmt<WIDE>::Word* nb, int* nbcnt, int kmax, float4* R4,
-               unsigned long long* edgecnt, unsigned* status) {
+               const float4* __restrict__ rref, unsigned long long* edgecnt, unsigned* status) {
   using L = Fmt<WIDE>;
   using Word = typename L::Word;
   extern __shared__ __align__(16) unsigned char s_raw[];  // [kmax / 4][blockDim.x] words
@@ -321,33 +405,26 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          // branch-free: the kernel value of every candidate (zero beyond
-          // the support) enters the sum only for an edge, and every slot
-          // value is stored at the next free slot, kept only for an edge
+          // every slot value is stored at the next free slot and kept only
+          // for an edge (no branch around the store)
           float3 dr;
           float d2;
           const bool e = q < rem && lean_edge<DIM>(ri, rj[q], c, cp, dr, d2);
-          float dist, inv_d;
-          dist_inv(d2, dist, inv_d);
-          const float w = kw<KER>(dist, c);
-          if (fluid) s0.add(e ? w : 0.f);
+          if (e && fluid) {
+            float dist, inv_d;
+            dist_inv(d2, dist, inv_d);
+            s0.add(kw<KER>(dist, c));
+          }
           L::put(srow, (size_t)bs, m < kmax ? m : kmax - 1, o[q]);
           m += e;
         }
       }
     } else {
-      lean_slow<DIM, WIDE>(N, i, ri, c, cp, b.P4, vl, vcnt, kv, cellid, start,
-                           [&](int j, const float4&, const float3&, float d2) {
-                             if (fluid) {
-                               float dist, inv_d;
-                               dist_inv(d2, dist, inv_d);
-                               s0.add(kw<KER>(dist, c));
-                             }
-                             int o;
-                             wide |= !L::enc(i, j, N, o);
-                             if (m < kmax) L::put(srow, (size_t)bs, m, o);
-                             ++m;
-                           });
+      const DensitySlow<DIM, KER, KAHAN, WIDE> r = density_slow<DIM, KER, KAHAN, WIDE>(
+          N, i, ri, fluid, s0, cp, b.P4, vl, vcnt, kv, cellid, start, rref, srow, bs, kmax);
+      s0 = r.s;
+      m = r.m;
+      wide = r.wide != 0;
     }
     cnt = tag == PAD ? 0 : m + (self_term ? 1 : 0);
     // a receiver whose senders do not fit the format keeps its count, flagged
@@ -366,76 +443,111 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
 }
 
 // ------------------------------------------------------------------ force
-// Standard acceleration with the transport-velocity stress (solver.py:216-256),
-// the transport-velocity acceleration (:199-213), artificial viscosity
-// (:404-428), g_ext and bc_fn, over the density pass's neighbour list; the
-// next sender's four records are in flight while a pair is evaluated, and the
-// list word after the current one a group ahead.
+// The receiver's own quantities of the force pass.
+struct ForceI {
+  float4 ri;
+  float3 ui, Ai, wi;
+  float rho_i, p_i, eta_i, Vi2, inv_mi;
+  bool fluid;
+};
+
+template <bool KAHAN>
+struct Acc6 {
+  Acc<KAHAN> ax, ay, az, tx, ty, tz;
+};
+
+// One pair of the standard acceleration with the transport-velocity stress
+// (solver.py:216-256), the transport-velocity acceleration (:199-213) and the
+// artificial viscosity (:404-428).
+template <int DIM, int KER, bool KAHAN>
+__device__ __forceinline__ void force_pair(const ForceI& I, const CaseDev& c, const int* meta,
+                                           int j, const float4& rj, const float4& Uj4,
+                                           const float4& Vj4, const float4& Rj,
+                                           const float3& dr, float d2, Acc6<KAHAN>& A) {
+  float dist, inv_d;
+  dist_inv(d2, dist, inv_d);
+  const float gw = kdw<KER>(dist, c);
+  const float rho_j = Rj.x, p_j = Rj.y, eta_j = Rj.w, m_j = rj.w;
+  const float Vj = __fdividef(m_j, rho_j);
+  const float cc = (I.Vi2 + Vj * Vj) * I.inv_mi * gw * inv_d;
+  const float3 uj = f3(Uj4);
+  const float3 vj = f3(Vj4);
+  const float eta_ij = __fdividef(2.f * I.eta_i * eta_j, I.eta_i + eta_j + kEps);
+  const float p_ij = __fdividef(rho_j * I.p_i + I.rho_i * p_j, I.rho_i + rho_j);
+  const float ki = dot3(I.wi, dr);
+  const float kj = dot3(make_float3(vj.x - uj.x, vj.y - uj.y, vj.z - uj.z), dr);
+  float3 a = make_float3(cc * (-p_ij * dr.x + 0.5f * (I.Ai.x * ki + rho_j * uj.x * kj) +
+                               eta_ij * (I.ui.x - uj.x)),
+                         cc * (-p_ij * dr.y + 0.5f * (I.Ai.y * ki + rho_j * uj.y * kj) +
+                               eta_ij * (I.ui.y - uj.y)),
+                         cc * (-p_ij * dr.z + 0.5f * (I.Ai.z * ki + rho_j * uj.z * kj) +
+                               eta_ij * (I.ui.z - uj.z)));
+  if (c.av_alpha != 0.0f && I.fluid && tag_of(meta[j]) == FLUID) {
+    const float rho_ab = 0.5f * (I.rho_i + rho_j);
+    const float num = m_j * c.av_alpha * c.av_hab * c.av_cab *
+                      ((I.ui.x - uj.x) * dr.x + (I.ui.y - uj.y) * dr.y + (I.ui.z - uj.z) * dr.z);
+    const float k = num * gw * inv_d / (rho_ab * (dist * dist + c.av_eps));
+    a.x += k * dr.x;
+    a.y += k * dr.y;
+    a.z += k * dr.z;
+  }
+  A.ax.add(a.x);
+  A.ay.add(a.y);
+  A.az.add(a.z);
+  const float ct = cc * c.p_bg_tvf;
+  A.tx.add(ct * dr.x);
+  A.ty.add(ct * dr.y);
+  A.tz.add(ct * dr.z);
+}
+
+// The force sums of a receiver whose neighbours did not fit its list: out of
+// line (see density_slow).
+template <int DIM, int KER, bool KAHAN, bool WIDE>
+__device__ __noinline__ Acc6<KAHAN> force_slow(int N, int i, ForceI I, Acc6<KAHAN> A,
+                                               const CaseDev* cp, Buffers b, const float4* R4,
+                                               const typename Fmt<WIDE>::Word* vl,
+                                               const int* vcnt, int kv, const int* cellid,
+                                               const int* start, const float4* rref) {
+  const CaseDev& c = *cp;
+  lean_slow<DIM, WIDE>(N, i, I.ri, c, cp, b.P4, vl, vcnt, kv, cellid, start, rref,
+                       [&](int j, const float4& rj, const float3& dr, float d2) {
+                         force_pair<DIM, KER, KAHAN>(I, c, b.META, j, rj, __ldg(b.U4 + j),
+                                                     __ldg(b.V4 + j), __ldg(R4 + j), dr, d2, A);
+                       });
+  return A;
+}
+
+// The force pass over the density pass's neighbour list, with g_ext and
+// bc_fn; the next sender's four records are in flight while a pair is
+// evaluated, and the list word after the current one a group ahead.
 template <int DIM, int KER, bool KAHAN, bool WIDE>
 __global__ void __launch_bounds__(256, 3)
 k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* g_arr,
              const float4* __restrict__ R4, const typename Fmt<WIDE>::Word* __restrict__ nb,
              const int* __restrict__ nbcnt, int kmax, const typename Fmt<WIDE>::Word* vl,
-             const int* vcnt, int kv, const int* cellid, const int* start, bool apply_bc,
-             unsigned* status) {
+             const int* vcnt, int kv, const int* cellid, const int* start, const float4* rref,
+             bool apply_bc, unsigned* status) {
   using L = Fmt<WIDE>;
   using Word = typename L::Word;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= N) return;
   const int tag = tag_of(b.META[i]);
-  const bool fluid_i = tag == FLUID;
-  const float4 ri = b.P4[i];
-  const float m_i = ri.w;
-  const float3 ui = f3(b.U4[i]);
+  ForceI I;
+  I.ri = b.P4[i];
+  I.fluid = tag == FLUID;
+  I.ui = f3(b.U4[i]);
   const float3 vi = f3(b.V4[i]);
   const float4 Ri = R4[i];
-  const float rho_i = Ri.x, p_i = Ri.y, eta_i = Ri.w;
-  const float Vi = m_i / rho_i;
-  const float Vi2 = Vi * Vi;
-  const float inv_mi = 1.0f / m_i;
-  const float3 Ai = make_float3(rho_i * ui.x, rho_i * ui.y, rho_i * ui.z);
-  const float3 wi = make_float3(vi.x - ui.x, vi.y - ui.y, vi.z - ui.z);
-  const float3 gi = g_ext<DIM>(c, ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
-  const bool av = c.av_alpha != 0.0f;
-  const float p_bg = c.p_bg_tvf;
-  Acc<KAHAN> ax, ay, az, tx, ty, tz;
-  auto pair = [&](int j, const float4& rj, const float4& Uj4, const float4& Vj4,
-                  const float4& Rj, const float3& dr, float d2) {
-    float dist, inv_d;
-    dist_inv(d2, dist, inv_d);
-    const float gw = kdw<KER>(dist, c);
-    const float rho_j = Rj.x, p_j = Rj.y, eta_j = Rj.w, m_j = rj.w;
-    const float Vj = __fdividef(m_j, rho_j);
-    const float cc = (Vi2 + Vj * Vj) * inv_mi * gw * inv_d;
-    const float3 uj = f3(Uj4);
-    const float3 vj = f3(Vj4);
-    const float eta_ij = __fdividef(2.f * eta_i * eta_j, eta_i + eta_j + kEps);
-    const float p_ij = __fdividef(rho_j * p_i + rho_i * p_j, rho_i + rho_j);
-    const float ki = dot3(wi, dr);
-    const float kj = dot3(make_float3(vj.x - uj.x, vj.y - uj.y, vj.z - uj.z), dr);
-    float3 a = make_float3(cc * (-p_ij * dr.x + 0.5f * (Ai.x * ki + rho_j * uj.x * kj) +
-                                 eta_ij * (ui.x - uj.x)),
-                           cc * (-p_ij * dr.y + 0.5f * (Ai.y * ki + rho_j * uj.y * kj) +
-                                 eta_ij * (ui.y - uj.y)),
-                           cc * (-p_ij * dr.z + 0.5f * (Ai.z * ki + rho_j * uj.z * kj) +
-                                 eta_ij * (ui.z - uj.z)));
-    if (av && fluid_i && tag_of(b.META[j]) == FLUID) {
-      const float rho_ab = 0.5f * (rho_i + rho_j);
-      const float num = m_j * c.av_alpha * c.av_hab * c.av_cab *
-                        ((ui.x - uj.x) * dr.x + (ui.y - uj.y) * dr.y + (ui.z - uj.z) * dr.z);
-      const float k = num * gw * inv_d / (rho_ab * (dist * dist + c.av_eps));
-      a.x += k * dr.x;
-      a.y += k * dr.y;
-      a.z += k * dr.z;
-    }
-    ax.add(a.x);
-    ay.add(a.y);
-    az.add(a.z);
-    const float ct = cc * p_bg;
-    tx.add(ct * dr.x);
-    ty.add(ct * dr.y);
-    tz.add(ct * dr.z);
-  };
+  I.rho_i = Ri.x;
+  I.p_i = Ri.y;
+  I.eta_i = Ri.w;
+  const float Vi = I.ri.w / I.rho_i;
+  I.Vi2 = Vi * Vi;
+  I.inv_mi = 1.0f / I.ri.w;
+  I.Ai = make_float3(I.rho_i * I.ui.x, I.rho_i * I.ui.y, I.rho_i * I.ui.z);
+  I.wi = make_float3(vi.x - I.ui.x, vi.y - I.ui.y, vi.z - I.ui.z);
+  const float3 gi = g_ext<DIM>(c, I.ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
+  Acc6<KAHAN> A;
   const int m = nbcnt[i];
   if (m <= kmax) {
     const Word* nbi = nb + i;
@@ -460,18 +572,15 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
       }
       float3 dr;
       float d2;
-      mi_dr<DIM>(ri, rc, c, dr, d2);
-      pair(jc, rc, uc, vc, Rc, dr, d2);
+      mi_dr<DIM>(I.ri, rc, c, dr, d2);
+      force_pair<DIM, KER, KAHAN>(I, c, b.META, jc, rc, uc, vc, Rc, dr, d2, A);
     }
   } else {
-    lean_slow<DIM, WIDE>(N, i, ri, c, cp, b.P4, vl, vcnt, kv, cellid, start,
-                         [&](int j, const float4& rj, const float3& dr, float d2) {
-                           pair(j, rj, __ldg(b.U4 + j), __ldg(b.V4 + j), __ldg(R4 + j), dr,
-                                d2);
-                         });
+    A = force_slow<DIM, KER, KAHAN, WIDE>(N, i, I, A, cp, b, R4, vl, vcnt, kv, cellid, start,
+                                          rref);
   }
-  float3 dudt = make_float3(ax.s + gi.x, ay.s + gi.y, az.s + gi.z);
-  float3 dvdt = make_float3(tx.s, ty.s, tz.s);
+  float3 dudt = make_float3(A.ax.s + gi.x, A.ay.s + gi.y, A.az.s + gi.z);
+  float3 dvdt = make_float3(A.tx.s, A.ty.s, A.tz.s);
   if (DIM == 2) {
     dudt.z = 0.f;
     dvdt.z = 0.f;
@@ -500,7 +609,7 @@ void forward_lean_t(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid
     const size_t smem = sizeof(Word) * (L.kmax / 4) * bt;
     k_density_lean<DIM, KER, KAHAN, WIDE><<<g, bt, smem, L.stream>>>(
         N, b, L.c1, L.cases, !L.mask_self, cellid, start, vl, L.vcnt, L.kv, nb, L.nbr_cnt,
-        L.kmax, R4, edgecnt, L.status);
+        L.kmax, R4, L.rref, edgecnt, L.status);
     count_launch(L);
     mark(L, 2);
     mark(L, 3);
@@ -508,7 +617,7 @@ void forward_lean_t(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid
   if (phases & 2) {
     k_force_lean<DIM, KER, KAHAN, WIDE><<<g, bt, 0, L.stream>>>(
         N, b, L.c1, L.cases, g_arr, R4, nb, L.nbr_cnt, L.kmax, vl, L.vcnt, L.kv, cellid, start,
-        apply_bc, L.status);
+        L.rref, apply_bc, L.status);
     count_launch(L);
     mark(L, 4);
   }
@@ -540,7 +649,7 @@ template <int DIM, bool WIDE>
 void verlet_lean_t(const LaunchCtx& L, Buffers b, const int* cellid, const int* start) {
   using Word = typename Fmt<WIDE>::Word;
   // the staging column of kv slots per thread stays within 48 KB per block
-  const int col = (int)sizeof(Word) * (L.kv / 4);
+  const int col = (WIDE ? 4 : 2) * L.kv;
   int bt = (49152 / col) / 32 * 32;
   bt = bt > 256 ? 256 : bt;
   const size_t smem = (size_t)col * bt;

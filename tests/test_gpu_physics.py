@@ -385,8 +385,17 @@ def test_drop_in_moving_wall_normals():
     for k in ("r", "u", "nw"):
         a, b = st[k].double(), got[k].double()
         assert float((a - b).abs().max()) <= 1e-5 * (float(b.abs().max()) + 1e-30), k
-    with pytest.raises(NotImplementedError):
-        integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, lambda r: r)
+    # a plain function as nw_fn (no GPU spec): the step is composed like the
+    # reference's and returns the same normals
+    nw_plain = setup.nw_fn.__call__
+    adv2 = integrator.si_euler(setup.tvf, wc.forward_wrapper(), shift, setup.bc_fn, nw_plain)
+    st2 = setup.to("cuda")
+    nb2 = fns.allocate(st2["r"])
+    for _ in range(5):
+        st2, nb2 = adv2(setup.dt, st2, nb2)
+    for k in ("r", "u", "nw"):
+        a, b = st2[k].double().cpu(), st[k].double().cpu()
+        assert float((a - b).abs().max()) <= 1e-5 * (float(b.abs().max()) + 1e-30), k
 
 
 def test_drop_in_advance_rejects_pageable_host_arrays():
