@@ -269,10 +269,9 @@ __global__ void __launch_bounds__(256)
 k_verlet_lean(int N, Buffers b, const CaseDev c, const int* __restrict__ cellid,
               const int* __restrict__ start, typename Fmt<WIDE>::Word* vl, int* vcnt, int kv) {
   using L = Fmt<WIDE>;
-  using Slot = typename std::conditional<WIDE, int, unsigned short>::type;
-  extern __shared__ __align__(16) unsigned char s_raw[];  // [kv][blockDim.x] slot values
+  extern __shared__ __align__(16) unsigned char s_raw[];  // [kv][blockDim.x] sender indices
   const int bs = blockDim.x;
-  Slot* col = reinterpret_cast<Slot*>(s_raw) + threadIdx.x;
+  int* col = reinterpret_cast<int*>(s_raw) + threadIdx.x;
   const int i = blockIdx.x * bs + threadIdx.x;
   if (i >= N) return;
   if (tag_of(b.META[i]) == PAD) {
@@ -282,32 +281,33 @@ k_verlet_lean(int N, Buffers b, const CaseDev c, const int* __restrict__ cellid,
   const float4 ri = b.P4[i];
   const float r2 = c.v_r2;
   int m = 0;
-  bool wide = false;
   box_rows<DIM>(c, cellid[i] - c.cell_off, ri, start, c.vrad[0], c.vrad[1], c.vrad[2], r2,
                 [&](int a0, int n0, int a1, int n1, float s1, float sy, float sz) {
-    const float qy = ri.y - sy, qz = ri.z - sz;
+    const float qx0 = ri.x, qx1 = ri.x - s1, qy = ri.y - sy, qz = ri.z - sz;
+    const int d1 = a1 - n0;
     const int n = n0 + n1;
 #pragma unroll 2
     for (int t = 0; t < n; ++t) {
       const bool second = t >= n0;
-      const int j = second ? a1 + (t - n0) : a0 + t;
+      const int j = t + (second ? d1 : a0);
       const float4 rj = __ldg(b.P4 + j);
-      const float dx = (ri.x - (second ? s1 : 0.f)) - rj.x, dy = qy - rj.y;
+      const float dx = (second ? qx1 : qx0) - rj.x, dy = qy - rj.y;
       const float dz = (DIM == 3) ? qz - rj.z : 0.f;
       const bool in = j != i && dx * dx + dy * dy + dz * dz < r2;
-      int o;
-      const bool fits = L::enc(i, j, N, o);
-      wide |= in && !fits;
-      col[(m < kv ? m : kv - 1) * bs] = (Slot)o;
+      col[(m < kv ? m : kv - 1) * bs] = j;
       m += in;
     }
   });
-  const bool listed = !wide && m <= kv;
-  vcnt[i] = listed ? m : kv + 1;
-  if (listed) {
+  bool wide = false;
+  if (m <= kv) {
     typename L::Word* out = vl + i;
-    for (int k = 0; k < m; ++k) L::put(out, (size_t)N, k, (int)col[k * bs]);
+    for (int k = 0; k < m; ++k) {
+      int o;
+      wide |= !L::enc(i, col[k * bs], N, o);
+      L::put(out, (size_t)N, k, o);
+    }
   }
+  vcnt[i] = (wide || m > kv) ? kv + 1 : m;
 }
 
 // Edge count for the NEIGHBOR_LIST_OVERFLOW test (one case). The capacity is
@@ -550,30 +550,36 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
   Acc6<KAHAN> A;
   const int m = nbcnt[i];
   if (m <= kmax) {
+    // groups of four list slots (slot positions known at compile time); the
+    // next sender's records are loaded while a pair is evaluated, and the
+    // next group's word during the current group
     const Word* nbi = nb + i;
-    Word w = nbi[0];  // (read even without neighbours: never used then)
-    Word wn = m > 4 ? nbi[N] : w;
-    int j = m > 0 ? L::dec(i, L::raw(w, 0), N) : i;
-    float4 rj = __ldg(b.P4 + j), uj = __ldg(b.U4 + j), vj = __ldg(b.V4 + j), Rj = __ldg(R4 + j);
-    for (int k = 0; k < m; ++k) {
-      const int jc = j;
-      const float4 rc = rj, uc = uj, vc = vj, Rc = Rj;
-      const int kn = k + 1;
-      if (kn < m) {
-        if ((kn & 3) == 0) {
-          w = wn;
-          if (kn + 4 < m) wn = nbi[(size_t)((kn >> 2) + 1) * N];
+    const int ng = (m + 3) >> 2;
+    Word wn = nbi[0];  // (read even without neighbours: never used then)
+    int jn = m > 0 ? L::dec(i, L::raw(wn, 0), N) : i;
+    float4 rn = __ldg(b.P4 + jn), un = __ldg(b.U4 + jn), vn = __ldg(b.V4 + jn),
+           Rn = __ldg(R4 + jn);
+    for (int g = 0; g < ng; ++g) {
+      const Word w = wn;
+      if (g + 1 < ng) wn = nbi[(size_t)(g + 1) * N];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int k = 4 * g + q;
+        if (k < m) {
+          const int jc = jn;
+          const float4 rc = rn, uc = un, vc = vn, Rc = Rn;
+          const int on = q < 3 ? L::raw(w, q + 1) : L::raw(wn, 0);
+          jn = k + 1 < m ? L::dec(i, on, N) : i;
+          rn = __ldg(b.P4 + jn);
+          un = __ldg(b.U4 + jn);
+          vn = __ldg(b.V4 + jn);
+          Rn = __ldg(R4 + jn);
+          float3 dr;
+          float d2;
+          mi_dr<DIM>(I.ri, rc, c, dr, d2);
+          force_pair<DIM, KER, KAHAN>(I, c, b.META, jc, rc, uc, vc, Rc, dr, d2, A);
         }
-        j = L::dec(i, L::raw(w, kn & 3), N);
-        rj = __ldg(b.P4 + j);
-        uj = __ldg(b.U4 + j);
-        vj = __ldg(b.V4 + j);
-        Rj = __ldg(R4 + j);
       }
-      float3 dr;
-      float d2;
-      mi_dr<DIM>(I.ri, rc, c, dr, d2);
-      force_pair<DIM, KER, KAHAN>(I, c, b.META, jc, rc, uc, vc, Rc, dr, d2, A);
     }
   } else {
     A = force_slow<DIM, KER, KAHAN, WIDE>(N, i, I, A, cp, b, R4, vl, vcnt, kv, cellid, start,
@@ -648,8 +654,8 @@ void forward_lean_k(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid
 template <int DIM, bool WIDE>
 void verlet_lean_t(const LaunchCtx& L, Buffers b, const int* cellid, const int* start) {
   using Word = typename Fmt<WIDE>::Word;
-  // the staging column of kv slots per thread stays within 48 KB per block
-  const int col = (WIDE ? 4 : 2) * L.kv;
+  // the staging column of kv sender indices per thread stays within 48 KB
+  const int col = 4 * L.kv;
   int bt = (49152 / col) / 32 * 32;
   bt = bt > 256 ? 256 : bt;
   const size_t smem = (size_t)col * bt;
