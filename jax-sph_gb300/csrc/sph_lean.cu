@@ -405,18 +405,18 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
         }
 #pragma unroll
         for (int q = 0; q < 4; ++q) {
-          // every slot value is stored at the next free slot and kept only
-          // for an edge (no branch around the store)
           float3 dr;
           float d2;
           const bool e = q < rem && lean_edge<DIM>(ri, rj[q], c, cp, dr, d2);
-          if (e && fluid) {
-            float dist, inv_d;
-            dist_inv(d2, dist, inv_d);
-            s0.add(kw<KER>(dist, c));
+          if (e) {
+            if (fluid) {
+              float dist, inv_d;
+              dist_inv(d2, dist, inv_d);
+              s0.add(kw<KER>(dist, c));
+            }
+            if (m < kmax) L::put(srow, (size_t)bs, m, o[q]);
+            ++m;
           }
-          L::put(srow, (size_t)bs, m < kmax ? m : kmax - 1, o[q]);
-          m += e;
         }
       }
     } else {
