@@ -191,7 +191,31 @@ void adjoint_t(const LaunchCtx& L, const Tape& t, float* mu, const float* la_in,
   k_adj_grad<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, la_in, mu, lr, lu, la_out);
 }
 
+// The tape slot of the step just taken, one thread per particle (the
+// neighbour list row by row, coalesced).
+__global__ void k_tape_record(long long N, Buffers b, const float4* R4, const int* nbr,
+                              const int* cnt, int kmax, int* t_orig, float4* t_P4, float4* t_U4,
+                              float4* t_R4, int* t_nbr, int* t_cnt) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  t_orig[k] = b.ORIG[k];
+  t_P4[k] = b.P4[k];
+  t_U4[k] = b.U4[k];
+  t_R4[k] = R4[k];
+  const int m = cnt[k];
+  t_cnt[k] = m;
+  const int e = m < kmax ? m : kmax;
+  for (int q = 0; q < e; ++q) t_nbr[(long long)q * N + k] = nbr[(long long)q * N + k];
+}
+
 }  // namespace
+
+void launch_tape_record(const LaunchCtx& L, Buffers b, const float4* R4, int* t_orig,
+                        float4* t_P4, float4* t_U4, float4* t_R4, int* t_nbr, int* t_cnt) {
+  const int g = (int)((L.N + kBlock - 1) / kBlock);
+  k_tape_record<<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.nbr, L.nbr_cnt, L.kmax, t_orig, t_P4,
+                                            t_U4, t_R4, t_nbr, t_cnt);
+}
 
 void launch_adjoint(const LaunchCtx& L, const int* orig, const float4* P4, const float4* U4,
                     const float4* R4, const int* nbr, const int* cnt, float* mu,

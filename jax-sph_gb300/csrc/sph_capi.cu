@@ -1383,20 +1383,12 @@ int sph_tape_record(SphHandle* h, int32_t slot, void* stream) try {
     return fail((int)SPH_ERR_INVALID_ARG, "tape slot out of range");
   if (!(h->from_forward && h->pending_bc))
     return fail((int)SPH_ERR_INVALID_ARG, "record the tape right after sph_step");
-  cudaStream_t st = (cudaStream_t)stream;
   const long long N = h->N;
   const Buffers& b = h->buf[0];
-  cudaError_t e = cudaSuccess;
-  auto cp = [&](void* dst, const void* src, size_t bytes) {
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
-  };
-  cp(h->t_orig + slot * N, b.ORIG, sizeof(int) * N);
-  cp(h->t_P4 + slot * N, b.P4, sizeof(float4) * N);
-  cp(h->t_U4 + slot * N, b.U4, sizeof(float4) * N);
-  cp(h->t_R4 + slot * N, h->R4, sizeof(float4) * N);
-  cp(h->t_nbr + (size_t)slot * h->kmax * N, h->nbr, sizeof(int) * h->kmax * N);
-  cp(h->t_cnt + slot * N, h->nbr_cnt, sizeof(int) * N);
-  return cuda_check(e, "tape record");
+  launch_tape_record(h->ctx((cudaStream_t)stream), b, h->R4, h->t_orig + slot * N,
+                     h->t_P4 + slot * N, h->t_U4 + slot * N, h->t_R4 + slot * N,
+                     h->t_nbr + (size_t)slot * h->kmax * N, h->t_cnt + slot * N);
+  return launch_status("tape record");
 } catch (...) {
   return host_error();
 }

@@ -772,6 +772,9 @@ void launch_renorm(const LaunchCtx& L, Buffers b, const float4* Rin, float4* Rou
 
 size_t scan_tmp_ints(long long n);
 
+// sph_adjoint.cu: copy the step just taken into a tape slot (one kernel).
+void launch_tape_record(const LaunchCtx& L, Buffers b, const float4* R4, int* t_orig,
+                        float4* t_P4, float4* t_U4, float4* t_R4, int* t_nbr, int* t_cnt);
 // sph_adjoint.cu: reverse of one recorded step (tape arrays of that step).
 void launch_adjoint(const LaunchCtx& L, const int* orig, const float4* P4, const float4* U4,
                     const float4* R4, const int* nbr, const int* cnt, float* mu,
