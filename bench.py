@@ -207,14 +207,22 @@ def fp64_error(setup, steps, device, threads):
     torch.set_num_threads(threads)
     with torch.no_grad():
         ref = oracle_rollout(setup, steps, torch.float64)
+        ref32 = oracle_rollout(setup, steps, torch.float32)
     side = torch.as_tensor(setup.box, dtype=torch.float64)
-    dr = oracle.space.periodic_displacement(side, got["r"].double().cpu() - ref["r"])
-    u64 = ref["u"]
-    return {"steps": steps, "against": "float64 oracle (CPU restatement of the reference step)",
-            "r_max_over_box": float(dr.abs().max() / side.max()),
-            "u_max_rel": float((got["u"].double().cpu() - u64).abs().max() / u64.abs().max()),
-            "rho_max_rel": float((got["rho"].double().cpu() - ref["rho"]).abs().max()
-                                 / setup.eos.rho_ref)}
+
+    def errors(st):
+        dr = oracle.space.periodic_displacement(side, st["r"].double().cpu() - ref["r"])
+        return {"r_max_over_box": float(dr.abs().max() / side.max()),
+                "u_max_rel": float((st["u"].double().cpu() - ref["u"]).abs().max()
+                                   / ref["u"].abs().max()),
+                "rho_max_rel": float((st["rho"].double().cpu() - ref["rho"]).abs().max()
+                                     / setup.eos.rho_ref)}
+
+    # the float32 oracle's own distance from the float64 run: what float32
+    # rounding of the same algorithm alone gives
+    return dict(errors(got), steps=steps,
+                against="float64 oracle (CPU restatement of the reference step)",
+                float32_oracle=errors(ref32))
 
 
 def reference_arm(args, ws, rank):
