@@ -325,16 +325,15 @@ __device__ __forceinline__ void count_edges1(int cnt, bool valid, unsigned long 
 }
 
 // ------------------------------------------------------------------ density
-// The density filter of a receiver whose candidates did not fit its list:
-// out of line, so that the rare walk does not take registers from the hot
-// loop; the case comes from its device copy.
+// The density filter of a receiver whose candidates did not fit its list
+// (the case from its device copy).
 template <int DIM, int KER, bool KAHAN, bool WIDE>
 struct DensitySlow {
   Acc<KAHAN> s;
   int m, wide;
 };
 template <int DIM, int KER, bool KAHAN, bool WIDE>
-__device__ __noinline__ DensitySlow<DIM, KER, KAHAN, WIDE> density_slow(
+__device__ __forceinline__ DensitySlow<DIM, KER, KAHAN, WIDE> density_slow(
     int N, int i, float4 ri, bool fluid, Acc<KAHAN> s0, const CaseDev* cp, const float4* P4,
     const typename Fmt<WIDE>::Word* vl, const int* vcnt, int kv, const int* cellid,
     const int* start, const float4* rref, typename Fmt<WIDE>::Word* srow, int bs, int kmax) {
@@ -500,10 +499,10 @@ __device__ __forceinline__ void force_pair(const ForceI& I, const CaseDev& c, co
   A.tz.add(ct * dr.z);
 }
 
-// The force sums of a receiver whose neighbours did not fit its list: out of
-// line (see density_slow).
+// The force sums of a receiver whose neighbours did not fit its list (the
+// case from its device copy).
 template <int DIM, int KER, bool KAHAN, bool WIDE>
-__device__ __noinline__ Acc6<KAHAN> force_slow(int N, int i, ForceI I, Acc6<KAHAN> A,
+__device__ __forceinline__ Acc6<KAHAN> force_slow(int N, int i, ForceI I, Acc6<KAHAN> A,
                                                const CaseDev* cp, Buffers b, const float4* R4,
                                                const typename Fmt<WIDE>::Word* vl,
                                                const int* vcnt, int kv, const int* cellid,
