@@ -36,7 +36,7 @@
 extern "C" {
 #endif
 
-#define SPH_ABI_VERSION 6
+#define SPH_ABI_VERSION 7
 
 /* Reference PartitionErrorCode bits (jax_sph/jax_md/partition.py:453-457). */
 #define SPH_NEIGHBOR_LIST_OVERFLOW 0x1u
@@ -289,25 +289,25 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream);
  * neighbour list frozen per step, the way the reference differentiates a
  * rollout with jax.grad(..., allow_int=True) (notebooks/iclr24_grads.ipynb,
  * notebooks/iclr24_inverse.ipynb). Covers one case of the SPH solver with
- * density summation, tvf = 0, no wall BC and no artificial viscosity.
- * sph_adjoint_init allocates a tape of `slots` steps. sph_tape_record saves
- * the forward data of the step just taken by sph_step into a slot.
- * sph_adjoint_step maps the adjoints (lam_r, lam_u, lam_a_in) of a recorded
- * step's outputs r, u, dudt to those of its inputs (lam_r, lam_u updated in
- * place, lam_a_out). Adjoint arrays are (n, dim) float32 device arrays in the
- * original particle order; lam_a_in and lam_a_out must differ. */
+ * density summation, any transport-velocity factor, optionally the no-slip
+ * generalized wall BC (no external force then) with a velocity bc_fn, and no
+ * artificial viscosity. sph_adjoint_init allocates a tape of `slots` steps.
+ * sph_tape_record saves the forward data of the step just taken by sph_step
+ * into a slot. sph_adjoint_step maps, in place, the adjoints of a recorded
+ * step's outputs r, u, dudt, dvdt (lam_r, lam_u, lam_a, lam_b) to those of its
+ * inputs. Adjoint arrays are (n, dim) float32 device arrays in the original
+ * particle order. */
 int sph_adjoint_init(SphHandle* h, int32_t slots);
 int sph_tape_record(SphHandle* h, int32_t slot, void* stream);
-int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u,
-                     const float* lam_a_in, float* lam_a_out, void* stream);
+int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u, float* lam_a,
+                     float* lam_b, void* stream);
 /* A checkpoint segment in one call each way. sph_tape_segment runs `nsteps`
  * steps like sph_step from the loaded state, recording step t into slot t
  * (nsteps <= slots). sph_adjoint_segment then applies sph_adjoint_step to
- * slots nsteps-1 down to 0, alternating lam_a and lam_a_tmp as the in/out
- * pair; the result ends in lam_a. */
+ * slots nsteps-1 down to 0. */
 int sph_tape_segment(SphHandle* h, int32_t nsteps, void* stream);
 int sph_adjoint_segment(SphHandle* h, int32_t nsteps, float* lam_r, float* lam_u, float* lam_a,
-                        float* lam_a_tmp, void* stream);
+                        float* lam_b, void* stream);
 
 /* Read (and optionally clear) the device status word. Synchronizes `stream`.
  * sph_set_state clears the word. */

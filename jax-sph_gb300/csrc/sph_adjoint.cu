@@ -1,33 +1,35 @@
 // Hand-written reverse of one si_euler step for the differentiable form.
 //
 // Forward step (integrator.py:22-56, solver.py:705-949) on the path this
-// reverse covers -- standard SPH, density summation, tvf = 0, periodic box,
-// fluid only, no artificial viscosity:
-//   u' = u + dt a,  r' = mod(r + dt u', L)
-//   rho_k = m_k sum_l W(d_kl),  p_k = P(rho_k)
-//   a'_k  = sum_j K_kj h_kj B_kj,  K_kj = (m_k^2/rho_k^2 + m_j^2/rho_j^2)/m_k,
-//           h = W'(d)/(d+eps),  B_kj = -ps_kj x_kj + et_kj (u'_k - u'_j),
-//           ps = (rho_j p_k + rho_k p_j)/(rho_k + rho_j),
-//           et = 2 eta_k eta_j/(eta_k + eta_j + eps),  x_kj = r'_k - r'_j
-// (the transport-velocity stress vanishes with v = u and contributes no
-// derivative because v and u move together). With the neighbour list frozen
-// (integer indices carry no gradient, as in the reference's
-// jax.grad(..., allow_int=True)), given the adjoints la of a', lr of r' and
-// lu of u' the reverse is
-//   mu_k  = sum_j h [dKa B.la_k - K_kj D_k x.la_k - dKb B.la_j + K_jk D_k x.la_j]
-//   lr'_k = lr_k + sum_j [K_kj(-ps h la_k + h' (B.la_k) x/(d+eps))
-//                         + K_jk(ps h la_j - h' (B.la_j) x/(d+eps))
-//                         + h x (mu_k m_k + mu_j m_j)]
-//   lu'_k = lu_k + sum_j h et (K_kj la_k - K_jk la_j) + dt lr'_k
-//   outputs: lr = lr'_k, lu = lu'_k, la = dt lu'_k
-// with dKa = dK_kj/drho_k = -2 m_k/rho_k^3, dKb = dK_jk/drho_k =
-// -2 m_k^2/(rho_k^3 m_j), D_k = dps/drho_k = (rho_j P'(rho_k) + p_j - ps) /
-// (rho_k + rho_j). Pairs are used symmetrically; edges whose two directions
-// differ only at exact cutoff ties carry W = W' = W'' = 0 there.
-//
-// Each recorded step keeps the sorted order, positions, velocities, density,
-// pressure and neighbour list of its forward pass ("tape slot"); the adjoint
-// vectors live in the original particle order.
+// reverse covers -- standard SPH with density summation, transport velocity
+// (any tvf), optionally the generalized no-slip wall BC (solver.py:431-530)
+// without gravity, bc_fn zeroing / prescribing wall velocities, no artificial
+// viscosity; one case:
+//   u' = u + dt a,  v' = u' + cv b,  x' = mod(x + dt v', L)        (kick-drift)
+//   rho_k = m_k sum_l W(d_kl), p_k = P(rho_k)                       (fluid k)
+//   walls w: S_w = sum_{j fluid} W_wj, ut_w = sum W_wj u'_j / (S_w + eps),
+//            vt_w likewise, p_w = sum W_wj p_j / (S_w + eps),
+//            rho_w = P^-1(p_w), u_w = 2 u'_w - ut_w, v_w = 2 v'_w - vt_w
+//   a_k = sum_j T_kj B_kj,  b_k = sum_j T_kj pbg x_kj,  T_kj = K_kj h_kj,
+//     K_kj = (V_k^2 + V_j^2)/m_k, V = m/rho, h = W'(d)/(d+eps), x_kj = x_k - x_j,
+//     B_kj = -ps_kj x + 1/2 (rho_k u_k (w_k.x) + rho_j u_j (w_j.x)) + et_kj (u_k - u_j),
+//     w = v - u, ps = (rho_j p_k + rho_k p_j)/(rho_k + rho_j),
+//     et = 2 eta_k eta_j/(eta_k + eta_j + eps)
+//   bc_fn: walls' a = b = 0 and u, v prescribed.
+// With the neighbour list frozen (integer indices carry no gradient, as in
+// the reference's jax.grad(..., allow_int=True)), the adjoints (la, lb) of the
+// outputs a, b, (lr, lu) of x', u' map back in four passes over the recorded
+// step (sorted order of that step; adjoint vectors in the original order):
+//   A  per particle, over its pairs in both roles: the force's adjoints of
+//      the pair inputs x, u, v, rho, p (F1..F3);
+//   B  per wall: S_w, ut_w, vt_w and the wall pressure's adjoint
+//      lp_w + lrho_w / P'(rho_w) (rho_w = P^-1(p_w));
+//   C  per fluid particle: the Shepard sums of its wall neighbours passed on
+//      to its u, v, p; the density adjoint mu = lrho + P'(rho) lp;
+//   D  per particle: position adjoint (force, summation density with mu,
+//      wall Shepard weights), then the kick-drift backwards.
+// Pairs are used symmetrically; edges whose two directions differ only at
+// exact cutoff ties carry W = W' = W'' = 0 there.
 #include "sph_internal.cuh"
 
 namespace sph {
@@ -64,169 +66,350 @@ template <int DIM>
 __device__ __forceinline__ float3 ld3(const float* a, long long o) {
   return make_float3(a[o * DIM], a[o * DIM + 1], DIM == 3 ? a[o * DIM + 2] : 0.f);
 }
+template <int DIM>
+__device__ __forceinline__ void st3(float* a, long long o, const float3& v) {
+  a[o * DIM] = v.x;
+  a[o * DIM + 1] = v.y;
+  if (DIM == 3) a[o * DIM + 2] = v.z;
+}
 __device__ __forceinline__ float dot(const float3& a, const float3& b) {
   return a.x * b.x + a.y * b.y + a.z * b.z;
 }
+__device__ __forceinline__ float3 f3v(const float4& a) { return make_float3(a.x, a.y, a.z); }
+__device__ __forceinline__ float3 operator+(const float3& a, const float3& b) {
+  return make_float3(a.x + b.x, a.y + b.y, a.z + b.z);
+}
+__device__ __forceinline__ float3 operator-(const float3& a, const float3& b) {
+  return make_float3(a.x - b.x, a.y - b.y, a.z - b.z);
+}
+__device__ __forceinline__ float3 operator*(float s, const float3& a) {
+  return make_float3(s * a.x, s * a.y, s * a.z);
+}
+__device__ __forceinline__ void acc(float3& a, const float3& b) {
+  a.x += b.x;
+  a.y += b.y;
+  a.z += b.z;
+}
 
-// Pair quantities shared by the two passes.
-template <int DIM, int KER>
-struct Pair {
-  float3 x;     // r'_k - r'_j (minimum image)
-  float inv, h, hp, K_kj, K_jk, ps, et, Dk;
-  float3 B;     // B_kj
-  __device__ __forceinline__ void eval(const float4& rk, const float4& rj, float rho_k,
-                                       float rho_j, float p_k, float p_j, float eta_k,
-                                       float eta_j, const float3& uk, const float3& uj,
-                                       const CaseDev& c) {
-    float d2;
-    pair_dr<DIM>(rk, rj, c, x, d2);
-    const float d = d2 > 0.f ? sqrtf(d2) : 0.f;
-    inv = 1.f / (d + kEps);
-    const float gw = kdw<KER>(d, c);
-    h = gw * inv;
-    hp = kddw<KER>(d, c) * inv - gw * inv * inv;
-    const float mk = rk.w, mj = rj.w;
-    const float vk = mk / rho_k, vj = mj / rho_j;
-    K_kj = (vk * vk + vj * vj) / mk;
-    K_jk = (vk * vk + vj * vj) / mj;
-    ps = (rho_j * p_k + rho_k * p_j) / (rho_k + rho_j);
-    et = 2.f * eta_k * eta_j / (eta_k + eta_j + kEps);
-    Dk = (rho_j * eos_dp(rho_k, c) + p_j - ps) / (rho_k + rho_j);
-    B = make_float3(-ps * x.x + et * (uk.x - uj.x), -ps * x.y + et * (uk.y - uj.y),
-                    -ps * x.z + et * (uk.z - uj.z));
-  }
-};
-
+// The recorded forward data of one step.
 struct Tape {
   const int* orig;
-  const float4 *P4, *U4, *R4;
+  const float4 *P4, *U4, *V4, *R4;
+  const int* meta;
   const int *nbr, *cnt;
   int kmax;
 };
 
-// Pass 1: density adjoint mu_k (sorted order of the recorded step).
+// Per-step scratch of the reverse (sorted order of the recorded step).
+struct Scratch {
+  float4 *F1, *F2, *F3;  // force adjoints: (x, rho), (u, p), (v, -)
+  float4 *WB, *WU, *WV;  // walls: (S + eps, lp_w, -, -), ut, vt
+  float4 *GU, *GV;       // fluid: wall-borne u adjoint and mu, v adjoint
+};
+
+// One particle's quantities as the force pass used them.
+struct Part {
+  float3 x, u, v;
+  float m, rho, p, eta;
+  bool wall;
+};
+__device__ __forceinline__ Part load(const Tape& t, int k) {
+  const float4 P = t.P4[k], U = t.U4[k], V = t.V4[k], R = t.R4[k];
+  Part q;
+  q.x = f3v(P);
+  q.m = P.w;
+  q.u = f3v(U);
+  q.v = f3v(V);
+  q.rho = R.x;
+  q.p = R.y;
+  q.eta = R.w;
+  q.wall = is_wall(tag_of(t.meta[k]));
+  return q;
+}
+
+// Minimum-image x_k - x_j, its length, W, h = W'/(d+eps) and dh/dd.
+template <int DIM, int KER>
+struct Geo {
+  float3 x;
+  float d, w, h, hd;
+  __device__ __forceinline__ void eval(const float4& pk, const float4& pj, const CaseDev& c) {
+    float d2;
+    pair_dr<DIM>(pk, pj, c, x, d2);
+    d = d2 > 0.f ? sqrtf(d2) : 0.f;
+    const float inv = 1.f / (d + kEps);
+    const float gw = kdw<KER>(d, c);
+    w = kw<KER>(d, c);
+    h = gw * inv;
+    hd = kddw<KER>(d, c) * inv - gw * inv * inv;
+  }
+};
+
+// Pass A: the force's adjoints of every particle's pair inputs, from its
+// pairs as receiver (with its own la, lb) and as sender (with the
+// neighbour's).
 template <int DIM, int KER>
 __global__ void __launch_bounds__(kBlock)
-k_adj_mu(long long N, Tape t, const CaseDev* cases, const float* __restrict__ la, float* mu,
-         unsigned* status) {
-  long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+k_adj_force(long long N, Tape t, const CaseDev* cases, const float* __restrict__ la,
+            const float* __restrict__ lb, Scratch s, unsigned* status) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (k >= N) return;
   const CaseDev& c = cases[0];
-  const float4 rk = t.P4[k], Uk = t.U4[k], Rk = t.R4[k];
-  const float3 uk = make_float3(Uk.x, Uk.y, Uk.z);
-  const float rho_k = Rk.x, p_k = Rk.y, eta_k = Rk.w, mk = rk.w;
-  const float3 lak = ld3<DIM>(la, t.orig[k]);
-  const float dKa = -2.f * mk / (rho_k * rho_k * rho_k);
+  const Part K = load(t, (int)k);
+  const float4 pk = t.P4[k];
+  const float3 zero = make_float3(0.f, 0.f, 0.f);
+  const float3 lak = K.wall ? zero : ld3<DIM>(la, t.orig[k]);
+  const float3 lbk = K.wall ? zero : ld3<DIM>(lb, t.orig[k]);
+  const float Vk2 = (K.m / K.rho) * (K.m / K.rho);
+  const float3 wk = K.v - K.u;
+  const float pbg = c.p_bg_tvf;
+  float3 gx = zero, gu = zero, gv = zero;
+  float grho = 0.f, gp = 0.f;
   const int m = t.cnt[k];
   if (m > t.kmax) atomicOr(status, SPH_ERR_INVALID_ARG);
-  float acc = 0.f;
   for (int q = 0; q < m && q < t.kmax; ++q) {
     const int j = t.nbr[(long long)q * N + k];
-    const float4 rj = t.P4[j], Uj = t.U4[j], Rj = t.R4[j];
-    Pair<DIM, KER> P;
-    P.eval(rk, rj, rho_k, Rj.x, p_k, Rj.y, eta_k, Rj.w, uk, make_float3(Uj.x, Uj.y, Uj.z), c);
-    const float3 laj = ld3<DIM>(la, t.orig[j]);
-    const float dKb = -2.f * mk * mk / (rho_k * rho_k * rho_k * rj.w);
-    acc += P.h * (dKa * dot(P.B, lak) - P.K_kj * P.Dk * dot(P.x, lak) - dKb * dot(P.B, laj) +
-                  P.K_jk * P.Dk * dot(P.x, laj));
+    const Part J = load(t, j);
+    Geo<DIM, KER> G;
+    G.eval(pk, t.P4[j], c);
+    const float3 laj = J.wall ? zero : ld3<DIM>(la, t.orig[j]);
+    const float3 lbj = J.wall ? zero : ld3<DIM>(lb, t.orig[j]);
+    const float Vj2 = (J.m / J.rho) * (J.m / J.rho);
+    const float3 wj = J.v - J.u;
+    const float rs = K.rho + J.rho;
+    const float ps = (J.rho * K.p + K.rho * J.p) / rs;
+    const float et = 2.f * K.eta * J.eta / (K.eta + J.eta + kEps);
+    const float3 x = G.x;  // x_k - x_j
+    const float wkx = dot(wk, x), wjx = dot(wj, x);
+    // pair (k receives from j)
+    {
+      const float Kkj = (Vk2 + Vj2) / K.m;
+      const float T = Kkj * G.h;
+      const float3 B = (-ps) * x + (0.5f * K.rho * wkx) * K.u + (0.5f * J.rho * wjx) * J.u +
+                       et * (K.u - J.u);
+      const float sc = dot(lak, B) + pbg * dot(lbk, x);
+      grho += sc * G.h * (-2.f * Vk2 / (K.rho * K.m));
+      const float lau_k = dot(lak, K.u), lau_j = dot(lak, J.u);
+      acc(gx, (sc * Kkj * G.hd / (G.d + kEps)) * x);
+      acc(gx, T * (-ps) * lak + (T * 0.5f * K.rho * lau_k) * wk + (T * 0.5f * J.rho * lau_j) * wj +
+                  (T * pbg) * lbk);
+      const float lps = -T * dot(lak, x);
+      gp += lps * J.rho / rs;
+      grho += lps * (J.p - ps) / rs + T * 0.5f * lau_k * wkx;
+      acc(gu, (T * 0.5f * K.rho * wkx + T * et) * lak - (T * 0.5f * K.rho * lau_k) * x);
+      acc(gv, (T * 0.5f * K.rho * lau_k) * x);
+    }
+    // pair (j receives from k): x' = -x
+    {
+      const float Kjk = (Vj2 + Vk2) / J.m;
+      const float T = Kjk * G.h;
+      const float3 xp = (-1.f) * x;
+      const float wkxp = -wkx, wjxp = -wjx;
+      const float3 B = (-ps) * xp + (0.5f * J.rho * wjxp) * J.u + (0.5f * K.rho * wkxp) * K.u +
+                       et * (J.u - K.u);
+      const float sc = dot(laj, B) + pbg * dot(lbj, xp);
+      grho += sc * G.h * (-2.f * Vk2 / (K.rho * J.m));
+      const float lau_j = dot(laj, J.u), lau_k = dot(laj, K.u);
+      // d x'/d x_k = -I
+      acc(gx, (-sc * Kjk * G.hd / (G.d + kEps)) * xp);
+      acc(gx, (-T) * ((-ps) * laj + (0.5f * J.rho * lau_j) * wj + (0.5f * K.rho * lau_k) * wk +
+                      pbg * lbj));
+      const float lps = -T * dot(laj, xp);
+      gp += lps * J.rho / rs;
+      grho += lps * (J.p - ps) / rs + T * 0.5f * lau_k * wkxp;
+      acc(gu, (T * 0.5f * K.rho * wkxp - T * et) * laj - (T * 0.5f * K.rho * lau_k) * xp);
+      acc(gv, (T * 0.5f * K.rho * lau_k) * xp);
+    }
   }
-  mu[k] = acc;
+  s.F1[k] = make_float4(gx.x, gx.y, gx.z, grho);
+  s.F2[k] = make_float4(gu.x, gu.y, gu.z, gp);
+  s.F3[k] = make_float4(gv.x, gv.y, gv.z, 0.f);
 }
 
-// Pass 2: adjoints of r, u and a before the step (original order).
+// Pass B: the walls' Shepard sums and wall-pressure adjoint.
 template <int DIM, int KER>
 __global__ void __launch_bounds__(kBlock)
-k_adj_grad(long long N, Tape t, const CaseDev* cases, const float* __restrict__ la_in,
-           const float* __restrict__ mu, float* lr, float* lu, float* la_out) {
-  long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+k_adj_wall(long long N, Tape t, const CaseDev* cases, Scratch s) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (k >= N) return;
+  if (!is_wall(tag_of(t.meta[k]))) return;
   const CaseDev& c = cases[0];
-  const float4 rk = t.P4[k], Uk = t.U4[k], Rk = t.R4[k];
-  const float3 uk = make_float3(Uk.x, Uk.y, Uk.z);
-  const float rho_k = Rk.x, p_k = Rk.y, eta_k = Rk.w, mk = rk.w;
-  const long long ok = t.orig[k];
-  const float3 lak = ld3<DIM>(la_in, ok);
-  const float muk_mk = mu[k] * mk;
-  float3 gr = make_float3(0.f, 0.f, 0.f), gu = make_float3(0.f, 0.f, 0.f);
+  const float4 pk = t.P4[k];
+  float S = 0.f;
+  float3 su = make_float3(0.f, 0.f, 0.f), sv = su;
   const int m = t.cnt[k];
   for (int q = 0; q < m && q < t.kmax; ++q) {
     const int j = t.nbr[(long long)q * N + k];
-    const float4 rj = t.P4[j], Uj = t.U4[j], Rj = t.R4[j];
-    Pair<DIM, KER> P;
-    P.eval(rk, rj, rho_k, Rj.x, p_k, Rj.y, eta_k, Rj.w, uk, make_float3(Uj.x, Uj.y, Uj.z), c);
-    const float3 laj = ld3<DIM>(la_in, t.orig[j]);
-    const float bk = dot(P.B, lak), bj = dot(P.B, laj);
-    const float sx = P.hp * P.inv * (P.K_kj * bk - P.K_jk * bj) + P.h * (muk_mk + mu[j] * rj.w);
-    const float sl = P.ps * P.h;
-    gr.x += -P.K_kj * sl * lak.x + P.K_jk * sl * laj.x + sx * P.x.x;
-    gr.y += -P.K_kj * sl * lak.y + P.K_jk * sl * laj.y + sx * P.x.y;
-    gr.z += -P.K_kj * sl * lak.z + P.K_jk * sl * laj.z + sx * P.x.z;
-    const float he = P.h * P.et;
-    gu.x += he * (P.K_kj * lak.x - P.K_jk * laj.x);
-    gu.y += he * (P.K_kj * lak.y - P.K_jk * laj.y);
-    gu.z += he * (P.K_kj * lak.z - P.K_jk * laj.z);
+    if (tag_of(t.meta[j]) != FLUID) continue;
+    Geo<DIM, KER> G;
+    G.eval(pk, t.P4[j], c);
+    S += G.w;
+    acc(su, G.w * f3v(t.U4[j]));
+    acc(sv, G.w * f3v(t.V4[j]));
   }
-  const float3 lrk = ld3<DIM>(lr, ok), luk = ld3<DIM>(lu, ok);
-  const float3 r_tot = make_float3(lrk.x + gr.x, lrk.y + gr.y, lrk.z + gr.z);
-  const float3 u_tot = make_float3(luk.x + gu.x + c.dt * r_tot.x, luk.y + gu.y + c.dt * r_tot.y,
-                                   luk.z + gu.z + c.dt * r_tot.z);
-  lr[ok * DIM] = r_tot.x;
-  lr[ok * DIM + 1] = r_tot.y;
-  lu[ok * DIM] = u_tot.x;
-  lu[ok * DIM + 1] = u_tot.y;
-  la_out[ok * DIM] = c.dt * u_tot.x;
-  la_out[ok * DIM + 1] = c.dt * u_tot.y;
-  if (DIM == 3) {
-    lr[ok * DIM + 2] = r_tot.z;
-    lu[ok * DIM + 2] = u_tot.z;
-    la_out[ok * DIM + 2] = c.dt * u_tot.z;
-  }
+  const float den = S + kEps;
+  const float4 F1 = s.F1[k], F2 = s.F2[k];
+  const float lp = F2.w + F1.w / eos_dp(t.R4[k].x, c);  // rho_w = P^-1(p_w)
+  s.WB[k] = make_float4(den, lp, 0.f, 0.f);
+  s.WU[k] = make_float4(su.x / den, su.y / den, su.z / den, 0.f);
+  s.WV[k] = make_float4(sv.x / den, sv.y / den, sv.z / den, 0.f);
 }
 
+// Pass C: what the walls' Shepard sums pass on to each fluid particle's u,
+// v and p, and its density adjoint mu.
 template <int DIM, int KER>
-void adjoint_t(const LaunchCtx& L, const Tape& t, float* mu, const float* la_in, float* la_out,
-               float* lr, float* lu) {
-  const int g = (int)((L.N + kBlock - 1) / kBlock);
-  k_adj_mu<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, la_in, mu, L.status);
-  k_adj_grad<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, la_in, mu, lr, lu, la_out);
+__global__ void __launch_bounds__(kBlock)
+k_adj_mu(long long N, Tape t, const CaseDev* cases, Scratch s, int walls) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const float3 zero = make_float3(0.f, 0.f, 0.f);
+  if (is_wall(tag_of(t.meta[k]))) {
+    s.GU[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    s.GV[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const CaseDev& c = cases[0];
+  float3 gu = zero, gv = zero;
+  float gp = 0.f;
+  if (walls) {
+    const float4 pk = t.P4[k];
+    const int m = t.cnt[k];
+    for (int q = 0; q < m && q < t.kmax; ++q) {
+      const int j = t.nbr[(long long)q * N + k];
+      if (!is_wall(tag_of(t.meta[j]))) continue;
+      Geo<DIM, KER> G;
+      G.eval(t.P4[j], pk, c);
+      const float4 WB = s.WB[j];
+      const float cw = G.w / WB.x;
+      // u_w = 2 u'_w - ut_w: the adjoint of ut_w is minus that of u_w
+      acc(gu, (-cw) * f3v(s.F2[j]));
+      acc(gv, (-cw) * f3v(s.F3[j]));
+      gp += cw * WB.y;
+    }
+  }
+  const float4 F1 = s.F1[k], F2 = s.F2[k];
+  const float mu = F1.w + eos_dp(t.R4[k].x, c) * (F2.w + gp);
+  s.GU[k] = make_float4(gu.x, gu.y, gu.z, mu);
+  s.GV[k] = make_float4(gv.x, gv.y, gv.z, 0.f);
+}
+
+// Pass D: position adjoints and the kick-drift backwards (lr, lu in place;
+// la, lb of the step's inputs into la_out, lb_out).
+template <int DIM, int KER>
+__global__ void __launch_bounds__(kBlock)
+k_adj_grad(long long N, Tape t, const CaseDev* cases, Scratch s, float* lr, float* lu,
+           float* la_out, float* lb_out) {
+  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (k >= N) return;
+  const CaseDev& c = cases[0];
+  const float3 zero = make_float3(0.f, 0.f, 0.f);
+  const Part K = load(t, (int)k);
+  const float4 pk = t.P4[k];
+  const float mu_k = K.wall ? 0.f : s.GU[k].w;
+  float3 gx = f3v(s.F1[k]);
+  // the wall's own Shepard terms (k a wall): adjoints of ut, vt, p_w
+  float4 WBk = make_float4(1.f, 0.f, 0.f, 0.f);
+  float3 lut = zero, lvt = zero, ut = zero, vt = zero;
+  if (K.wall) {
+    WBk = s.WB[k];
+    lut = (-1.f) * f3v(s.F2[k]);
+    lvt = (-1.f) * f3v(s.F3[k]);
+    ut = f3v(s.WU[k]);
+    vt = f3v(s.WV[k]);
+  }
+  const int m = t.cnt[k];
+  for (int q = 0; q < m && q < t.kmax; ++q) {
+    const int j = t.nbr[(long long)q * N + k];
+    const Part J = load(t, j);
+    Geo<DIM, KER> G;
+    G.eval(pk, t.P4[j], c);
+    // summation density (fluid receivers), both directions
+    const float mu_j = J.wall ? 0.f : s.GU[j].w;
+    acc(gx, (G.h * (mu_k * K.m + mu_j * J.m)) * G.x);
+    if (K.wall && !J.wall) {
+      // dW_kj/dx_k = h x_kj, weight of j in the wall's Shepard sums
+      const float cs = (dot(lut, J.u - ut) + dot(lvt, J.v - vt) + WBk.y * (J.p - K.p)) / WBk.x;
+      acc(gx, (cs * G.h) * G.x);
+    } else if (!K.wall && J.wall) {
+      const float4 WB = s.WB[j];
+      const float3 lutj = (-1.f) * f3v(s.F2[j]), lvtj = (-1.f) * f3v(s.F3[j]);
+      const float cs = (dot(lutj, K.u - f3v(s.WU[j])) + dot(lvtj, K.v - f3v(s.WV[j])) +
+                        WB.y * (K.p - J.p)) /
+                       WB.x;
+      // the pair (j, k) seen from the wall: x_jk = -x_kj, and x_k enters with -I
+      acc(gx, (cs * G.h) * G.x);
+    }
+  }
+  const long long ok = t.orig[k];
+  const float3 lx = ld3<DIM>(lr, ok) + gx;
+  if (K.wall) {
+    // the walls' velocities and rates are prescribed by bc_fn
+    st3<DIM>(lr, ok, lx);
+    st3<DIM>(lu, ok, zero);
+    st3<DIM>(la_out, ok, zero);
+    st3<DIM>(lb_out, ok, zero);
+    return;
+  }
+  float3 lv = f3v(s.F3[k]) + f3v(s.GV[k]);
+  float3 lvel = ld3<DIM>(lu, ok) + f3v(s.F2[k]) + f3v(s.GU[k]);
+  lv = lv + c.dt * lx;       // x' = x + dt v'
+  lvel = lvel + lv;          // v' = u' + cv b
+  st3<DIM>(lr, ok, lx);
+  st3<DIM>(lu, ok, lvel);     // u' = u + dt a
+  st3<DIM>(la_out, ok, c.dt * lvel);
+  st3<DIM>(lb_out, ok, c.cv * lv);
 }
 
 // The tape slot of the step just taken, one thread per particle (the
 // neighbour list row by row, coalesced).
 __global__ void k_tape_record(long long N, Buffers b, const float4* R4, const int* nbr,
                               const int* cnt, int kmax, int* t_orig, float4* t_P4, float4* t_U4,
-                              float4* t_R4, int* t_nbr, int* t_cnt) {
+                              float4* t_V4, float4* t_R4, int* t_meta, int* t_nbr, int* t_cnt) {
   const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (k >= N) return;
   t_orig[k] = b.ORIG[k];
   t_P4[k] = b.P4[k];
   t_U4[k] = b.U4[k];
+  t_V4[k] = b.V4[k];
   t_R4[k] = R4[k];
+  t_meta[k] = b.META[k];
   const int m = cnt[k];
   t_cnt[k] = m;
   const int e = m < kmax ? m : kmax;
   for (int q = 0; q < e; ++q) t_nbr[(long long)q * N + k] = nbr[(long long)q * N + k];
 }
 
+template <int DIM, int KER>
+void adjoint_t(const LaunchCtx& L, const Tape& t, const Scratch& s, const float* la,
+               const float* lb, float* la_out, float* lb_out, float* lr, float* lu,
+               int walls) {
+  const int g = (int)((L.N + kBlock - 1) / kBlock);
+  k_adj_force<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, la, lb, s, L.status);
+  if (walls) k_adj_wall<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s);
+  k_adj_mu<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s, walls);
+  k_adj_grad<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s, lr, lu, la_out, lb_out);
+}
+
 }  // namespace
 
 void launch_tape_record(const LaunchCtx& L, Buffers b, const float4* R4, int* t_orig,
-                        float4* t_P4, float4* t_U4, float4* t_R4, int* t_nbr, int* t_cnt) {
+                        float4* t_P4, float4* t_U4, float4* t_V4, float4* t_R4, int* t_meta,
+                        int* t_nbr, int* t_cnt) {
   const int g = (int)((L.N + kBlock - 1) / kBlock);
   k_tape_record<<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.nbr, L.nbr_cnt, L.kmax, t_orig, t_P4,
-                                            t_U4, t_R4, t_nbr, t_cnt);
+                                            t_U4, t_V4, t_R4, t_meta, t_nbr, t_cnt);
 }
 
-void launch_adjoint(const LaunchCtx& L, const int* orig, const float4* P4, const float4* U4,
-                    const float4* R4, const int* nbr, const int* cnt, float* mu,
-                    const float* la_in, float* la_out, float* lr, float* lu) {
-  Tape t{orig, P4, U4, R4, nbr, cnt, L.kmax};
+void launch_adjoint(const LaunchCtx& L, const AdjTape& at, const AdjScratch& as, const float* la,
+                    const float* lb, float* la_out, float* lb_out, float* lr, float* lu,
+                    int walls) {
+  Tape t{at.orig, at.P4, at.U4, at.V4, at.R4, at.meta, at.nbr, at.cnt, L.kmax};
+  Scratch s{as.F1, as.F2, as.F3, as.WB, as.WU, as.WV, as.GU, as.GV};
   if (L.dim == 3) {
-    if (L.kernel == SPH_KERNEL_QSK) adjoint_t<3, 0>(L, t, mu, la_in, la_out, lr, lu);
-    else adjoint_t<3, 1>(L, t, mu, la_in, la_out, lr, lu);
+    if (L.kernel == SPH_KERNEL_QSK) adjoint_t<3, 0>(L, t, s, la, lb, la_out, lb_out, lr, lu, walls);
+    else adjoint_t<3, 1>(L, t, s, la, lb, la_out, lb_out, lr, lu, walls);
   } else {
-    if (L.kernel == SPH_KERNEL_QSK) adjoint_t<2, 0>(L, t, mu, la_in, la_out, lr, lu);
-    else adjoint_t<2, 1>(L, t, mu, la_in, la_out, lr, lu);
+    if (L.kernel == SPH_KERNEL_QSK) adjoint_t<2, 0>(L, t, s, la, lb, la_out, lb_out, lr, lu, walls);
+    else adjoint_t<2, 1>(L, t, s, la, lb, la_out, lb_out, lr, lu, walls);
   }
 }
 

@@ -90,10 +90,11 @@ struct SphHandle {
   // adjoint tape: per recorded step the sorted order, P4, U4, R4 and the
   // neighbour list of its forward pass
   int tape_slots = 0;
-  int* t_orig = nullptr;
-  float4 *t_P4 = nullptr, *t_U4 = nullptr, *t_R4 = nullptr;
+  int *t_orig = nullptr, *t_meta = nullptr;
+  float4 *t_P4 = nullptr, *t_U4 = nullptr, *t_V4 = nullptr, *t_R4 = nullptr;
   int *t_nbr = nullptr, *t_cnt = nullptr;
-  float* t_mu = nullptr;
+  float4* t_scr = nullptr;              // reverse scratch: 8 planes of N
+  float *t_la = nullptr, *t_lb = nullptr;  // the step inputs' dudt/dvdt adjoints
   std::vector<void*> allocs;
 
   template <typename T>
@@ -1320,20 +1321,26 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) try 
 int sph_adjoint_init(SphHandle* h, int32_t slots) try {
   if (!h || slots <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
   const SphConfig& c = h->cfg;
-  if (c.solver != SPH_SOLVER_SPH || c.is_rho_evol || c.is_bc_trick || c.is_heat_conduction ||
+  if (c.solver != SPH_SOLVER_SPH || c.is_rho_evol || c.is_heat_conduction || c.is_free_slip ||
       h->n_cases != 1)
     return fail((int)SPH_ERR_INVALID_ARG,
-                "the adjoint covers one case of the SPH solver with density summation and "
-                "no wall boundary condition");
+                "the adjoint covers one case of the SPH solver with density summation and, "
+                "optionally, the no-slip generalized wall BC");
   const CaseDev& cd = h->hc[0];
-  if (cd.cv != 0.0f || cd.av_alpha != 0.0f)
-    return fail((int)SPH_ERR_INVALID_ARG, "the adjoint needs tvf = 0 and no artificial viscosity");
+  if (cd.av_alpha != 0.0f)
+    return fail((int)SPH_ERR_INVALID_ARG, "the adjoint needs no artificial viscosity");
+  if (c.is_bc_trick && (cd.g_kind != SPH_GEXT_ZERO || cd.bc_kind == SPH_BC_SOLID_ZERO_P ||
+                        cd.bc_kind == SPH_BC_HT))
+    return fail((int)SPH_ERR_INVALID_ARG,
+                "the adjoint of the wall BC covers no external force and velocity-only bc_fn");
   if (h->tape_slots) return fail((int)SPH_ERR_INVALID_ARG, "adjoint tape already initialised");
   const long long N = h->N;
-  int rc = h->alloc(&h->t_orig, (size_t)slots * N) | h->alloc(&h->t_P4, (size_t)slots * N) |
-           h->alloc(&h->t_U4, (size_t)slots * N) | h->alloc(&h->t_R4, (size_t)slots * N) |
-           h->alloc(&h->t_nbr, (size_t)slots * h->kmax * N) |
-           h->alloc(&h->t_cnt, (size_t)slots * N) | h->alloc(&h->t_mu, N);
+  const size_t S = (size_t)slots * N;
+  int rc = h->alloc(&h->t_orig, S) | h->alloc(&h->t_meta, S) | h->alloc(&h->t_P4, S) |
+           h->alloc(&h->t_U4, S) | h->alloc(&h->t_V4, S) | h->alloc(&h->t_R4, S) |
+           h->alloc(&h->t_nbr, S * h->kmax) | h->alloc(&h->t_cnt, S) |
+           h->alloc(&h->t_scr, 8 * (size_t)N) | h->alloc(&h->t_la, 3 * (size_t)N) |
+           h->alloc(&h->t_lb, 3 * (size_t)N);
   if (rc) return rc;
   h->tape_slots = slots;
   return 0;
@@ -1355,24 +1362,13 @@ int sph_tape_segment(SphHandle* h, int32_t nsteps, void* stream) try {
 }
 
 int sph_adjoint_segment(SphHandle* h, int32_t nsteps, float* lam_r, float* lam_u, float* lam_a,
-                        float* lam_a_tmp, void* stream) try {
+                        float* lam_b, void* stream) try {
   if (!h || nsteps < 0 || nsteps > h->tape_slots)
     return fail((int)SPH_ERR_INVALID_ARG, "segment longer than the tape");
-  if (!lam_a || !lam_a_tmp || lam_a == lam_a_tmp)
-    return fail((int)SPH_ERR_INVALID_ARG, "adjoint arrays missing or aliased");
-  float* in = lam_a;
-  float* out = lam_a_tmp;
   for (int t = nsteps - 1; t >= 0; --t) {
-    int rc = sph_adjoint_step(h, t, lam_r, lam_u, in, out, stream);
+    int rc = sph_adjoint_step(h, t, lam_r, lam_u, lam_a, lam_b, stream);
     if (rc) return rc;
-    float* x = in;
-    in = out;
-    out = x;
   }
-  if (in != lam_a)
-    return cuda_check(cudaMemcpyAsync(lam_a, in, sizeof(float) * h->N * h->cfg.dim,
-                                      cudaMemcpyDeviceToDevice, (cudaStream_t)stream),
-                      "adjoint copy");
   return 0;
 } catch (...) {
   return host_error();
@@ -1386,24 +1382,33 @@ int sph_tape_record(SphHandle* h, int32_t slot, void* stream) try {
   const long long N = h->N;
   const Buffers& b = h->buf[0];
   launch_tape_record(h->ctx((cudaStream_t)stream), b, h->R4, h->t_orig + slot * N,
-                     h->t_P4 + slot * N, h->t_U4 + slot * N, h->t_R4 + slot * N,
+                     h->t_P4 + slot * N, h->t_U4 + slot * N, h->t_V4 + slot * N,
+                     h->t_R4 + slot * N, h->t_meta + slot * N,
                      h->t_nbr + (size_t)slot * h->kmax * N, h->t_cnt + slot * N);
   return launch_status("tape record");
 } catch (...) {
   return host_error();
 }
 
-int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u,
-                     const float* lam_a_in, float* lam_a_out, void* stream) try {
+int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u, float* lam_a,
+                     float* lam_b, void* stream) try {
   if (!h || slot < 0 || slot >= h->tape_slots)
     return fail((int)SPH_ERR_INVALID_ARG, "tape slot out of range");
-  if (!lam_r || !lam_u || !lam_a_in || !lam_a_out || lam_a_in == lam_a_out)
-    return fail((int)SPH_ERR_INVALID_ARG, "adjoint arrays missing or aliased");
+  if (!lam_r || !lam_u || !lam_a || !lam_b)
+    return fail((int)SPH_ERR_INVALID_ARG, "adjoint arrays missing");
   const long long N = h->N;
-  LaunchCtx L = h->ctx((cudaStream_t)stream);
-  launch_adjoint(L, h->t_orig + slot * N, h->t_P4 + slot * N, h->t_U4 + slot * N,
-                 h->t_R4 + slot * N, h->t_nbr + (size_t)slot * h->kmax * N,
-                 h->t_cnt + slot * N, h->t_mu, lam_a_in, lam_a_out, lam_r, lam_u);
+  cudaStream_t st = (cudaStream_t)stream;
+  LaunchCtx L = h->ctx(st);
+  AdjTape t{h->t_orig + slot * N, h->t_P4 + slot * N, h->t_U4 + slot * N,
+            h->t_V4 + slot * N,   h->t_R4 + slot * N, h->t_meta + slot * N,
+            h->t_nbr + (size_t)slot * h->kmax * N, h->t_cnt + slot * N};
+  float4* p = h->t_scr;
+  AdjScratch s{p, p + N, p + 2 * N, p + 3 * N, p + 4 * N, p + 5 * N, p + 6 * N, p + 7 * N};
+  launch_adjoint(L, t, s, lam_a, lam_b, h->t_la, h->t_lb, lam_r, lam_u, h->cfg.is_bc_trick);
+  const size_t bytes = sizeof(float) * (size_t)N * h->cfg.dim;
+  cudaError_t e = cudaMemcpyAsync(lam_a, h->t_la, bytes, cudaMemcpyDeviceToDevice, st);
+  if (e == cudaSuccess) e = cudaMemcpyAsync(lam_b, h->t_lb, bytes, cudaMemcpyDeviceToDevice, st);
+  if (e != cudaSuccess) return cuda_check(e, "adjoint copy");
   return launch_status("adjoint step");
 } catch (...) {
   return host_error();

@@ -772,13 +772,27 @@ void launch_renorm(const LaunchCtx& L, Buffers b, const float4* Rin, float4* Rou
 
 size_t scan_tmp_ints(long long n);
 
-// sph_adjoint.cu: copy the step just taken into a tape slot (one kernel).
+// sph_adjoint.cu: the recorded forward data of one step and the reverse's
+// per-step scratch (sorted order of that step).
+struct AdjTape {
+  const int* orig;
+  const float4 *P4, *U4, *V4, *R4;
+  const int* meta;
+  const int *nbr, *cnt;
+};
+struct AdjScratch {
+  float4 *F1, *F2, *F3, *WB, *WU, *WV, *GU, *GV;
+};
+// Copy the step just taken into a tape slot (one kernel).
 void launch_tape_record(const LaunchCtx& L, Buffers b, const float4* R4, int* t_orig,
-                        float4* t_P4, float4* t_U4, float4* t_R4, int* t_nbr, int* t_cnt);
-// sph_adjoint.cu: reverse of one recorded step (tape arrays of that step).
-void launch_adjoint(const LaunchCtx& L, const int* orig, const float4* P4, const float4* U4,
-                    const float4* R4, const int* nbr, const int* cnt, float* mu,
-                    const float* la_in, float* la_out, float* lr, float* lu);
+                        float4* t_P4, float4* t_U4, float4* t_V4, float4* t_R4, int* t_meta,
+                        int* t_nbr, int* t_cnt);
+// Reverse of one recorded step: lr, lu in place, la/lb (adjoints of the
+// step's dudt/dvdt outputs) to la_out/lb_out (those of its inputs). `walls`:
+// the generalized wall BC ran in the step.
+void launch_adjoint(const LaunchCtx& L, const AdjTape& t, const AdjScratch& s, const float* la,
+                    const float* lb, float* la_out, float* lb_out, float* lr, float* lu,
+                    int walls);
 
 // sph_capi.cu: per-case device constants from the ABI parameters; returns
 // non-zero and sets `err` on invalid input.

@@ -130,7 +130,7 @@ def load(build_if_missing=True):
     for name in EXPORTS:
         if name not in ("sph_abi_version", "sph_last_error"):
             getattr(lib, name).restype = I
-    if lib.sph_abi_version() != 6:
+    if lib.sph_abi_version() != 7:
         raise RuntimeError("libsph_gb300 ABI version mismatch")
     _LIB = lib
     return lib
@@ -305,20 +305,26 @@ class Engine:
         """Run ``nsteps`` steps, recording step t into tape slot t."""
         _check(self.lib.sph_tape_segment(self.h, int(nsteps), _stream()))
 
-    def adjoint_segment(self, nsteps, lam_r, lam_u, lam_a, lam_a_tmp):
-        """Reverse slots nsteps-1 .. 0; the dudt adjoint ends in ``lam_a``."""
+    def adjoint_segment(self, nsteps, lam_r, lam_u, lam_a, lam_b):
+        """Reverse slots nsteps-1 .. 0, all four adjoints in place."""
+        self._adjoint_arrays(lam_r, lam_u, lam_a, lam_b)
         _check(self.lib.sph_adjoint_segment(self.h, int(nsteps), _ptr(lam_r), _ptr(lam_u),
-                                            _ptr(lam_a), _ptr(lam_a_tmp), _stream()))
+                                            _ptr(lam_a), _ptr(lam_b), _stream()))
 
     def tape_record(self, slot):
         _check(self.lib.sph_tape_record(self.h, int(slot), _stream()))
 
-    def adjoint_step(self, slot, lam_r, lam_u, lam_a_in, lam_a_out):
-        for t in (lam_r, lam_u, lam_a_in, lam_a_out):
+    @staticmethod
+    def _adjoint_arrays(*ts):
+        for t in ts:
             if not (t.is_cuda and t.is_contiguous() and t.dtype == torch.float32):
                 raise ValueError("adjoint arrays must be contiguous float32 CUDA tensors")
+
+    def adjoint_step(self, slot, lam_r, lam_u, lam_a, lam_b):
+        """Reverse one recorded step, all four adjoints in place."""
+        self._adjoint_arrays(lam_r, lam_u, lam_a, lam_b)
         _check(self.lib.sph_adjoint_step(self.h, int(slot), _ptr(lam_r), _ptr(lam_u),
-                                         _ptr(lam_a_in), _ptr(lam_a_out), _stream()))
+                                         _ptr(lam_a), _ptr(lam_b), _stream()))
 
     def set_wall_layer(self, layer, offset, cutoff):
         """Recompute the wall normals every step from a static fine wall layer

@@ -21,15 +21,18 @@ from .simulate import Simulation
 
 
 class AdjointRollout:
-    """``steps`` si_euler steps of one case, differentiable w.r.t. the initial velocity.
+    """``steps`` si_euler steps of one case, differentiable w.r.t. the initial
+    positions and velocities.
 
-    The initial velocity enters as ``u = v = u0`` (the reference initialises
-    ``v`` with ``u``, case_setup.py:167-168) with ``dudt = 0``.
+    Covers the SPH solver with density summation, any transport-velocity
+    factor and, optionally, the no-slip generalized wall BC with a velocity
+    ``bc_fn`` (the reference's lid-driven cavity). ``forward(u0)`` starts from
+    the case's initial state with ``u = v = u0`` (the reference initialises
+    ``v`` with ``u``, case_setup.py:167-168) and ``dudt = dvdt = 0``; ``run``
+    starts from any state.
     """
 
     def __init__(self, setup, steps, checkpoint_every=10, device="cuda"):
-        if setup.tvf != 0.0:
-            raise NotImplementedError("the adjoint covers tvf = 0")
         self.setup = setup
         self.steps = int(steps)
         self.k = int(checkpoint_every)
@@ -55,9 +58,10 @@ class AdjointRollout:
         st["dvdt"] = torch.zeros_like(st["dvdt"])
         return st
 
-    def forward(self, u0):
-        """Run the rollout from initial velocity ``u0``; returns the final positions."""
-        self.sim.load([self._initial(u0)])
+    def run(self, state0):
+        """Run the rollout from ``state0`` (a state dict); returns the final
+        state (device tensors, original order), keeping the checkpoints."""
+        self.sim.load([state0])
         self.checkpoints = []
         done = 0
         while done < self.steps:
@@ -68,26 +72,35 @@ class AdjointRollout:
         code = self.engine.read_status(clear=True)
         if code & (_lib.ERR_NONFINITE | _lib.ERR_INVALID_ARG | _lib.ERR_CUDA):
             raise _lib.SphError(code, "rollout failed")
-        return self.sim.state()[0]["r"].clone()
+        return self.sim.state(split=False)
 
-    def backward(self, lam_r):
-        """Adjoints (d loss/d u0, d loss/d r0) for d loss/d r_T = ``lam_r``."""
+    def forward(self, u0):
+        """Run the rollout from initial velocity ``u0``; returns the final positions."""
+        return self.run(self._initial(u0))["r"].clone()
+
+    def backward(self, lam_r, lam_u=None):
+        """Adjoints of the initial state for those of the final positions
+        (``lam_r``) and velocities (``lam_u``): returns (d loss/d u0,
+        d loss/d r0); those of the initial dudt and dvdt are kept in
+        ``self.lam_dudt`` and ``self.lam_dvdt``."""
         shape = lam_r.shape
         lr = lam_r.detach().to(self.device, torch.float32).contiguous().clone()
-        lu = torch.zeros_like(lr)
-        la, tmp = torch.zeros_like(lr), torch.zeros_like(lr)
+        lu = (torch.zeros_like(lr) if lam_u is None else
+              lam_u.detach().to(self.device, torch.float32).contiguous().clone())
+        la, lb = torch.zeros_like(lr), torch.zeros_like(lr)
         for seg in reversed(range(len(self.checkpoints))):
             # recompute the segment from its checkpoint, recording its steps,
             # then sweep it backwards (one library call each)
             self.sim.restore(self.checkpoints[seg])
             n = min(self.k, self.steps - seg * self.k)
             self.engine.tape_segment(n)
-            self.engine.adjoint_segment(n, lr, lu, la, tmp)
+            self.engine.adjoint_segment(n, lr, lu, la, lb)
         code = self.engine.read_status(clear=True)
         if code & _lib.ERR_INVALID_ARG:
             raise _lib.SphError(code, "a particle has more neighbours than the adjoint tape holds")
-        # u0 enters the first step as u; v0 = u0 does not reach the dynamics
-        # when tvf = 0, and dudt starts at zero
+        self.lam_dudt, self.lam_dvdt = la.reshape(shape), lb.reshape(shape)
+        # u0 enters the first step as u; v0 does not reach the dynamics (the
+        # kick recomputes v from u and dvdt)
         return lu.reshape(shape), lr.reshape(shape)
 
 

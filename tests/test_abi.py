@@ -36,7 +36,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_abi_version_and_error_string(lib):
     lib.sph_abi_version.restype = ctypes.c_int
-    assert lib.sph_abi_version() == 6
+    assert lib.sph_abi_version() == 7
     lib.sph_last_error.restype = ctypes.c_char_p
     assert isinstance(lib.sph_last_error(), bytes)
 

@@ -109,3 +109,62 @@ def test_adjoint_checkpointing_is_exact(problem):
         (g,) = torch.autograd.grad(loss, u0)
         grads.append(g)
     assert torch.equal(grads[0], grads[1]) and torch.equal(grads[1], grads[2])
+
+
+# ---------------------------------------------------------------- the full step
+# The reference's own gradient check (notebooks/iclr24_grads.ipynb, cell 5):
+# d/dr0 of 0.5 * sum(u_T^2) after a few si_euler steps, here against torch
+# autograd through the float64 oracle rollout (frozen lists, like
+# jax.grad(..., allow_int=True)): the transport-velocity TGV and the
+# lid-driven cavity with the generalized wall BC and its moving lid.
+
+GRAD_STEPS = 5
+
+
+def _gpu_state_after(setup, steps):
+    """A float32 state a few steps in (lattice at rest is too symmetric)."""
+    from jaxsph_gb300 import simulate
+
+    sim = simulate.Simulation(setup)
+    sim.run(steps)
+    st = sim.state()[0]
+    full = {k: v for k, v in setup.state.items()}
+    full.update({k: st[k] for k in st})
+    return {k: v.detach().clone().cuda() for k, v in full.items()}
+
+
+def _oracle_grad(setup, state0):
+    """Loss 0.5 sum(u_T^2) and its gradient w.r.t. the initial positions."""
+    solver, fns, bc, st = oracle_case(setup, torch.float64, state=state0)
+    r0 = st["r"].clone().requires_grad_(True)
+    st = dict(st, r=r0)
+    nb = fns.allocate(r0.detach())
+    for _ in range(GRAD_STEPS):
+        st, nb = oracle.sph.si_euler_advance(setup.dt, setup.tvf, st, nb, fns, solver, bc)
+    loss = 0.5 * (st["u"] ** 2).sum()
+    (g,) = torch.autograd.grad(loss, r0)
+    return float(loss), g
+
+
+def _gpu_grad(setup, state0):
+    roll = adjoint.AdjointRollout(setup, GRAD_STEPS, checkpoint_every=GRAD_STEPS)
+    out = roll.run(state0)
+    u = out["u"]
+    loss = 0.5 * float((u.double() ** 2).sum())
+    _, lr0 = roll.backward(torch.zeros_like(out["r"]), u.clone())
+    return loss, lr0.double().cpu()
+
+
+@pytest.mark.parametrize("name", ["tgv2d_tvf", "ldc_walls"])
+def test_full_step_gradient_matches_float64_autograd(name):
+    if name == "tgv2d_tvf":
+        setup = cases.tgv(dim=2, dx=1.0 / 16, kernel="WC2K", tvf=1.0)
+    else:  # the notebook's cavity: N = 20, viscosity 0.1
+        setup = cases.lid_driven_cavity(dx=1.0 / 20, viscosity=0.1)
+    state0 = _gpu_state_after(setup, 10)
+    loss, g = _gpu_grad(setup, state0)
+    loss64, g64 = _oracle_grad(setup, {k: v.cpu() for k, v in state0.items()})
+    rel = ((g - g64).norm() / g64.norm()).item()
+    print(f"{name}: loss {loss:.6e} vs {loss64:.6e}, gradient rel L2 {rel:.2e}")
+    assert abs(loss - loss64) <= 1e-5 * abs(loss64)
+    assert rel <= 1e-4, rel
