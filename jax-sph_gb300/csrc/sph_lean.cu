@@ -360,7 +360,8 @@ __device__ __forceinline__ DensitySlow<DIM, KER, KAHAN, WIDE> density_slow(
 // included unless masked; fluid receivers), Tait / Riemann EOS, and the
 // step's neighbour list (staged in shared memory, written k-major) for the
 // force pass. Candidates are filtered four at a time: one list word, four
-// independent position gathers.
+// independent position gathers. R4 = (rho, p, V^2 = (m / rho)^2, eta): the
+// force pass takes the volumes from there.
 template <int DIM, int KER, bool KAHAN, bool WIDE>
 __global__ void __launch_bounds__(256, 4)
 k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_term,
@@ -435,7 +436,8 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
     const float rho_i = b.U4[i].w;
     const float rho_new = fluid ? ri.w * s0.s : rho_i;
     const float p_new = eos_p(rho_new, c);
-    R4[i] = make_float4(rho_new, p_new, b.A4[i].w, b.ETA[i]);
+    const float V = ri.w / rho_new;
+    R4[i] = make_float4(rho_new, p_new, V * V, b.ETA[i]);
     if (!isfinite(rho_new) || !isfinite(p_new)) atomicOr(status, SPH_ERR_NONFINITE);
   }
   count_edges1(cnt, valid, edgecnt, cp, status);
@@ -457,18 +459,18 @@ struct Acc6 {
 
 // One pair of the standard acceleration with the transport-velocity stress
 // (solver.py:216-256), the transport-velocity acceleration (:199-213) and the
-// artificial viscosity (:404-428).
-template <int DIM, int KER, bool KAHAN>
+// artificial viscosity (:404-428, decided at compile time). The volumes
+// squared, V^2 = (m / rho)^2, come from the density pass (R4.z).
+template <int DIM, int KER, bool KAHAN, bool AV>
 __device__ __forceinline__ void force_pair(const ForceI& I, const CaseDev& c, const int* meta,
-                                           int j, const float4& rj, const float4& Uj4,
-                                           const float4& Vj4, const float4& Rj,
-                                           const float3& dr, float d2, Acc6<KAHAN>& A) {
+                                             int j, const float4& rj, const float4& Uj4,
+                                             const float4& Vj4, const float4& Rj,
+                                             const float3& dr, float d2, Acc6<KAHAN>& A) {
   float dist, inv_d;
   dist_inv(d2, dist, inv_d);
   const float gw = kdw<KER>(dist, c);
-  const float rho_j = Rj.x, p_j = Rj.y, eta_j = Rj.w, m_j = rj.w;
-  const float Vj = __fdividef(m_j, rho_j);
-  const float cc = (I.Vi2 + Vj * Vj) * I.inv_mi * gw * inv_d;
+  const float rho_j = Rj.x, p_j = Rj.y, eta_j = Rj.w;
+  const float cc = (I.Vi2 + Rj.z) * I.inv_mi * gw * inv_d;
   const float3 uj = f3(Uj4);
   const float3 vj = f3(Vj4);
   const float eta_ij = __fdividef(2.f * I.eta_i * eta_j, I.eta_i + eta_j + kEps);
@@ -481,7 +483,8 @@ __device__ __forceinline__ void force_pair(const ForceI& I, const CaseDev& c, co
                                eta_ij * (I.ui.y - uj.y)),
                          cc * (-p_ij * dr.z + 0.5f * (I.Ai.z * ki + rho_j * uj.z * kj) +
                                eta_ij * (I.ui.z - uj.z)));
-  if (c.av_alpha != 0.0f && I.fluid && tag_of(meta[j]) == FLUID) {
+  if (AV && I.fluid && tag_of(meta[j]) == FLUID) {
+    const float m_j = rj.w;
     const float rho_ab = 0.5f * (I.rho_i + rho_j);
     const float num = m_j * c.av_alpha * c.av_hab * c.av_cab *
                       ((I.ui.x - uj.x) * dr.x + (I.ui.y - uj.y) * dr.y + (I.ui.z - uj.z) * dr.z);
@@ -501,31 +504,35 @@ __device__ __forceinline__ void force_pair(const ForceI& I, const CaseDev& c, co
 
 // The force sums of a receiver whose neighbours did not fit its list (the
 // case from its device copy).
-template <int DIM, int KER, bool KAHAN, bool WIDE>
+template <int DIM, int KER, bool KAHAN, bool WIDE, bool AV>
 __device__ __forceinline__ Acc6<KAHAN> force_slow(int N, int i, ForceI I, Acc6<KAHAN> A,
-                                               const CaseDev* cp, Buffers b, const float4* R4,
-                                               const typename Fmt<WIDE>::Word* vl,
-                                               const int* vcnt, int kv, const int* cellid,
-                                               const int* start, const float4* rref) {
+                                                 const CaseDev* cp, Buffers b,
+                                                 const float4* R4,
+                                                 const typename Fmt<WIDE>::Word* vl,
+                                                 const int* vcnt, int kv, const int* cellid,
+                                                 const int* start, const float4* rref) {
   const CaseDev& c = *cp;
   lean_slow<DIM, WIDE>(N, i, I.ri, c, cp, b.P4, vl, vcnt, kv, cellid, start, rref,
                        [&](int j, const float4& rj, const float3& dr, float d2) {
-                         force_pair<DIM, KER, KAHAN>(I, c, b.META, j, rj, __ldg(b.U4 + j),
-                                                     __ldg(b.V4 + j), __ldg(R4 + j), dr, d2, A);
+                         force_pair<DIM, KER, KAHAN, AV>(I, c, b.META, j, rj,
+                                                           __ldg(b.U4 + j), __ldg(b.V4 + j),
+                                                           __ldg(R4 + j), dr, d2, A);
                        });
   return A;
 }
 
-// The force pass over the density pass's neighbour list, with g_ext and
-// bc_fn; the next sender's four records are in flight while a pair is
-// evaluated, and the list word after the current one a group ahead.
-template <int DIM, int KER, bool KAHAN, bool WIDE>
+// The force pass over the density pass's neighbour list and its
+// R4 = (rho, p, V^2, eta), with g_ext and bc_fn; the next sender's four
+// records are in flight while a pair is evaluated, and the list word after
+// the current one a group ahead. drho/dt is the receiver's own (a summation
+// density carries it over).
+template <int DIM, int KER, bool KAHAN, bool WIDE, bool AV>
 __global__ void __launch_bounds__(256, 3)
 k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* g_arr,
-             const float4* __restrict__ R4, const typename Fmt<WIDE>::Word* __restrict__ nb,
-             const int* __restrict__ nbcnt, int kmax, const typename Fmt<WIDE>::Word* vl,
-             const int* vcnt, int kv, const int* cellid, const int* start, const float4* rref,
-             bool apply_bc, unsigned* status) {
+               const float4* __restrict__ R4, const typename Fmt<WIDE>::Word* __restrict__ nb,
+               const int* __restrict__ nbcnt, int kmax, const typename Fmt<WIDE>::Word* vl,
+               const int* vcnt, int kv, const int* cellid, const int* start, const float4* rref,
+               bool apply_bc, unsigned* status) {
   using L = Fmt<WIDE>;
   using Word = typename L::Word;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -537,11 +544,11 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
   I.ui = f3(b.U4[i]);
   const float3 vi = f3(b.V4[i]);
   const float4 Ri = R4[i];
+  const float drhodt = b.A4[i].w;
   I.rho_i = Ri.x;
   I.p_i = Ri.y;
   I.eta_i = Ri.w;
-  const float Vi = I.ri.w / I.rho_i;
-  I.Vi2 = Vi * Vi;
+  I.Vi2 = Ri.z;
   I.inv_mi = 1.0f / I.ri.w;
   I.Ai = make_float3(I.rho_i * I.ui.x, I.rho_i * I.ui.y, I.rho_i * I.ui.z);
   I.wi = make_float3(vi.x - I.ui.x, vi.y - I.ui.y, vi.z - I.ui.z);
@@ -549,9 +556,6 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
   Acc6<KAHAN> A;
   const int m = nbcnt[i];
   if (m <= kmax) {
-    // groups of four list slots (slot positions known at compile time); the
-    // next sender's records are loaded while a pair is evaluated, and the
-    // next group's word during the current group
     const Word* nbi = nb + i;
     const int ng = (m + 3) >> 2;
     Word wn = nbi[0];  // (read even without neighbours: never used then)
@@ -576,13 +580,13 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
           float3 dr;
           float d2;
           mi_dr<DIM>(I.ri, rc, c, dr, d2);
-          force_pair<DIM, KER, KAHAN>(I, c, b.META, jc, rc, uc, vc, Rc, dr, d2, A);
+          force_pair<DIM, KER, KAHAN, AV>(I, c, b.META, jc, rc, uc, vc, Rc, dr, d2, A);
         }
       }
     }
   } else {
-    A = force_slow<DIM, KER, KAHAN, WIDE>(N, i, I, A, cp, b, R4, vl, vcnt, kv, cellid, start,
-                                          rref);
+    A = force_slow<DIM, KER, KAHAN, WIDE, AV>(N, i, I, A, cp, b, R4, vl, vcnt, kv, cellid,
+                                                start, rref);
   }
   float3 dudt = make_float3(A.ax.s + gi.x, A.ay.s + gi.y, A.az.s + gi.z);
   float3 dvdt = make_float3(A.tx.s, A.ty.s, A.tz.s);
@@ -596,7 +600,7 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
   }
   if (!isfinite(dudt.x) || !isfinite(dudt.y) || !isfinite(dudt.z))
     atomicOr(status, SPH_ERR_NONFINITE);
-  b.A4[i] = make_float4(dudt.x, dudt.y, dudt.z, Ri.z);
+  b.A4[i] = make_float4(dudt.x, dudt.y, dudt.z, drhodt);
   b.A2[i] = make_float4(dvdt.x, dvdt.y, dvdt.z, 0.f);
 }
 
@@ -620,9 +624,14 @@ void forward_lean_t(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid
     mark(L, 3);
   }
   if (phases & 2) {
-    k_force_lean<DIM, KER, KAHAN, WIDE><<<g, bt, 0, L.stream>>>(
-        N, b, L.c1, L.cases, g_arr, R4, nb, L.nbr_cnt, L.kmax, vl, L.vcnt, L.kv, cellid, start,
-        L.rref, apply_bc, L.status);
+    if (L.c1.av_alpha != 0.0f)
+      k_force_lean<DIM, KER, KAHAN, WIDE, true><<<g, bt, 0, L.stream>>>(
+          N, b, L.c1, L.cases, g_arr, R4, nb, L.nbr_cnt, L.kmax, vl, L.vcnt, L.kv, cellid,
+          start, L.rref, apply_bc, L.status);
+    else
+      k_force_lean<DIM, KER, KAHAN, WIDE, false><<<g, bt, 0, L.stream>>>(
+          N, b, L.c1, L.cases, g_arr, R4, nb, L.nbr_cnt, L.kmax, vl, L.vcnt, L.kv, cellid,
+          start, L.rref, apply_bc, L.status);
     count_launch(L);
     mark(L, 4);
   }
