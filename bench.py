@@ -428,7 +428,7 @@ def adjoint_form(device, steps=100, checkpoint_every=10, fp64=True):
     a = cases.tgv_perturbed(n_side=128, seed=1)
     b = cases.tgv_perturbed(n_side=128, seed=2)
     target = adjoint.AdjointRollout(b, steps, checkpoint_every).forward(b.state["u"].to(device))
-    roll = adjoint.AdjointRollout(a, steps, checkpoint_every, device=device)
+    roll = adjoint.AdjointRollout(a, steps, checkpoint_every, device=device, autotune=True)
     u0 = a.state["u"].to(device)
 
     def gradient():
@@ -454,7 +454,7 @@ def adjoint_form(device, steps=100, checkpoint_every=10, fp64=True):
                "loss_rel": abs(float(loss) - loss64) / abs(loss64),
                "against": "torch autograd through the float64 oracle rollout "
                           "(neighbour lists frozen per step)"}
-    plain = simulate.Simulation(a, device=device)
+    plain = simulate.Simulation(a, device=device, autotune=True)
     plain.run(3)
     torch.cuda.synchronize()
     t0 = time.perf_counter()
@@ -466,7 +466,8 @@ def adjoint_form(device, steps=100, checkpoint_every=10, fp64=True):
                         f"gradient of the final-position MSE w.r.t. the initial velocity",
             "value": a.n * steps / t_grad, "unit": UNIT,
             "note": "forward (with checkpoints) + reverse sweep, wall clock",
-            "checkpoint_every": checkpoint_every, "loss": float(loss.detach()),
+            "checkpoint_every": checkpoint_every, "block_size": roll.sim.block_size,
+            "plain_block_size": plain.block_size, "loss": float(loss.detach()),
             "grad_norm": float(g.norm()), "timed_gradients": reps,
             "plain_forward_value": a.n * steps / t_plain,
             "ratio_vs_plain_forward": t_plain / t_grad, "error_vs_fp64": err}
@@ -531,8 +532,7 @@ def gpu_arm(args, ws, rank, local):
     ncu = KERNELS[dom]["ncu"] or {}
     step_ms_mean = total_ms / args.steps
     step_achieved = STEP_BYTES * n / (step_ms_mean * 1e-3) / 1e9
-    cfg = workload_config(args, n, ws)
-    cfg["candidate_rebuilds"] = rebuilds
+    cfg = workload_config(args, n, ws)  # identical to the reference arm's
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": args.steps,
         "warmup": max(args.warmup, 3), "ms_per_step": step_ms_mean, "higher_is_better": True,
@@ -553,6 +553,7 @@ def gpu_arm(args, ws, rank, local):
                      "step": {"alg_bytes_per_particle": STEP_BYTES, "achieved": step_achieved,
                               "frac": step_achieved / hbm}},
         "kernels": table,
+        "candidate_rebuilds": rebuilds,
         "status": status_report(status),
         "gpu_launches": launches,
         "clocks": clocks.summary(),
@@ -567,10 +568,14 @@ def gpu_arm(args, ws, rank, local):
                        "d2h_bytes_per_step": d2h, "steps_redone_on_overflow": redone,
                        "path": "si_euler drop-in advance on a pinned host state: each step "
                                "reads its inputs from and writes its result to host memory"}
-    if rank == 0 and not args.no_forms:
-        line["forms"] = {"batched": batched_form(device, args.batched_steps,
-                                                 fp64=not args.no_cpu),
-                         "adjoint": adjoint_form(device, fp64=not args.no_cpu)}
+    forms = [] if args.no_forms else [f for f in args.forms.split(",") if f]
+    if rank == 0 and forms:
+        line["forms"] = {}
+        if "batched" in forms:
+            line["forms"]["batched"] = batched_form(device, args.batched_steps,
+                                                    fp64=not args.no_cpu)
+        if "adjoint" in forms:
+            line["forms"]["adjoint"] = adjoint_form(device, fp64=not args.no_cpu)
     if rank == 0 and ws == 1 and not args.no_cpu:
         # a bounded sample: steps of the full case until ~10 s of CPU work
         rate, steps, secs, n_cpu, warm = cpu_oracle_rate(64, 40, 10.0, threads, warmup=3,
@@ -593,6 +598,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--no-forms", action="store_true",
                     help="skip the batched/adjoint form measurements on their own workloads")
+    ap.add_argument("--forms", default="batched,adjoint",
+                    help="comma-separated forms to measure on their own workloads")
     ap.add_argument("--skin", type=float, default=0.1,
                     help="Verlet skin as a fraction of the cutoff (0: rebuild every step)")
     ap.add_argument("--batched-steps", type=int, default=1000,

@@ -378,15 +378,29 @@ __global__ void k_tape_record(long long N, Buffers b, const float4* R4, const in
   for (int q = 0; q < e; ++q) t_nbr[(long long)q * N + k] = nbr[(long long)q * N + k];
 }
 
+// Threads per block of the reverse passes: small cases (the differentiable
+// form's 16,384 particles) in blocks small enough to reach every SM.
+inline int adj_block(long long n) {
+  int sms = 0, dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    sms = 0;
+  if (sms <= 0) return kBlock;
+  for (int bt = 64; bt < kBlock; bt *= 2)
+    if ((n + bt - 1) / bt <= 2LL * sms) return bt;
+  return kBlock;
+}
+
 template <int DIM, int KER>
 void adjoint_t(const LaunchCtx& L, const Tape& t, const Scratch& s, const float* la,
                const float* lb, float* la_out, float* lb_out, float* lr, float* lu,
                int walls) {
-  const int g = (int)((L.N + kBlock - 1) / kBlock);
-  k_adj_force<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, la, lb, s, L.status);
-  if (walls) k_adj_wall<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s);
-  k_adj_mu<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s, walls);
-  k_adj_grad<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s, lr, lu, la_out, lb_out);
+  const int bt = adj_block(L.N);
+  const int g = (int)((L.N + bt - 1) / bt);
+  k_adj_force<DIM, KER><<<g, bt, 0, L.stream>>>(L.N, t, L.cases, la, lb, s, L.status);
+  if (walls) k_adj_wall<DIM, KER><<<g, bt, 0, L.stream>>>(L.N, t, L.cases, s);
+  k_adj_mu<DIM, KER><<<g, bt, 0, L.stream>>>(L.N, t, L.cases, s, walls);
+  k_adj_grad<DIM, KER><<<g, bt, 0, L.stream>>>(L.N, t, L.cases, s, lr, lu, la_out, lb_out);
 }
 
 }  // namespace

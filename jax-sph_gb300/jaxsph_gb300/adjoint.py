@@ -32,14 +32,14 @@ class AdjointRollout:
     starts from any state.
     """
 
-    def __init__(self, setup, steps, checkpoint_every=10, device="cuda"):
+    def __init__(self, setup, steps, checkpoint_every=10, device="cuda", autotune=False):
         self.setup = setup
         self.steps = int(steps)
         self.k = int(checkpoint_every)
         # canonical order: a segment recomputed from its checkpoint (which
         # rebuilds the candidate lists at other steps) equals the forward
-        # rollout bit for bit
-        self.sim = Simulation(setup, device=device, canonical_order=True)
+        # rollout bit for bit; the block size changes no result
+        self.sim = Simulation(setup, device=device, canonical_order=True, autotune=autotune)
         self.engine = self.sim.engine
         self.engine.adjoint_init(self.k)
         self.device = torch.device(device)
