@@ -55,9 +55,9 @@ KERNELS = {
     "rebuild": {"kernel": "k_hash_count + scan + k_scatter + k_permute + k_verlet_lean "
                           "(every few steps, per-step average)", "alg_bytes": None, "ncu": None},
     "density": {"kernel": "k_density_lean", "alg_bytes": DENSITY_BYTES,
-                "ncu": {"dram_bytes": 134.7, "fma_pipe": 0.238, "issue_active": 0.587}},
+                "ncu": {"dram_bytes": 118.6, "fma_pipe": 0.238, "issue_active": 0.595}},
     "force": {"kernel": "k_force_lean", "alg_bytes": FORCE_BYTES,
-              "ncu": {"dram_bytes": 133.2, "fma_pipe": 0.429, "issue_active": 0.713}},
+              "ncu": {"dram_bytes": 149.2, "fma_pipe": 0.452, "issue_active": 0.703}},
 }
 # Status bits of the device status word (include/sph_gb300.h), for the line.
 STATUS_BITS = {0x1: "NEIGHBOR_LIST_OVERFLOW", 0x2: "CELL_LIST_OVERFLOW",
@@ -418,6 +418,11 @@ def oracle_gradient(setup, u0, target, steps):
     return float(loss), g
 
 
+def _min_image(d, box):
+    side = torch.as_tensor(box, dtype=d.dtype, device=d.device)
+    return d - side * torch.round(d / side)
+
+
 def adjoint_form(device, steps=100, checkpoint_every=10, fp64=True):
     """The differentiable form on its own workload: gradient of the final
     positions' mean squared distance to a target rollout (another seed) with
@@ -447,6 +452,21 @@ def adjoint_form(device, steps=100, checkpoint_every=10, fp64=True):
         loss, g = gradient()
     torch.cuda.synchronize()
     t_grad = (time.perf_counter() - t0) / reps
+    # where a gradient's time goes (CUDA events on the current stream): the
+    # forward rollout with its checkpoints, the recomputation of every
+    # segment with its tape, and the reverse sweeps
+    f0, f1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    f0.record()
+    r_final = roll.forward(u0)
+    f1.record()
+    segs = []
+    # d/dr of the mean squared minimum-image distance
+    lam_r = 2.0 * _min_image(r_final - target, a.box) / a.n
+    roll.backward(lam_r, timer=segs)
+    torch.cuda.synchronize()
+    phases = {"forward_rollout_ms": f0.elapsed_time(f1),
+              "recompute_with_tape_ms": sum(e[0].elapsed_time(e[1]) for e in segs),
+              "reverse_sweep_ms": sum(e[1].elapsed_time(e[2]) for e in segs)}
     err = None
     if fp64:
         loss64, g64 = oracle_gradient(a, u0, target, steps)
@@ -469,6 +489,7 @@ def adjoint_form(device, steps=100, checkpoint_every=10, fp64=True):
             "checkpoint_every": checkpoint_every, "block_size": roll.sim.block_size,
             "plain_block_size": plain.block_size, "loss": float(loss.detach()),
             "grad_norm": float(g.norm()), "timed_gradients": reps,
+            "phases": dict(phases, plain_rollout_ms=1e3 * t_plain),
             "plain_forward_value": a.n * steps / t_plain,
             "ratio_vs_plain_forward": t_plain / t_grad, "error_vs_fp64": err}
 

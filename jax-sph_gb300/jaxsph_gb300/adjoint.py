@@ -78,11 +78,13 @@ class AdjointRollout:
         """Run the rollout from initial velocity ``u0``; returns the final positions."""
         return self.run(self._initial(u0))["r"].clone()
 
-    def backward(self, lam_r, lam_u=None):
+    def backward(self, lam_r, lam_u=None, timer=None):
         """Adjoints of the initial state for those of the final positions
         (``lam_r``) and velocities (``lam_u``): returns (d loss/d u0,
         d loss/d r0); those of the initial dudt and dvdt are kept in
-        ``self.lam_dudt`` and ``self.lam_dvdt``."""
+        ``self.lam_dudt`` and ``self.lam_dvdt``. ``timer``: a list that gets,
+        per checkpoint segment, three CUDA events recorded before the
+        recomputation, between it and the reverse sweep, and after the sweep."""
         shape = lam_r.shape
         lr = lam_r.detach().to(self.device, torch.float32).contiguous().clone()
         lu = (torch.zeros_like(lr) if lam_u is None else
@@ -93,8 +95,16 @@ class AdjointRollout:
             # then sweep it backwards (one library call each)
             self.sim.restore(self.checkpoints[seg])
             n = min(self.k, self.steps - seg * self.k)
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)] if timer is not None else None
+            if ev:
+                ev[0].record()
             self.engine.tape_segment(n)
+            if ev:
+                ev[1].record()
             self.engine.adjoint_segment(n, lr, lu, la, lb)
+            if ev:
+                ev[2].record()
+                timer.append(ev)
         code = self.engine.read_status(clear=True)
         if code & _lib.ERR_INVALID_ARG:
             raise _lib.SphError(code, "a particle has more neighbours than the adjoint tape holds")
