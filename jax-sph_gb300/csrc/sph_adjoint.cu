@@ -91,6 +91,19 @@ __device__ __forceinline__ void acc(float3& a, const float3& b) {
   a.z += b.z;
 }
 
+// Lanes per particle of the reverse passes: S consecutive lanes of a warp
+// share one particle, each summing every S-th of its pairs; the S partial
+// sums are then added by a butterfly of shuffles (a fixed order: the result
+// is the same on every run). Every lane of a warp takes part in the
+// shuffles, so no lane leaves early.
+__device__ __forceinline__ float group_sum(float v, int S) {
+  for (int o = S >> 1; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ float3 group_sum(float3 v, int S) {
+  return make_float3(group_sum(v.x, S), group_sum(v.y, S), group_sum(v.z, S));
+}
+
 // The recorded forward data of one step.
 struct Tape {
   const int* orig;
@@ -150,9 +163,12 @@ struct Geo {
 template <int DIM, int KER>
 __global__ void __launch_bounds__(kBlock)
 k_adj_force(long long N, Tape t, const CaseDev* cases, const float* __restrict__ la,
-            const float* __restrict__ lb, Scratch s, unsigned* status) {
-  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (k >= N) return;
+            const float* __restrict__ lb, Scratch s, unsigned* status, int S) {
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long k0 = gt / S;
+  const int sub = (int)(gt % S);
+  const bool valid = k0 < N;
+  const long long k = valid ? k0 : N - 1;  // idle lanes shadow the last particle
   const CaseDev& c = cases[0];
   const Part K = load(t, (int)k);
   const float4 pk = t.P4[k];
@@ -165,8 +181,9 @@ k_adj_force(long long N, Tape t, const CaseDev* cases, const float* __restrict__
   float3 gx = zero, gu = zero, gv = zero;
   float grho = 0.f, gp = 0.f;
   const int m = t.cnt[k];
-  if (m > t.kmax) atomicOr(status, SPH_ERR_INVALID_ARG);
-  for (int q = 0; q < m && q < t.kmax; ++q) {
+  if (valid && sub == 0 && m > t.kmax) atomicOr(status, SPH_ERR_INVALID_ARG);
+  const int mq = valid ? (m < t.kmax ? m : t.kmax) : 0;
+  for (int q = sub; q < mq; q += S) {
     const int j = t.nbr[(long long)q * N + k];
     const Part J = load(t, j);
     Geo<DIM, KER> G;
@@ -220,6 +237,12 @@ k_adj_force(long long N, Tape t, const CaseDev* cases, const float* __restrict__
       acc(gv, (T * 0.5f * K.rho * lau_k) * xp);
     }
   }
+  gx = group_sum(gx, S);
+  gu = group_sum(gu, S);
+  gv = group_sum(gv, S);
+  grho = group_sum(grho, S);
+  gp = group_sum(gp, S);
+  if (!valid || sub != 0) return;
   s.F1[k] = make_float4(gx.x, gx.y, gx.z, grho);
   s.F2[k] = make_float4(gu.x, gu.y, gu.z, gp);
   s.F3[k] = make_float4(gv.x, gv.y, gv.z, 0.f);
@@ -228,25 +251,32 @@ k_adj_force(long long N, Tape t, const CaseDev* cases, const float* __restrict__
 // Pass B: the walls' Shepard sums and wall-pressure adjoint.
 template <int DIM, int KER>
 __global__ void __launch_bounds__(kBlock)
-k_adj_wall(long long N, Tape t, const CaseDev* cases, Scratch s) {
-  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (k >= N) return;
-  if (!is_wall(tag_of(t.meta[k]))) return;
+k_adj_wall(long long N, Tape t, const CaseDev* cases, Scratch s, int S) {
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long k0 = gt / S;
+  const int sub = (int)(gt % S);
+  const long long k = k0 < N ? k0 : N - 1;
+  const bool valid = k0 < N && is_wall(tag_of(t.meta[k]));  // uniform over the S lanes
   const CaseDev& c = cases[0];
   const float4 pk = t.P4[k];
-  float S = 0.f;
+  float Sw = 0.f;
   float3 su = make_float3(0.f, 0.f, 0.f), sv = su;
   const int m = t.cnt[k];
-  for (int q = 0; q < m && q < t.kmax; ++q) {
+  const int mq = valid ? (m < t.kmax ? m : t.kmax) : 0;
+  for (int q = sub; q < mq; q += S) {
     const int j = t.nbr[(long long)q * N + k];
     if (tag_of(t.meta[j]) != FLUID) continue;
     Geo<DIM, KER> G;
     G.eval(pk, t.P4[j], c);
-    S += G.w;
+    Sw += G.w;
     acc(su, G.w * f3v(t.U4[j]));
     acc(sv, G.w * f3v(t.V4[j]));
   }
-  const float den = S + kEps;
+  Sw = group_sum(Sw, S);
+  su = group_sum(su, S);
+  sv = group_sum(sv, S);
+  if (!valid || sub != 0) return;
+  const float den = Sw + kEps;
   const float4 F1 = s.F1[k], F2 = s.F2[k];
   const float lp = F2.w + F1.w / eos_dp(t.R4[k].x, c);  // rho_w = P^-1(p_w)
   s.WB[k] = make_float4(den, lp, 0.f, 0.f);
@@ -258,22 +288,22 @@ k_adj_wall(long long N, Tape t, const CaseDev* cases, Scratch s) {
 // v and p, and its density adjoint mu.
 template <int DIM, int KER>
 __global__ void __launch_bounds__(kBlock)
-k_adj_mu(long long N, Tape t, const CaseDev* cases, Scratch s, int walls) {
-  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (k >= N) return;
+k_adj_mu(long long N, Tape t, const CaseDev* cases, Scratch s, int walls, int S) {
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long k0 = gt / S;
+  const int sub = (int)(gt % S);
+  const long long k = k0 < N ? k0 : N - 1;
+  const bool valid = k0 < N;
   const float3 zero = make_float3(0.f, 0.f, 0.f);
-  if (is_wall(tag_of(t.meta[k]))) {
-    s.GU[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    s.GV[k] = make_float4(0.f, 0.f, 0.f, 0.f);
-    return;
-  }
+  const bool wall = is_wall(tag_of(t.meta[k]));  // uniform over the S lanes
   const CaseDev& c = cases[0];
   float3 gu = zero, gv = zero;
   float gp = 0.f;
   if (walls) {
     const float4 pk = t.P4[k];
     const int m = t.cnt[k];
-    for (int q = 0; q < m && q < t.kmax; ++q) {
+    const int mq = (valid && !wall) ? (m < t.kmax ? m : t.kmax) : 0;
+    for (int q = sub; q < mq; q += S) {
       const int j = t.nbr[(long long)q * N + k];
       if (!is_wall(tag_of(t.meta[j]))) continue;
       Geo<DIM, KER> G;
@@ -285,6 +315,15 @@ k_adj_mu(long long N, Tape t, const CaseDev* cases, Scratch s, int walls) {
       acc(gv, (-cw) * f3v(s.F3[j]));
       gp += cw * WB.y;
     }
+    gu = group_sum(gu, S);
+    gv = group_sum(gv, S);
+    gp = group_sum(gp, S);
+  }
+  if (!valid || sub != 0) return;
+  if (wall) {
+    s.GU[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    s.GV[k] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
   }
   const float4 F1 = s.F1[k], F2 = s.F2[k];
   const float mu = F1.w + eos_dp(t.R4[k].x, c) * (F2.w + gp);
@@ -297,15 +336,18 @@ k_adj_mu(long long N, Tape t, const CaseDev* cases, Scratch s, int walls) {
 template <int DIM, int KER>
 __global__ void __launch_bounds__(kBlock)
 k_adj_grad(long long N, Tape t, const CaseDev* cases, Scratch s, float* lr, float* lu,
-           float* la_out, float* lb_out) {
-  const long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (k >= N) return;
+           float* la_out, float* lb_out, int S) {
+  const long long gt = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const long long k0 = gt / S;
+  const int sub = (int)(gt % S);
+  const bool valid = k0 < N;
+  const long long k = valid ? k0 : N - 1;
   const CaseDev& c = cases[0];
   const float3 zero = make_float3(0.f, 0.f, 0.f);
   const Part K = load(t, (int)k);
   const float4 pk = t.P4[k];
   const float mu_k = K.wall ? 0.f : s.GU[k].w;
-  float3 gx = f3v(s.F1[k]);
+  float3 gx = zero;
   // the wall's own Shepard terms (k a wall): adjoints of ut, vt, p_w
   float4 WBk = make_float4(1.f, 0.f, 0.f, 0.f);
   float3 lut = zero, lvt = zero, ut = zero, vt = zero;
@@ -317,7 +359,8 @@ k_adj_grad(long long N, Tape t, const CaseDev* cases, Scratch s, float* lr, floa
     vt = f3v(s.WV[k]);
   }
   const int m = t.cnt[k];
-  for (int q = 0; q < m && q < t.kmax; ++q) {
+  const int mq = valid ? (m < t.kmax ? m : t.kmax) : 0;
+  for (int q = sub; q < mq; q += S) {
     const int j = t.nbr[(long long)q * N + k];
     const Part J = load(t, j);
     Geo<DIM, KER> G;
@@ -339,6 +382,8 @@ k_adj_grad(long long N, Tape t, const CaseDev* cases, Scratch s, float* lr, floa
       acc(gx, (cs * G.h) * G.x);
     }
   }
+  gx = group_sum(gx, S) + f3v(s.F1[k]);
+  if (!valid || sub != 0) return;
   const long long ok = t.orig[k];
   const float3 lx = ld3<DIM>(lr, ok) + gx;
   if (K.wall) {
@@ -378,29 +423,32 @@ __global__ void k_tape_record(long long N, Buffers b, const float4* R4, const in
   for (int q = 0; q < e; ++q) t_nbr[(long long)q * N + k] = nbr[(long long)q * N + k];
 }
 
-// Threads per block of the reverse passes: small cases (the differentiable
-// form's 16,384 particles) in blocks small enough to reach every SM.
-inline int adj_block(long long n) {
+// Lanes per particle of the reverse passes (1, 2, 4 or 8): as many as keep
+// about two full waves of 256-thread blocks on the device, so that a small
+// case (the differentiable form's 16,384 particles) still fills every SM.
+inline int adj_lanes(long long n) {
   int sms = 0, dev = 0;
   if (cudaGetDevice(&dev) != cudaSuccess ||
-      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
-    sms = 0;
-  if (sms <= 0) return kBlock;
-  for (int bt = 64; bt < kBlock; bt *= 2)
-    if ((n + bt - 1) / bt <= 2LL * sms) return bt;
-  return kBlock;
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms <= 0)
+    return 1;
+  const long long target = 2LL * sms * 2048;  // threads
+  int S = 1;
+  while (S < 8 && n * (2 * S) <= target) S *= 2;
+  return S;
 }
 
 template <int DIM, int KER>
 void adjoint_t(const LaunchCtx& L, const Tape& t, const Scratch& s, const float* la,
                const float* lb, float* la_out, float* lb_out, float* lr, float* lu,
                int walls) {
-  const int bt = adj_block(L.N);
-  const int g = (int)((L.N + bt - 1) / bt);
-  k_adj_force<DIM, KER><<<g, bt, 0, L.stream>>>(L.N, t, L.cases, la, lb, s, L.status);
-  if (walls) k_adj_wall<DIM, KER><<<g, bt, 0, L.stream>>>(L.N, t, L.cases, s);
-  k_adj_mu<DIM, KER><<<g, bt, 0, L.stream>>>(L.N, t, L.cases, s, walls);
-  k_adj_grad<DIM, KER><<<g, bt, 0, L.stream>>>(L.N, t, L.cases, s, lr, lu, la_out, lb_out);
+  const int S = adj_lanes(L.N);
+  const long long threads = L.N * S;
+  const int g = (int)((threads + kBlock - 1) / kBlock);
+  k_adj_force<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, la, lb, s, L.status, S);
+  if (walls) k_adj_wall<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s, S);
+  k_adj_mu<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s, walls, S);
+  k_adj_grad<DIM, KER><<<g, kBlock, 0, L.stream>>>(L.N, t, L.cases, s, lr, lu, la_out, lb_out,
+                                                    S);
 }
 
 }  // namespace

@@ -79,7 +79,8 @@ def _check_rollout(setup, steps):
             side, a["r"].double().cpu() - ref["r"]).norm(dim=1).mean().item()
 
     print({k: f"gpu {a:.2e} / float32 oracle {b:.2e}" for k, (a, b, _) in res.items()},
-          f"mean |dr| gpu {mean_drift(got):.2e} / float32 oracle {mean_drift(ref32):.2e}")
+          f"mean |dr| gpu {mean_drift(got):.2e} / float32 oracle {mean_drift(ref32):.2e}",
+          f"E_kin float64 {e64:.4e}")
     for k, (e_gpu, e_f32, floor) in res.items():
         assert e_gpu <= max(floor, 10 * e_f32), (k, e_gpu, e_f32, floor)
     assert _sets_bit_exact(setup, got["r"].cuda())
