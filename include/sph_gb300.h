@@ -272,6 +272,12 @@ int sph_set_block_size(SphHandle* h, int32_t threads);
 /* Kernel launches issued by one si_euler step of this handle (without a
  * candidate-list rebuild). */
 int sph_step_launch_count(SphHandle* h, int32_t* count);
+/* Which passes and list format serve this handle's steps: 0 the generic
+ * passes (32-bit sender indices), 1 the lean passes with 16-bit offset
+ * lists, 2 the lean passes with 32-bit index lists (the lean passes serve one
+ * periodic case with standard SPH, density summation and no wall BC). A
+ * diagnostic: no reference interface corresponds to it. */
+int sph_list_format(SphHandle* h, int32_t* format);
 /* Candidate-list rebuilds run so far by this handle's steps and the kernel
  * launches one rebuild adds to a step. Synchronizes `stream`. */
 int sph_rebuild_stats(SphHandle* h, int64_t* rebuilds, int32_t* kernels_per_rebuild,

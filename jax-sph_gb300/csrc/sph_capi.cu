@@ -1283,6 +1283,14 @@ int sph_step_launch_count(SphHandle* h, int32_t* count) try {
   return host_error();
 }
 
+int sph_list_format(SphHandle* h, int32_t* format) try {
+  if (!h || !format) return fail((int)SPH_ERR_INVALID_ARG, "null argument");
+  *format = h->lean;
+  return 0;
+} catch (...) {
+  return host_error();
+}
+
 int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) try {
   if (!h || !ms || nsteps <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
   if (!h->has_state) return fail((int)SPH_ERR_INVALID_ARG, "no state loaded");

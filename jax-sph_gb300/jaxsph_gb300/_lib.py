@@ -79,7 +79,8 @@ EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sp
            "sph_step_launch_count", "sph_profile_step", "sph_adjoint_init", "sph_tape_record",
            "sph_adjoint_step", "sph_read_status", "sph_read_status_async", "sph_diagnostics",
            "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance", "sph_set_wall_layer",
-           "sph_neighbour_counts", "sph_tape_segment", "sph_adjoint_segment"]
+           "sph_neighbour_counts", "sph_tape_segment", "sph_adjoint_segment",
+           "sph_list_format"]
 
 _LIB = None
 
@@ -111,6 +112,7 @@ def load(build_if_missing=True):
     lib.sph_step.argtypes = [V, ctypes.c_int32, V]
     lib.sph_set_block_size.argtypes = [V, ctypes.c_int32]
     lib.sph_step_launch_count.argtypes = [V, P(ctypes.c_int32)]
+    lib.sph_list_format.argtypes = [V, P(ctypes.c_int32)]
     lib.sph_profile_step.argtypes = [V, ctypes.c_int32, P(ctypes.c_float), V]
     lib.sph_adjoint_init.argtypes = [V, ctypes.c_int32]
     lib.sph_tape_record.argtypes = [V, ctypes.c_int32, V]
@@ -289,6 +291,12 @@ class Engine:
         c = ctypes.c_int32(0)
         _check(self.lib.sph_step_launch_count(self.h, ctypes.byref(c)))
         return int(c.value)
+
+    def list_format(self):
+        """0: generic passes; 1 / 2: lean passes with 16-bit / 32-bit lists."""
+        f = ctypes.c_int32(0)
+        _check(self.lib.sph_list_format(self.h, ctypes.byref(f)))
+        return int(f.value)
 
     def profile(self, nsteps, split=False):
         """Average per-step milliseconds of (kick + rebuilds, density, wall,

@@ -159,6 +159,9 @@ def test_handle_entry_points_reject_a_null_handle(lib):
     assert lib.sph_step(None, 1, None) == _lib.ERR_INVALID_ARG
     assert lib.sph_forward(None, None) == _lib.ERR_INVALID_ARG
     assert lib.sph_nl_update(None, None) == _lib.ERR_INVALID_ARG
+    fmt = ctypes.c_int32(-1)
+    assert lib.sph_list_format(None, ctypes.byref(fmt)) == _lib.ERR_INVALID_ARG
+    assert fmt.value == -1
     assert b"null" in lib.sph_last_error()
     cfg = _lib.SphConfig(dim=2)
     h = ctypes.c_void_p()
