@@ -423,6 +423,18 @@ __device__ __forceinline__ int ref_cell_occupancy(const CaseDev& c, int cell_loc
   return occ;
 }
 
+// int32(r / cs), the cell hash's index along an axis of cell size cs: r * inv_cs
+// lies within 1.5 * 2^-23 (relative) of the correctly rounded quotient, so its
+// floor is the hash's unless it lies that close to an integer; only then (and
+// for negative or non-finite r) the division decides.
+__device__ __forceinline__ int hash_index(float r, float cs, float inv_cs) {
+  const float q = r * inv_cs;
+  const float f = q - floorf(q);
+  const float tol = fmaxf(q, 1.0f) * 4.8e-7f;
+  if (q >= 0.f && f > tol && f < 1.0f - tol) return (int)q;
+  return __float2int_rz(__fdiv_rn(r, cs));
+}
+
 // Index of the reference's cell of r within its case (the reference's hash,
 // jax_md/partition.py:367-368): the binned cell coordinates divided by sub,
 // clamped into the grid. Returns -1 for a non-finite position.
@@ -433,8 +445,11 @@ __device__ __forceinline__ int ref_cell_hash(const float4& r, const CaseDev& c) 
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
     if (!isfinite(rr[d])) return -1;
-    const int n = c.nc[d] / c.sub[d];
-    int ix = c.nc[d] > 1 ? __float2int_rz(__fdiv_rn(rr[d], c.cell_size[d])) / c.sub[d] : 0;
+    // sub is 1 or 2 (fine cells of half the reference's size): division by
+    // it is a shift, and the fine index int32(r / cs) is hash_index's
+    const int sh = c.sub[d] - 1;
+    const int n = c.nc[d] >> sh;
+    int ix = c.nc[d] > 1 ? hash_index(rr[d], c.cell_size[d], c.inv_cs[d]) >> sh : 0;
     ix = ix < 0 ? 0 : (ix >= n ? n - 1 : ix);
     h += ix * mult;
     mult *= n;
@@ -451,27 +466,16 @@ __device__ __forceinline__ int ref_cell_hash(const float4& r, const CaseDev& c) 
 // the cutoff are always adjacent (the band's margin exceeds the hash's
 // rounding), so only the band's candidates take this test.
 //
-// int32(r / cs), the cell hash's index along an axis of cell size cs: r * inv_cs
-// lies within 1.5 * 2^-23 (relative) of the correctly rounded quotient, so its
-// floor is the hash's unless it lies that close to an integer; only then (and
-// for negative or non-finite r) the division decides.
-__device__ __forceinline__ int hash_index(float r, float cs, float inv_cs) {
-  const float q = r * inv_cs;
-  const float f = q - floorf(q);
-  const float tol = fmaxf(q, 1.0f) * 4.8e-7f;
-  if (q >= 0.f && f > tol && f < 1.0f - tol) return (int)q;
-  return __float2int_rz(__fdiv_rn(r, cs));
-}
-
 template <int DIM>
 __device__ __forceinline__ bool ref_adjacent(const float4& a, const float4& b, const CaseDev& c) {
   const float pa[3] = {a.x, a.y, a.z}, pb[3] = {b.x, b.y, b.z};
 #pragma unroll
   for (int d = 0; d < DIM; ++d) {
-    const int n = c.nc[d] / c.sub[d];
+    const int sh = c.sub[d] - 1;  // sub is 1 or 2
+    const int n = c.nc[d] >> sh;
     if (n < 3) continue;
-    int ia = hash_index(pa[d], c.cell_size[d], c.inv_cs[d]) / c.sub[d];
-    int ib = hash_index(pb[d], c.cell_size[d], c.inv_cs[d]) / c.sub[d];
+    int ia = hash_index(pa[d], c.cell_size[d], c.inv_cs[d]) >> sh;
+    int ib = hash_index(pb[d], c.cell_size[d], c.inv_cs[d]) >> sh;
     ia = ia < 0 ? 0 : (ia >= n ? n - 1 : ia);
     ib = ib < 0 ? 0 : (ib >= n ? n - 1 : ib);
     const int k = ia > ib ? ia - ib : ib - ia;
@@ -495,12 +499,13 @@ __device__ __forceinline__ bool ref_adjacent_d(const float4& a, const float4& b,
   const float pa[3] = {a.x, a.y, a.z}, pb[3] = {b.x, b.y, b.z}, pd[3] = {d.x, d.y, d.z};
 #pragma unroll
   for (int k = 0; k < DIM; ++k) {
-    const int n = c.nc[k] / c.sub[k];
+    const int sh = c.sub[k] - 1;  // sub is 1 or 2
+    const int n = c.nc[k] >> sh;
     if (n < 3) continue;
     const float cref = c.cell_size[k] * (float)c.sub[k];
     if (fabsf(pd[k]) < cref * (1.0f - (float)(4 * n + 8) * 1.2e-7f)) continue;
-    int ia = hash_index(pa[k], c.cell_size[k], c.inv_cs[k]) / c.sub[k];
-    int ib = hash_index(pb[k], c.cell_size[k], c.inv_cs[k]) / c.sub[k];
+    int ia = hash_index(pa[k], c.cell_size[k], c.inv_cs[k]) >> sh;
+    int ib = hash_index(pb[k], c.cell_size[k], c.inv_cs[k]) >> sh;
     ia = ia < 0 ? 0 : (ia >= n ? n - 1 : ia);
     ib = ib < 0 ? 0 : (ib >= n ? n - 1 : ib);
     const int s = ia > ib ? ia - ib : ib - ia;
