@@ -390,6 +390,7 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
     if (vc <= kv) {
       const Word* vli = vl + i;
       const int ng = (vc + 3) >> 2;
+      unsigned long long band = 0;  // list slots of candidates in the band
       Word wn = vli[0];  // (read even without candidates: never used then)
       for (int g = 0; g < ng; ++g) {
         const Word w = wn;
@@ -407,7 +408,13 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
         for (int q = 0; q < 4; ++q) {
           float3 dr;
           float d2;
-          const bool e = q < rem && lean_edge<DIM>(ri, rj[q], c, cp, dr, d2);
+          mi_dr<DIM>(ri, rj[q], c, dr, d2);
+          const bool e = q < rem && d2 < c.cut_lo;
+          // a candidate in the band around the cutoff is decided after the
+          // loop: few receivers have one, but nearly every group of a warp
+          // would otherwise run the reference metric for some lane
+          const int k = 4 * g + q;
+          if (q < rem && !e && d2 < c.cut_hi && k < 64) band |= 1ull << k;
           if (e) {
             if (fluid) {
               float dist, inv_d;
@@ -417,6 +424,34 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
             if (m < kmax) L::put(srow, (size_t)bs, m, o[q]);
             ++m;
           }
+        }
+      }
+      // the band's candidates in list order (slots beyond the mask's 64
+      // re-tested): the reference metric decides (jax_md/partition.py:897),
+      // and an edge joins the list after the others
+      for (int k = 0; k < vc; ++k) {
+        if (k < 64) {
+          if (!band) {
+            k = 63;  // no more masked slots
+            continue;
+          }
+          k = __ffsll((long long)band) - 1;
+          band &= band - 1;
+        }
+        const int o = L::raw(vli[(size_t)(k >> 2) * N], k & 3);
+        const float4 rj = __ldg(b.P4 + L::dec(i, o, N));
+        float3 dr;
+        float d2;
+        mi_dr<DIM>(ri, rj, c, dr, d2);
+        if (k >= 64 && !(!(d2 < c.cut_lo) && d2 < c.cut_hi)) continue;
+        if (exact_edge<DIM>(ri, rj, cp)) {
+          if (fluid) {
+            float dist, inv_d;
+            dist_inv(d2, dist, inv_d);
+            s0.add(kw<KER>(dist, c));
+          }
+          if (m < kmax) L::put(srow, (size_t)bs, m, o);
+          ++m;
         }
       }
     } else {
