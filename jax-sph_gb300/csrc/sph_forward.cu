@@ -198,13 +198,29 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
       int ja = cand(0, (int)i), jb = cand(1, ja);
       int jc = cand(2, ja), jd = cand(3, jc);
       float4 ra = __ldg(b.P4 + ja), rb = __ldg(b.P4 + jb);
+      // fast cases decide the candidates in the band around the cutoff after
+      // the loop (list slots in a mask; slots past 64 re-tested): a receiver
+      // has few, but a warp would otherwise run the reference metric in
+      // nearly every iteration for some lane
+      unsigned long long band = 0;
       for (int k = 0; k < vc; k += 2) {
         const bool v1 = k + 1 < vc;
         const float4 rc = __ldg(b.P4 + jc), rd = __ldg(b.P4 + jd);
         const int je = cand(k + 4, jc), jf = cand(k + 5, je);
         float d2a, d2b;
-        const bool ea = edge_mi_d2<DIM>(ri, ra, lo, hi, c, cp, d2a);
-        const bool eb = v1 && edge_mi_d2<DIM>(ri, rb, lo, hi, c, cp, d2b);
+        bool ea, eb;
+        if (c.fast) {
+          float3 dr;
+          pair_dr<DIM>(ri, ra, c, dr, d2a);
+          pair_dr<DIM>(ri, rb, c, dr, d2b);
+          ea = d2a < lo;
+          eb = v1 && d2b < lo;
+          if (!ea && d2a < hi && k < 64) band |= 1ull << k;
+          if (v1 && !eb && d2b < hi && k + 1 < 64) band |= 1ull << (k + 1);
+        } else {
+          ea = edge_mi_d2<DIM>(ri, ra, lo, hi, c, cp, d2a);
+          eb = v1 && edge_mi_d2<DIM>(ri, rb, lo, hi, c, cp, d2b);
+        }
         if (sum_here) {
           if (ea) s0.add(kw<KER>(d2a > 0.f ? sqrtf(d2a) : 0.f, c));
           if (eb) s0.add(kw<KER>(d2b > 0.f ? sqrtf(d2b) : 0.f, c));
@@ -219,6 +235,31 @@ k_density(long long N, Buffers b, const CaseDev* cases, const int* cellid, const
         rb = rd;
         jc = je;
         jd = jf;
+      }
+      // the band's candidates in list order; their edges join the list after
+      // the others (W and W' vanish at the cutoff)
+      if (c.fast) {
+        for (int k = 0; k < vc; ++k) {
+          if (k < 64) {
+            if (!band) {
+              k = 63;  // no more masked slots
+              continue;
+            }
+            k = __ffsll((long long)band) - 1;
+            band &= band - 1;
+          }
+          const int j = vli[(long long)k * N];
+          const float4 rj = __ldg(b.P4 + j);
+          float3 dr;
+          float d2;
+          pair_dr<DIM>(ri, rj, c, dr, d2);
+          if (k >= 64 && !(!(d2 < lo) && d2 < hi)) continue;
+          if (exact_edge<DIM>(ri, rj, cp)) {
+            if (sum_here) s0.add(kw<KER>(d2 > 0.f ? sqrtf(d2) : 0.f, c));
+            s_nbr[(m < kmax ? m : kmax - 1) * bs + tid] = j;
+            ++m;
+          }
+        }
       }
     } else {
       for_each_edge_slow<DIM>(N, i, ri, c, cp, b.P4, cellid, start, nl,
