@@ -312,6 +312,19 @@ int sph_adjoint_step(SphHandle* h, int32_t slot, float* lam_r, float* lam_u, flo
  * (nsteps <= slots). sph_adjoint_segment then applies sph_adjoint_step to
  * slots nsteps-1 down to 0. */
 int sph_tape_segment(SphHandle* h, int32_t nsteps, void* stream);
+/* Device snapshots of a handle's state between two steps, for the
+ * differentiable form's checkpoints: sph_snapshot_init allocates `slots`
+ * snapshots (the resident particle set, the pending forward result, the
+ * binning and the candidate lists: ~0.5 KB per particle each);
+ * sph_snapshot_save copies the state after an sph_step into a slot and
+ * sph_snapshot_restore copies it back, so that the following steps repeat
+ * the saved ones bit for bit (including the order in which pairs are summed)
+ * without re-binning. SPH solver with density summation, no heat conduction.
+ * Replaces the reference's in-memory JAX tape (notebooks/iclr24_grads.ipynb):
+ * no counterpart of its own. */
+int sph_snapshot_init(SphHandle* h, int32_t slots);
+int sph_snapshot_save(SphHandle* h, int32_t slot, void* stream);
+int sph_snapshot_restore(SphHandle* h, int32_t slot, void* stream);
 int sph_adjoint_segment(SphHandle* h, int32_t nsteps, float* lam_r, float* lam_u, float* lam_a,
                         float* lam_b, void* stream);
 

@@ -95,6 +95,11 @@ struct SphHandle {
   int *t_nbr = nullptr, *t_cnt = nullptr;
   float4* t_scr = nullptr;              // reverse scratch: 8 planes of N
   float *t_la = nullptr, *t_lb = nullptr;  // the step inputs' dudt/dvdt adjoints
+  // device snapshots of the state a steady handle carries between steps
+  int snap_slots = 0;
+  unsigned char* snap = nullptr;
+  size_t snap_stride = 0;
+  std::vector<char> snap_ok;
   std::vector<void*> allocs;
 
   template <typename T>
@@ -711,7 +716,8 @@ int sph_update_cases(SphHandle* h, const SphCase* cases, int32_t n_cases) try {
   }
   h->cases.assign(cases, cases + n_cases);
   h->hc = next;
-  const int lean = lean_config(h->cfg, n_cases, h->hc[0]);
+  // a handle with an adjoint tape keeps the generic passes (32-bit lists)
+  const int lean = h->tape_slots ? 0 : lean_config(h->cfg, n_cases, h->hc[0]);
   if (lean != h->lean) {
     // the list format changes with the passes: the lists must be rebuilt
     h->lean = lean;
@@ -925,6 +931,40 @@ int pinned_host(const void* p, const char* name, bool* host, void** mapped = nul
   return fail((int)SPH_ERR_INVALID_ARG,
               std::string(name) + ": host arrays must be pinned (page-locked) memory");
 }
+
+// The device arrays a steady handle carries from one step to the next: the
+// resident particle set, the pending forward result, the binning (cells,
+// starts, inverse permutation), the rebuild reference positions and the
+// candidate lists. Everything else is rebuilt or reset inside a step.
+std::vector<std::pair<void*, size_t>> carried_state(const SphHandle* h) {
+  const size_t N = (size_t)h->N;
+  const Buffers& b = h->buf[0];
+  std::vector<std::pair<void*, size_t>> r = {
+      {b.P4, sizeof(float4) * N},   {b.U4, sizeof(float4) * N},
+      {b.V4, sizeof(float4) * N},   {b.A4, sizeof(float4) * N},
+      {b.A2, sizeof(float4) * N},   {b.ETA, sizeof(float) * N},
+      {b.META, sizeof(int) * N},    {b.ORIG, sizeof(int) * N},
+      {h->R4, sizeof(float4) * N},  {h->cellid, sizeof(int) * N},
+      {h->start, sizeof(int) * ((size_t)h->C + 1)}, {h->rref, sizeof(float4) * N},
+      {h->vl, sizeof(int) * (size_t)h->kv * N},     {h->vcnt, sizeof(int) * N},
+      {h->inv, sizeof(int) * N}};
+  if (b.NW4) r.push_back({b.NW4, sizeof(float4) * N});
+  if (b.RD) r.push_back({b.RD, sizeof(double4_32a) * N});
+  return r;
+}
+
+int snap_copy(SphHandle* h, int slot, bool save, cudaStream_t st) {
+  size_t off = (size_t)slot * h->snap_stride;
+  for (const auto& reg : carried_state(h)) {
+    unsigned char* dst = h->snap + off;
+    cudaError_t e = save ? cudaMemcpyAsync(dst, reg.first, reg.second, cudaMemcpyDeviceToDevice, st)
+                         : cudaMemcpyAsync(reg.first, dst, reg.second, cudaMemcpyDeviceToDevice, st);
+    if (e != cudaSuccess) return cuda_check(e, "snapshot copy");
+    off += (reg.second + 255) & ~size_t(255);
+  }
+  return 0;
+}
+
 }  // namespace
 
 extern "C" {
@@ -1326,6 +1366,51 @@ int sph_profile_step(SphHandle* h, int32_t nsteps, float* ms, void* stream) try 
   return host_error();
 }
 
+int sph_snapshot_init(SphHandle* h, int32_t slots) try {
+  if (!h || slots <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
+  if (h->snap_slots) return fail((int)SPH_ERR_INVALID_ARG, "snapshots already initialised");
+  const SphConfig& c = h->cfg;
+  if (c.solver != SPH_SOLVER_SPH || c.is_rho_evol || c.is_heat_conduction)
+    return fail((int)SPH_ERR_INVALID_ARG,
+                "snapshots cover the SPH solver with density summation, no heat conduction");
+  size_t stride = 0;
+  for (const auto& reg : carried_state(h)) stride += (reg.second + 255) & ~size_t(255);
+  int rc = h->alloc(&h->snap, stride * (size_t)slots);
+  if (rc) return rc;
+  h->snap_stride = stride;
+  h->snap_slots = slots;
+  h->snap_ok.assign((size_t)slots, 0);
+  return 0;
+} catch (...) {
+  return host_error();
+}
+
+int sph_snapshot_save(SphHandle* h, int32_t slot, void* stream) try {
+  if (!h || slot < 0 || slot >= h->snap_slots)
+    return fail((int)SPH_ERR_INVALID_ARG, "snapshot slot out of range");
+  if (!h->has_state || !steady(h))
+    return fail((int)SPH_ERR_INVALID_ARG, "a snapshot is taken between two steps (after sph_step)");
+  int rc = snap_copy(h, slot, true, (cudaStream_t)stream);
+  if (!rc) h->snap_ok[(size_t)slot] = 1;
+  return rc;
+} catch (...) {
+  return host_error();
+}
+
+int sph_snapshot_restore(SphHandle* h, int32_t slot, void* stream) try {
+  if (!h || slot < 0 || slot >= h->snap_slots || !h->snap_ok[(size_t)slot])
+    return fail((int)SPH_ERR_INVALID_ARG, "no snapshot in that slot");
+  int rc = snap_copy(h, slot, false, (cudaStream_t)stream);
+  if (rc) return rc;
+  // the state between two steps: binned, lists built, a forward result and
+  // bc_fn pending (what sph_snapshot_save required)
+  h->has_state = h->binned = h->lists = h->from_forward = h->pending_bc = true;
+  h->fresh = false;
+  return 0;
+} catch (...) {
+  return host_error();
+}
+
 int sph_adjoint_init(SphHandle* h, int32_t slots) try {
   if (!h || slots <= 0) return fail((int)SPH_ERR_INVALID_ARG, "bad argument");
   const SphConfig& c = h->cfg;
@@ -1342,6 +1427,13 @@ int sph_adjoint_init(SphHandle* h, int32_t slots) try {
     return fail((int)SPH_ERR_INVALID_ARG,
                 "the adjoint of the wall BC covers no external force and velocity-only bc_fn");
   if (h->tape_slots) return fail((int)SPH_ERR_INVALID_ARG, "adjoint tape already initialised");
+  if (h->lean) {
+    // the tape records 32-bit sender indices: the generic passes serve the
+    // handle from now on (lists in their format are built at the next step)
+    h->lean = 0;
+    h->lists = false;
+    drop_graph(h);
+  }
   const long long N = h->N;
   const size_t S = (size_t)slots * N;
   int rc = h->alloc(&h->t_orig, S) | h->alloc(&h->t_meta, S) | h->alloc(&h->t_P4, S) |

@@ -80,7 +80,7 @@ EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sp
            "sph_adjoint_step", "sph_read_status", "sph_read_status_async", "sph_diagnostics",
            "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance", "sph_set_wall_layer",
            "sph_neighbour_counts", "sph_tape_segment", "sph_adjoint_segment",
-           "sph_list_format"]
+           "sph_list_format", "sph_snapshot_init", "sph_snapshot_save", "sph_snapshot_restore"]
 
 _LIB = None
 
@@ -113,6 +113,9 @@ def load(build_if_missing=True):
     lib.sph_set_block_size.argtypes = [V, ctypes.c_int32]
     lib.sph_step_launch_count.argtypes = [V, P(ctypes.c_int32)]
     lib.sph_list_format.argtypes = [V, P(ctypes.c_int32)]
+    lib.sph_snapshot_init.argtypes = [V, ctypes.c_int32]
+    lib.sph_snapshot_save.argtypes = [V, ctypes.c_int32, V]
+    lib.sph_snapshot_restore.argtypes = [V, ctypes.c_int32, V]
     lib.sph_profile_step.argtypes = [V, ctypes.c_int32, P(ctypes.c_float), V]
     lib.sph_adjoint_init.argtypes = [V, ctypes.c_int32]
     lib.sph_tape_record.argtypes = [V, ctypes.c_int32, V]
@@ -291,6 +294,17 @@ class Engine:
         c = ctypes.c_int32(0)
         _check(self.lib.sph_step_launch_count(self.h, ctypes.byref(c)))
         return int(c.value)
+
+    def snapshot_init(self, slots):
+        _check(self.lib.sph_snapshot_init(self.h, int(slots)))
+
+    def snapshot_save(self, slot):
+        """Copy the state between two steps into device snapshot ``slot``."""
+        _check(self.lib.sph_snapshot_save(self.h, int(slot), _stream()))
+
+    def snapshot_restore(self, slot):
+        """Copy snapshot ``slot`` back: the next steps repeat the saved ones bit for bit."""
+        _check(self.lib.sph_snapshot_restore(self.h, int(slot), _stream()))
 
     def list_format(self):
         """0: generic passes; 1 / 2: lean passes with 16-bit / 32-bit lists."""

@@ -3,12 +3,14 @@
 The reference differentiates whole rollouts with ``jax.grad`` (integer
 neighbour indices carry no gradient, so the list is frozen per step;
 ``notebooks/iclr24_grads.ipynb``, ``notebooks/iclr24_inverse.ipynb``) and
-keeps the whole tape in memory. Here the forward rollout stores the state
-every ``checkpoint_every`` steps; the reverse sweep re-runs each segment
-forward (bit-identical to the original forward), records its steps on the
-GPU tape and applies the hand-written reverse step (``sph_adjoint_step``,
+keeps the whole tape in memory. Here the forward rollout keeps a device
+snapshot of the engine's state (particles in their binned order, binning,
+candidate lists) every ``checkpoint_every`` steps; the reverse sweep restores
+each segment's snapshot, re-runs the segment forward (bit-identical to the
+original forward, pair sums in the same order), records its steps on the GPU
+tape and applies the hand-written reverse step (``sph_adjoint_step``,
 ``csrc/sph_adjoint.cu``) from the last step to the first. Memory is one
-segment of per-step data plus the checkpoints.
+segment of per-step data plus the snapshots.
 
 ``rollout`` wraps it as a ``torch.autograd.Function``: the gradient of any
 torch loss of the final positions flows back to the initial velocity.
@@ -36,14 +38,17 @@ class AdjointRollout:
         self.setup = setup
         self.steps = int(steps)
         self.k = int(checkpoint_every)
-        # canonical order: a segment recomputed from its checkpoint (which
-        # rebuilds the candidate lists at other steps) equals the forward
-        # rollout bit for bit; the block size changes no result
-        self.sim = Simulation(setup, device=device, canonical_order=True, autotune=autotune)
+        # a segment restarts from a device snapshot of the engine's state, so
+        # its recomputation equals the forward rollout bit for bit; the block
+        # size changes no result
+        self.sim = Simulation(setup, device=device, autotune=autotune)
         self.engine = self.sim.engine
         self.engine.adjoint_init(self.k)
+        self.segments = -(-self.steps // self.k)
+        if self.segments > 1:
+            self.engine.snapshot_init(self.segments - 1)
         self.device = torch.device(device)
-        self.checkpoints = []
+        self.start = None
         self._base = None
 
     def _initial(self, u0):
@@ -60,12 +65,16 @@ class AdjointRollout:
 
     def run(self, state0):
         """Run the rollout from ``state0`` (a state dict); returns the final
-        state (device tensors, original order), keeping the checkpoints."""
-        self.sim.load([state0])
-        self.checkpoints = []
+        state (device tensors, original order), keeping the checkpoints: the
+        initial state, then a device snapshot at every segment boundary."""
+        self.sim.load([state0])  # capacities, as the reference's allocate
+        # the first segment starts where its recomputation will: a loaded state
+        self.start = self.sim.state(split=False)
+        self.sim.restore(self.start)
         done = 0
-        while done < self.steps:
-            self.checkpoints.append(self.sim.state(split=False))
+        for seg in range(self.segments):
+            if seg > 0:
+                self.engine.snapshot_save(seg - 1)
             n = min(self.k, self.steps - done)
             self.engine.step(n)
             done += n
@@ -90,10 +99,13 @@ class AdjointRollout:
         lu = (torch.zeros_like(lr) if lam_u is None else
               lam_u.detach().to(self.device, torch.float32).contiguous().clone())
         la, lb = torch.zeros_like(lr), torch.zeros_like(lr)
-        for seg in reversed(range(len(self.checkpoints))):
+        for seg in reversed(range(self.segments)):
             # recompute the segment from its checkpoint, recording its steps,
             # then sweep it backwards (one library call each)
-            self.sim.restore(self.checkpoints[seg])
+            if seg == 0:
+                self.sim.restore(self.start)
+            else:
+                self.engine.snapshot_restore(seg - 1)
             n = min(self.k, self.steps - seg * self.k)
             ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)] if timer is not None else None
             if ev:

@@ -160,7 +160,7 @@ class WCSPH:
             # (the neighbour set of every step is exact either way)
             e = _lib.Engine(nl_fns.config(**self.solver_flags(), verlet_skin=0.1), [case])
             self._engines = {key: e}
-        elif bytes(e.cases[0]) != bytes(case):
+        elif e.cases[0] is not case and bytes(e.cases[0]) != bytes(case):
             e.update_cases([case])
         return e
 
@@ -245,7 +245,8 @@ class WCSPH:
         # its fields are known to be valid and its view is already built
         last = self._last_host
         vin = None
-        if (last is not None and last[0] is state and last[3] is self.engine(nl_fns, case)
+        eng = self.engine(nl_fns, case)
+        if (last is not None and last[0] is state and last[3] is eng
                 and all(state.get(k) is t for k, t in last[1].items())):
             st, vin = last[1], last[2]
         else:
@@ -253,13 +254,13 @@ class WCSPH:
                             self.is_heat_conduction)
         self._last_host = None
         thr = nl_fns.threshold_sq
-        ref = torch.as_tensor(neighbors.reference_position)
+        ref = torch.as_tensor(neighbors.reference_position) if thr > 0.0 else None
         status = None
         host = st is not None
         if nw_fn is not None:
-            self._wall_layer(self.engine(nl_fns, case), nw_fn)
+            self._wall_layer(eng, nw_fn)
         if host:
-            e = self.engine(nl_fns, case)
+            e = eng
             cap = neighbors.cell_list_capacity
             e.nl_set_capacity(cap if cap is not None else 2 ** 31 - 1, neighbors.max_occupancy)
             # a summation carries drho/dt over unchanged (solver.py:794-796):
