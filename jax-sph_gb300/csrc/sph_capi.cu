@@ -100,6 +100,7 @@ struct SphHandle {
   unsigned char* snap = nullptr;
   size_t snap_stride = 0;
   std::vector<char> snap_ok;
+  std::vector<int> snap_fmt;  // list format of the passes when the slot was saved
   std::vector<void*> allocs;
 
   template <typename T>
@@ -1380,6 +1381,7 @@ int sph_snapshot_init(SphHandle* h, int32_t slots) try {
   h->snap_stride = stride;
   h->snap_slots = slots;
   h->snap_ok.assign((size_t)slots, 0);
+  h->snap_fmt.assign((size_t)slots, 0);
   return 0;
 } catch (...) {
   return host_error();
@@ -1391,7 +1393,10 @@ int sph_snapshot_save(SphHandle* h, int32_t slot, void* stream) try {
   if (!h->has_state || !steady(h))
     return fail((int)SPH_ERR_INVALID_ARG, "a snapshot is taken between two steps (after sph_step)");
   int rc = snap_copy(h, slot, true, (cudaStream_t)stream);
-  if (!rc) h->snap_ok[(size_t)slot] = 1;
+  if (!rc) {
+    h->snap_ok[(size_t)slot] = 1;
+    h->snap_fmt[(size_t)slot] = h->lean;
+  }
   return rc;
 } catch (...) {
   return host_error();
@@ -1400,6 +1405,9 @@ int sph_snapshot_save(SphHandle* h, int32_t slot, void* stream) try {
 int sph_snapshot_restore(SphHandle* h, int32_t slot, void* stream) try {
   if (!h || slot < 0 || slot >= h->snap_slots || !h->snap_ok[(size_t)slot])
     return fail((int)SPH_ERR_INVALID_ARG, "no snapshot in that slot");
+  if (h->snap_fmt[(size_t)slot] != h->lean)
+    return fail((int)SPH_ERR_INVALID_ARG,
+                "the snapshot's candidate lists are in another format than the passes now use");
   int rc = snap_copy(h, slot, false, (cudaStream_t)stream);
   if (rc) return rc;
   // the state between two steps: binned, lists built, a forward result and

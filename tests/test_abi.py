@@ -162,7 +162,10 @@ def test_handle_entry_points_reject_a_null_handle(lib):
     fmt = ctypes.c_int32(-1)
     assert lib.sph_list_format(None, ctypes.byref(fmt)) == _lib.ERR_INVALID_ARG
     assert fmt.value == -1
-    assert b"null" in lib.sph_last_error()
+    assert lib.sph_snapshot_init(None, 1) == _lib.ERR_INVALID_ARG
+    assert lib.sph_snapshot_save(None, 0, None) == _lib.ERR_INVALID_ARG
+    assert lib.sph_snapshot_restore(None, 0, None) == _lib.ERR_INVALID_ARG
+    assert b"null" in lib.sph_last_error() or b"slot" in lib.sph_last_error()
     cfg = _lib.SphConfig(dim=2)
     h = ctypes.c_void_p()
     assert lib.sph_create(ctypes.byref(cfg), None, 0, ctypes.byref(h)) == _lib.ERR_INVALID_ARG
