@@ -405,7 +405,27 @@ k_adj_grad(long long N, Tape t, const CaseDev* cases, Scratch s, float* lr, floa
 }
 
 // The tape slot of the step just taken, one thread per particle (the
-// neighbour list row by row, coalesced).
+// neighbour list row by row, coalesced), its senders as 32-bit sorted
+// indices whatever the passes' list format: FMT 0 32-bit rows (generic
+// passes), 1 words of four 16-bit offsets j - i modulo N, 2 words of four
+// 32-bit indices (the lean passes).
+template <int FMT>
+__device__ __forceinline__ int list_sender(const int* nbr, long long N, long long k, int q) {
+  if (FMT == 0) return nbr[(long long)q * N + k];
+  if (FMT == 1) {
+    const uint2 w = reinterpret_cast<const uint2*>(nbr)[(long long)(q >> 2) * N + k];
+    const unsigned h = (q & 2) ? w.y : w.x;
+    long long j = k + (int)(short)(unsigned short)(h >> ((q & 1) * 16));
+    j += j < 0 ? N : 0;
+    j -= j >= N ? N : 0;
+    return (int)j;
+  }
+  const int4 w = reinterpret_cast<const int4*>(nbr)[(long long)(q >> 2) * N + k];
+  const int r = q & 3;
+  return r == 0 ? w.x : (r == 1 ? w.y : (r == 2 ? w.z : w.w));
+}
+
+template <int FMT>
 __global__ void k_tape_record(long long N, Buffers b, const float4* R4, const int* nbr,
                               const int* cnt, int kmax, int* t_orig, float4* t_P4, float4* t_U4,
                               float4* t_V4, float4* t_R4, int* t_meta, int* t_nbr, int* t_cnt) {
@@ -420,7 +440,7 @@ __global__ void k_tape_record(long long N, Buffers b, const float4* R4, const in
   const int m = cnt[k];
   t_cnt[k] = m;
   const int e = m < kmax ? m : kmax;
-  for (int q = 0; q < e; ++q) t_nbr[(long long)q * N + k] = nbr[(long long)q * N + k];
+  for (int q = 0; q < e; ++q) t_nbr[(long long)q * N + k] = list_sender<FMT>(nbr, N, k, q);
 }
 
 // Lanes per particle of the reverse passes (1, 2, 4 or 8): as many as keep
@@ -457,8 +477,13 @@ void launch_tape_record(const LaunchCtx& L, Buffers b, const float4* R4, int* t_
                         float4* t_P4, float4* t_U4, float4* t_V4, float4* t_R4, int* t_meta,
                         int* t_nbr, int* t_cnt) {
   const int g = (int)((L.N + kBlock - 1) / kBlock);
-  k_tape_record<<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.nbr, L.nbr_cnt, L.kmax, t_orig, t_P4,
-                                            t_U4, t_V4, t_R4, t_meta, t_nbr, t_cnt);
+#define SPH_TAPE(F)                                                                          \
+  k_tape_record<F><<<g, kBlock, 0, L.stream>>>(L.N, b, R4, L.nbr, L.nbr_cnt, L.kmax, t_orig,  \
+                                               t_P4, t_U4, t_V4, t_R4, t_meta, t_nbr, t_cnt)
+  if (L.lean == 1) SPH_TAPE(1);
+  else if (L.lean == 2) SPH_TAPE(2);
+  else SPH_TAPE(0);
+#undef SPH_TAPE
 }
 
 void launch_adjoint(const LaunchCtx& L, const AdjTape& at, const AdjScratch& as, const float* la,

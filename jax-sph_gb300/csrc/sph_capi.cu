@@ -717,8 +717,7 @@ int sph_update_cases(SphHandle* h, const SphCase* cases, int32_t n_cases) try {
   }
   h->cases.assign(cases, cases + n_cases);
   h->hc = next;
-  // a handle with an adjoint tape keeps the generic passes (32-bit lists)
-  const int lean = h->tape_slots ? 0 : lean_config(h->cfg, n_cases, h->hc[0]);
+  const int lean = lean_config(h->cfg, n_cases, h->hc[0]);
   if (lean != h->lean) {
     // the list format changes with the passes: the lists must be rebuilt
     h->lean = lean;
@@ -1435,13 +1434,6 @@ int sph_adjoint_init(SphHandle* h, int32_t slots) try {
     return fail((int)SPH_ERR_INVALID_ARG,
                 "the adjoint of the wall BC covers no external force and velocity-only bc_fn");
   if (h->tape_slots) return fail((int)SPH_ERR_INVALID_ARG, "adjoint tape already initialised");
-  if (h->lean) {
-    // the tape records 32-bit sender indices: the generic passes serve the
-    // handle from now on (lists in their format are built at the next step)
-    h->lean = 0;
-    h->lists = false;
-    drop_graph(h);
-  }
   const long long N = h->N;
   const size_t S = (size_t)slots * N;
   int rc = h->alloc(&h->t_orig, S) | h->alloc(&h->t_meta, S) | h->alloc(&h->t_P4, S) |
