@@ -397,25 +397,9 @@ int rebuild(SphHandle* h, cudaStream_t st, bool from_forward, bool apply_bc,
   LaunchCtx L = h->ctx(st);
   const Buffers& A = h->buf[0];
   const Buffers& B = h->buf[1];
-  const size_t N = (size_t)h->N;
-  cudaError_t e = cudaSuccess;
-  auto cp = [&](void* dst, const void* src, size_t bytes) {
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, st);
-  };
-  cp(B.P4, A.P4, sizeof(float4) * N);
-  cp(B.U4, A.U4, sizeof(float4) * N);
-  cp(B.V4, A.V4, sizeof(float4) * N);
-  cp(B.A4, A.A4, sizeof(float4) * N);
-  cp(B.A2, A.A2, sizeof(float4) * N);
-  cp(B.ETA, A.ETA, sizeof(float) * N);
-  cp(B.META, A.META, sizeof(int) * N);
-  cp(B.ORIG, A.ORIG, sizeof(int) * N);
-  if (A.NW4) cp(B.NW4, A.NW4, sizeof(float4) * N);
-  if (A.RD) cp(B.RD, A.RD, sizeof(double4_32a) * N);
-  if (A.TH4) cp(B.TH4, A.TH4, sizeof(float4) * N);
-  if (e != cudaSuccess) return cuda_check(e, "rebuild copy");
+  // the hashing kernel copies the resident set into the scratch set first
   launch_bin(L, B, A, h->R4, h->cellid, h->count, h->start, h->keyc, h->keys, h->tsrc, h->tkey,
-             h->tcell, h->scan_tmp, h->C, false, from_forward, apply_bc, h->rref);
+             h->tcell, h->scan_tmp, h->C, false, from_forward, apply_bc, h->rref, &A);
   if (lists) launch_verlet(L, A, h->cellid, h->start);
   return launch_status("rebuild");
 }

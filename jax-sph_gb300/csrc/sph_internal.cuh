@@ -718,10 +718,12 @@ void launch_pack(const LaunchCtx& L, const SphStateView& s, Buffers out,
 void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateView& s,
                    bool from_forward, bool apply_bc, const float* ref = nullptr,
                    float thr_sq = 0.f, const int* inv = nullptr);
+// `copy_src`: the resident set, copied into `in` by the hashing kernel first
+// (a rebuild's scratch copy).
 void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,
                 int* count, int* start, int* keyc, int* keys, int* tsrc, int* tkey, int* tcell,
                 int* scan_tmp, long long total_cells, bool drift, bool from_forward,
-                bool apply_bc, float4* rref);
+                bool apply_bc, float4* rref, const Buffers* copy_src = nullptr);
 // In-place kick-drift of a step on the resident buffers, with the per-step
 // reference-cell occupancy test and the rebuild test.
 void launch_kick(const LaunchCtx& L, Buffers b, const float4* R4, long long ref_cells,

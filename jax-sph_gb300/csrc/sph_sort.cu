@@ -225,13 +225,29 @@ __device__ __forceinline__ void kick_drift64(float4& r, double4_32a& rd, float3&
   }
 }
 
+// With `copy`, each thread first copies its particle's records from `src`
+// into `in` (the scratch set the sort reads from): a rebuild's copy of the
+// resident set rides along with the hashing instead of a copy per array.
 template <int DIM>
 __global__ void k_hash_count(long long N, Buffers in, const float4* R4, const CaseDev* cases,
                              int* count, int* keyc, int* keys, unsigned* status, bool drift,
-                             bool from_forward, bool apply_bc) {
+                             bool from_forward, bool apply_bc, Buffers src, bool copy) {
   long long k = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   bool valid = k < N;
   int cell = 0;
+  if (valid && copy) {
+    in.P4[k] = src.P4[k];
+    in.U4[k] = src.U4[k];
+    in.V4[k] = src.V4[k];
+    in.A4[k] = src.A4[k];
+    in.A2[k] = src.A2[k];
+    in.ETA[k] = src.ETA[k];
+    in.META[k] = src.META[k];
+    in.ORIG[k] = src.ORIG[k];
+    if (src.NW4) in.NW4[k] = src.NW4[k];
+    if (src.RD) in.RD[k] = src.RD[k];
+    if (src.TH4) in.TH4[k] = src.TH4[k];
+  }
   if (valid) {
     int meta = in.META[k];
     const CaseDev& c = cases[case_of(meta)];
@@ -691,15 +707,18 @@ void launch_unpack(const LaunchCtx& L, Buffers in, const float4* R4, SphStateVie
 void launch_bin(const LaunchCtx& L, Buffers in, Buffers out, const float4* R4, int* cellid,
                 int* count, int* start, int* keyc, int* keys, int* tsrc, int* tkey, int* tcell,
                 int* scan_tmp, long long total_cells, bool drift, bool from_forward,
-                bool apply_bc, float4* rref) {
+                bool apply_bc, float4* rref, const Buffers* copy_src) {
   cudaMemsetAsync(count, 0, sizeof(int) * (total_cells + 1), L.stream);
   int g = nblocks(L.N);
+  const Buffers src = copy_src ? *copy_src : in;
   if (L.dim == 3)
     k_hash_count<3><<<g, kBlock, 0, L.stream>>>(L.N, in, R4, L.cases, count, keyc, keys,
-                                                 L.status, drift, from_forward, apply_bc);
+                                                 L.status, drift, from_forward, apply_bc, src,
+                                                 copy_src != nullptr);
   else
     k_hash_count<2><<<g, kBlock, 0, L.stream>>>(L.N, in, R4, L.cases, count, keyc, keys,
-                                                 L.status, drift, from_forward, apply_bc);
+                                                 L.status, drift, from_forward, apply_bc, src,
+                                                 copy_src != nullptr);
   count_launch(L, 3 + launch_scan(L.stream, count, start, total_cells, scan_tmp));
   k_scatter<<<g, kBlock, 0, L.stream>>>(L.N, keyc, keys, start, in.ORIG, tsrc, tkey, tcell);
   if (L.dim == 3)
