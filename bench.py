@@ -51,13 +51,14 @@ KICK_BYTES = 104          # kick-drift: reads r,m,u,v,dudt,dvdt,eta,tag (56 B); 
 # (dram__bytes_read.sum + dram__bytes_write.sum, cold caches), FMA-pipe and
 # issue activity.
 KERNELS = {
-    "kick": {"kernel": "k_kick", "alg_bytes": KICK_BYTES, "ncu": None},
+    "kick": {"kernel": "k_kick", "alg_bytes": KICK_BYTES,
+             "ncu": {"dram_bytes": 100.6, "fma_pipe": 0.067, "issue_active": 0.280}},
     "rebuild": {"kernel": "k_hash_count + scan + k_scatter + k_permute + k_verlet_lean "
                           "(every few steps, per-step average)", "alg_bytes": None, "ncu": None},
     "density": {"kernel": "k_density_lean", "alg_bytes": DENSITY_BYTES,
-                "ncu": {"dram_bytes": 118.6, "fma_pipe": 0.238, "issue_active": 0.595}},
+                "ncu": {"dram_bytes": 118.4, "fma_pipe": 0.249, "issue_active": 0.658}},
     "force": {"kernel": "k_force_lean", "alg_bytes": FORCE_BYTES,
-              "ncu": {"dram_bytes": 149.2, "fma_pipe": 0.452, "issue_active": 0.703}},
+              "ncu": {"dram_bytes": 149.2, "fma_pipe": 0.426, "issue_active": 0.688}},
 }
 # Status bits of the device status word (include/sph_gb300.h), for the line.
 STATUS_BITS = {0x1: "NEIGHBOR_LIST_OVERFLOW", 0x2: "CELL_LIST_OVERFLOW",
