@@ -197,3 +197,23 @@ def test_snapshot_restore_repeats_steps_bit_for_bit(canonical):
     again = sim.state()[0]
     for k in ("r", "u", "v", "dudt", "dvdt", "rho", "p"):
         assert torch.equal(first[k], again[k]), k
+
+
+def test_snapshot_misuse_is_refused():
+    """A snapshot is taken between two steps and restored only from a saved slot."""
+    from jaxsph_gb300 import _lib, simulate
+
+    setup = cases.tgv_perturbed(n_side=16, seed=6)
+    sim = simulate.Simulation(setup)
+    sim.engine.snapshot_init(2)
+    with pytest.raises(_lib.SphError):
+        sim.engine.snapshot_save(0)  # a freshly loaded state: no step taken yet
+    with pytest.raises(_lib.SphError):
+        sim.engine.snapshot_restore(1)  # nothing saved there
+    sim.run(2)
+    sim.engine.snapshot_save(1)
+    with pytest.raises(_lib.SphError):
+        sim.engine.snapshot_save(2)  # beyond the slots
+    sim.engine.snapshot_restore(1)
+    with pytest.raises(_lib.SphError):
+        sim.engine.snapshot_init(1)  # once per handle
