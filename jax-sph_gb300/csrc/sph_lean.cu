@@ -170,24 +170,28 @@ __device__ __forceinline__ void box_rows(const CaseDev& c, int cell, const float
                               : ri.z - (float)(cz + dz + 1) * c.cell_size[2]) - m;
       pz2 = g > 0.f ? g * g : 0.f;
     }
+    if (pz2 >= R2) continue;  // no row of this plane reaches the particle's sphere
     for (int dy = -ry; dy <= ry; ++dy) {
       const float gy = (float)max(abs(dy) - 1, 0) * c.cell_size[1];
       const float g2 = gz2 + gy * gy;
       if (g2 >= R2) continue;
-      int yw = cy + dy;
-      float sy = 0.f;
-      if (yw < 0) { yw += ny; sy = -c.box[1]; }
-      else if (yw >= ny) { yw -= ny; sy = c.box[1]; }
-      const int kx = min(rx, 1 + (int)(sqrt_up(R2 - g2) * c.inv_cs[0]));
-      int xa = cx - kx, xb = cx + kx;
-      // the chord of the particle's sphere through this row
+      // the particle's own gap to the row: a row its sphere does not reach
+      // holds no candidate and is skipped before any of its bookkeeping
       float p2 = pz2;
       if (dy != 0) {
         const float g = (dy > 0 ? (float)(cy + dy) * c.cell_size[1] - ri.y
                                 : ri.y - (float)(cy + dy + 1) * c.cell_size[1]) - m;
         p2 += g > 0.f ? g * g : 0.f;
       }
-      if (p2 < R2) {
+      if (p2 >= R2) continue;
+      int yw = cy + dy;
+      float sy = 0.f;
+      if (yw < 0) { yw += ny; sy = -c.box[1]; }
+      else if (yw >= ny) { yw -= ny; sy = c.box[1]; }
+      const int kx = min(rx, 1 + (int)(sqrt_up(R2 - g2) * c.inv_cs[0]));
+      int xa = cx - kx, xb = cx + kx;
+      {
+        // the chord of the particle's sphere through this row
         const float w = sqrt_up(R2 - p2) + m;
         const float lo = floorf((ri.x - w) * c.inv_cs[0]);
         const float hi = floorf((ri.x + w) * c.inv_cs[0]);
@@ -195,8 +199,6 @@ __device__ __forceinline__ void box_rows(const CaseDev& c, int cell, const float
         const int tb = (int)fminf(fmaxf(hi, (float)xa), (float)xb);
         xa = ta;
         xb = tb;
-      } else {
-        xb = xa - 1;  // no cell of this row reaches the sphere
       }
       const int row = (zw * ny + yw) * nx;
       int a0, e0, a1 = 0, e1 = 0;
