@@ -69,7 +69,8 @@ enum {
   SPH_GEXT_ZERO = 0,   /* TGV, LDC (cases/tgv.py:53, cases/ldc.py:124) */
   SPH_GEXT_CONST = 1,  /* g everywhere (DB: (0,-g), cases/db.py:123-126) */
   SPH_GEXT_BAND_X = 2, /* g.x where band_lo < y < band_hi (PF, cases/pf.py:122-131) */
-  SPH_GEXT_ARRAY = 3   /* per-particle array from SphStateView.g_ext */
+  SPH_GEXT_ARRAY = 3,  /* per-particle array from SphStateView.g_ext */
+  SPH_GEXT_REVERSE_X = 4 /* g.x where y <= band_hi, -g.x above it (RPF, cases/rpf.py:58-63) */
 };
 
 /* Boundary condition bc_fn(state) applied after the forward pass by a step. */

@@ -337,6 +337,10 @@ int sph::make_case(const SphConfig& cfg, const SphCase& in, long long p_off, lon
   c.delta_coef = (float)(in.diff_alpha * in.h * in.c_ref * in.rho_ref);
   // rho_evol_fn_delta_wrapper(delta, support = h, c_ref) (solver.py:33-105, :693)
   c.delta_rho_coef = (float)(in.c_ref * in.diff_delta * in.h);
+  if (in.g_kind < SPH_GEXT_ZERO || in.g_kind > SPH_GEXT_REVERSE_X) {
+    err = "unknown g_kind";
+    return -1;
+  }
   c.g_kind = in.g_kind;
   for (int d = 0; d < 3; ++d) {
     c.g[d] = (float)in.g[d];

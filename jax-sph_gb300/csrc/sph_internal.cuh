@@ -243,6 +243,8 @@ __device__ __forceinline__ float3 g_ext(const CaseDev& c, const float4& r, const
     g = make_float3(c.g[0], c.g[1], c.g[2]);
   } else if (c.g_kind == SPH_GEXT_BAND_X) {
     if (r.y < c.g_hi && r.y > c.g_lo) g.x = c.g[0];
+  } else if (c.g_kind == SPH_GEXT_REVERSE_X) {
+    g.x = r.y > c.g_hi ? -c.g[0] : c.g[0];
   } else if (c.g_kind == SPH_GEXT_ARRAY && garr) {
     g.x = garr[(size_t)orig * DIM + 0];
     g.y = garr[(size_t)orig * DIM + 1];

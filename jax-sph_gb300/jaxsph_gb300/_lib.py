@@ -29,7 +29,7 @@ ERR_HOST = 0x4000
 KERNELS = {"QSK": 0, "WC2K": 1}
 SOLVERS = {"SPH": 0, "RIE": 1, "DELTA": 2}
 EOS_TAIT, EOS_RIEMANN = 0, 1
-GEXT_ZERO, GEXT_CONST, GEXT_BAND_X, GEXT_ARRAY = 0, 1, 2, 3
+GEXT_ZERO, GEXT_CONST, GEXT_BAND_X, GEXT_ARRAY, GEXT_REVERSE_X = 0, 1, 2, 3, 4
 BC_NONE, BC_SOLID_ZERO, BC_SOLID_ZERO_P, BC_LID, BC_HT = 0, 1, 2, 3, 4
 NL_JAXMD, NL_MATSCIPY = 0, 1
 TAG_PAD = -1  # Tag.PAD_VALUE (utils.py:25)

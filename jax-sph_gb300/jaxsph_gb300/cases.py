@@ -74,6 +74,9 @@ class GExt:
         elif k == _lib.GEXT_BAND_X:
             band = (r[:, 1] < hi) & (r[:, 1] > lo)
             res[:, 0] = torch.where(band, torch.full_like(r[:, 0], g[0]), torch.zeros_like(r[:, 0]))
+        elif k == _lib.GEXT_REVERSE_X:
+            res[:, 0] = torch.where(r[:, 1] > hi, torch.full_like(r[:, 0], -g[0]),
+                                    torch.full_like(r[:, 0], g[0]))
         return res
 
 
@@ -489,6 +492,63 @@ def couette(dx=0.0166666, n_walls=3, viscosity=100.0, u_ref=1.25, u_x_wall=1.25,
                    bc=BC(_lib.BC_LID, (u_x_wall, 0.0, 0.0)), nw=nw, dtype=dtype,
                    wall_layer=_wall_layer(dx, n_walls, np.array([0.0, dxn]), walls, dtype),
                    **kw)
+
+
+def cube_of_water(dx=0.05, n_walls=3, dtype=np.float32, t_end=1.0, dt=None, **kw):
+    """2D cube of water falling in a walled box (cases/cw.py, cases/cw.yaml): SPH with
+    the generalized wall BC and density evolution, gravity -1 in y, the fluid's
+    initial velocity (0, -0.5)."""
+    L_wall, H_wall, L, H = 1.0, 1.0, 0.3, 0.3
+    cube_offset = np.array([0.5, 0.5])
+    dxn = n_walls * dx
+    box = np.array([L_wall, H_wall]) + 2 * dxn
+    r_w = pos_box_2d(np.array([L_wall, H_wall]), dx, n_walls, dtype)
+    r_f = _add(pos_init_cartesian_2d(np.array([L, H]), dx, dtype), dxn + cube_offset, dtype)
+    r = np.concatenate([r_w, r_f])
+    tag = np.concatenate([np.full(len(r_w), SOLID_WALL), np.full(len(r_f), FLUID)])
+    # CW._init_velocity2D: every particle u_init; bc_fn then zeroes the walls
+    v = np.tile(np.array([0.0, -0.5]), (len(r), 1))
+    g = 1.0
+    opts = dict(is_bc_trick=True, density_evolution=True)
+    opts.update(kw)
+    return _finish("cw", 2, dx, box, r, tag, v, g_ext_magnitude=g, t_end=t_end, dt=dt,
+                   g_ext=GExt(_lib.GEXT_CONST, (0.0, -g, 0.0)), bc=BC(_lib.BC_SOLID_ZERO_P),
+                   dtype=dtype, **opts)
+
+
+def reverse_poiseuille(dim=2, dx=0.025, dtype=np.float32, t_end=100.0, dt=0.0005, **kw):
+    """Reverse Poiseuille flow (cases/rpf.py, cases/rpf.yaml): a periodic box
+    [1, 2] (3D: [1, 2, 0.5]) filled with fluid at rest, body force +1 in x
+    below y = 1 and -1 above; viscosity 0.1, background pressure 0.05 p_ref."""
+    box = np.array([1.0, 2.0]) if dim == 2 else np.array([1.0, 2.0, 0.5])
+    r = _grid(box, dx, dtype)
+    tag = np.full(len(r), FLUID)
+    v = np.zeros_like(r, dtype=np.float64)
+    g = 1.0
+    opts = dict(viscosity=0.1, p_bg_factor=0.05)
+    opts.update(kw)
+    return _finish("rpf", dim, dx, box, r, tag, v, g_ext_magnitude=g, t_end=t_end, dt=dt,
+                   g_ext=GExt(_lib.GEXT_REVERSE_X, (g, 0.0, 0.0), (1.0, 1.0)),
+                   dtype=dtype, **opts)
+
+
+def unit_cube(dim=2, dx=0.02, dtype=np.float32, t_end=1.0, dt=None, **kw):
+    """The reference's unit-test case (cases/ut.py, cases/ut.yaml): a cube of
+    water (0.5 on a side) falling under gravity -1 in y through a periodic box
+    1 on a side, SPH with density evolution, no walls."""
+    L_wall, L, H = 1.0, 0.5, 0.5
+    cube_offset = np.full(dim, 0.25)
+    box = np.full(dim, L_wall)
+    cube = np.array([L, H]) if dim == 2 else np.array([L, L, H])
+    r = _add(_grid(cube, dx, dtype), cube_offset, dtype)
+    tag = np.full(len(r), FLUID)
+    v = np.zeros_like(r, dtype=np.float64)
+    g = 1.0
+    gv = (0.0, -g, 0.0)
+    opts = dict(density_evolution=True)
+    opts.update(kw)
+    return _finish("ut", dim, dx, box, r, tag, v, g_ext_magnitude=g, t_end=t_end, dt=dt,
+                   g_ext=GExt(_lib.GEXT_CONST, gv), dtype=dtype, **opts)
 
 
 def fourier_perturbation(r, sigma=0.1, kmax=8, seed=1):

@@ -26,7 +26,21 @@ def oracle_g(setup):
         return f
     if spec["kind"] == _lib.GEXT_BAND_X:
         return _band(spec)
+    if spec["kind"] == _lib.GEXT_REVERSE_X:
+        return _reverse(spec)
     return oracle.sph.g_ext_zero
+
+
+def _reverse(spec):
+    # RPF._external_acceleration_fn (cases/rpf.py:58-63)
+    y0 = spec["band"][1]
+    g = spec["g"][0]
+
+    def f(r):
+        res = torch.zeros_like(r)
+        res[:, 0] = torch.where(r[:, 1] > y0, -torch.ones_like(r[:, 0]), torch.ones_like(r[:, 0]))
+        return res * g
+    return f
 
 
 def _band(spec):

@@ -132,6 +132,7 @@ def _valid_case():
     ("case.r_cutoff", 0.0, b"r_cutoff"),
     ("case.box", -1.0, b"box"),
     ("case.bc_kind", 9, b"bc_kind"),
+    ("case.g_kind", 9, b"g_kind"),
 ])
 def test_create_validates_config_and_cases_before_allocating(lib, field, value, word):
     """Every rejected configuration returns SPH_ERR_INVALID_ARG with a message

@@ -84,11 +84,45 @@ def test_cavity_channel_batch_shapes():
     assert pf.g_ext_fn.spec["g"][0] == pytest.approx(8 * eta * 1.25)
 
 
+def test_cube_of_water_layout():
+    # cases/cw.py + cw.yaml: walls of the unit box first, the 0.3 cube at (0.5, 0.5)
+    s = cases.cube_of_water()
+    tag, r, u = s.state["tag"], s.state["r"], s.state["u"]
+    assert s.n == 312 and int((tag == 1).sum()) == 276 and (tag[:276] == 1).all()
+    f = tag == 0
+    assert torch.allclose(r[f].min(0).values, torch.tensor([0.675, 0.675]))
+    assert torch.all(u[f] == torch.tensor([0.0, -0.5])) and torch.all(u[~f] == 0.0)
+    assert (s.state["p"][~f] == 0).all()  # bc_fn at initialisation
+    assert s.solver["is_rho_evol"] and s.solver["is_bc_trick"]
+
+
+def test_reverse_poiseuille_force_flips_at_y1():
+    # cases/rpf.py: +g in x for y <= 1, -g above; no walls
+    s = cases.reverse_poiseuille()
+    assert s.n == 3200 and bool((s.state["tag"] == 0).all()) and s.dt == 0.0005
+    r = torch.tensor([[0.5, 0.5], [0.5, 1.0], [0.5, 1.0001], [0.5, 1.9]])
+    assert s.g_ext_fn(r)[:, 0].tolist() == [1.0, 1.0, -1.0, -1.0]
+    assert s.p_bg == pytest.approx(0.05 * 100.0)
+    assert cases.reverse_poiseuille(dim=3, dx=0.05).n == 20 * 40 * 10
+
+
+def test_unit_cube_layout():
+    # cases/ut.py + ut.yaml: a 0.5 cube of fluid at 0.25 in a periodic unit box
+    s = cases.unit_cube()
+    r = s.state["r"]
+    assert s.n == 625 and torch.allclose(r.min(0).values, torch.tensor([0.26, 0.26]))
+    assert torch.allclose(r.max(0).values, torch.tensor([0.74, 0.74]))
+    assert s.solver["is_rho_evol"] and not s.solver["is_bc_trick"]
+
+
 @pytest.mark.parametrize("make", [lambda: cases.dam_break(dx=0.05),
                                   lambda: cases.lid_driven_cavity(dx=0.05),
                                   lambda: cases.poiseuille(dx=0.05),
                                   lambda: cases.couette(dx=0.05),
-                                  lambda: cases.heat_transfer(dx=0.05)])
+                                  lambda: cases.heat_transfer(dx=0.05),
+                                  lambda: cases.cube_of_water(),
+                                  lambda: cases.reverse_poiseuille(dx=0.05),
+                                  lambda: cases.unit_cube(dx=0.05)])
 def test_descriptors_match_oracle_callbacks(make):
     s = make()
     g = torch.Generator().manual_seed(0)

@@ -67,6 +67,10 @@ def small_cases():
                                                      density_evolution=True),
         # moving lid with Riemann walls: normals recomputed every step
         "ldc_rie": lambda: cases.lid_driven_cavity(dx=0.04, solver_name="RIE"),
+        "cw_sph_evol": lambda: cases.cube_of_water(),
+        "rpf_sph": lambda: cases.reverse_poiseuille(dx=0.05),
+        "rpf3d_sph": lambda: cases.reverse_poiseuille(dim=3, dx=0.1),
+        "ut_sph_evol": lambda: cases.unit_cube(dx=0.04),
     }
 
 
