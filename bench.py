@@ -59,6 +59,10 @@ KERNELS = {
                 "ncu": {"dram_bytes": 118.4, "fma_pipe": 0.249, "issue_active": 0.658}},
     "force": {"kernel": "k_force_lean", "alg_bytes": FORCE_BYTES,
               "ncu": {"dram_bytes": 149.2, "fma_pipe": 0.426, "issue_active": 0.688}},
+    # the force pass with its senders staged in shared memory (--force-variant staged)
+    # (profiles/k_force_staged_tgv3d_64.md)
+    "force_staged": {"kernel": "k_force_staged", "alg_bytes": FORCE_BYTES,
+                     "ncu": {"dram_bytes": 153.2, "fma_pipe": 0.252, "issue_active": 0.486}},
 }
 # Status bits of the device status word (include/sph_gb300.h), for the line.
 STATUS_BITS = {0x1: "NEIGHBOR_LIST_OVERFLOW", 0x2: "CELL_LIST_OVERFLOW",
@@ -496,12 +500,14 @@ def adjoint_form(device, steps=100, checkpoint_every=10, fp64=True):
 
 
 def gpu_arm(args, ws, rank, local):
-    from jaxsph_gb300 import cases, simulate
+    from jaxsph_gb300 import _lib, cases, simulate
 
     torch.cuda.set_device(local)
     device = torch.device("cuda", local)
     setup = cases.tgv(dim=3, dx=2 * np.pi / args.n_side)
     sim = simulate.Simulation(setup, device=device, skin=args.skin)
+    variants = {"gather": _lib.FORCE_GATHER, "staged": _lib.FORCE_STAGED}
+    sim.engine.set_force_variant(variants[args.force_variant])
     # warm-up through run(): it polls the status word and re-allocates the
     # capacities on overflow, as the reference driver does
     sim.run(max(args.warmup, 3), check_every=1)
@@ -531,6 +537,11 @@ def gpu_arm(args, ws, rank, local):
     # per-kernel times, measured with CUDA events on the stream the kernels
     # are launched on (eager steps; the host reads each rebuild decision)
     _, dens_ms, _, force_ms, kick_ms, rb_ms = sim.engine.profile(20, split=True)
+    # the other force-pass variant on the same state (same results, other time)
+    other = "staged" if args.force_variant == "gather" else "gather"
+    sim.engine.set_force_variant(variants[other])
+    force_other_ms = sim.engine.profile(20, split=True)[3]
+    sim.engine.set_force_variant(variants[args.force_variant])
     peaks_path = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(peaks_path):
         peaks = json.load(open(peaks_path))
@@ -538,9 +549,12 @@ def gpu_arm(args, ws, rank, local):
     else:
         hbm, peak_src = 6800.0, "fallback"
     times = {"kick": kick_ms, "rebuild": rb_ms, "density": dens_ms, "force": force_ms}
+    kernels = dict(KERNELS)
+    if args.force_variant == "staged":
+        kernels["force"] = dict(KERNELS["force_staged"])
     table = {}
     for name, ms in times.items():
-        k = KERNELS[name]
+        k = kernels[name]
         row = {"kernel": k["kernel"], "ms": ms, "alg_bytes_per_particle": k["alg_bytes"]}
         if k["alg_bytes"] and ms > 0:
             gbs = k["alg_bytes"] * n / (ms * 1e-3) / 1e9
@@ -551,7 +565,7 @@ def gpu_arm(args, ws, rank, local):
     # the dominant single kernel (the rebuild is several kernels)
     dom = max(("kick", "density", "force"), key=lambda x: times[x])
     d = table[dom]
-    ncu = KERNELS[dom]["ncu"] or {}
+    ncu = kernels[dom]["ncu"] or {}
     step_ms_mean = total_ms / args.steps
     step_achieved = STEP_BYTES * n / (step_ms_mean * 1e-3) / 1e9
     cfg = workload_config(args, n, ws)  # identical to the reference arm's
@@ -575,6 +589,8 @@ def gpu_arm(args, ws, rank, local):
                      "step": {"alg_bytes_per_particle": STEP_BYTES, "achieved": step_achieved,
                               "frac": step_achieved / hbm}},
         "kernels": table,
+        "force_variant": args.force_variant,
+        "force_variants_ms": {args.force_variant: force_ms, other: force_other_ms},
         "candidate_rebuilds": rebuilds,
         "status": status_report(status),
         "gpu_launches": launches,
@@ -626,6 +642,9 @@ def main():
                     help="Verlet skin as a fraction of the cutoff (0: rebuild every step)")
     ap.add_argument("--batched-steps", type=int, default=1000,
                     help="steps of the batched form (the configuration's 1,000)")
+    ap.add_argument("--force-variant", default="gather", choices=["gather", "staged"],
+                    help="how the force pass reads its senders: gathered from global memory "
+                         "(default) or staged in shared memory one plane of cells at a time")
     ap.add_argument("--n-side", type=int, default=64,
                     help="particles per side of the 3D TGV lattice (64 = the benchmark case)")
     args = ap.parse_args()

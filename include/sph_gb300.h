@@ -270,6 +270,14 @@ int sph_set_wall_layer(SphHandle* h, const float* layer, int64_t m, const double
 /* Threads per block of the density, wall and force passes (a multiple of 32
  * in [32, 256]; default 256). A tuning knob: results do not depend on it. */
 int sph_set_block_size(SphHandle* h, int32_t threads);
+/* How the force pass of the lean passes (sph_list_format 1 or 2) reads its
+ * senders: SPH_FORCE_GATHER (default) gathers each sender's records from
+ * global memory; SPH_FORCE_STAGED stages a block's senders in shared memory
+ * one plane of cells at a time. Same pairs in the same order with the same
+ * arithmetic: results do not depend on it. The generic passes ignore it. A
+ * tuning knob: no reference interface corresponds to it. */
+enum { SPH_FORCE_GATHER = 0, SPH_FORCE_STAGED = 1 };
+int sph_set_force_variant(SphHandle* h, int32_t variant);
 /* Kernel launches issued by one si_euler step of this handle (without a
  * candidate-list rebuild). */
 int sph_step_launch_count(SphHandle* h, int32_t* count);

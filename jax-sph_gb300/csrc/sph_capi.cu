@@ -69,6 +69,7 @@ struct SphHandle {
   cudaStream_t cs[kCopyStreams] = {};
   cudaEvent_t fork = nullptr, join[kCopyStreams] = {};
   int block = 256;        // threads per block of the forward passes
+  int force_variant = SPH_FORCE_GATHER;  // lean force pass: gathered or staged senders
   int lean = 0;           // served by the lean passes (sph_lean.cu): list format
   unsigned* status = nullptr;
   unsigned long long* edgecnt = nullptr;
@@ -146,6 +147,7 @@ struct SphHandle {
     L.dscr = dscr;
     L.block = block;
     L.lean = lean;
+    L.force_variant = force_variant;
     L.c1 = hc[0];
     L.launches = const_cast<int*>(&launch_count);
     L.ev = ev;
@@ -1297,6 +1299,17 @@ int sph_set_block_size(SphHandle* h, int32_t threads) try {
   if (threads < 32 || threads > 256 || threads % 32)
     return fail((int)SPH_ERR_INVALID_ARG, "block size must be a multiple of 32 in [32, 256]");
   h->block = threads;
+  drop_graph(h);
+  return 0;
+} catch (...) {
+  return host_error();
+}
+
+int sph_set_force_variant(SphHandle* h, int32_t variant) try {
+  if (!h) return fail((int)SPH_ERR_INVALID_ARG, "null handle");
+  if (variant != SPH_FORCE_GATHER && variant != SPH_FORCE_STAGED)
+    return fail((int)SPH_ERR_INVALID_ARG, "variant must be SPH_FORCE_GATHER or SPH_FORCE_STAGED");
+  h->force_variant = variant;
   drop_graph(h);
   return 0;
 } catch (...) {

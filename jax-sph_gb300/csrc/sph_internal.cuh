@@ -695,6 +695,7 @@ struct LaunchCtx {
   float4* dscr;           // delta-SPH density scratch: 5 planes of N float4
   int block;              // threads per block of the forward passes (<= 256)
   int lean;               // lean passes (sph_lean.cu): 0 no, 1 16-bit lists, 2 32-bit
+  int force_variant;      // SPH_FORCE_*: how the lean force pass reads its senders
   CaseDev c1;             // the single case (the lean passes take it by value)
   int* launches;          // optional host counter of kernel launches
   cudaEvent_t* ev;        // optional phase events: bin start, bin end, density end,

@@ -27,6 +27,8 @@
 //    from the fast reciprocal; the float32 tolerances against the float64
 //    oracle hold either way, and membership never depends on them (it is
 //    decided on squared distances, exactly as in the generic passes).
+#include <algorithm>
+#include <cmath>
 #include <type_traits>
 
 #include "sph_pairs.cuh"
@@ -641,6 +643,218 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
   b.A2[i] = make_float4(dvdt.x, dvdt.y, dvdt.z, 0.f);
 }
 
+// ------------------------------------------------------------------ staged force
+// The force pass with its senders staged in shared memory, one plane of
+// cells at a time (the tiled form of the pass). A block's receivers are
+// consecutive in the sorted order; when they share one plane of the binning,
+// the senders of their lists lie in the planes dz = -rz..rz around it, and in
+// each plane in the rows within the list radius of the receivers' rows --
+// one or two contiguous ranges of the sorted order (two where the rows wrap
+// around the periodic y face). Stage s copies plane s's ranges (four records
+// per sender: r + m, u, v, R4) into shared memory; every receiver then walks
+// its list from where it stopped, taking a sender from shared memory while it
+// lies in the staged ranges and stopping at the first one that lies in a
+// later stage's. A sender in no staged range (a list entry of the cutoff band,
+// appended after the walk order; rows beyond the tile's capacity) is read from
+// global memory in place. Each receiver thus evaluates its pairs in list order
+// with the same arithmetic as k_force_lean: the results are the same bits.
+// Blocks whose receivers span two planes stage nothing.
+constexpr int kMaxStages = 9;
+
+struct StageWin {
+  int a0, n0, a1, n1;
+};
+
+// The ranges of stage s (plane dz = s - rz) for receivers in cells ca..cb of
+// one plane (row indices ya..yb), truncated to `cap` senders.
+template <int DIM>
+__device__ __forceinline__ StageWin stage_window(const CaseDev& c, const int* cs, int cz, int ya,
+                                                 int yb, int dz, int cap) {
+  StageWin w{0, 0, 0, 0};
+  const int nx = c.nc[0], ny = c.nc[1], nz = (DIM == 3) ? c.nc[2] : 1;
+  // rows whose cell boxes lie within the list radius of the receivers' rows
+  // (the gaps box_rows skips on; larger by the rounding margin)
+  const float R = sqrt_up(c.v_r2) + 2.f * c.trim_m;
+  const float gz = (float)max(abs(dz) - 1, 0) * c.cell_size[2];
+  const float rem = R * R - ((DIM == 3) ? gz * gz : 0.f);
+  if (rem <= 0.f) return w;
+  const int ky = min(c.vrad[1], 1 + (int)(sqrt_up(rem) * (1.0f / c.cell_size[1])));
+  int zw = cz + dz;
+  zw += zw < 0 ? nz : 0;
+  zw -= zw >= nz ? nz : 0;
+  const int base = zw * ny;
+  const int yl = ya - ky, yh = yb + ky;
+  if (yh - yl + 1 >= ny) {
+    w.a0 = cs[base * nx];
+    w.n0 = cs[(base + ny) * nx] - w.a0;
+  } else if (yl < 0) {
+    w.a0 = cs[(base + yl + ny) * nx];
+    w.n0 = cs[(base + ny) * nx] - w.a0;
+    w.a1 = cs[base * nx];
+    w.n1 = cs[(base + yh + 1) * nx] - w.a1;
+  } else if (yh >= ny) {
+    w.a0 = cs[(base + yl) * nx];
+    w.n0 = cs[(base + ny) * nx] - w.a0;
+    w.a1 = cs[base * nx];
+    w.n1 = cs[(base + yh - ny + 1) * nx] - w.a1;
+  } else {
+    w.a0 = cs[(base + yl) * nx];
+    w.n0 = cs[(base + yh + 1) * nx] - w.a0;
+  }
+  w.n0 = min(w.n0, cap);
+  w.n1 = min(w.n1, cap - w.n0);
+  return w;
+}
+
+__device__ __forceinline__ int win_slot(const StageWin& w, int j) {
+  if ((unsigned)(j - w.a0) < (unsigned)w.n0) return j - w.a0;
+  if ((unsigned)(j - w.a1) < (unsigned)w.n1) return w.n0 + (j - w.a1);
+  return -1;
+}
+
+template <int DIM, int KER, bool KAHAN, bool WIDE, bool AV>
+__global__ void __launch_bounds__(128, 5)
+k_force_staged(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* g_arr,
+               const float4* __restrict__ R4, const typename Fmt<WIDE>::Word* __restrict__ nb,
+               const int* __restrict__ nbcnt, int kmax, const typename Fmt<WIDE>::Word* vl,
+               const int* vcnt, int kv, const int* cellid, const int* start, const float4* rref,
+               bool apply_bc, unsigned* status, int cap) {
+  using L = Fmt<WIDE>;
+  using Word = typename L::Word;
+  extern __shared__ __align__(16) float4 s_rec[];  // [4][cap]: r + m, u, v, R4
+  __shared__ StageWin s_win[kMaxStages];
+  __shared__ int s_ns;
+  const int i0 = blockIdx.x * blockDim.x;
+  const int i = i0 + threadIdx.x;
+  const bool live = i < N;
+  if (threadIdx.x < kMaxStages) {
+    // every thread of the first warp finds the block's plane; thread s
+    // computes stage s
+    const int* cs = start + c.cell_off;
+    const int nx = c.nc[0], ny = c.nc[1], nz = (DIM == 3) ? c.nc[2] : 1;
+    const int i1 = min(i0 + (int)blockDim.x, N) - 1;
+    const int ca = cellid[i0] - c.cell_off, cb = cellid[i1] - c.cell_off;
+    const int za = ca / (nx * ny), zb = cb / (nx * ny);
+    const int rz = (DIM == 3) ? c.vrad[2] : 0;
+    const int ns = 2 * rz + 1;
+    // one plane per block, no plane visited twice, within the stage table
+    const bool ok = za == zb && ns <= kMaxStages && ns <= nz;
+    const int s = threadIdx.x;
+    if (ok && s < ns)
+      s_win[s] = stage_window<DIM>(c, cs, za, (ca / nx) % ny, (cb / nx) % ny, s - rz, cap);
+    if (s == 0) s_ns = ok ? ns : 0;
+  }
+  ForceI I;
+  int tag = PAD, m = 0;
+  float drhodt = 0.f;
+  float3 gi = make_float3(0.f, 0.f, 0.f);
+  if (live) {
+    tag = tag_of(b.META[i]);
+    I.ri = b.P4[i];
+    I.fluid = tag == FLUID;
+    I.ui = f3(b.U4[i]);
+    const float3 vi = f3(b.V4[i]);
+    const float4 Ri = R4[i];
+    drhodt = b.A4[i].w;
+    I.rho_i = Ri.x;
+    I.p_i = Ri.y;
+    I.eta_i = Ri.w;
+    I.Vi2 = Ri.z;
+    I.inv_mi = 1.0f / I.ri.w;
+    I.Ai = make_float3(I.rho_i * I.ui.x, I.rho_i * I.ui.y, I.rho_i * I.ui.z);
+    I.wi = make_float3(vi.x - I.ui.x, vi.y - I.ui.y, vi.z - I.ui.z);
+    gi = g_ext<DIM>(c, I.ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
+    m = nbcnt[i];
+  }
+  const bool listed = live && m <= kmax;
+  Acc6<KAHAN> A;
+  const Word* nbi = nb + (live ? i : 0);
+  int k = 0, wg = -1;
+  Word w{};
+  __syncthreads();
+  const int ns = s_ns;
+  // stages 0..ns-1, then a last pass without a staged range for what is left
+  // (one evaluation site for every listed pair)
+  for (int s = 0; s <= ns; ++s) {
+    StageWin cur{0, 0, 0, 0};
+    if (s < ns) {  // uniform over the block
+      if (s > 0) __syncthreads();  // the previous stage's reads are done
+      cur = s_win[s];
+      const int nw = cur.n0 + cur.n1;
+      for (int t = threadIdx.x; t < nw; t += blockDim.x) {
+        const int j = t < cur.n0 ? cur.a0 + t : cur.a1 + (t - cur.n0);
+        s_rec[t] = __ldg(b.P4 + j);
+        s_rec[cap + t] = __ldg(b.U4 + j);
+        s_rec[2 * cap + t] = __ldg(b.V4 + j);
+        s_rec[3 * cap + t] = __ldg(R4 + j);
+      }
+      __syncthreads();
+    }
+    if (!listed) continue;
+    while (k < m) {
+      if ((k >> 2) != wg) {
+        wg = k >> 2;
+        w = nbi[(size_t)wg * N];
+      }
+      const int j = L::dec(i, L::raw(w, k & 3), N);
+      const int t = win_slot(cur, j);
+      float4 rj, uj, vj, Rj;
+      if (t >= 0) {
+        rj = s_rec[t];
+        uj = s_rec[cap + t];
+        vj = s_rec[2 * cap + t];
+        Rj = s_rec[3 * cap + t];
+      } else {
+        bool later = false;
+        for (int s2 = s + 1; s2 < ns; ++s2) later |= win_slot(s_win[s2], j) >= 0;
+        if (later) break;
+        rj = __ldg(b.P4 + j);
+        uj = __ldg(b.U4 + j);
+        vj = __ldg(b.V4 + j);
+        Rj = __ldg(R4 + j);
+      }
+      float3 dr;
+      float d2;
+      mi_dr<DIM>(I.ri, rj, c, dr, d2);
+      force_pair<DIM, KER, KAHAN, AV>(I, c, b.META, j, rj, uj, vj, Rj, dr, d2, A);
+      ++k;
+    }
+  }
+  if (!live) return;
+  if (!listed) {
+    A = force_slow<DIM, KER, KAHAN, WIDE, AV>(N, i, I, A, cp, b, R4, vl, vcnt, kv, cellid,
+                                                start, rref);
+  }
+  float3 dudt = make_float3(A.ax.s + gi.x, A.ay.s + gi.y, A.az.s + gi.z);
+  float3 dvdt = make_float3(A.tx.s, A.ty.s, A.tz.s);
+  if (DIM == 2) {
+    dudt.z = 0.f;
+    dvdt.z = 0.f;
+  }
+  if (apply_bc) {
+    dudt = bc_acc(dudt, tag, c);
+    dvdt = bc_acc(dvdt, tag, c);
+  }
+  if (!isfinite(dudt.x) || !isfinite(dudt.y) || !isfinite(dudt.z))
+    atomicOr(status, SPH_ERR_NONFINITE);
+  b.A4[i] = make_float4(dudt.x, dudt.y, dudt.z, drhodt);
+  b.A2[i] = make_float4(dvdt.x, dvdt.y, dvdt.z, 0.f);
+}
+
+// Senders staged per stage: the rows a block of `bt` receivers spans at the
+// case's mean row occupancy, plus the list radius' rows on each side, with a
+// tenth in reserve (a stage holding more reads the rest from global memory).
+inline int staged_capacity(const CaseDev& c, int dim, int bt) {
+  const double rows = (double)c.nc[1] * (dim == 3 ? (double)c.nc[2] : 1.0);
+  const double per_row = (double)c.n / rows;
+  const double spanned = std::ceil(bt / std::max(per_row, 1.0)) + 1.0;
+  const double win = (spanned + 2.0 * c.vrad[1]) * per_row * 1.1;
+  // at most 46 KB per block: with the static stage table within the 48 KB a
+  // launch may take without opting in
+  const int cap = (int)std::min(win, 46.0 * 1024 / 64);
+  return std::max(32, std::min((cap + 31) / 32 * 32, 736));
+}
+
 template <int DIM, int KER, bool KAHAN, bool WIDE>
 void forward_lean_t(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid,
                     const int* start, unsigned long long* edgecnt, const float* g_arr,
@@ -660,7 +874,21 @@ void forward_lean_t(const LaunchCtx& L, Buffers b, float4* R4, const int* cellid
     mark(L, 2);
     mark(L, 3);
   }
-  if (phases & 2) {
+  if ((phases & 2) && L.force_variant == SPH_FORCE_STAGED) {
+    const int sb = 128;
+    const int cap = staged_capacity(L.c1, L.dim, sb);
+    const size_t smem = sizeof(float4) * 4 * (size_t)cap;
+    if (L.c1.av_alpha != 0.0f)
+      k_force_staged<DIM, KER, KAHAN, WIDE, true><<<nblocks(N, sb), sb, smem, L.stream>>>(
+          N, b, L.c1, L.cases, g_arr, R4, nb, L.nbr_cnt, L.kmax, vl, L.vcnt, L.kv, cellid,
+          start, L.rref, apply_bc, L.status, cap);
+    else
+      k_force_staged<DIM, KER, KAHAN, WIDE, false><<<nblocks(N, sb), sb, smem, L.stream>>>(
+          N, b, L.c1, L.cases, g_arr, R4, nb, L.nbr_cnt, L.kmax, vl, L.vcnt, L.kv, cellid,
+          start, L.rref, apply_bc, L.status, cap);
+    count_launch(L);
+    mark(L, 4);
+  } else if (phases & 2) {
     if (L.c1.av_alpha != 0.0f)
       k_force_lean<DIM, KER, KAHAN, WIDE, true><<<g, bt, 0, L.stream>>>(
           N, b, L.c1, L.cases, g_arr, R4, nb, L.nbr_cnt, L.kmax, vl, L.vcnt, L.kv, cellid,

@@ -30,6 +30,7 @@ KERNELS = {"QSK": 0, "WC2K": 1}
 SOLVERS = {"SPH": 0, "RIE": 1, "DELTA": 2}
 EOS_TAIT, EOS_RIEMANN = 0, 1
 GEXT_ZERO, GEXT_CONST, GEXT_BAND_X, GEXT_ARRAY, GEXT_REVERSE_X = 0, 1, 2, 3, 4
+FORCE_GATHER, FORCE_STAGED = 0, 1
 BC_NONE, BC_SOLID_ZERO, BC_SOLID_ZERO_P, BC_LID, BC_HT = 0, 1, 2, 3, 4
 NL_JAXMD, NL_MATSCIPY = 0, 1
 TAG_PAD = -1  # Tag.PAD_VALUE (utils.py:25)
@@ -76,6 +77,7 @@ class SphNLCapacity(ctypes.Structure):
 EXPORTS = ["sph_abi_version", "sph_last_error", "sph_create", "sph_destroy", "sph_update_cases",
            "sph_set_state", "sph_get_state", "sph_nl_allocate", "sph_nl_set_capacity",
            "sph_nl_update", "sph_nl_edges", "sph_forward", "sph_step", "sph_set_block_size",
+           "sph_set_force_variant",
            "sph_step_launch_count", "sph_profile_step", "sph_adjoint_init", "sph_tape_record",
            "sph_adjoint_step", "sph_read_status", "sph_read_status_async", "sph_diagnostics",
            "sph_nl_edges_noalloc", "sph_rebuild_stats", "sph_advance", "sph_set_wall_layer",
@@ -111,6 +113,7 @@ def load(build_if_missing=True):
     lib.sph_forward.argtypes = [V, V]
     lib.sph_step.argtypes = [V, ctypes.c_int32, V]
     lib.sph_set_block_size.argtypes = [V, ctypes.c_int32]
+    lib.sph_set_force_variant.argtypes = [V, ctypes.c_int32]
     lib.sph_step_launch_count.argtypes = [V, P(ctypes.c_int32)]
     lib.sph_list_format.argtypes = [V, P(ctypes.c_int32)]
     lib.sph_snapshot_init.argtypes = [V, ctypes.c_int32]
@@ -289,6 +292,11 @@ class Engine:
 
     def set_block_size(self, threads):
         _check(self.lib.sph_set_block_size(self.h, int(threads)))
+
+    def set_force_variant(self, variant):
+        """FORCE_GATHER or FORCE_STAGED: how the lean force pass reads its
+        senders (the same results either way)."""
+        _check(self.lib.sph_set_force_variant(self.h, int(variant)))
 
     def launch_count(self):
         c = ctypes.c_int32(0)

@@ -166,6 +166,7 @@ def test_handle_entry_points_reject_a_null_handle(lib):
     assert lib.sph_snapshot_init(None, 1) == _lib.ERR_INVALID_ARG
     assert lib.sph_snapshot_save(None, 0, None) == _lib.ERR_INVALID_ARG
     assert lib.sph_snapshot_restore(None, 0, None) == _lib.ERR_INVALID_ARG
+    assert lib.sph_set_force_variant(None, _lib.FORCE_STAGED) == _lib.ERR_INVALID_ARG
     assert b"null" in lib.sph_last_error() or b"slot" in lib.sph_last_error()
     cfg = _lib.SphConfig(dim=2)
     h = ctypes.c_void_p()
