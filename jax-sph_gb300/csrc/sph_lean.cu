@@ -486,7 +486,7 @@ k_density_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, int self_te
 // The receiver's own quantities of the force pass.
 struct ForceI {
   float4 ri;
-  float3 ui, Ai, wi;
+  float3 ui, hAi, wi;  // hAi = rho_i u_i / 2
   float rho_i, p_i, eta_i, Vi2, inv_mi;
   bool fluid;
 };
@@ -516,17 +516,18 @@ __device__ __forceinline__ void force_pair(const ForceI& I, const CaseDev& c, co
   const float p_ij = __fdividef(rho_j * I.p_i + I.rho_i * p_j, I.rho_i + rho_j);
   const float ki = dot3(I.wi, dr);
   const float kj = dot3(make_float3(vj.x - uj.x, vj.y - uj.y, vj.z - uj.z), dr);
-  float3 a = make_float3(cc * (-p_ij * dr.x + 0.5f * (I.Ai.x * ki + rho_j * uj.x * kj) +
-                               eta_ij * (I.ui.x - uj.x)),
-                         cc * (-p_ij * dr.y + 0.5f * (I.Ai.y * ki + rho_j * uj.y * kj) +
-                               eta_ij * (I.ui.y - uj.y)),
-                         cc * (-p_ij * dr.z + 0.5f * (I.Ai.z * ki + rho_j * uj.z * kj) +
-                               eta_ij * (I.ui.z - uj.z)));
+  // the stress term (A_i ki + rho_j u_j kj) / 2 as (A_i / 2) ki + (rho_j kj / 2) u_j:
+  // the halvings are exact, rho_j kj / 2 is formed once per pair
+  const float hk = 0.5f * rho_j * kj;
+  const float3 du = make_float3(I.ui.x - uj.x, I.ui.y - uj.y, I.ui.z - uj.z);
+  float3 a = make_float3(cc * (fmaf(-p_ij, dr.x, fmaf(I.hAi.x, ki, hk * uj.x)) + eta_ij * du.x),
+                         cc * (fmaf(-p_ij, dr.y, fmaf(I.hAi.y, ki, hk * uj.y)) + eta_ij * du.y),
+                         cc * (fmaf(-p_ij, dr.z, fmaf(I.hAi.z, ki, hk * uj.z)) + eta_ij * du.z));
   if (AV && I.fluid && tag_of(meta[j]) == FLUID) {
     const float m_j = rj.w;
     const float rho_ab = 0.5f * (I.rho_i + rho_j);
     const float num = m_j * c.av_alpha * c.av_hab * c.av_cab *
-                      ((I.ui.x - uj.x) * dr.x + (I.ui.y - uj.y) * dr.y + (I.ui.z - uj.z) * dr.z);
+                      (du.x * dr.x + du.y * dr.y + du.z * dr.z);
     const float k = num * gw * inv_d / (rho_ab * (dist * dist + c.av_eps));
     a.x += k * dr.x;
     a.y += k * dr.y;
@@ -589,7 +590,8 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
   I.eta_i = Ri.w;
   I.Vi2 = Ri.z;
   I.inv_mi = 1.0f / I.ri.w;
-  I.Ai = make_float3(I.rho_i * I.ui.x, I.rho_i * I.ui.y, I.rho_i * I.ui.z);
+  I.hAi = make_float3(0.5f * (I.rho_i * I.ui.x), 0.5f * (I.rho_i * I.ui.y),
+                      0.5f * (I.rho_i * I.ui.z));
   I.wi = make_float3(vi.x - I.ui.x, vi.y - I.ui.y, vi.z - I.ui.z);
   const float3 gi = g_ext<DIM>(c, I.ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
   Acc6<KAHAN> A;
@@ -761,9 +763,10 @@ k_force_staged(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float
     I.eta_i = Ri.w;
     I.Vi2 = Ri.z;
     I.inv_mi = 1.0f / I.ri.w;
-    I.Ai = make_float3(I.rho_i * I.ui.x, I.rho_i * I.ui.y, I.rho_i * I.ui.z);
+    I.hAi = make_float3(0.5f * (I.rho_i * I.ui.x), 0.5f * (I.rho_i * I.ui.y),
+                        0.5f * (I.rho_i * I.ui.z));
     I.wi = make_float3(vi.x - I.ui.x, vi.y - I.ui.y, vi.z - I.ui.z);
-    gi = g_ext<DIM>(c, I.ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
+    gi =g_ext<DIM>(c, I.ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
     m = nbcnt[i];
   }
   const bool listed = live && m <= kmax;
