@@ -653,7 +653,10 @@ k_force_lean(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float* 
 // each plane in the rows within the list radius of the receivers' rows --
 // one or two contiguous ranges of the sorted order (two where the rows wrap
 // around the periodic y face). Stage s copies plane s's ranges (four records
-// per sender: r + m, u, v, R4) into shared memory; every receiver then walks
+// per sender: r + m, u, v, R4) into shared memory with 1-D bulk copies, one
+// per range and record array, whose bytes complete an mbarrier phase (a copy
+// that does not complete within the poll limit sets SPH_ERR_TIMEOUT and the
+// pass reads every sender from global memory instead); every receiver then walks
 // its list from where it stopped, taking a sender from shared memory while it
 // lies in the staged ranges and stopping at the first one that lies in a
 // later stage's. A sender in no staged range (a list entry of the cutoff band,
@@ -708,6 +711,51 @@ __device__ __forceinline__ StageWin stage_window(const CaseDev& c, const int* cs
   return w;
 }
 
+// 1-D bulk copies (cp.async.bulk) of global ranges into shared memory, their
+// completion counted in bytes on an mbarrier; every wait is bounded.
+__device__ __forceinline__ unsigned smem_u32(const void* p) {
+  return (unsigned)__cvta_generic_to_shared(p);
+}
+__device__ __forceinline__ void mbar_init(unsigned long long* bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count)
+               : "memory");
+  asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+}
+// orders this thread's earlier shared-memory accesses before later
+// async-proxy (bulk copy) writes
+__device__ __forceinline__ void fence_proxy_async_smem() {
+  asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+__device__ __forceinline__ void mbar_expect_tx(unsigned long long* bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+// dst and src 16-byte aligned, bytes a multiple of 16
+__device__ __forceinline__ void bulk_to_smem(void* dst, const void* src, unsigned bytes,
+                                             unsigned long long* bar) {
+  asm volatile(
+      "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::
+          "r"(smem_u32(dst)),
+      "l"(src), "r"(bytes), "r"(smem_u32(bar))
+      : "memory");
+}
+// polls phase `parity` of the barrier at most `polls` times (false: gave up)
+__device__ __forceinline__ bool mbar_wait(unsigned long long* bar, unsigned parity, int polls) {
+  for (int it = 0; it < polls; ++it) {
+    unsigned done;
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(smem_u32(bar)), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+constexpr int kStagePolls = 1 << 20;
+
 __device__ __forceinline__ int win_slot(const StageWin& w, int j) {
   if ((unsigned)(j - w.a0) < (unsigned)w.n0) return j - w.a0;
   if ((unsigned)(j - w.a1) < (unsigned)w.n1) return w.n0 + (j - w.a1);
@@ -726,6 +774,8 @@ k_force_staged(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float
   extern __shared__ __align__(16) float4 s_rec[];  // [4][cap]: r + m, u, v, R4
   __shared__ StageWin s_win[kMaxStages];
   __shared__ int s_ns;
+  __shared__ __align__(8) unsigned long long s_bar;  // completion of a stage's copies
+  if (threadIdx.x == 0) mbar_init(&s_bar, 1);
   const int i0 = blockIdx.x * blockDim.x;
   const int i = i0 + threadIdx.x;
   const bool live = i < N;
@@ -766,7 +816,7 @@ k_force_staged(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float
     I.hAi = make_float3(0.5f * (I.rho_i * I.ui.x), 0.5f * (I.rho_i * I.ui.y),
                         0.5f * (I.rho_i * I.ui.z));
     I.wi = make_float3(vi.x - I.ui.x, vi.y - I.ui.y, vi.z - I.ui.z);
-    gi =g_ext<DIM>(c, I.ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
+    gi = g_ext<DIM>(c, I.ri, g_arr, c.g_kind == SPH_GEXT_ARRAY ? b.ORIG[i] : 0);
     m = nbcnt[i];
   }
   const bool listed = live && m <= kmax;
@@ -776,22 +826,44 @@ k_force_staged(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float
   Word w{};
   __syncthreads();
   const int ns = s_ns;
+  int nstage = ns;  // stages staged in shared memory (0 once a copy timed out)
+  unsigned phase = 0u;
   // stages 0..ns-1, then a last pass without a staged range for what is left
   // (one evaluation site for every listed pair)
   for (int s = 0; s <= ns; ++s) {
     StageWin cur{0, 0, 0, 0};
-    if (s < ns) {  // uniform over the block
-      if (s > 0) __syncthreads();  // the previous stage's reads are done
+    if (s < nstage) {  // uniform over the block
+      if (s > 0) {
+        fence_proxy_async_smem();
+        __syncthreads();  // the previous stage's reads are done
+      }
       cur = s_win[s];
       const int nw = cur.n0 + cur.n1;
-      for (int t = threadIdx.x; t < nw; t += blockDim.x) {
-        const int j = t < cur.n0 ? cur.a0 + t : cur.a1 + (t - cur.n0);
-        s_rec[t] = __ldg(b.P4 + j);
-        s_rec[cap + t] = __ldg(b.U4 + j);
-        s_rec[2 * cap + t] = __ldg(b.V4 + j);
-        s_rec[3 * cap + t] = __ldg(R4 + j);
+      if (nw > 0) {
+        // the stage's ranges of the four record arrays: one bulk copy each
+        if (threadIdx.x == 0) {
+          mbar_expect_tx(&s_bar, 64u * (unsigned)nw);
+          const float4* src[4] = {b.P4, b.U4, b.V4, R4};
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            if (cur.n0 > 0)
+              bulk_to_smem(s_rec + q * cap, src[q] + cur.a0, 16u * (unsigned)cur.n0, &s_bar);
+            if (cur.n1 > 0)
+              bulk_to_smem(s_rec + q * cap + cur.n0, src[q] + cur.a1, 16u * (unsigned)cur.n1,
+                           &s_bar);
+          }
+        }
+        const bool ok = mbar_wait(&s_bar, phase, kStagePolls);
+        if (__syncthreads_or(!ok)) {
+          // a copy that did not complete: report it, wait (bounded) for what
+          // is in flight, and read every sender from global memory instead
+          if (threadIdx.x == 0) atomicOr(status, SPH_ERR_TIMEOUT);
+          mbar_wait(&s_bar, phase, kStagePolls);
+          nstage = 0;
+          cur = StageWin{0, 0, 0, 0};
+        }
+        phase ^= 1u;
       }
-      __syncthreads();
     }
     if (!listed) continue;
     while (k < m) {
@@ -809,7 +881,7 @@ k_force_staged(int N, Buffers b, const CaseDev c, const CaseDev* cp, const float
         Rj = s_rec[3 * cap + t];
       } else {
         bool later = false;
-        for (int s2 = s + 1; s2 < ns; ++s2) later |= win_slot(s_win[s2], j) >= 0;
+        for (int s2 = s + 1; s2 < nstage; ++s2) later |= win_slot(s_win[s2], j) >= 0;
         if (later) break;
         rj = __ldg(b.P4 + j);
         uj = __ldg(b.U4 + j);
