@@ -670,8 +670,8 @@ struct StageWin {
   int a0, n0, a1, n1;
 };
 
-// The ranges of stage s (plane dz = s - rz) for receivers in cells ca..cb of
-// one plane (row indices ya..yb), truncated to `cap` senders.
+// The ranges of the stage at plane offset dz for receivers in rows ya..yb of
+// plane cz, truncated to `cap` senders.
 template <int DIM>
 __device__ __forceinline__ StageWin stage_window(const CaseDev& c, const int* cs, int cz, int ya,
                                                  int yb, int dz, int cap) {

@@ -50,6 +50,19 @@ def test_status_bits_match_the_header():
     assert len(set(bits.values())) == len(bits)  # every bit distinct
 
 
+def test_enum_values_match_the_header():
+    src = open(HEADER).read()
+    enums = dict(re.findall(r"SPH_(\w+) = (\d+)", src))
+    assert len(enums) >= 20
+    for name, value in enums.items():
+        group, _, member = name.partition("_")
+        if group in ("KERNEL", "SOLVER"):
+            mirror = getattr(_lib, group + "S")[member]
+        else:
+            mirror = getattr(_lib, name)
+        assert mirror == int(value), name
+
+
 def test_create_rejects_bad_arguments_without_touching_the_gpu(lib):
     lib.sph_create.restype = ctypes.c_int
     cfg = _lib.SphConfig(dim=4)
